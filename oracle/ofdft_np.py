@@ -1,0 +1,1117 @@
+"""numpy restatement of the reference OF-DFT hot path (TEST INFRASTRUCTURE ONLY).
+
+This module is the oracle the CUDA path is checked against.  It is our own
+restatement of the algorithms in Quantum-MultiScale/DFTpy; every function
+names the reference file:line it follows.  The reference computes in float64
+/ complex128 throughout, and so does this module.  Third-party calls the
+reference makes (numpy pocketfft, scipy FITPACK splrep/splev, scipy.special
+erfc/erfcinv, scipy's MINPACK-2 line search) are made here too, so that the
+oracle's arithmetic is the reference's arithmetic.
+
+Conventions (reference src/dftpy/field.py:413-430, :779-804):
+  * a real field is a C-ordered (n0, n1, n2) float64 array;
+  * ``fft(f)`` = numpy ``rfftn(f) * dV``; ``ifft(F)`` = ``irfftn(F, s=nr) / dV``;
+  * G vectors: integer fftfreq indices times the reciprocal lattice
+    ``2*pi*inv(lattice).T`` (src/dftpy/grid.py:384-415, :584-620).
+"""
+import math
+
+import numpy as np
+from scipy import special as sp
+from scipy.interpolate import splev, splrep
+
+C_TF = 2.87123400018819181594      # src/dftpy/constants.py:82
+ZERO = 1e-30                        # src/dftpy/constants.py:85
+
+# CODATA-2014 Bohr (Angstrom) and Hartree (eV), as ase.units derives them.
+_e, _me, _hp = 1.6021766208e-19, 9.10938356e-31, 6.626070040e-34
+_eps0 = 1.0 / (4.0e-7 * math.pi) / 299792458.0 ** 2
+_hbar = _hp / (2.0 * math.pi)
+BOHR = 4.0e10 * math.pi * _eps0 * _hbar ** 2 / _me / _e ** 2
+HARTREE = _me * _e ** 3 / 16.0 / math.pi ** 2 / _eps0 ** 2 / _hbar ** 2
+
+
+# --------------------------------------------------------------------------
+# grid
+# --------------------------------------------------------------------------
+class Grid:
+    """Direct grid + half-complex reciprocal grid (src/dftpy/grid.py:8-60, :480-620)."""
+
+    def __init__(self, lattice, nr):
+        self.lattice = np.asarray(lattice, dtype=np.float64).reshape(3, 3)
+        self.nr = np.array(nr, dtype=np.int64)
+        self.nnr = int(np.prod(self.nr))
+        self.volume = abs(float(np.linalg.det(self.lattice)))
+        self.dV = self.volume / self.nnr
+        self.nrG = self.nr.copy()
+        self.nrG[-1] = self.nr[-1] // 2 + 1
+        # reciprocal lattice, rows b_j (grid.py:384-415)
+        self.rlattice = (2.0 * np.pi * np.linalg.inv(self.lattice)).T
+        self._g = None
+        self._gg = None
+        self._mask = None
+
+    @property
+    def g(self):
+        if self._g is None:  # grid.py:584-620 (fftfreq on axes 0,1; rfftfreq on axis 2)
+            ax = [np.fft.fftfreq(self.nr[0], d=1.0 / self.nr[0]),
+                  np.fft.fftfreq(self.nr[1], d=1.0 / self.nr[1]),
+                  np.fft.rfftfreq(self.nr[2], d=1.0 / self.nr[2])]
+            S = np.asarray(np.meshgrid(*ax, indexing="ij"))
+            self._g = np.einsum("j...,jk->k...", S, self.rlattice)
+        return self._g
+
+    @property
+    def gg(self):
+        if self._gg is None:  # grid.py:523-530
+            g = self.g
+            self._gg = np.einsum("lijk,lijk->ijk", g, g)
+        return self._gg
+
+    @property
+    def q(self):
+        return np.sqrt(self.gg)  # grid.py:517-521
+
+    @property
+    def invgg(self):
+        gg = self.gg.copy()  # grid.py:532-541: G=0 -> 0
+        gg[0, 0, 0] = 1.0
+        inv = 1.0 / gg
+        inv[0, 0, 0] = 0.0
+        return inv
+
+    @property
+    def mask(self):
+        """Half-space mask that counts each +-G pair once (grid.py:658-695, serial case)."""
+        if self._mask is None:
+            nr = self.nr
+            D = nr // 2
+            M = nr % 2
+            m = np.ones(tuple(self.nrG), dtype=bool)
+            m[0, D[1] + 1:, 0] = False
+            m[D[0] + 1:, :, 0] = False
+            if M[2] == 0:
+                m[0, 0, D[2]] = False
+                m[0, D[1] + 1:, D[2]] = False
+                m[D[0] + 1:, :, D[2]] = False
+                if M[1] == 0:
+                    m[0, D[1], D[2]] = False
+                if M[0] == 0:
+                    m[D[0], 0, D[2]] = False
+                    m[D[0], D[1] + 1:, D[2]] = False
+            if M[0] == 0:
+                m[D[0], D[1] + 1:, 0] = False
+                if M[1] == 0:
+                    m[D[0], D[1], 0] = False
+            if M[1] == 0:
+                m[0, D[1], 0] = False
+            if np.all(M == 0):
+                m[D[0], D[1], D[2]] = False
+            self._mask = m
+        return self._mask
+
+    def guess_ecut(self):
+        """grid.py:363-366 with RPgrid.g2max = 2*ecut (grid.py:722-723)."""
+        lengths = np.sqrt((self.lattice ** 2).sum(axis=1))
+        sp1 = lengths / self.nr
+        sp2 = lengths / (self.nr - 1)
+        spacing = 0.5 * (sp1 + sp2)
+        return np.pi ** 2 / (2 * spacing.max() ** 2)
+
+
+def fft(f, grid):
+    """DirectField.fft: rfftn times dV (field.py:413-430)."""
+    return np.fft.rfftn(f) * grid.dV
+
+
+def ifft(F, grid):
+    """ReciprocalField.ifft(force_real=True): irfftn / dV (field.py:779-804)."""
+    return np.fft.irfftn(F, s=tuple(grid.nr), axes=(0, 1, 2)) / grid.dV
+
+
+# --------------------------------------------------------------------------
+# KEDF: TF, vW
+# --------------------------------------------------------------------------
+def tf(rho, grid, x=1.0, calc=("E", "V")):
+    """Thomas-Fermi (kedf/tf.py:13-35, :66-80); PowerInt(rho,5,3) = cbrt(rho^5) (math_utils.py:158)."""
+    out = {}
+    if "E" in calc:
+        r5 = rho * rho * rho * rho * rho
+        ed = np.cbrt(r5) * ((3.0 / 10.0) * (3.0 * np.pi ** 2) ** (2.0 / 3.0))
+        out["E"] = ed.sum() * grid.dV * x
+    if "V" in calc:
+        fac = (3.0 / 10.0) * (5.0 / 3.0) * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+        out["V"] = fac * np.cbrt(rho * rho) * x
+    return out
+
+
+def vw(rho, grid, y=1.0, calc=("E", "V")):
+    """von Weizsaecker (kedf/vw.py:29-53 potential, :84-94 energy, :115-131)."""
+    tol = 1e-30
+    rhom = rho.copy()
+    rhom[~(rho > 0)] = tol
+    sq = np.sqrt(rhom)
+    a = ifft(fft(sq, grid) * grid.gg, grid) * 0.5
+    sq[np.abs(sq) < tol] = tol
+    pot = a / sq
+    out = {}
+    if "E" in calc:
+        m = rho > 0
+        out["E"] = np.einsum("i,i->", rho[m], pot[m]) * grid.dV * y
+    if "V" in calc:
+        out["V"] = pot * y
+    return out
+
+
+# --------------------------------------------------------------------------
+# XC: LDA (Slater + Perdew-Zunger 81)
+# --------------------------------------------------------------------------
+PZ = dict(a=0.0311, b=-0.048, c=0.0020, d=-0.0116, gamma=-0.1423, beta1=1.0529, beta2=0.3334)
+
+
+def lda(rho, grid, calc=("E", "V")):
+    """Built-in LDA (xc/semilocal_xc.py:283-341), unpolarised branch only."""
+    a, b, c, d = PZ["a"], PZ["b"], PZ["c"], PZ["d"]
+    gamma, beta1, beta2 = PZ["gamma"], PZ["beta1"], PZ["beta2"]
+    rc = np.cbrt(rho)
+    rc[rc < 1e-30] = 1e-30
+    Rs = np.cbrt(3.0 / (4.0 * np.pi)) / rc
+    rs1 = Rs < 1
+    rs2 = ~rs1
+    Rs2sqrt = np.sqrt(Rs[rs2])
+    out = {}
+    if "E" in calc:
+        ex = -3.0 / 4.0 * np.cbrt(3.0 / np.pi) * rc
+        ex[rs1] += a * np.log(Rs[rs1]) + b + c * Rs[rs1] * np.log(Rs[rs1]) + d * Rs[rs1]
+        ex[rs2] += gamma / (1.0 + beta1 * Rs2sqrt + beta2 * Rs[rs2])
+        out["E"] = np.einsum("ijk,ijk->", ex, rho) * grid.dV
+    if "V" in calc:
+        pot = np.cbrt(-3.0 / np.pi) * rc
+        pot[rs1] += (np.log(Rs[rs1]) * (a + 2.0 / 3 * c * Rs[rs1]) + b - 1.0 / 3 * a
+                     + 1.0 / 3 * (2 * d - c) * Rs[rs1])
+        pot[rs2] += ((gamma + (7.0 / 6.0 * gamma * beta1) * Rs2sqrt + (4.0 / 3.0 * gamma * beta2 * Rs[rs2]))
+                     / (1.0 + beta1 * Rs2sqrt + beta2 * Rs[rs2]) ** 2)
+        out["V"] = pot
+    return out
+
+
+# --------------------------------------------------------------------------
+# Hartree
+# --------------------------------------------------------------------------
+def hartree(rho, grid, calc=("E", "V")):
+    """Hartree (functional/hartree.py:24-45): v_H(G) = 4 pi rho(G)/G^2, G=0 -> 0."""
+    vh = ifft(fft(rho, grid) * grid.invgg * 4 * np.pi, grid)
+    out = {"V": vh}
+    if "E" in calc:
+        out["E"] = np.einsum("ijk,ijk->", vh, rho) * grid.dV / 2.0
+    return out
+
+
+_hartree_fn = hartree
+
+
+# --------------------------------------------------------------------------
+# Lindhard / Wang-Teter
+# --------------------------------------------------------------------------
+_LARGE = [-0.13714285714285712, -6.39999999999999875e-2, -3.77825602968460128e-2,
+          -2.51824061652633074e-2, -1.80879839616166146e-2, -1.36715733124818332e-2,
+          -1.07236045520990083e-2, -8.65192783339199453e-3, -7.1372762502456763e-3,
+          -5.9945117538835746e-3, -5.10997527675418131e-3, -4.41060829979912465e-3,
+          -3.84763737842981233e-3, -3.38745061493813488e-3, -3.00624946457977689e-3]
+
+
+def lindhard(eta, lbda, mu, tol=1e-10):
+    """Inverse Lindhard function, 4 branches (kedf/kernel.py:14-136).
+
+    Branch order matters where conditions overlap: normal, then zero, one,
+    large overwrite in that order (kernel.py:26-35)."""
+    eta = np.asarray(eta, dtype=np.float64)
+    tol2 = tol / 10
+    cond0 = (eta > tol2) & (np.abs(eta - 1.0) > tol2)
+    cond1 = eta < tol
+    cond2 = np.abs(eta - 1.0) < tol
+    cond3 = eta > 3.65
+    out = eta.copy()
+    e = eta[cond0]
+    out[cond0] = (1.0 / (0.5 + 0.25 * (1.0 - e ** 2) * np.log((1.0 + e) / np.abs(1.0 - e)) / e)
+                  - 3.0 * mu * e ** 2 - lbda)
+    e = eta[cond1]
+    out[cond1] = 1.0 - lbda + e ** 2 * (1.0 / 3.0 - 3.0 * mu)
+    e = eta[cond2]
+    out[cond2] = 2.0 - lbda - 3.0 * mu + 20.0 * (e - 1.0)
+    e = eta[cond3]
+    inv2 = 1.0 / e ** 2
+    acc = _LARGE[-1] * inv2
+    for coef in _LARGE[-2::-1]:
+        acc = inv2 * (coef + acc)
+    out[cond3] = 3.0 * (1.0 - mu) * e ** 2 - lbda - 0.6 + acc
+    return out
+
+
+def wt_kernel(grid, rho0, x=1.0, alpha=5.0 / 6.0, beta=5.0 / 6.0):
+    """WTKernel (kernel.py:325-334): F(q/2kF0; x, 1) * 5/(9 a b rho0^(a+b-5/3)) * C_TF."""
+    tkf = 2.0 * (3.0 * rho0 * np.pi ** 2) ** (1.0 / 3.0)
+    cTF = 0.3 * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+    factor = 5.0 / (9.0 * alpha * beta * rho0 ** (alpha + beta - 5.0 / 3.0)) * cTF
+    return lindhard(grid.q / tkf, x, 1.0) * factor
+
+
+class WT:
+    """Wang-Teter nonlocal term (kedf/wt.py:109-132) with the kernel cache of
+    wt.py:58-73 (rebuilt when rho0 moves by more than 1e-6 or the shape changes)."""
+
+    def __init__(self, x=1.0, alpha=5.0 / 6.0, beta=5.0 / 6.0, rho0=None):
+        self.x, self.alpha, self.beta, self.rho0 = x, alpha, beta, rho0
+        self._saved_rho0 = 0.0
+        self._shape = None
+        self._kernel = None
+
+    def kernel(self, rho, grid):
+        rho0 = self.rho0 if self.rho0 is not None else rho.mean()
+        if abs(self._saved_rho0 - rho0) > 1e-6 or rho.shape != self._shape:
+            self._kernel = wt_kernel(grid, rho0, self.x, self.alpha, self.beta)
+            self._saved_rho0, self._shape = rho0, rho.shape
+        return self._kernel
+
+    def __call__(self, rho, grid, calc=("E", "V")):
+        K = self.kernel(rho, grid)
+        a, b = self.alpha, self.beta
+        rhoc = rho.copy()
+        rhoc[rho < ZERO] = ZERO                     # wt.py:15-18 (clamp, restored after)
+        out = {}
+        if abs(b - a) < 1e-9:
+            rb = rhoc ** b
+            pot = 2.0 * a * (rb / rhoc) * ifft(fft(rb, grid) * K, grid)   # wt.py:19-23
+            if "V" in calc:
+                out["V"] = pot
+            if "E" in calc:
+                if "V" in calc:
+                    ed = pot * rho / (2 * a)                              # wt.py:124-125
+                else:
+                    ed = ifft(fft(rb, grid) * K, grid) * rb               # wt.py:44-56
+                out["E"] = ed.sum() * grid.dV
+        else:
+            ra, rb = rhoc ** a, rhoc ** b
+            if "V" in calc:
+                pot = a * rhoc ** (a - 1.0) * ifft(fft(rb, grid) * K, grid)
+                pot += b * rhoc ** (b - 1.0) * ifft(fft(ra, grid) * K, grid)
+                out["V"] = pot
+            if "E" in calc:
+                out["E"] = (ifft(fft(rb, grid) * K, grid) * ra).sum() * grid.dV
+        return out
+
+
+# --------------------------------------------------------------------------
+# density-dependent kernel (LWT family; the "WGC table" workload)
+# --------------------------------------------------------------------------
+def wt_kernel_table(eta, x=1.0):
+    """WTKernelTable (kernel.py:344-352): F(eta; x, 1) * (4/5) C_TF, alpha/beta ignored."""
+    factor = 4.0 / 5.0 * 0.3 * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+    return lindhard(eta, x, 1.0) * factor
+
+
+def kernel_kf(q, kf, tck, etamax):
+    """LWTKernelKf (kernel.py:379-405) for a spline table: splev(q/kf) below etamax,
+    the value at etamax above it, element [0,0,0] zeroed when q there is 0."""
+    eta = q / kf
+    K = np.empty_like(q)
+    c0 = eta < etamax
+    limit = splev(etamax, tck)
+    if c0.any():
+        K[c0] = splev(eta[c0], tck)
+    K[~c0] = limit
+    if q[0, 0, 0] < ZERO:
+        K[0, 0, 0] = 0.0
+    return K
+
+
+def guess_kf_bound(kf_l, kf_r, saved, kfmin=None, kfmax=None, kftol=1e-3):
+    """kedf/lwt.py:36-79 (with the persistent kfmin/kfmax state in ``saved``)."""
+    kfmin_prev = saved.get("kfmin")
+    kfmax_prev = saved.get("kfmax")
+    if kfmin is not None and kfmax is not None:
+        return [kfmin, kfmax]
+    if kfmin_prev is None:
+        kfmin_prev = 10
+        if kfmin is None:
+            kfmin = kf_l
+    if kfmax_prev is None:
+        kfmax_prev = 1.0
+        if kfmax is None:
+            kfmax = kf_r
+    if kfmin is None or kfmin > kfmin_prev:
+        kfmin = kfmin_prev
+    if kfmax is None or kfmax < kfmax_prev:
+        kfmax = kfmax_prev
+    if kfmin > kf_l:
+        kfl = [1e-5, 1e-4, 5e-3, 1e-3, 5e-3, 1e-2, 5e-2, 0.1, 0.5, 1.0]
+        ratio = kf_l / kfmin
+        for i in range(len(kfl) - 1, 0, -1):
+            if ratio > kfl[i]:
+                kfmin *= kfl[i]
+                break
+    if kfmin < kftol:
+        kfmin = kftol
+    if kfmax < kf_r:
+        dk = kf_r - kfmax
+        kfmax += (np.round(dk / 0.5) + 1) * 0.5
+    saved["kfmin"] = kfmin
+    saved["kfmax"] = kfmax
+    return [kfmin, kfmax]
+
+
+def node_list(kfMin, kfMax, nsp=None, delta=None, ratio=1.15):
+    """Reference k_F nodes (lwt.py:174-190)."""
+    if nsp is not None:
+        if kfMax - kfMin < 1e-3:
+            kfl = np.asarray([kfMin, kfMax], dtype=np.float64)
+        else:
+            kfl = kfMin + (kfMax - kfMin) / (nsp - 1) * np.arange(nsp)
+    elif delta is not None:
+        n = int(np.ceil((kfMax - kfMin) / delta)) + 1
+        kfl = np.linspace(kfMin, kfMax, n)
+    else:
+        n = int(np.ceil(np.log(kfMax / kfMin) / np.log(ratio))) + 1
+        kfl = kfMin * ratio ** np.arange(n)
+    kfl = np.array(kfl, dtype=np.float64)
+    kfl[0] -= 1e-16
+    kfl[-1] += 1e-16
+    return kfl
+
+
+class LWT:
+    """Density-dependent nonlocal kernel by k_F-node interpolation
+    (kedf/lwt.py:502-568 table build, :82-341 potential and energy).
+
+    The interval loop, the node arithmetic and the membership tests follow the
+    reference exactly (including its quirks: points exactly at the first/last
+    node belong to no interval; the first node has a 'small-k_F' branch).
+    ``interp`` is 'linear' or 'hermite'.  MGP lump factors are not supported.
+    """
+
+    def __init__(self, x=1.0, alpha=5.0 / 6.0, beta=5.0 / 6.0, etamax=50.0, neta=50000,
+                 order=3, interp="linear", kdd=3, ratio=1.15, nsp=None, delta=None,
+                 kfmin=None, kfmax=None, ldw=None):
+        self.x, self.alpha, self.beta = x, alpha, beta
+        self.etamax, self.neta, self.order = etamax, neta, order
+        self.interp, self.kdd, self.ratio, self.nsp, self.delta = interp, kdd, ratio, nsp, delta
+        self.kfmin, self.kfmax, self.ldw = kfmin, kfmax, ldw
+        self.saved = {"kfmin": None, "kfmax": None, "shape": None}
+        self.tables()
+
+    def tables(self):
+        """lwt.py:535-566 (kerneltype 'WT', order 3)."""
+        eta = np.linspace(0, self.etamax, self.neta)
+        table = wt_kernel_table(eta, self.x)
+        self.tck = splrep(eta, table, k=self.order)
+        deriv = splev(eta, self.tck, der=1) * (-1.0 * eta)
+        self.tckD = splrep(eta, deriv, k=self.order)
+
+    def __call__(self, rho, grid, calc=("E", "V")):
+        """LWTPotentialEnergy (lwt.py:82-341), streamed interval by interval like the
+        reference so that memory stays O(grid)."""
+        alpha, beta = self.alpha, self.beta
+        q = grid.q
+        kf = 2.0 * np.cbrt(3.0 * np.pi ** 2 * rho)                     # lwt.py:106
+        out = {}
+        if abs(kf.max() - kf.min()) < 1e-8:                           # lwt.py:115-124 (HEG)
+            if "E" in calc:
+                out["E"] = 0.0
+            if "V" in calc:
+                out["V"] = np.zeros_like(rho)
+            return out
+        kfb = guess_kf_bound(kf.min(), kf.max(), self.saved, self.kfmin, self.kfmax)
+        vcalc = "V" in calc
+        kdd = self.kdd if vcalc else 1
+        if (kf > kfb[1]).any():                                       # lwt.py:145-146
+            kf = np.minimum(kf, kfb[1])
+        kfMin = max(kf.min(), kfb[0]) if self.kfmin is None else self.kfmin
+        kfMax = kf.max() if self.kfmax is None else self.kfmax
+        kfl = node_list(kfMin, kfMax, self.nsp, self.delta, self.ratio)
+        nsp = len(kfl)
+        rhoc = rho.copy()                                             # lwt.py:206-221
+        rhoc[~(rho > 0)] = 1e-30
+        rA = rhoc ** alpha
+        rA1 = rA / rhoc
+        if abs(alpha - beta) < 1e-8:
+            rB, rB1 = rA, rA1
+        else:
+            rB = rhoc ** beta
+            rB1 = rB / rhoc
+        rBG = fft(rB, grid)
+        hermite = self.interp == "hermite"
+        mcalc = kdd > 1 or hermite
+        pot1 = np.zeros_like(rho)
+        pot3 = np.zeros_like(rho)
+        pot2G = None
+
+        def node(j):
+            K = kernel_kf(q, kfl[j], self.tck, self.etamax)
+            p = ifft(K * rBG, grid)
+            if mcalc:
+                KD = kernel_kf(q, kfl[j], self.tckD, self.etamax) / kfl[j]
+                return K, p, KD, ifft(KD * rBG, grid)
+            return K, p, None, None
+
+        K0, p0, KD0, m0 = node(0)
+        small = kf < kfl[0] + 1e-18                                   # lwt.py:254-266
+        t = (kf - kfl[0]) / kfl[0]
+        pot1[small] = p0[small] * t[small]
+        if kdd > 1:
+            pot2G = K0 * fft(rA * np.where(small, t, 0.0), grid)
+        for i in range(nsp - 1):                                      # lwt.py:213-306
+            K1, p1, KD1, m1 = node(i + 1)
+            m = np.logical_and(kf > kfl[i], kf < kfl[i + 1] + 1e-18)
+            u = np.where(m, rA, 0.0)
+            Dkf = kfl[i + 1] - kfl[i]
+            t = (kf - kfl[i]) / Dkf
+            if not hermite:
+                t0 = 1 - t
+                pot1[m] = p0[m] * t0[m] + p1[m] * t[m]
+                if kdd > 1:
+                    pot2G = pot2G + K0 * fft(u * t0, grid) + K1 * fft(u * t, grid)
+                    if kdd == 3:
+                        pot3[m] = m0[m] * t0[m] + m1[m] * t[m]
+            else:
+                t2 = t * t
+                t3 = t2 * t
+                h00 = 2.0 * t3 - 3.0 * t2 + 1.0
+                h10 = t3 - 2.0 * t2 + t
+                h01 = 1.0 - h00
+                h11 = t3 - t2
+                pot1[m] = h00[m] * p0[m] + h01[m] * p1[m] + Dkf * (h10[m] * m0[m] + h11[m] * m1[m])
+                if kdd > 1:
+                    pot2G = pot2G + (K0 * fft(u * h00, grid) + K1 * fft(u * h01, grid)
+                                     + Dkf * (KD0 * fft(u * h10, grid) + KD1 * fft(u * h11, grid)))
+                    if kdd == 3:
+                        tm, t2m = t[m], t2[m]
+                        h00D = 6.0 * t2m - 6 * tm
+                        h10D = 3.0 * t2m - 4 * tm + 1.0
+                        h01D = -h00D
+                        h11D = 3.0 * t2m - 2 * tm
+                        pot3[m] = (h00D * p0[m] + h01D * p1[m]) / Dkf + h10D * m0[m] + h11D * m1[m]
+            K0, p0, KD0, m0 = K1, p1, KD1, m1
+        if vcalc:
+            pot2 = ifft(pot2G, grid) if pot2G is not None else pot1.copy()
+        ldw = 1.0 / 6.0 if self.ldw is None else self.ldw            # lwt.py:315-322
+        factor = np.ones_like(rho)
+        rhov = rho.max()
+        lm = rho < 1e-6
+        ld = max(0.1, ldw)
+        factor[lm] = np.abs(rho[lm]) ** ld / (rhov ** ld)
+        factor[rho < 0] = 0.0
+        pot1 = pot1 * factor
+        if "E" in calc:
+            out["E"] = (rA * pot1).sum() * grid.dV                    # lwt.py:326-327
+        if vcalc:
+            pot2 = pot2 * factor
+            pot3 = pot3 * factor
+            out["V"] = alpha * rA1 * pot1 + beta * rB1 * pot2 + (kf / 3.0) * rA1 * pot3
+        return out
+
+
+
+# --------------------------------------------------------------------------
+# pseudopotential: recpot I/O, radial lines, PME structure factor
+# --------------------------------------------------------------------------
+def write_recpot(fname, gmax_bohr_inv, v_ha_bohr3, header="synthetic"):
+    """CASTEP .recpot writer (format of functional/pseudo/recpot.py:11-42): eV*A^3 on a
+    uniform G grid from 0 to gmax (A^-1), three values per line, terminator '1000'."""
+    v = np.asarray(v_ha_bohr3) * HARTREE * BOHR ** 3
+    gmax = gmax_bohr_inv / BOHR
+    lines = ["START COMMENT", header, "END COMMENT", "3     5", repr(float(gmax))]
+    for i in range(0, len(v), 3):
+        lines.append("  ".join("%.17e" % x for x in v[i:i + 3]))
+    lines.append("1000")
+    with open(fname, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def read_recpot(fname):
+    """recpot.py:11-42: returns (gp [Bohr^-1], vp [Ha Bohr^3], zval)."""
+    with open(fname) as f:
+        lines = f.readlines()
+    ibegin = 0
+    iend = None
+    for i, line in enumerate(lines):
+        if "END COMMENT" in line:
+            ibegin = i + 3
+        elif ibegin > 1 and (line.strip() == "1000" or len(line.strip()) == 1):
+            iend = i
+            break
+    vals = " ".join(l.strip() for l in lines[ibegin:iend]).split()
+    gmax = float(lines[ibegin - 1].strip()) * BOHR
+    v = np.array(vals, dtype=np.float64) / HARTREE / BOHR ** 3
+    r = np.linspace(0, gmax, num=len(v))
+    zval = round((v[0] - v[1]) * (r[1] ** 2) / (4.0 * np.pi))
+    return r, v, zval
+
+
+def synthetic_pp(Z, rc, A=15.0, npts=4096, gmax=40.0):
+    """v(G) = -4 pi Z/G^2 exp(-G^2 rc^2/4) + A exp(-G^2 rc^2/4), G=0 limit A + pi Z rc^2."""
+    g = np.linspace(0.0, gmax, npts)
+    v = np.empty_like(g)
+    e = np.exp(-g[1:] ** 2 * rc ** 2 / 4.0)
+    v[1:] = -4.0 * np.pi * Z / g[1:] ** 2 * e + A * e
+    v[0] = A + np.pi * Z * rc ** 2
+    return g, v
+
+
+def quartic(f, dx):
+    """math_utils.quartic_interpolation (math_utils.py:390-400)."""
+    t0 = f[2]
+    t1 = 2.0 * f[0] - 16.0 * f[1] + 16.0 * f[3] - 2.0 * f[4]
+    t2 = -f[0] + 16.0 * f[1] - 30.0 * f[2] + 16.0 * f[3] - f[4]
+    t3 = -2.0 * f[0] + 4.0 * f[1] - 4.0 * f[3] + 2.0 * f[4]
+    t4 = f[0] - 4.0 * f[1] + 6.0 * f[2] - 4.0 * f[3] + f[4]
+    return t0 + dx * (t1 + dx * (t2 + dx * (t3 + dx * t4))) / 24.0
+
+
+def vline(grid, gp, vp):
+    """LocalPseudo.calc_vlines (pseudo/__init__.py:398-423) with the spline of
+    ReadPseudo.get_vloc_interp (:689-706): splrep(gp[1:], vp[1:], k=3)."""
+    tck = splrep(gp[1:], vp[1:], k=3)
+    q = grid.q
+    out = np.zeros_like(q)
+    m = q < gp[-1]
+    if m.any():
+        out[m] = splev(q[m], tck, der=0)
+    m = q < gp[1]
+    dp = gp[1] - gp[0]
+    out[m] = quartic([vp[2], vp[1], vp[0], vp[1], vp[2]], q[m] / dp)
+    return out
+
+
+def bspline_Mn(x, order):
+    """CBspline.calc_Mn (ewald.py:63-82): Mn[n] = M_order(x + n - 1), n = 1..order."""
+    Mn = np.zeros(order + 1)
+    Mn[1] = x
+    Mn[2] = 1.0 - x
+    for i in range(3, order + 1):
+        for j in range(0, i):
+            n = i - j
+            Mn[n] = (x + n - 1) * Mn[n] + (j + 1 - x) * Mn[n - 1]
+            Mn[n] /= i - 1
+    return Mn
+
+
+def bspline_Mn_full(x, order_full, order):
+    """calc_Mn(x, order) of an object built for ``order_full`` (array length order_full+1)."""
+    Mn = np.zeros(order_full + 1)
+    Mn[1] = x
+    Mn[2] = 1.0 - x
+    for i in range(3, order + 1):
+        for j in range(0, i):
+            n = i - j
+            Mn[n] = (x + n - 1) * Mn[n] + (j + 1 - x) * Mn[n - 1]
+            Mn[n] /= i - 1
+    return Mn
+
+
+def bspline_barray(grid, order=10):
+    """CBspline._calc_bm + Barray (ewald.py:44-55, :84-101)."""
+    Mn = bspline_Mn(1.0, order)
+    bm = []
+    for d in range(3):
+        qd = 2.0 * np.pi * np.arange(grid.nrG[d]) / grid.nr[d]
+        tmp = np.exp(-1j * (order - 1.0) * qd)
+        fac = np.zeros_like(tmp)
+        for k in range(1, order):
+            fac += Mn[k] * np.exp(-1j * k * qd)
+        bm.append(tmp / fac)
+    return np.einsum("i,j,k->ijk", bm[0], bm[1], bm[2])
+
+
+def scaled_positions(pos, lattice):
+    """ase get_scaled_positions(wrap=True): fractional coordinates wrapped to [0,1)."""
+    fr = np.linalg.solve(np.asarray(lattice).T, np.asarray(pos, dtype=np.float64).T).T
+    fr = fr % 1.0
+    fr[fr == 1.0] = 0.0
+    return fr
+
+
+def pme_qarray(grid, frac, weights, order=10):
+    """CBspline.get_PME_Qarray / _calc_PME_Qarray (ewald.py:137-194): spread each atom's
+    order^3 B-spline stencil (indices mod n) with weight ``weights[a]``."""
+    Q = np.zeros(tuple(grid.nr))
+    ix = np.arange(order)
+    for a in range(len(frac)):
+        Up = frac[a] * grid.nr
+        fl = np.floor(Up).astype(np.int64)
+        Mn = [bspline_Mn(Up[d] - np.floor(Up[d]), order)[1:] for d in range(3)]
+        l = [np.mod(1 + fl[d] - ix, grid.nr[d]) for d in range(3)]
+        val = weights[a] * np.einsum("i,j,k->ijk", Mn[0], Mn[1], Mn[2])
+        # each stencil point is distinct for n >= order, so plain fancy += is exact
+        Q[np.ix_(l[0], l[1], l[2])] += val
+    return Q
+
+
+class LocalPseudo:
+    """LocalPseudo (pseudo/__init__.py:74-452, :505-571): v_loc on the grid by PME
+    (B-spline structure factor) or by the exact structure factor."""
+
+    def __init__(self, grid, pos, species, tables, PME=True, order=10):
+        """tables: list of (gp, vp) per species index; species: int array per atom."""
+        self.grid, self.PME, self.order = grid, PME, order
+        self.pos = np.asarray(pos, dtype=np.float64)
+        self.species = np.asarray(species)
+        self.tables = tables
+        self.vlines = [vline(grid, gp, vp) for gp, vp in tables]
+        self._vreal = None
+
+    @property
+    def vreal(self):
+        if self._vreal is None:
+            g = self.grid
+            v = np.zeros(tuple(g.nrG), dtype=np.complex128)
+            if self.PME:          # _PP_Reciprocal_PME (:437-452)
+                frac = scaled_positions(self.pos, g.lattice)
+                for s in range(len(self.tables)):
+                    sel = self.species == s
+                    Q = pme_qarray(g, frac[sel], np.ones(sel.sum()), self.order)
+                    v = v + self.vlines[s] * fft(Q, g)
+                v = v * bspline_barray(g, self.order) * g.nnr / g.volume
+            else:                 # _PP_Reciprocal (:425-435)
+                gv = g.g
+                for s in range(len(self.tables)):
+                    for a in np.nonzero(self.species == s)[0]:
+                        strf = np.exp(-1j * np.einsum("lijk,l->ijk", gv, self.pos[a]))
+                        v += self.vlines[s] * strf
+            self._vreal = ifft(v, g)
+        return self._vreal
+
+    def __call__(self, rho, calc=("E", "V")):
+        out = {"V": self.vreal}
+        if "E" in calc:
+            out["E"] = np.einsum("ijk,ijk->", self.vreal, rho) * self.grid.dV
+        return out
+
+    def forces(self, rho):
+        g = self.grid
+        rhoG = fft(rho, g)
+        nat = len(self.pos)
+        F = np.zeros((nat, 3))
+        if not self.PME:      # _Force (:505-521)
+            mask = g.mask
+            gv = g.g
+            for a in range(nat):
+                istrf = np.exp(1j * np.einsum("lijk,l->ijk", gv, self.pos[a]))
+                den = self.vlines[self.species[a]][mask] * (rhoG[mask] * istrf[mask]).imag
+                for j in range(3):
+                    F[a, j] = np.einsum("i,i->", gv[j][mask], den)
+            return F * 2.0 / g.volume
+        # _ForcePME (:523-571)
+        B = np.conjugate(bspline_barray(g, self.order))
+        denG = rhoG * B
+        cell_inv = g.rlattice.T / 2 / np.pi
+        frac = scaled_positions(self.pos, g.lattice)
+        o = self.order
+        ix = np.arange(o)
+        for s in range(len(self.tables)):
+            dGV = denG * self.vlines[s]
+            dGV[0, 0, 0] = 0.0
+            rhoPB = ifft(dGV, g)
+            for a in np.nonzero(self.species == s)[0]:
+                F[a] = -_pme_gather_grad(g, frac[a], o, cell_inv, rhoPB)
+        return F
+
+
+def _pme_gather_grad(grid, frac, o, cell_inv, field):
+    """sum over the B-spline stencil of (dQ/du . cell_inv) * field (ewald.py:846-862)."""
+    Up = frac * grid.nr
+    fl = np.floor(Up).astype(np.int64)
+    Mn = [bspline_Mn(Up[d] - np.floor(Up[d]), o) for d in range(3)]
+    M2 = [bspline_Mn_full(Up[d] - np.floor(Up[d]), o, o - 1) for d in range(3)]
+    dM = [M2[d][1:] - M2[d][:-1] for d in range(3)]
+    Mv = [Mn[d][1:] for d in range(3)]
+    dQ = np.empty((3, o, o, o))
+    dQ[0] = grid.nr[0] * np.einsum("i,j,k->ijk", dM[0], Mv[1], Mv[2])
+    dQ[1] = grid.nr[1] * np.einsum("i,j,k->ijk", Mv[0], dM[1], Mv[2])
+    dQ[2] = grid.nr[2] * np.einsum("i,j,k->ijk", Mv[0], Mv[1], dM[2])
+    ix = np.arange(o)
+    l = [np.mod(1 + fl[d] - ix, grid.nr[d]) for d in range(3)]
+    fv = field[np.ix_(l[0], l[1], l[2])]
+    return np.einsum("d,dk->k", np.einsum("dijk,ijk->d", dQ, fv), cell_inv)
+
+
+# --------------------------------------------------------------------------
+# Ewald
+# --------------------------------------------------------------------------
+def erfcinv(y):
+    return sp.erfcinv(y)
+
+
+class Ewald:
+    """Ewald ion-ion energy and forces (ewald.py:197-864).  The real-space sum is the
+    exact truncated image sum of Energy_real (:281-325); for orthorhombic cells the
+    reference's windowed Energy_real_fast2 (:372-446) visits the same pairs."""
+
+    def __init__(self, grid, pos, charges, precision=1e-8, PME=True, order=10):
+        self.grid = grid
+        self.pos = np.asarray(pos, dtype=np.float64)
+        self.q = np.asarray(charges, dtype=np.float64)
+        self.precision, self.PME, self.order = precision, PME, order
+        gmax = np.sqrt(2.0 * grid.guess_ecut())
+        self.eta = self.best_eta(precision, gmax)
+
+    def best_eta(self, precision, gmax):
+        """Get_Best_eta (ewald.py:256-278)."""
+        q2 = np.sum(self.q * self.q)
+        nat = len(self.q)
+        eta = 1.6
+        while True:
+            up = 4.0 * np.pi * nat * q2 * np.sqrt(eta / np.pi) * sp.erfc(gmax / 2.0 * np.sqrt(1.0 / eta))
+            if up < precision:
+                return eta
+            eta = eta - 0.01
+
+    def _images(self):
+        L = np.sqrt(np.einsum("ij->i", self.grid.lattice ** 2))
+        rmax = erfcinv(self.precision / 3.0) / np.sqrt(self.eta)
+        N = np.ceil(rmax / L).astype(np.int64)
+        shifts = np.array([[ix, iy, iz] for ix in range(-N[0], N[0] + 1)
+                           for iy in range(-N[1], N[1] + 1) for iz in range(-N[2], N[2] + 1)],
+                          dtype=np.float64)
+        return shifts @ self.grid.lattice, rmax
+
+    def energy_real(self):
+        R, Rcut = self._images()
+        es = np.sqrt(self.eta)
+        E = 0.0
+        for i in range(len(self.pos)):
+            d = self.pos[None, :, :] - R[:, None, :] - self.pos[i][None, None, :]
+            d = np.sqrt((d * d).sum(-1))
+            qq = np.broadcast_to(self.q[None, :], d.shape)
+            m = (d < Rcut) & (d > 0.001)
+            E += self.q[i] * np.sum(qq[m] * sp.erfc(es * d[m]) / d[m])
+        return E / 2.0
+
+    def energy_corr(self):
+        """Energy_corr (ewald.py:468-482)."""
+        dc = -np.sqrt(self.eta / np.pi) * np.sum(self.q * self.q)
+        gz = -4.0 * np.pi * (1.0 / (4.0 * self.eta * self.grid.volume) / 2.0) * np.sum(self.q) ** 2
+        return dc + gz
+
+    def _qgrid(self):
+        frac = scaled_positions(self.pos, self.grid.lattice)
+        return pme_qarray(self.grid, frac, self.q, self.order), frac
+
+    def energy_rec(self):
+        g = self.grid
+        if self.PME:      # Energy_rec_PME (:786-807)
+            Q, _ = self._qgrid()
+            strf = fft(Q, g) * bspline_barray(g, self.order)
+            s2 = (np.conjugate(strf) * strf)
+            m = g.mask
+            e = np.sum(s2[m] * np.exp(-g.gg[m] / (4.0 * self.eta)) * g.invgg[m])
+            return 4.0 * np.pi * e.real / g.volume / g.dV ** 2
+        # Energy_rec (:449-466)
+        strf = np.zeros(tuple(g.nrG), dtype=np.complex128)
+        for a in range(len(self.pos)):
+            strf += np.exp(-1j * np.einsum("lijk,l->ijk", g.g, self.pos[a])) * self.q[a]
+        s2 = np.conjugate(strf) * strf
+        m = g.mask
+        e = np.sum(s2[m] * np.exp(-g.gg[m] / (4.0 * self.eta)) * g.invgg[m])
+        return 4.0 * np.pi * e.real / g.volume
+
+    def energy(self):
+        return self.energy_corr() + self.energy_real() + self.energy_rec()
+
+    def forces_real(self):
+        """Forces_real (ewald.py:541-577)."""
+        R, Rcut = self._images()
+        es = np.sqrt(self.eta)
+        F = np.zeros((len(self.pos), 3))
+        for i in range(len(self.pos)):
+            rj = (self.pos[None, :, :] - R[:, None, :]).reshape(-1, 3)
+            qj = np.broadcast_to(self.q[None, :], (len(R), len(self.q))).ravel()
+            dv = self.pos[i][None, :] - rj
+            d = np.sqrt((dv * dv).sum(-1))
+            m = (d < Rcut) & (d > 0.001)
+            x = d[m] * es
+            w = sp.erfc(x) / x ** 3 + 2.0 / np.sqrt(np.pi) * np.exp(-x ** 2) / x ** 2
+            F[i] = self.q[i] * np.einsum("ij,i->j", dv[m] * qj[m][:, None], w)
+        return F * es ** 3
+
+    def forces_rec(self):
+        g = self.grid
+        if self.PME:      # Forces_rec_PME (:810-864)
+            Q, frac = self._qgrid()
+            B = bspline_barray(g, self.order)
+            strf = fft(Q, g) * (B * np.conjugate(B))
+            strf *= np.exp(-g.gg / (4.0 * self.eta)) * g.invgg
+            conv = ifft(strf, g)
+            cell_inv = np.linalg.inv(g.lattice)
+            F = np.zeros((len(self.pos), 3))
+            for a in range(len(self.pos)):
+                F[a] = -_pme_gather_grad(g, frac[a], self.order, cell_inv, conv) * self.q[a]
+            return F * 4.0 * np.pi / g.dV
+        # Forces_rec (:580-607)
+        strf = np.zeros(tuple(g.nrG), dtype=np.complex128)
+        for a in range(len(self.pos)):
+            strf += np.exp(-1j * np.einsum("lijk,l->ijk", g.g, self.pos[a])) * self.q[a]
+        m = g.mask
+        F = np.empty((len(self.pos), 3))
+        w = np.exp(-g.gg[m] / (4.0 * self.eta)) * g.invgg[m]
+        for a in range(len(self.pos)):
+            s = np.exp(-1j * np.einsum("lijk,l->ijk", g.g, self.pos[a]))[m] * self.q[a]
+            F[a] = np.einsum("ij,j->i", g.g[:, m], (s.real * strf.imag[m] - s.imag * strf.real[m]) * w)
+        return F * 8.0 * np.pi / g.volume
+
+    def forces(self):
+        return self.forces_real() + self.forces_rec()
+
+
+# --------------------------------------------------------------------------
+# total functional
+# --------------------------------------------------------------------------
+class Total:
+    """TotalFunctional.get_energy_potential (total_functional.py:115-146): sum of terms
+    plus the Ewald energy.  ``terms`` are callables (rho, calc) -> {'E','V'}."""
+
+    def __init__(self, grid, terms, ewald_energy=None):
+        self.grid, self.terms, self.ewald_energy = grid, terms, ewald_energy
+
+    def __call__(self, rho, calc=("E", "V")):
+        E = 0.0
+        V = np.zeros_like(rho) if "V" in calc else None
+        parts = {}
+        for name, fn in self.terms:
+            o = fn(rho, calc)
+            if "E" in calc:
+                parts[name] = o["E"]
+                E += o["E"]
+            if "V" in calc:
+                V += o["V"]
+        if self.ewald_energy is not None and "E" in calc:
+            parts["II"] = self.ewald_energy
+            E += self.ewald_energy
+        return {"E": E, "V": V, "parts": parts}
+
+
+def make_terms(grid, kedf="TFVW", xc=True, hartree=True, pseudo=None, **kw):
+    """KEDF name dispatch (kedf/__init__.py:27-69) for TF, VW, TFVW, WT, LWT."""
+    terms = []
+    names = {"TF": ("TF",), "VW": ("VW",), "TFVW": ("TF", "VW"), "WT": ("TF", "VW", "WT-NL"),
+             "LWT": ("TF", "VW", "LWT-NL")}[kedf.upper()]
+    for n in names:
+        if n == "TF":
+            terms.append(("TF", lambda r, c: tf(r, grid, kw.get("x", 1.0), c)))
+        elif n == "VW":
+            terms.append(("VW", lambda r, c: vw(r, grid, kw.get("y", 1.0), c)))
+        elif n == "WT-NL":
+            wt = WT(x=kw.get("x", 1.0), alpha=kw.get("alpha", 5.0 / 6.0), beta=kw.get("beta", 5.0 / 6.0),
+                    rho0=kw.get("rho0"))
+            terms.append(("NL", lambda r, c, wt=wt: wt(r, grid, c)))
+        elif n == "LWT-NL":
+            lw = LWT(**{k: v for k, v in kw.items() if k in (
+                "x", "alpha", "beta", "etamax", "neta", "interp", "kdd", "ratio", "nsp", "delta", "kfmin", "kfmax", "ldw")})
+            terms.append(("NL", lambda r, c, lw=lw: lw(r, grid, c)))
+    if xc:
+        terms.append(("XC", lambda r, c: lda(r, grid, c)))
+    if hartree:
+        terms.append(("H", lambda r, c: _hartree_fn(r, grid, c)))
+    if pseudo is not None:
+        terms.append(("PP", lambda r, c: pseudo(r, c)))
+    return terms
+
+
+# --------------------------------------------------------------------------
+# density optimisation
+# --------------------------------------------------------------------------
+def optimize(evaluator, rho0, grid, method="TN", maxiter=100, maxfun=50, maxls=30, econv=1e-5,
+             c1=1e-4, c2=0.2, xtol=1e-12, ncheck=2, maxcor=6, h0=1.0, trace=None):
+    """Optimization.optimize_rho (optimization/optimization.py:283-525) for one spin,
+    algorithm EMM, vector 'Orthogonalization', line search = scipy line_search_wolfe1
+    started at theta=1 (math_utils.py:37-52: alpha0 is not forwarded).
+    ``evaluator(rho, calc)`` returns {'E','V'}.  Returns (rho, info)."""
+    from scipy.optimize._linesearch import line_search_wolfe1
+    dV = grid.dV
+    mask = rho0 > 0
+    phi = np.where(mask, np.sqrt(np.where(mask, rho0, 0.0)), 1e-300)
+    phi *= np.sqrt(rho0.sum() / (phi * phi).sum())
+    rho = phi * phi
+    f = evaluator(rho, ("E", "V"))
+    N = rho.sum() * dV
+    mu = (f["V"] * rho).sum() * dV / N
+    res = (f["V"] - mu) * phi
+    resA, dirA = [res], []
+    Ehist = [f["E"]]
+    lb = {"s": [], "y": [], "rho": []}
+    converged = 2
+    nfev = 1
+    for it in range(1, maxiter):
+        if method == "TN":
+            p, nd = _tn_direction(evaluator, resA[-1], phi, mu, maxfun)
+            nfev += nd
+        elif method == "LBFGS":
+            p = _lbfgs_direction(resA, lb, h0)
+        else:
+            p = _cg_direction(resA, dirA, method)
+        p, theta0 = _orth_norm(p, phi, dV)
+        if (f["V"] * phi * p).sum() * 2.0 > 0:                   # :373-380 uphill -> steepest descent
+            p, theta0 = _orth_norm(-resA[-1], phi, dV)
+
+        cache = {}
+
+        def vd(theta):
+            key = float(theta)
+            if key not in cache:
+                nphi = phi * np.cos(theta) + p * np.sin(theta)
+                fr = evaluator(nphi * nphi, ("E", "V"))
+                p2 = p * np.cos(theta) - phi * np.sin(theta)
+                grad = 2.0 * (fr["V"] * nphi * p2).sum() * dV
+                cache.clear()
+                cache[key] = (fr["E"], grad, nphi, fr)
+            return cache[key]
+
+        v0 = (f["E"], 2.0 * (f["V"] * phi * p).sum() * dV, phi, f)
+        cache[0.0] = v0
+        cnt = [0]
+
+        def fn(x):
+            cnt[0] += 1
+            return vd(x)[0]
+
+        def fp(x):
+            return vd(x)[1]
+
+        ls = line_search_wolfe1(fn, fp, 0.0, 1.0, gfk=v0[1], old_fval=v0[0], c1=c1, c2=c2,
+                                amax=np.pi, amin=0.0, xtol=xtol)
+        nfev += cnt[0]
+        theta = ls[0]
+        if theta is None:
+            converged = 1
+            break
+        _, _, nphi, fnew = vd(theta)
+        old_phi, phi = phi, nphi
+        rho = phi * phi
+        f = fnew
+        N = rho.sum() * dV
+        mu = (f["V"] * rho).sum() * dV / N
+        res = (f["V"] - mu) * phi
+        resA.append(res)
+        if method == "LBFGS":
+            _lbfgs_update(lb, phi - old_phi, resA[-1] - resA[-2], maxcor)
+        Ehist.append(f["E"])
+        resN = (res * res).sum() * dV
+        if trace is not None:
+            trace.append((it, f["E"], resN))
+        if _check_conv(Ehist, econv, ncheck):
+            converged = 0
+            break
+        dirA.append(p)
+        if len(resA) > 2:
+            resA.pop(0)
+        if len(dirA) > 2:
+            dirA.pop(0)
+    return rho, {"converged": converged, "mu": mu, "energy": f["E"], "niter": it, "nfev": nfev,
+                 "dP": float((res * res).sum() * dV)}
+
+
+def _check_conv(E, econv, ncheck):
+    """check_converge (optimization.py:527-540)."""
+    if len(E) - 1 < ncheck:
+        return False
+    for i in range(ncheck):
+        if abs(E[-2 - i] - E[-1]) > econv:
+            return False
+    return True
+
+
+def _orth_norm(p, phi, dV):
+    """OrthogonalNormalization (optimization.py:205-226)."""
+    Ne = (phi * phi).sum() * dV
+    p = p - ((p * phi).sum() * dV / Ne) * phi
+    pN = (p * p).sum() * dV
+    theta = np.sqrt(pN / Ne)
+    return p * np.sqrt(Ne / pN), theta
+
+
+def _tn_direction(evaluator, res0, phi, mu, maxfun):
+    """get_direction_TN (optimization.py:92-148): CG on finite-difference Hessian products."""
+    eps = 1.0e-9
+    d = np.zeros_like(res0)
+    r = -res0.copy()
+    p = r.copy()
+    r0 = (r * r).sum()
+    rconv = r0 * 0.1
+    best = d
+    rl = [1e10]
+    it = 0
+    for it in range(maxfun):
+        phi1 = phi + eps * p
+        fv = evaluator(phi1 * phi1, ("V",))
+        Ap = ((fv["V"] - mu) * phi1 - res0) / eps
+        pAp = (p * Ap).sum()
+        if pAp < 0.0:
+            if it == 0:
+                d = r0 / pAp * p
+            break
+        a = r0 / pAp
+        d = d + a * p
+        r = r - a * Ap
+        r1 = (r * r).sum()
+        if r1 < min(rl):
+            best = d.copy()
+        rl.append(r1)
+        if r1 < rconv:
+            break
+        elif r1 > 1000 * min(rl[:-1]):
+            d = best
+            break
+        elif it > 10 and abs(r0 - r1) < 0.1 * r0:
+            d = best
+            break
+        beta = r1 / r0
+        r0 = r1
+        p = r + beta * p
+    return d, it + 1
+
+
+def _lbfgs_update(lb, dx, dg, bound):
+    """LBFGS.update (math_utils.py:307-325): keeps at most bound+1 pairs."""
+    if len(lb["s"]) > bound:
+        lb["s"].pop(0)
+        lb["y"].pop(0)
+        lb["rho"].pop(0)
+    lb["s"].append(dx)
+    lb["y"].append(dg)
+    lb["rho"].append(1.0 / (dg * dx).sum())
+
+
+def _lbfgs_direction(resA, lb, h0):
+    """Optimization.get_direction_LBFGS (optimization.py:150-171); first loop skips i=0."""
+    q = -resA[-1]
+    al = np.zeros(len(lb["s"]))
+    for i in range(len(lb["s"]) - 1, 0, -1):
+        a = lb["rho"][i] * (lb["s"][i] * q).sum()
+        al[i] = a
+        q = q - a * lb["y"][i]
+    if not h0:
+        gamma = 1.0 if len(lb["s"]) < 1 else (lb["s"][-1] * lb["y"][-1]).sum() / (lb["y"][-1] * lb["y"][-1]).sum()
+        d = gamma * q
+    else:
+        d = h0 * q
+    for i in range(len(lb["s"])):
+        b = lb["rho"][i] * (lb["y"][i] * d).sum()
+        d = d + lb["s"][i] * (al[i] - b)
+    return d
+
+
+def _cg_direction(resA, dirA, method="CG-HS"):
+    """get_direction_CG (math_utils.py:328-361)."""
+    if len(resA) == 1:
+        beta = 0.0
+    elif method in ("CG-HS", "CG") and len(dirA) > 0:
+        dr = resA[-1] - resA[-2]
+        beta = (resA[-1] * dr).sum() / (dirA[-1] * dr).sum()
+    elif method == "CG-PR":
+        beta = max((resA[-1] * (resA[-1] - resA[-2])).sum() / (resA[-2] ** 2).sum(), 0.0)
+    elif method == "CG-DY" and len(dirA) > 0:
+        beta = (resA[-1] ** 2).sum() / (dirA[-1] * (resA[-1] - resA[-2])).sum()
+    else:
+        beta = (resA[-1] ** 2).sum() / (resA[-2] ** 2).sum()
+    if not dirA:
+        return -resA[-1]
+    return -resA[-1] + beta * dirA[-1]

@@ -1,0 +1,371 @@
+"""Benchmark: E+V evaluations/s of the 256^3 density-dependent-kernel workload.
+
+Workload (one "step" = one TotalFunctional E+V evaluation): fcc Al 8x8x8
+supercell (2048 atoms, a = 7.60 Bohr, seeded Gaussian displacements sigma =
+0.15 Bohr), 256^3 grid, KEDF = TF + vW + k_F-node nonlocal kernel with 64
+nodes (alpha = (5+sqrt 5)/6, beta = (5-sqrt 5)/6, kdd = 3, linear
+interpolation, 50000-point table to eta = 50), LDA, Hartree and the analytic
+local pseudopotential (PME), plus the Ewald energy.  Synthetic, seeded data.
+
+value     FP32-mixed E+V evaluations/s with rho resident in HBM
+fp64      the same for the plain FP64 path
+e2e       E+V evaluations/s through the public API from pinned host memory:
+          host->device copy of rho, the evaluation, device->host copy of V
+roofline  the dominant kernel of this library, bytes it must move / its
+          CUDA-event time, against the measured HBM copy bandwidth
+cpu_baseline  the numpy restatement of the reference on the host (sampled)
+
+``--impl reference`` times that CPU restatement alone (sampled per step).
+Under torchrun each rank runs an independent replica (the single-system path
+does not shard); rank 0 prints the JSON line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+METRIC = "E+V evals/s & time-to-ground-state at 256^3 WGC: FP32-mixed vs FP64 on one GB300"
+WGC = dict(alpha=(5 + 5 ** 0.5) / 6, beta=(5 - 5 ** 0.5) / 6)
+HBM_FALLBACK = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=256, help="grid points per axis")
+    p.add_argument("--reps", type=int, default=8, help="fcc supercell repetitions")
+    p.add_argument("--nsp", type=int, default=64)
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--gs", action="store_true", help="also time the ground-state optimisation")
+    return p.parse_args()
+
+
+def workload(n, reps):
+    from dftpy_gb300 import synthetic as syn
+    lat, pos = syn.fcc_supercell(7.60, reps, sigma=0.15, seed=2048)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    rho = syn.atomic_density(lat, (n, n, n), pos, [3.0] * len(pos), width=1.4, floor=0.002)
+    return lat, pos, gp, vp, rho
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    fn = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(fn) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+# --------------------------------------------------------------- CPU legs
+def oracle_sample(lat, pos, gp, vp, rho, nsp, intervals=1):
+    """Time the numpy restatement of the reference on this workload: the fixed
+    part of one E+V plus ``intervals`` of the nsp-1 node intervals, then
+    extrapolate to a full evaluation.  Returns (seconds per E+V, details)."""
+    from oracle import ofdft_np as O
+    O.set_fft_workers(os.cpu_count() or 1)
+    n = rho.shape[0]
+    g = O.Grid(lat, rho.shape)
+    pp = O.LocalPseudo(g, pos, np.zeros(len(pos), dtype=int), [(gp, vp)], PME=True)
+    pp.vreal  # setup, not timed (the reference caches v_loc too)
+    t0 = time.perf_counter()
+    for fn in (O.tf, O.vw, O.lda, O.hartree):
+        fn(rho, g)
+    pp(rho)
+    t_local = time.perf_counter() - t0
+    lw = O.LWT(nsp=nsp, kdd=3, interp="linear", **WGC)
+    t_fixed, t_int = lw.timed_sample(rho, g, intervals)
+    per_eval = t_local + t_fixed + (nsp - 1) * t_int
+    return per_eval, {"t_local_s": t_local, "t_nl_fixed_s": t_fixed, "t_interval_s": t_int, "grid": n}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    lat, pos, gp, vp, rho = workload(args.n, args.reps)
+    times = []
+    for it in range(args.warmup + args.steps):
+        t, det = oracle_sample(lat, pos, gp, vp, rho, args.nsp)
+        if it >= args.warmup:
+            times.append(t)
+    per = float(np.mean(times))
+    cores = os.cpu_count() or 1
+    sample = ("%d^3, %d atoms: local terms + nonlocal fixed part + 1 of %d node intervals per step, "
+              "extrapolated to all intervals; numpy elementwise on 1 thread, FFTs on %d threads" %
+              (args.n, len(pos), args.nsp - 1, cores))
+    line = {"metric": METRIC, "value": 1.0 / per, "unit": "evals/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": config(args, len(pos)),
+            "cpu_baseline": {"value": 1.0 / per, "unit": "evals/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": 1.0 / per, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config(args, nat):
+    return {"workload": "fcc Al %dx%dx%d (%d atoms), %d^3 grid, TF+vW+kF-node NL kernel (nsp=%d, kdd=3, "
+                        "linear, WGC alpha/beta) + LDA + Hartree + PME local PP + Ewald"
+                        % (args.reps, args.reps, args.reps, nat, args.n, args.n, args.nsp),
+            "grid": [args.n] * 3, "atoms": nat, "nsp": args.nsp,
+            "l2": "per-step working set (tens of GB) far exceeds the 126 MB L2; a 512 MB buffer is "
+                  "written between timed steps",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+# --------------------------------------------------------------- GPU arm
+def gpu_arm(args):
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    lat, pos, gp, vp, rho_np = workload(args.n, args.reps)
+    nat = len(pos)
+    grid = D.DirectGrid(lat, (args.n,) * 3)
+    ions = D.Ions(symbols=["Al"] * nat, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+    ke = D.Functional(type="KEDF", name="LWT", nsp=args.nsp, kdd=3, interp="linear", **WGC)
+    tot = D.TotalFunctional(KineticEnergyFunctional=ke, XCFunctional=D.Functional(type="XC", name="LDA"),
+                            HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def run(dtype, steps, warmup, profile=False, sampler=None):
+        rho = D.DirectField(grid, data=rho_np, dtype=dtype)
+        ev = tot.evaluator(grid, dtype)
+        tot.prepare(ev, grid, dtype)
+        V = torch.empty_like(rho.as_subclass(torch.Tensor))
+        calc = _lib.CALC_E | _lib.CALC_V
+        for _ in range(warmup):
+            E, _ = ev.compute(rho, calc, out=V)
+        lib = _lib.load()
+        if profile:
+            _lib.check(lib.ofdft_eval_profile(ev.h, 1))
+        barrier()
+        if sampler:
+            sampler.start()
+        st = torch.cuda.current_stream()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        t0.record(st)
+        for _ in range(steps):
+            flush.fill_(1.0)
+            E, _ = ev.compute(rho, calc, out=V)
+        t1.record(st)
+        barrier()
+        wall = time.perf_counter() - w0
+        clocks = sampler.stop() if sampler else None
+        ms = t0.elapsed_time(t1)
+        prof = None
+        if profile:
+            ms_c = (_lib.C.c_double * 8)()
+            by_c = (_lib.C.c_double * 8)()
+            la_c = (_lib.C.c_longlong * 8)()
+            ncls = _lib.C.c_int()
+            _lib.check(lib.ofdft_eval_profile_read(ev.h, 8, ms_c, by_c, la_c, _lib.C.byref(ncls)))
+            _lib.check(lib.ofdft_eval_profile(ev.h, 0))
+            prof = {lib.ofdft_profile_class_name(i).decode(): {"ms": ms_c[i], "bytes": by_c[i], "launches": la_c[i]}
+                    for i in range(ncls.value)}
+        nsp_used, launches = ev.stats()
+        return {"ms_total": ms, "wall_s": wall, "E": float(E[_lib.E_TOTAL]), "clocks": clocks, "prof": prof,
+                "nsp_used": nsp_used, "launches": launches}
+
+    def maxrank(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- FP32-mixed headline, with clock sampling and per-kernel events
+    sampler = ClockSampler(local)
+    r32 = run(torch.float32, args.steps, args.warmup, profile=True, sampler=sampler)
+    ms32 = maxrank(r32["ms_total"]) / args.steps
+    out = {"metric": METRIC, "value": world * 1e3 / ms32, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (f64 reductions)", "data": "synthetic (seeded)",
+           "config": config(args, nat), "clocks": r32["clocks"], "energy_f32": r32["E"],
+           "gpu_launches": r32["launches"] * args.steps}
+    # ---- roofline of the dominant own kernel
+    peak, src = hbm_peak()
+    own = {k: v for k, v in r32["prof"].items() if k != "cufft" and v["launches"] > 0}
+    dom = max(own, key=lambda k: own[k]["ms"])
+    d = own[dom]
+    per_launch_bytes = d["bytes"] / d["launches"]
+    per_launch_ms = d["ms"] / d["launches"]
+    ach = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                       "frac": ach / peak, "traffic": None, "peak_source": src,
+                       "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
+    tot_ms = sum(v["ms"] for v in r32["prof"].values())
+    out["kernels"] = {k: {"share": v["ms"] / tot_ms if tot_ms else 0.0, "ms_per_step": v["ms"] / args.steps,
+                          "GBps": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None,
+                          "launches_per_step": v["launches"] / args.steps}
+                      for k, v in r32["prof"].items()}
+    s32 = 4
+    n3 = args.n ** 3
+    algo_bytes = (2 * 198 + 3) * s32 * n3 if args.nsp == 64 else None
+    if algo_bytes:
+        out["eval_roofline"] = {"algorithmic_bytes": algo_bytes, "achieved": algo_bytes / (ms32 * 1e-3) / 1e9,
+                                "frac": algo_bytes / (ms32 * 1e-3) / 1e9 / peak, "unit": "GB/s",
+                                "note": "(2*n_FFT+3)*s*N with n_FFT=198, s=4"}
+    # ---- FP64 path
+    if not args.no_fp64:
+        k64 = max(2, args.steps // 3)
+        r64 = run(torch.float64, k64, 1)
+        ms64 = maxrank(r64["ms_total"]) / k64
+        out["fp64"] = {"value": world * 1e3 / ms64, "unit": "evals/s", "ms_per_step": ms64, "steps": k64,
+                       "energy": r64["E"]}
+        out["fp32_vs_fp64"] = {"speedup": ms64 / ms32, "dE_per_atom": (r32["E"] - r64["E"]) / nat}
+    # ---- end to end through the public API from pinned host memory
+    rho_h = torch.from_numpy(rho_np.astype(np.float32)).pin_memory()
+    v_h = torch.empty_like(rho_h).pin_memory()
+    ke_f = D.DirectField(grid, data=rho_h, dtype=torch.float32)
+    for _ in range(2):
+        o = tot(D.DirectField(grid, data=rho_h.to("cuda", non_blocking=True), dtype=torch.float32))
+        v_h.copy_(o.potential.as_subclass(torch.Tensor), non_blocking=True)
+    barrier()
+    k_e2e = max(3, args.steps // 2)
+    w0 = time.perf_counter()
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(k_e2e):
+        rd = rho_h.to("cuda", non_blocking=True)
+        o = tot(D.DirectField(grid, data=rd, dtype=torch.float32))
+        v_h.copy_(o.potential.as_subclass(torch.Tensor), non_blocking=True)
+        _ = o.energy
+    e1.record(st)
+    barrier()
+    ms_e2e = maxrank(e0.elapsed_time(e1)) / k_e2e
+    out["e2e"] = {"value": world * 1e3 / ms_e2e, "unit": "evals/s", "h2d_bytes_per_step": rho_h.numel() * 4,
+                  "d2h_bytes_per_step": v_h.numel() * 4 + 8, "ms_per_step": ms_e2e,
+                  "path": "TotalFunctional.compute on a DirectField copied from pinned host memory"}
+    del ke_f
+    # ---- optional ground state
+    if args.gs:
+        out["time_to_ground_state"] = ground_state(D, tot, grid, rho_np, nat)
+    # ---- CPU baseline on rank 0
+    if rank == 0 and not args.no_cpu:
+        per, det = oracle_sample(lat, pos, gp, vp, rho_np, args.nsp)
+        cores = os.cpu_count() or 1
+        out["cpu_baseline"] = {"value": 1.0 / per, "unit": "evals/s", "cores": cores, "kind": "port",
+                               "sample": "%d^3 WGC E+V: local terms + nonlocal fixed part + 1 of %d node "
+                                         "intervals, extrapolated; FFTs on %d threads" % (args.n, args.nsp - 1,
+                                                                                           cores),
+                               "detail": det}
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def ground_state(D, tot, grid, rho_np, nat):
+    import torch
+    res = {}
+    for name, dtype in (("f32_mixed", torch.float32), ("f64", torch.float64)):
+        rho0 = D.DirectField(grid, dtype=dtype) + float(rho_np.mean())
+        opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
+                             optimization_options={"econv": 1e-6 * nat, "maxiter": 200})
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rho = opt.optimize_rho(guess_rho=rho0)
+        torch.cuda.synchronize()
+        res[name] = {"seconds": time.perf_counter() - t0, "energy": float(opt.functional.energy),
+                     "converged": int(opt.converged), "niter": opt.result.niter, "nfev": opt.result.nfev}
+    return res
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1175 @@
+// Total functional evaluator: fused real-space pre/post passes, fused G-space
+// kernels around cuFFT, and the density-dependent (k_F-node) nonlocal kernel.
+//
+// One E+V evaluation (TotalFunctional.compute, src/dftpy/functional/
+// total_functional.py:107-146) is:
+//   pre-pass   read rho (+ v_loc): TF, LDA and PP energies and potentials,
+//              sqrt(rho) for vW, rho^beta / rho^alpha and k_F for the nonlocal
+//              term, float64 block partials of every energy and of
+//              min/max k_F and max rho;
+//   R2C        rho (Hartree), sqrt(rho) (vW), rho^beta (+ rho^alpha);
+//   G-space    4 pi/G^2, G^2/2 and the Wang-Teter kernel applied in place,
+//              G computed from the index (nothing stored);
+//   C2R        back to real space;
+//   k_F nodes  (density-dependent kernel only) batched per-node kernels, C2R,
+//              interpolation, hat-weighted R2C and the pot2 accumulation;
+//   post-pass  combine everything into V and the remaining energies.
+#include "common.cuh"
+#include "host_math.h"
+
+#include <algorithm>
+#include <cstring>
+
+using namespace ofdft;
+
+namespace {
+
+constexpr double kZERO = 1e-30;  // src/dftpy/constants.py:85
+constexpr int kMaxNodes = 4096;
+
+struct Consts {
+    double cTF_E, cTF_V;             // TF energy / potential prefactors
+    double lda_rs, lda_ex, lda_vx;   // cbrt(3/(4 pi)), -3/4 cbrt(3/pi), cbrt(-3/pi)
+    double threepi2;                 // 3 pi^2
+    double cTF_wt;                   // 0.3 (3 pi^2)^(2/3)
+};
+
+Consts make_consts() {
+    Consts c;
+    const double pi = M_PI;
+    c.cTF_E = (3.0 / 10.0) * std::pow(3.0 * pi * pi, 2.0 / 3.0);
+    c.cTF_V = (3.0 / 10.0) * (5.0 / 3.0) * std::pow(3.0 * pi * pi, 2.0 / 3.0);
+    c.lda_rs = std::cbrt(3.0 / (4.0 * pi));
+    c.lda_ex = -3.0 / 4.0 * std::cbrt(3.0 / pi);
+    c.lda_vx = std::cbrt(-3.0 / pi);
+    c.threepi2 = 3.0 * pi * pi;
+    c.cTF_wt = 0.3 * std::pow(3.0 * pi * pi, 2.0 / 3.0);
+    return c;
+}
+
+// PZ81 correlation parameters, unpolarised (xc/semilocal_xc.py:287-293)
+__constant__ double cPZ[7] = {0.0311, -0.048, 0.0020, -0.0116, -0.1423, 1.0529, 0.3334};
+
+template <typename T>
+struct PreArgs {
+    const T* rho;
+    const T* vloc;
+    T* V;
+    T* sq;
+    T* rb;
+    T* ra;
+    T* kf;
+    long long N;
+    int tf, vw, xc, pp, nl, lwt, same_ab, wantV;
+    int nl_is_lwt;  // clamp rule: LWT clamps rho<=0, WT clamps rho<1e-30
+    double tf_x;
+    double alpha, beta;
+    Consts k;
+};
+
+// slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho
+constexpr int PRE_NS = 7;
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* partials) {
+    double acc[PRE_NS] = {0.0, 0.0, 0.0, 0.0, INFINITY, -INFINITY, -INFINITY};
+    const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
+        const double r = (double)a.rho[i];
+        double v = 0.0;
+        acc[3] += r;
+        acc[6] = fmax(acc[6], r);
+        if (a.tf) {
+            // PowerInt(rho, 5, 3): repeated products then cbrt (math_utils.py:158-176)
+            double r5 = r * r;
+            r5 *= r;
+            r5 *= r;
+            r5 *= r;
+            acc[0] += cbrt(r5) * a.k.cTF_E;
+            if (a.wantV) v += a.k.cTF_V * cbrt(r * r) * a.tf_x;
+        }
+        if (a.xc) {
+            // built-in LDA, Slater exchange + PZ81 (xc/semilocal_xc.py:283-319)
+            double rc = cbrt(r);
+            if (rc < 1e-30) rc = 1e-30;
+            double Rs = a.k.lda_rs / rc;
+            double ex, vx;
+            if (Rs < 1.0) {
+                double lr = log(Rs);
+                ex = a.k.lda_ex * rc + (cPZ[0] * lr + cPZ[1] + cPZ[2] * Rs * lr + cPZ[3] * Rs);
+                vx = a.k.lda_vx * rc +
+                     (lr * (cPZ[0] + 2.0 / 3 * cPZ[2] * Rs) + cPZ[1] - 1.0 / 3 * cPZ[0] +
+                      1.0 / 3 * (2 * cPZ[3] - cPZ[2]) * Rs);
+            } else {
+                double s = sqrt(Rs);
+                double den = 1.0 + cPZ[5] * s + cPZ[6] * Rs;
+                ex = a.k.lda_ex * rc + cPZ[4] / den;
+                vx = a.k.lda_vx * rc +
+                     (cPZ[4] + (7.0 / 6.0 * cPZ[4] * cPZ[5]) * s + (4.0 / 3.0 * cPZ[4] * cPZ[6] * Rs)) / (den * den);
+            }
+            acc[1] += ex * r;
+            v += vx;
+        }
+        if (a.pp) {
+            double vl = (double)a.vloc[i];
+            acc[2] += vl * r;
+            v += vl;
+        }
+        if (a.vw) a.sq[i] = (T)sqrt(r > 0.0 ? r : 1e-30);  // kedf/vw.py:34-44
+        if (a.nl) {
+            double rc = a.nl_is_lwt ? (r > 0.0 ? r : 1e-30) : (r < kZERO ? kZERO : r);
+            double pb = pow(rc, a.beta);
+            a.rb[i] = (T)pb;
+            if (!a.same_ab) a.ra[i] = (T)pow(rc, a.alpha);
+        }
+        if (a.lwt) {
+            double kf = 2.0 * cbrt(a.k.threepi2 * r);  // kedf/lwt.py:106
+            a.kf[i] = (T)kf;
+            double kfr = (double)(T)kf;
+            acc[4] = fmin(acc[4], kfr);
+            acc[5] = fmax(acc[5], kfr);
+        }
+        if (a.wantV) a.V[i] = (T)v;
+    }
+    block_reduce_store<PRE_NS>(acc, kinds, partials);
+}
+
+// --------------------------------------------------------------- G space
+template <typename T>
+struct GArgs {
+    typename Cplx<T>::type* rhoG;  // in: FFT(rho)  out: v_H(G)/N
+    typename Cplx<T>::type* sqG;   // in: FFT(sqrt rho) out: G^2/2 FFT / N
+    typename Cplx<T>::type* rbG;   // in: FFT(rho^beta) out: K FFT / N (WT)
+    typename Cplx<T>::type* raG;   // in: FFT(rho^alpha) out: K FFT / N (WT, alpha != beta)
+    T* wtK;                        // cached WT kernel (Nc)
+    const double* wtstate;         // [saved rho0, recompute flag, tkf, factor]
+    double wt_x;
+    Geo geo;
+    double invN;
+};
+
+__device__ inline double lindhard_dev(double eta, double lbda, double mu) {
+    const double tol = 1e-10, tol2 = tol / 10;
+    double out = eta;
+    if (eta > tol2 && fabs(eta - 1.0) > tol2)
+        out = 1.0 / (0.5 + 0.25 * (1.0 - eta * eta) * log((1.0 + eta) / fabs(1.0 - eta)) / eta) - 3.0 * mu * eta * eta -
+              lbda;
+    if (eta < tol) out = 1.0 - lbda + eta * eta * (1.0 / 3.0 - 3.0 * mu);
+    if (fabs(eta - 1.0) < tol) out = 2.0 - lbda - 3.0 * mu + 20.0 * (eta - 1.0);
+    if (eta > 3.65) {
+        const double c[15] = {-0.13714285714285712, -6.39999999999999875e-2, -3.77825602968460128e-2,
+                              -2.51824061652633074e-2, -1.80879839616166146e-2, -1.36715733124818332e-2,
+                              -1.07236045520990083e-2, -8.65192783339199453e-3, -7.1372762502456763e-3,
+                              -5.9945117538835746e-3, -5.10997527675418131e-3, -4.41060829979912465e-3,
+                              -3.84763737842981233e-3, -3.38745061493813488e-3, -3.00624946457977689e-3};
+        double inv2 = 1.0 / (eta * eta);
+        double acc = c[14] * inv2;
+#pragma unroll
+        for (int k = 13; k >= 0; --k) acc = inv2 * (c[k] + acc);
+        out = 3.0 * (1.0 - mu) * eta * eta - lbda - 0.6 + acc;
+    }
+    return out;
+}
+
+template <typename T>
+__global__ void k_gspace(GArgs<T> a) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const bool recompute = a.wtK && a.wtstate[1] != 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.geo.Nc; i += stride) {
+        double gg = gsq(a.geo, i);
+        if (a.rhoG) {  // Hartree: 4 pi / G^2, G=0 -> 0 (hartree.py:33-35, grid.py:532-541)
+            double f = (i == 0) ? 0.0 : 4.0 * M_PI / gg * a.invN;
+            auto z = a.rhoG[i];
+            z.x = (T)(z.x * f);
+            z.y = (T)(z.y * f);
+            a.rhoG[i] = z;
+        }
+        if (a.sqG) {  // vW: G^2 (vw.py:45-51) with the 1/2 folded in
+            double f = 0.5 * gg * a.invN;
+            auto z = a.sqG[i];
+            z.x = (T)(z.x * f);
+            z.y = (T)(z.y * f);
+            a.sqG[i] = z;
+        }
+        if (a.wtK) {  // Wang-Teter kernel (kernel.py:325-334), cached per rho0
+            double K;
+            if (recompute) {
+                double q = sqrt(gg);
+                K = lindhard_dev(q / a.wtstate[2], a.wt_x, 1.0) * a.wtstate[3];
+                a.wtK[i] = (T)K;
+            } else {
+                K = (double)a.wtK[i];
+            }
+            double f = K * a.invN;
+            auto z = a.rbG[i];
+            z.x = (T)(z.x * f);
+            z.y = (T)(z.y * f);
+            a.rbG[i] = z;
+            if (a.raG) {
+                auto w = a.raG[i];
+                w.x = (T)(w.x * f);
+                w.y = (T)(w.y * f);
+                a.raG[i] = w;
+            }
+        }
+    }
+}
+
+// device-side WT kernel cache decision (wt.py:58-73): rebuild when rho0 moves by > 1e-6
+__global__ void k_wt_plan(const double* results, double* state, double rho0_fixed, double invN, double alpha,
+                          double beta, double cTF) {
+    double rho0 = rho0_fixed > 0.0 ? rho0_fixed : results[3] * invN;
+    bool first = state[4] == 0.0;
+    if (first || fabs(state[0] - rho0) > 1e-6) {
+        state[0] = rho0;
+        state[1] = 1.0;
+        state[2] = 2.0 * pow(3.0 * rho0 * (M_PI * M_PI), 1.0 / 3.0);
+        state[3] = 5.0 / (9.0 * alpha * beta * pow(rho0, alpha + beta - 5.0 / 3.0)) * cTF;
+        state[4] = 1.0;
+    } else {
+        state[1] = 0.0;
+    }
+}
+
+// ----------------------------------------------------- density-dependent kernel
+// Kernel table K(eta) and derivative table -eta K'(eta) as cubic pieces on the
+// uniform eta grid of the reference (lwt.py:535-566).
+template <typename T>
+struct Table {
+    const T* c;      // 4 per interval
+    const T* cd;     // derivative table
+    int nint;        // neta - 1
+    double step, inv_step, etamax;
+    double limit, limitd;  // values at etamax
+};
+
+template <typename T>
+__device__ inline double spline_eval(const T* c, int nint, double step, double inv_step, double eta) {
+    int l = (int)(eta * inv_step);
+    l = l < 0 ? 0 : (l >= nint ? nint - 1 : l);
+    double u = eta - (double)l * step;
+    const T* q = c + 4 * (long long)l;
+    return (double)q[0] + u * ((double)q[1] + u * ((double)q[2] + u * (double)q[3]));
+}
+
+struct Nodes {
+    const double* k;     // node k_F
+    const double* invk;  // 1/k
+};
+
+// X_j = K_j(G) FFT(rho^beta)/N and Y_j = K'_j(G)/k_j FFT(rho^beta)/N for the
+// chunk's nodes (LWTKernelKf, kernel.py:379-405; lwt.py:226-251)
+template <typename T>
+__global__ void k_lwt_nodes(const typename Cplx<T>::type* __restrict__ rbG, typename Cplx<T>::type* __restrict__ XY,
+                            Table<T> tab, Nodes nd, int j0, int nb, int mcalc, Geo geo, double invN) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        double q = sqrt(gsq(geo, i));
+        auto z = rbG[i];
+        double zr = (double)z.x * invN, zi = (double)z.y * invN;
+        for (int jj = 0; jj < nb; ++jj) {
+            const int j = j0 + jj;
+            double eta = q * nd.invk[j];
+            double K, KD = 0.0;
+            if (eta < tab.etamax) {
+                K = spline_eval(tab.c, tab.nint, tab.step, tab.inv_step, eta);
+                if (mcalc) KD = spline_eval(tab.cd, tab.nint, tab.step, tab.inv_step, eta);
+            } else {
+                K = tab.limit;
+                KD = tab.limitd;
+            }
+            if (i == 0) K = KD = 0.0;
+            typename Cplx<T>::type o;
+            o.x = (T)(K * zr);
+            o.y = (T)(K * zi);
+            XY[(long long)jj * geo.Nc + i] = o;
+            if (mcalc) {
+                double kd = KD * nd.invk[j];
+                o.x = (T)(kd * zr);
+                o.y = (T)(kd * zi);
+                XY[(long long)(nb + jj) * geo.Nc + i] = o;
+            }
+        }
+    }
+}
+
+// pot2G (+)= sum_j K_j(G) U_j(G)/N [+ K'_j/k_j UD_j(G)/N] (lwt.py:266-296)
+template <typename T>
+__global__ void k_lwt_pot2(const typename Cplx<T>::type* __restrict__ U, typename Cplx<T>::type* __restrict__ pot2G,
+                           Table<T> tab, Nodes nd, int j0, int nb, int hermite, int first, Geo geo, double invN) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        double q = sqrt(gsq(geo, i));
+        double sr = 0.0, si = 0.0;
+        if (!first) {
+            sr = (double)pot2G[i].x;
+            si = (double)pot2G[i].y;
+        }
+        for (int jj = 0; jj < nb; ++jj) {
+            const int j = j0 + jj;
+            double eta = q * nd.invk[j];
+            double K, KD = 0.0;
+            if (eta < tab.etamax) {
+                K = spline_eval(tab.c, tab.nint, tab.step, tab.inv_step, eta);
+                if (hermite) KD = spline_eval(tab.cd, tab.nint, tab.step, tab.inv_step, eta);
+            } else {
+                K = tab.limit;
+                KD = tab.limitd;
+            }
+            if (i == 0) K = KD = 0.0;
+            auto u = U[(long long)jj * geo.Nc + i];
+            sr += K * invN * (double)u.x;
+            si += K * invN * (double)u.y;
+            if (hermite) {
+                double kd = KD * nd.invk[j] * invN;
+                auto w = U[(long long)(nb + jj) * geo.Nc + i];
+                sr += kd * (double)w.x;
+                si += kd * (double)w.y;
+            }
+        }
+        typename Cplx<T>::type o;
+        o.x = (T)sr;
+        o.y = (T)si;
+        pot2G[i] = o;
+    }
+}
+
+// per-point interval membership of the reference (lwt.py:252-306):
+// interval i holds kf in (k_i, k_{i+1} + 1e-18); 'small' holds kf < k_0 + 1e-18.
+struct Member {
+    int ilast, iprev;  // last / previous containing interval, -1 if none
+    bool small;
+};
+
+__device__ inline Member membership(double kf, const double* kn, const double* kup, int m) {
+    // c = number of nodes strictly below kf
+    int lo = 0, hi = m;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (kn[mid] < kf) lo = mid + 1;
+        else hi = mid;
+    }
+    const int c = lo;
+    Member r;
+    r.ilast = -1;
+    r.iprev = -1;
+    int i1 = c - 1, i2 = c - 2;
+    bool in1 = (i1 >= 0 && i1 <= m - 2 && kf < kup[i1 + 1]);
+    bool in2 = (i2 >= 0 && i2 <= m - 2 && kf < kup[i2 + 1]);
+    if (in1) {
+        r.ilast = i1;
+        if (in2) r.iprev = i2;
+    } else if (in2) {
+        r.ilast = i2;
+    }
+    r.small = kf < kup[0];
+    return r;
+}
+
+template <typename T>
+struct InterpArgs {
+    const T* kf;
+    const T* rA;
+    const T* PM;  // P planes then M planes of the chunk
+    T* pot1;
+    T* pot3;
+    T* u;         // nb (linear) or 2 nb (hermite) planes
+    const double* kn;
+    const double* kup;  // k_i + 1e-18
+    int m, j0, nb, kdd, hermite, mcalc, first;
+    double kfclip;
+    long long N;
+};
+
+template <typename T>
+__global__ void k_lwt_interp(InterpArgs<T> a) {
+    extern __shared__ double sh[];
+    double* kn = sh;
+    double* kup = sh + a.m;
+    for (int t = threadIdx.x; t < a.m; t += blockDim.x) {
+        kn[t] = a.kn[t];
+        kup[t] = a.kup[t];
+    }
+    __syncthreads();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const int j1 = a.j0 + a.nb;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < a.N; r += stride) {
+        double kf = fmin((double)a.kf[r], a.kfclip);
+        Member mb = membership(kf, kn, kup, a.m);
+        double p1 = 0.0, p3 = 0.0;
+        // weights of nodes il (lower) and il+1 (upper) of the deciding interval
+        auto P = [&](int j) { return (double)a.PM[(long long)(j - a.j0) * a.N + r]; };
+        auto M = [&](int j) { return (double)a.PM[(long long)(a.nb + j - a.j0) * a.N + r]; };
+        if (mb.ilast >= 0) {
+            const int i = mb.ilast;
+            const double D = kn[i + 1] - kn[i];
+            const double t = (kf - kn[i]) / D;
+            if (!a.hermite) {
+                const double t0 = 1.0 - t;
+                if (i >= a.j0 && i < j1) {
+                    p1 += P(i) * t0;
+                    if (a.kdd == 3) p3 += M(i) * t0;
+                }
+                if (i + 1 >= a.j0 && i + 1 < j1) {
+                    p1 += P(i + 1) * t;
+                    if (a.kdd == 3) p3 += M(i + 1) * t;
+                }
+            } else {
+                const double t2 = t * t, t3 = t2 * t;
+                const double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = t3 - 2.0 * t2 + t, h01 = 1.0 - h00,
+                             h11 = t3 - t2;
+                const double h00D = 6.0 * t2 - 6 * t, h10D = 3.0 * t2 - 4 * t + 1.0, h01D = -h00D,
+                             h11D = 3.0 * t2 - 2 * t;
+                if (i >= a.j0 && i < j1) {
+                    p1 += h00 * P(i) + D * h10 * M(i);
+                    if (a.kdd == 3) p3 += h00D * P(i) / D + h10D * M(i);
+                }
+                if (i + 1 >= a.j0 && i + 1 < j1) {
+                    p1 += h01 * P(i + 1) + D * h11 * M(i + 1);
+                    if (a.kdd == 3) p3 += h01D * P(i + 1) / D + h11D * M(i + 1);
+                }
+            }
+        } else if (mb.small) {
+            const double ts = (kf - kn[0]) / kn[0];
+            if (a.j0 == 0) p1 += P(0) * ts;
+        }
+        if (a.first) {
+            a.pot1[r] = (T)p1;
+            if (a.kdd == 3) a.pot3[r] = (T)p3;
+        } else {
+            a.pot1[r] = (T)((double)a.pot1[r] + p1);
+            if (a.kdd == 3) a.pot3[r] = (T)((double)a.pot3[r] + p3);
+        }
+        if (a.kdd > 1) {
+            // hat weights W_j (and WD_j for hermite) of every containing interval
+            const double rA = (double)a.rA[r];
+            int ints[2] = {mb.ilast, mb.iprev};
+            double w[4] = {0, 0, 0, 0};  // weights for nodes base, base+1 (W) and (WD)
+            int base = mb.ilast >= 0 ? (mb.iprev >= 0 ? mb.iprev : mb.ilast) : 0;
+            // up to three distinct nodes: base, base+1, base+2
+            double W[3] = {0, 0, 0}, WD[3] = {0, 0, 0};
+            for (int q = 0; q < 2; ++q) {
+                const int i = ints[q];
+                if (i < 0) continue;
+                const double D = kn[i + 1] - kn[i];
+                const double t = (kf - kn[i]) / D;
+                if (!a.hermite) {
+                    W[i - base] += 1.0 - t;
+                    W[i + 1 - base] += t;
+                } else {
+                    const double t2 = t * t, t3 = t2 * t;
+                    const double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = t3 - 2.0 * t2 + t, h01 = 1.0 - h00,
+                                 h11 = t3 - t2;
+                    W[i - base] += h00;
+                    W[i + 1 - base] += h01;
+                    WD[i - base] += D * h10;
+                    WD[i + 1 - base] += D * h11;
+                }
+            }
+            (void)w;
+            double ws0 = 0.0;
+            if (mb.small) ws0 = (kf - kn[0]) / kn[0];
+            for (int jj = 0; jj < a.nb; ++jj) {
+                const int j = a.j0 + jj;
+                double wj = 0.0, wdj = 0.0;
+                const int d = j - base;
+                if (mb.ilast >= 0 && d >= 0 && d < 3) {
+                    wj = W[d];
+                    wdj = WD[d];
+                }
+                if (j == 0) wj += ws0;
+                a.u[(long long)jj * a.N + r] = (T)(rA * wj);
+                if (a.hermite) a.u[(long long)(a.nb + jj) * a.N + r] = (T)(rA * wdj);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- post-pass
+template <typename T>
+struct PostArgs {
+    const T* rho;
+    T* V;
+    const T* sq;
+    const T* lap;   // (1/2) IFFT(G^2 FFT(sqrt rho)) (already normalised)
+    const T* vH;
+    const T* nl1;   // IFFT(K FFT(rho^beta))
+    const T* nl2;   // IFFT(K FFT(rho^alpha)) (alpha != beta)
+    const T* rb;
+    const T* ra;
+    // LWT
+    const T* kf;
+    const T* pot1;
+    const T* pot2;
+    const T* pot3;
+    long long N;
+    int vw, h, wt, lwt, same_ab, wantV, kdd;
+    double vw_y;
+    double alpha, beta;  // of the active nonlocal term
+    double rhomax, ld, kfclip;
+};
+
+// slots: 0 vW, 1 Hartree, 2 NL
+constexpr int POST_NS = 3;
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double* partials) {
+    double acc[POST_NS] = {0.0, 0.0, 0.0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
+        const double r = (double)a.rho[i];
+        double v = a.wantV ? (double)a.V[i] : 0.0;
+        if (a.vw) {
+            double s = (double)a.sq[i];
+            if (fabs(s) < 1e-30) s = 1e-30;
+            double pw = (double)a.lap[i] / s;
+            if (r > 0.0) acc[0] += r * pw;
+            v += pw * a.vw_y;
+        }
+        if (a.h) {
+            double vh = (double)a.vH[i];
+            acc[1] += vh * r;
+            v += vh;
+        }
+        if (a.wt) {
+            double rc = r < kZERO ? kZERO : r;
+            double pb = (double)a.rb[i];
+            double c1 = (double)a.nl1[i];
+            if (a.same_ab) {
+                double pot = 2.0 * a.alpha * (pb / rc) * c1;  // wt.py:19-23
+                if (a.wantV) {
+                    acc[2] += pot * r / (2.0 * a.alpha);      // wt.py:124-125
+                    v += pot;
+                } else {
+                    acc[2] += c1 * pb;                        // wt.py:44-56
+                }
+            } else {
+                double pa = (double)a.ra[i];
+                acc[2] += c1 * pa;
+                if (a.wantV) v += a.alpha * (pa / rc) * c1 + a.beta * (pb / rc) * (double)a.nl2[i];
+            }
+        }
+        if (a.lwt) {
+            // low-density factor (lwt.py:315-322) and the final combination (:324-339)
+            double f = 1.0;
+            if (r < 1e-6) f = pow(fabs(r), a.ld) / pow(a.rhomax, a.ld);
+            if (r < 0.0) f = 0.0;
+            double rc = r > 0.0 ? r : 1e-30;
+            double pa = a.same_ab ? (double)a.rb[i] : (double)a.ra[i];
+            double p1 = (double)a.pot1[i] * f;
+            acc[2] += pa * p1;
+            if (a.wantV) {
+                double pb = (double)a.rb[i];
+                double p2 = (a.kdd > 1 ? (double)a.pot2[i] : (double)a.pot1[i]) * f;
+                double p3 = (a.kdd == 3 ? (double)a.pot3[i] : 0.0) * f;
+                double kf = fmin((double)a.kf[i], a.kfclip);
+                v += a.alpha * (pa / rc) * p1 + (a.beta * (pb / rc) * p2 + (kf / 3.0) * (pa / rc) * p3);
+            }
+        }
+        if (a.wantV) a.V[i] = (T)v;
+    }
+    block_sum_store<POST_NS>(acc, partials);
+}
+
+template <typename T>
+__global__ void k_zero(T* p, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = (T)0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ handle
+struct ofdft_eval {
+    ofdft_grid* g = nullptr;
+    ofdft_config cfg;
+    Consts k;
+    Scratch sc;
+    void* vloc = nullptr;  // grid precision
+    bool have_vloc = false;
+    double* wtstate = nullptr;  // device [rho0, flag, tkf, factor, init]
+    // density-dependent kernel
+    void* tab_c = nullptr;
+    void* tab_cd = nullptr;
+    int tab_nint = 0;
+    double tab_step = 0, tab_limit = 0, tab_limitd = 0;
+    double* d_nodes = nullptr;  // [k (kMaxNodes), 1/k, k+1e-18]
+    double* h_nodes = nullptr;  // pinned staging
+    bool kf_set_min = false, kf_set_max = false;
+    double kf_st_min = 0, kf_st_max = 0;
+    int last_nsp = 0, last_launches = 0;
+    // per-kernel-class CUDA-event profiling
+    static constexpr int kClasses = 8;
+    bool prof = false;
+    std::vector<cudaEvent_t> evs;   // pool, two per recorded launch
+    std::vector<int> rec_cls;       // class of each recorded launch
+    std::vector<double> rec_bytes;  // algorithmic bytes of each recorded launch
+    double prof_ms[kClasses] = {0};
+    double prof_bytes[kClasses] = {0};
+    long long prof_launches[kClasses] = {0};
+};
+
+ofdft_grid* e_grid(ofdft_eval* e) { return e->g; }
+
+namespace {
+
+enum ProfClass { P_PREPASS = 0, P_GSPACE, P_LWT_NODES, P_LWT_INTERP, P_LWT_POT2, P_POSTPASS, P_REDUCE, P_CUFFT };
+const char* kProfNames[ofdft_eval::kClasses] = {"prepass", "gspace", "lwt_nodes", "lwt_interp",
+                                                 "lwt_pot2", "postpass", "reduce", "cufft"};
+
+// Record a start event for one launch of class cls moving `bytes` algorithmic bytes.
+int prof_begin(ofdft_eval* e, int cls, double bytes, cudaStream_t st) {
+    if (!e->prof) return -1;
+    const int idx = (int)e->rec_cls.size();
+    while ((int)e->evs.size() < 2 * (idx + 1)) {
+        cudaEvent_t ev;
+        OFDFT_CK(cudaEventCreate(&ev));
+        e->evs.push_back(ev);
+    }
+    e->rec_cls.push_back(cls);
+    e->rec_bytes.push_back(bytes);
+    OFDFT_CK(cudaEventRecord(e->evs[2 * idx], st));
+    return idx;
+}
+
+void prof_end(ofdft_eval* e, int idx, cudaStream_t st) {
+    if (idx < 0) return;
+    OFDFT_CK(cudaEventRecord(e->evs[2 * idx + 1], st));
+}
+
+// after the stream has been synchronised: fold recorded launches into the totals
+void prof_collect(ofdft_eval* e) {
+    for (size_t i = 0; i < e->rec_cls.size(); ++i) {
+        float ms = 0.f;
+        OFDFT_CK(cudaEventElapsedTime(&ms, e->evs[2 * i], e->evs[2 * i + 1]));
+        e->prof_ms[e->rec_cls[i]] += ms;
+        e->prof_bytes[e->rec_cls[i]] += e->rec_bytes[i];
+        e->prof_launches[e->rec_cls[i]] += 1;
+    }
+    e->rec_cls.clear();
+    e->rec_bytes.clear();
+}
+
+// run `f` (one launch) between profiling events
+template <class F>
+void timed(ofdft_eval* e, int cls, double bytes, cudaStream_t st, F&& f) {
+    int idx = prof_begin(e, cls, bytes, st);
+    f();
+    prof_end(e, idx, st);
+}
+
+template <typename T>
+void build_table(ofdft_eval* e) {
+    const ofdft_config& c = e->cfg;
+    const int neta = c.lwt_neta;
+    const double etamax = c.lwt_etamax;
+    std::vector<double> eta(neta), y(neta);
+    // numpy linspace(0, etamax, neta)
+    const double step = etamax / (double)(neta - 1);
+    for (int i = 0; i < neta; ++i) eta[i] = (double)i * step;
+    eta[neta - 1] = etamax;
+    // WTKernelTable (kernel.py:344-352): F(eta; x, 1) * (4/5) * 0.3 (3 pi^2)^(2/3)
+    const double factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
+    for (int i = 0; i < neta; ++i) y[i] = lindhard(eta[i], c.lwt_x, 1.0) * factor;
+    CubicSpline S;
+    S.fit(eta, y);
+    std::vector<double> yd(neta);
+    for (int i = 0; i < neta; ++i) yd[i] = S.deriv(eta[i]) * (-1.0 * eta[i]);  // lwt.py:556
+    CubicSpline SD;
+    SD.fit(eta, yd);
+    const int nint = neta - 1;
+    std::vector<T> hc(4 * (size_t)nint), hcd(4 * (size_t)nint);
+    for (size_t i = 0; i < hc.size(); ++i) {
+        hc[i] = (T)S.c[i];
+        hcd[i] = (T)SD.c[i];
+    }
+    OFDFT_CK(cudaMalloc(&e->tab_c, hc.size() * sizeof(T)));
+    OFDFT_CK(cudaMalloc(&e->tab_cd, hcd.size() * sizeof(T)));
+    OFDFT_CK(cudaMemcpy(e->tab_c, hc.data(), hc.size() * sizeof(T), cudaMemcpyHostToDevice));
+    OFDFT_CK(cudaMemcpy(e->tab_cd, hcd.data(), hcd.size() * sizeof(T), cudaMemcpyHostToDevice));
+    e->tab_nint = nint;
+    e->tab_step = step;
+    e->tab_limit = S.eval(etamax);
+    e->tab_limitd = SD.eval(etamax);
+}
+
+template <typename T>
+Table<T> table_of(const ofdft_eval* e) {
+    Table<T> t;
+    t.c = (const T*)e->tab_c;
+    t.cd = (const T*)e->tab_cd;
+    t.nint = e->tab_nint;
+    t.step = e->tab_step;
+    t.inv_step = 1.0 / e->tab_step;
+    t.etamax = e->cfg.lwt_etamax;
+    t.limit = e->tab_limit;
+    t.limitd = e->tab_limitd;
+    return t;
+}
+
+struct LwtPlan {
+    bool active = false;  // false: homogeneous density, NL term is zero
+    std::vector<double> nodes;
+    double kfclip = INFINITY;
+};
+
+template <typename T>
+void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energies, cudaStream_t st) {
+    ofdft_grid* g = e->g;
+    const ofdft_config& c = e->cfg;
+    const long long N = g->N, Nc = g->Nc;
+    const bool wantV = (calc & OFDFT_CALC_V) != 0;
+    const bool tf = c.kedf_terms & OFDFT_KE_TF, vw = c.kedf_terms & OFDFT_KE_VW;
+    const bool wt = c.kedf_terms & OFDFT_KE_WT, lwt = c.kedf_terms & OFDFT_KE_LWT;
+    const bool nl = wt || lwt;
+    const double alpha = wt ? c.wt_alpha : c.lwt_alpha, beta = wt ? c.wt_beta : c.lwt_beta;
+    const bool same_ab = wt ? std::fabs(beta - alpha) < 1e-9 : std::fabs(alpha - beta) < 1e-8;
+    const bool h = c.hartree != 0, xc = c.xc_lda != 0, pp = c.pseudo != 0 && e->have_vloc;
+    OFDFT_REQUIRE(!(c.pseudo && !e->have_vloc), "ofdft_eval_compute: pseudo enabled but no v_loc set");
+    OFDFT_REQUIRE(!(wantV && !V), "ofdft_eval_compute: V requested but v_out is NULL");
+    int launches = 0;
+    const size_t rb = g->real_bytes(), cb = g->cplx_bytes();
+    using C = typename Cplx<T>::type;
+
+    T* Vw = wantV ? V : nullptr;
+    T* sq = vw ? (T*)e->sc.get("sq", rb) : nullptr;
+    T* rbp = nl ? (T*)e->sc.get("rb", rb) : nullptr;
+    T* rap = (nl && !same_ab) ? (T*)e->sc.get("ra", rb) : nullptr;
+    T* kfv = lwt ? (T*)e->sc.get("kf", rb) : nullptr;
+
+    // ---- pre-pass
+    PreArgs<T> pa;
+    pa.rho = rho;
+    pa.vloc = pp ? (const T*)e->vloc : nullptr;
+    pa.V = Vw;
+    pa.sq = sq;
+    pa.rb = rbp;
+    pa.ra = rap;
+    pa.kf = kfv;
+    pa.N = N;
+    pa.tf = tf;
+    pa.vw = vw;
+    pa.xc = xc;
+    pa.pp = pp;
+    pa.nl = nl;
+    pa.lwt = lwt;
+    pa.same_ab = same_ab;
+    pa.wantV = wantV;
+    pa.nl_is_lwt = lwt;
+    pa.tf_x = c.tf_x;
+    pa.alpha = alpha;
+    pa.beta = beta;
+    pa.k = e->k;
+    const double s = (double)sizeof(T), Nd = (double)N, Ncd = (double)Nc;
+    {
+        // algorithmic bytes: read rho (+ v_loc); write V, sqrt(rho), rho^beta (+ rho^alpha), k_F as active
+        double b = Nd * s * (1 + pp + wantV + vw + nl + (nl && !same_ab) + lwt);
+        timed(e, P_PREPASS, b, st, [&] { k_prepass<T><<<g->red_blocks, RED_THREADS, 0, st>>>(pa, g->d_partials); });
+    }
+    OFDFT_LAUNCH_CHECK();
+    unsigned long long kinds = (1ull << (2 * 4)) | (2ull << (2 * 5)) | (2ull << (2 * 6));
+    timed(e, P_REDUCE, (double)g->red_blocks * PRE_NS * 8, st, [&] {
+        reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, PRE_NS, kinds, g->d_results);
+    });
+    OFDFT_LAUNCH_CHECK();
+    launches += 2;
+    auto r2c = [&](const void* in, void* out, int batch) {
+        timed(e, P_CUFFT, 2.0 * Nd * s * batch, st, [&] { g->exec_r2c(in, out, batch, st); });
+    };
+    auto c2r = [&](void* in, void* out, int batch) {
+        timed(e, P_CUFFT, 2.0 * Nd * s * batch, st, [&] { g->exec_c2r(in, out, batch, st); });
+    };
+
+    // ---- WT kernel cache decision on the device
+    T* wtK = nullptr;
+    if (wt) {
+        wtK = (T*)e->sc.get("wtK", (size_t)Nc * sizeof(T));
+        k_wt_plan<<<1, 1, 0, st>>>(g->d_results, e->wtstate, c.wt_rho0, 1.0 / (double)N, c.wt_alpha, c.wt_beta,
+                                   e->k.cTF_wt);
+        OFDFT_LAUNCH_CHECK();
+        launches++;
+    }
+
+    // ---- k_F node plan on the host (needs min/max k_F and max rho)
+    LwtPlan lp;
+    double rhomax = 0.0;
+    if (lwt) {
+        OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, PRE_NS * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+        const double kf_l = g->h_results[4], kf_r = g->h_results[5];
+        rhomax = g->h_results[6];
+        if (std::fabs(kf_r - kf_l) >= 1e-8) {  // lwt.py:115-124
+            lp.active = true;
+            const bool fmin_ = !std::isnan(c.lwt_kfmin), fmax_ = !std::isnan(c.lwt_kfmax);
+            double b0, b1;
+            guess_kf_bound(kf_l, kf_r, fmin_, c.lwt_kfmin, fmax_, c.lwt_kfmax, e->kf_set_min, e->kf_st_min,
+                           e->kf_set_max, e->kf_st_max, b0, b1);
+            lp.kfclip = b1;
+            double kmin_c = std::min(kf_l, b1), kmax_c = std::min(kf_r, b1);
+            double kfMin = fmin_ ? c.lwt_kfmin : std::max(kmin_c, b0);
+            double kfMax = fmax_ ? c.lwt_kfmax : kmax_c;
+            lp.nodes = kf_nodes(kfMin, kfMax, c.lwt_nsp, c.lwt_delta, c.lwt_ratio);
+            OFDFT_REQUIRE((int)lp.nodes.size() <= kMaxNodes && lp.nodes.size() >= 2,
+                          "density-dependent kernel: %zu nodes (max %d)", lp.nodes.size(), kMaxNodes);
+            const int m = (int)lp.nodes.size();
+            for (int i = 0; i < m; ++i) {
+                e->h_nodes[i] = lp.nodes[i];
+                e->h_nodes[kMaxNodes + i] = 1.0 / lp.nodes[i];
+                e->h_nodes[2 * kMaxNodes + i] = lp.nodes[i] + 1e-18;
+            }
+            OFDFT_CK(cudaMemcpyAsync(e->d_nodes, e->h_nodes, 3 * kMaxNodes * sizeof(double), cudaMemcpyHostToDevice,
+                                     st));
+        }
+        e->last_nsp = lp.active ? (int)lp.nodes.size() : 0;
+    }
+
+    // ---- forward transforms
+    C* rhoG = h ? (C*)e->sc.get("rhoG", cb) : nullptr;
+    C* sqG = vw ? (C*)e->sc.get("sqG", cb) : nullptr;
+    C* rbG = nl ? (C*)e->sc.get("rbG", cb) : nullptr;
+    C* raG = (wt && !same_ab) ? (C*)e->sc.get("raG", cb) : nullptr;
+    if (h) r2c(rho, rhoG, 1);
+    if (vw) r2c(sq, sqG, 1);
+    if (wt || (lwt && lp.active)) r2c(rbp, rbG, 1);
+    if (raG) r2c(rap, raG, 1);
+
+    // ---- fused G-space multipliers
+    if (h || vw || wt) {
+        GArgs<T> ga;
+        ga.rhoG = rhoG;
+        ga.sqG = sqG;
+        ga.rbG = wt ? rbG : nullptr;
+        ga.raG = raG;
+        ga.wtK = wtK;
+        ga.wtstate = e->wtstate;
+        ga.wt_x = c.wt_x;
+        ga.geo = g->geo;
+        ga.invN = 1.0 / (double)N;
+        // read + write of each active complex plane (+ the cached WT kernel)
+        double b = Ncd * 2 * s * 2 * (h + vw + wt + (raG != nullptr)) + (wt ? Ncd * s : 0.0);
+        timed(e, P_GSPACE, b, st, [&] { k_gspace<T><<<blocks_for(Nc, 256, g->sms * 16), 256, 0, st>>>(ga); });
+        OFDFT_LAUNCH_CHECK();
+        launches++;
+    }
+    T* vH = h ? (T*)e->sc.get("vH", rb) : nullptr;
+    T* lap = vw ? (T*)e->sc.get("lap", rb) : nullptr;
+    T* nl1 = wt ? (T*)e->sc.get("nl1", rb) : nullptr;
+    T* nl2 = (wt && !same_ab) ? (T*)e->sc.get("nl2", rb) : nullptr;
+    if (h) c2r(rhoG, vH, 1);
+    if (vw) c2r(sqG, lap, 1);
+    if (wt) c2r(rbG, nl1, 1);
+    if (nl2) c2r(raG, nl2, 1);
+
+    // ---- density-dependent kernel
+    T *pot1 = nullptr, *pot2 = nullptr, *pot3 = nullptr;
+    int kdd = wantV ? c.lwt_kdd : 1;
+    if (lwt && lp.active) {
+        const int m = (int)lp.nodes.size();
+        const bool hermite = c.lwt_interp == OFDFT_INTERP_HERMITE;
+        const bool mcalc = kdd > 1 || hermite;
+        // nodes per batched pass from the free memory: per node 2 complex + 2 real + (1|2) real planes
+        size_t per_node = 2 * cb + 2 * rb + (hermite ? 2 : 1) * rb;
+        size_t freeb = 0, totalb = 0;
+        cudaMemGetInfo(&freeb, &totalb);
+        int B = c.lwt_max_batch > 0 ? c.lwt_max_batch : 64;
+        long long fit = (long long)(0.5 * (double)freeb) / (long long)per_node;
+        if (fit < B) B = (int)std::max(1LL, fit);
+        B = std::min(B, m);
+        pot1 = (T*)e->sc.get("pot1", rb);
+        if (kdd == 3) pot3 = (T*)e->sc.get("pot3", rb);
+        C* pot2G = kdd > 1 ? (C*)e->sc.get("pot2G", cb) : nullptr;
+        C* XY = (C*)e->sc.get("lwtXY", (size_t)2 * B * cb);
+        T* PM = (T*)e->sc.get("lwtPM", (size_t)2 * B * rb);
+        T* U = kdd > 1 ? (T*)e->sc.get("lwtU", (size_t)(hermite ? 2 : 1) * B * rb) : nullptr;
+        Nodes nd;
+        nd.k = e->d_nodes;
+        nd.invk = e->d_nodes + kMaxNodes;
+        Table<T> tab = table_of<T>(e);
+        const int gblk = blocks_for(Nc, 256, g->sms * 16);
+        const int rblk = blocks_for(N, 256, g->sms * 16);
+        for (int j0 = 0; j0 < m; j0 += B) {
+            const int nb = std::min(B, m - j0);
+            const int nplanes = mcalc ? 2 * nb : nb;
+            // read FFT(rho^beta) once, write one complex plane per node (two with derivatives)
+            timed(e, P_LWT_NODES, Ncd * 2 * s * (1 + nplanes), st, [&] {
+                k_lwt_nodes<T><<<gblk, 256, 0, st>>>(rbG, XY, tab, nd, j0, nb, mcalc, g->geo, 1.0 / (double)N);
+            });
+            OFDFT_LAUNCH_CHECK();
+            c2r(XY, PM, nplanes);
+            InterpArgs<T> ia;
+            ia.kf = kfv;
+            ia.rA = same_ab ? rbp : rap;
+            ia.PM = PM;
+            ia.pot1 = pot1;
+            ia.pot3 = pot3;
+            ia.u = U;
+            ia.kn = e->d_nodes;
+            ia.kup = e->d_nodes + 2 * kMaxNodes;
+            ia.m = m;
+            ia.j0 = j0;
+            ia.nb = nb;
+            ia.kdd = kdd;
+            ia.hermite = hermite;
+            ia.mcalc = mcalc;
+            ia.first = j0 == 0;
+            ia.kfclip = lp.kfclip;
+            ia.N = N;
+            {
+                // read k_F and rho^alpha; gather the two (four with derivatives) node values of each
+                // point; write pot1 (+pot3), reading them back after the first pass; write the hat planes
+                const int upl = kdd > 1 ? (hermite ? 2 * nb : nb) : 0;
+                const int gat = kdd == 3 || hermite ? 4 : 2;
+                const int accs = 1 + (kdd == 3);
+                double b = Nd * s * (2 + gat + accs * (j0 == 0 ? 1 : 2) + upl);
+                timed(e, P_LWT_INTERP, b, st,
+                      [&] { k_lwt_interp<T><<<rblk, 256, 2 * m * sizeof(double), st>>>(ia); });
+            }
+            OFDFT_LAUNCH_CHECK();
+            launches += 2;
+            if (kdd > 1) {
+                const int upl = hermite ? 2 * nb : nb;
+                r2c(U, XY, upl);
+                timed(e, P_LWT_POT2, Ncd * 2 * s * (upl + (j0 == 0 ? 1 : 2)), st, [&] {
+                    k_lwt_pot2<T><<<gblk, 256, 0, st>>>(XY, pot2G, tab, nd, j0, nb, hermite, j0 == 0, g->geo,
+                                                         1.0 / (double)N);
+                });
+                OFDFT_LAUNCH_CHECK();
+                launches += 1;
+            }
+        }
+        if (kdd > 1) {
+            pot2 = (T*)e->sc.get("pot2", rb);
+            c2r(pot2G, pot2, 1);
+        }
+    }
+
+    // ---- post-pass
+    PostArgs<T> qa;
+    qa.rho = rho;
+    qa.V = Vw;
+    qa.sq = sq;
+    qa.lap = lap;
+    qa.vH = vH;
+    qa.nl1 = nl1;
+    qa.nl2 = nl2;
+    qa.rb = rbp;
+    qa.ra = rap;
+    qa.kf = kfv;
+    qa.pot1 = pot1;
+    qa.pot2 = pot2;
+    qa.pot3 = pot3;
+    qa.N = N;
+    qa.vw = vw;
+    qa.h = h;
+    qa.wt = wt;
+    qa.lwt = lwt && lp.active;
+    qa.same_ab = same_ab;
+    qa.wantV = wantV;
+    qa.kdd = kdd;
+    qa.vw_y = c.vw_y;
+    qa.alpha = alpha;
+    qa.beta = beta;
+    qa.rhomax = rhomax;
+    qa.ld = std::max(0.1, c.lwt_ldw);
+    qa.kfclip = lp.kfclip;
+    {
+        const bool lw = lwt && lp.active;
+        int reads = 1 + wantV + 2 * vw + h + (wt ? 2 + !same_ab * 2 : 0) +
+                    (lw ? 1 + 1 + !same_ab + 1 + (kdd > 1) + (kdd == 3) : 0);
+        double b = Nd * s * (reads + wantV);
+        timed(e, P_POSTPASS, b, st,
+              [&] { k_postpass<T><<<g->red_blocks, RED_THREADS, 0, st>>>(qa, g->d_partials); });
+    }
+    OFDFT_LAUNCH_CHECK();
+    timed(e, P_REDUCE, (double)g->red_blocks * POST_NS * 8, st, [&] {
+        reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, POST_NS, 0ull, g->d_results + 16);
+    });
+    OFDFT_LAUNCH_CHECK();
+    launches += 2;
+    OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 24 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    OFDFT_CK(cudaStreamSynchronize(st));
+    if (e->prof) prof_collect(e);
+    const double* R = g->h_results;
+    const double dV = g->dV;
+    double* E = energies;
+    for (int i = 0; i < OFDFT_NE; ++i) E[i] = 0.0;
+    E[OFDFT_E_TF] = tf ? R[0] * dV * c.tf_x : 0.0;
+    E[OFDFT_E_XC] = xc ? R[1] * dV : 0.0;
+    E[OFDFT_E_PP] = pp ? R[2] * dV : 0.0;
+    E[OFDFT_E_NELEC] = R[3] * dV;
+    E[OFDFT_E_VW] = vw ? R[16] * dV * c.vw_y : 0.0;
+    E[OFDFT_E_H] = h ? R[17] * dV / 2.0 : 0.0;
+    if (wt) E[OFDFT_E_NL] = R[18] * dV;
+    if (lwt) E[OFDFT_E_NL] = lp.active ? R[18] * dV : 0.0;
+    E[OFDFT_E_II] = c.ewald_energy;
+    E[OFDFT_E_TOTAL] = E[OFDFT_E_TF] + E[OFDFT_E_VW] + E[OFDFT_E_NL] + E[OFDFT_E_XC] + E[OFDFT_E_H] + E[OFDFT_E_PP] +
+                       E[OFDFT_E_II];
+    e->last_launches = launches;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ofdft_config_default(ofdft_config* c) {
+    memset(c, 0, sizeof(*c));
+    c->kedf_terms = OFDFT_KE_TF | OFDFT_KE_VW;
+    c->tf_x = 1.0;
+    c->vw_y = 1.0;
+    c->wt_alpha = c->wt_beta = 5.0 / 6.0;
+    c->wt_x = 1.0;
+    c->wt_rho0 = 0.0;
+    c->lwt_alpha = c->lwt_beta = 5.0 / 6.0;
+    c->lwt_x = 1.0;
+    c->lwt_nsp = 0;
+    c->lwt_delta = 0.0;
+    c->lwt_ratio = 1.15;
+    c->lwt_kdd = 3;
+    c->lwt_interp = OFDFT_INTERP_LINEAR;
+    c->lwt_etamax = 50.0;
+    c->lwt_neta = 50000;
+    c->lwt_kfmin = NAN;
+    c->lwt_kfmax = NAN;
+    c->lwt_ldw = 1.0 / 6.0;
+    c->lwt_max_batch = 0;
+    c->xc_lda = 1;
+    c->hartree = 1;
+    c->pseudo = 0;
+    c->ewald_energy = 0.0;
+}
+
+int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) {
+    return guard([&] {
+        OFDFT_REQUIRE(g && cfg && out, "ofdft_eval_create: null argument");
+        const ofdft_config& c = *cfg;
+        OFDFT_REQUIRE(!((c.kedf_terms & OFDFT_KE_WT) && (c.kedf_terms & OFDFT_KE_LWT)),
+                      "only one nonlocal KEDF term at a time");
+        if (c.kedf_terms & OFDFT_KE_LWT) {
+            OFDFT_REQUIRE(c.lwt_kdd >= 1 && c.lwt_kdd <= 3, "lwt_kdd must be 1, 2 or 3");
+            OFDFT_REQUIRE(c.lwt_neta >= 4 && c.lwt_etamax > 0, "bad kernel table size");
+            OFDFT_REQUIRE(c.lwt_interp == OFDFT_INTERP_LINEAR || c.lwt_interp == OFDFT_INTERP_HERMITE,
+                          "lwt_interp must be linear or hermite");
+            OFDFT_REQUIRE(c.lwt_nsp > 0 || c.lwt_delta > 0 || c.lwt_ratio > 1.0, "need nsp, delta or ratio > 1");
+            OFDFT_REQUIRE(c.lwt_nsp != 1, "nsp must be >= 2");
+        }
+        auto* e = new ofdft_eval();
+        e->g = g;
+        e->cfg = c;
+        e->k = make_consts();
+        try {
+            OFDFT_CK(cudaMalloc(&e->wtstate, 8 * sizeof(double)));
+            OFDFT_CK(cudaMemset(e->wtstate, 0, 8 * sizeof(double)));
+            if (c.kedf_terms & OFDFT_KE_LWT) {
+                if (g->prec == OFDFT_F64) build_table<double>(e);
+                else build_table<float>(e);
+                OFDFT_CK(cudaMalloc(&e->d_nodes, 3 * kMaxNodes * sizeof(double)));
+                OFDFT_CK(cudaMallocHost(&e->h_nodes, 3 * kMaxNodes * sizeof(double)));
+            }
+        } catch (...) {
+            ofdft_eval_destroy(e);
+            throw;
+        }
+        *out = e;
+    });
+}
+
+void ofdft_eval_destroy(ofdft_eval* e) {
+    if (!e) return;
+    e->sc.release_all();
+    if (e->vloc) cudaFree(e->vloc);
+    if (e->wtstate) cudaFree(e->wtstate);
+    if (e->tab_c) cudaFree(e->tab_c);
+    if (e->tab_cd) cudaFree(e->tab_cd);
+    if (e->d_nodes) cudaFree(e->d_nodes);
+    if (e->h_nodes) cudaFreeHost(e->h_nodes);
+    for (auto ev : e->evs) cudaEventDestroy(ev);
+    delete e;
+}
+
+int ofdft_eval_set_vloc(ofdft_eval* e, const void* vloc_dev, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && vloc_dev, "ofdft_eval_set_vloc: null argument");
+        if (!e->vloc) OFDFT_CK(cudaMalloc(&e->vloc, e->g->real_bytes()));
+        OFDFT_CK(cudaMemcpyAsync(e->vloc, vloc_dev, e->g->real_bytes(), cudaMemcpyDeviceToDevice, (cudaStream_t)s));
+        e->have_vloc = true;
+    });
+}
+
+int ofdft_eval_set_ewald(ofdft_eval* e, double energy) {
+    return guard([&] {
+        OFDFT_REQUIRE(e, "ofdft_eval_set_ewald: null evaluator");
+        e->cfg.ewald_energy = energy;
+    });
+}
+
+int ofdft_eval_compute(ofdft_eval* e, const void* rho, void* v_out, unsigned calc, double* energies, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && rho && energies, "ofdft_eval_compute: null argument");
+        OFDFT_REQUIRE(calc & (OFDFT_CALC_E | OFDFT_CALC_V), "ofdft_eval_compute: calc must include E or V");
+        if (e->g->prec == OFDFT_F64)
+            compute_t<double>(e, (const double*)rho, (double*)v_out, calc, energies, (cudaStream_t)s);
+        else
+            compute_t<float>(e, (const float*)rho, (float*)v_out, calc, energies, (cudaStream_t)s);
+    });
+}
+
+int ofdft_eval_get_kfbounds(const ofdft_eval* e, double* kfmin, double* kfmax) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && kfmin && kfmax, "ofdft_eval_get_kfbounds: null argument");
+        *kfmin = e->kf_set_min ? e->kf_st_min : NAN;
+        *kfmax = e->kf_set_max ? e->kf_st_max : NAN;
+    });
+}
+
+int ofdft_eval_set_kfbounds(ofdft_eval* e, double kfmin, double kfmax) {
+    return guard([&] {
+        OFDFT_REQUIRE(e, "ofdft_eval_set_kfbounds: null evaluator");
+        e->kf_set_min = !std::isnan(kfmin);
+        e->kf_st_min = kfmin;
+        e->kf_set_max = !std::isnan(kfmax);
+        e->kf_st_max = kfmax;
+    });
+}
+
+int ofdft_eval_profile(ofdft_eval* e, int enable) {
+    return guard([&] {
+        OFDFT_REQUIRE(e, "ofdft_eval_profile: null evaluator");
+        e->prof = enable != 0;
+        for (int i = 0; i < ofdft_eval::kClasses; ++i) {
+            e->prof_ms[i] = 0.0;
+            e->prof_bytes[i] = 0.0;
+            e->prof_launches[i] = 0;
+        }
+        e->rec_cls.clear();
+        e->rec_bytes.clear();
+    });
+}
+
+int ofdft_eval_profile_read(const ofdft_eval* e, int max_classes, double* ms, double* bytes, long long* launches,
+                            int* nclasses) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && nclasses, "ofdft_eval_profile_read: null argument");
+        const int n = std::min(max_classes, (int)ofdft_eval::kClasses);
+        for (int i = 0; i < n; ++i) {
+            if (ms) ms[i] = e->prof_ms[i];
+            if (bytes) bytes[i] = e->prof_bytes[i];
+            if (launches) launches[i] = e->prof_launches[i];
+        }
+        *nclasses = ofdft_eval::kClasses;
+    });
+}
+
+const char* ofdft_profile_class_name(int i) {
+    return (i >= 0 && i < ofdft_eval::kClasses) ? kProfNames[i] : nullptr;
+}
+
+int ofdft_eval_last_stats(const ofdft_eval* e, int* nsp, int* launches) {
+    return guard([&] {
+        OFDFT_REQUIRE(e, "ofdft_eval_last_stats: null evaluator");
+        if (nsp) *nsp = e->last_nsp;
+        if (launches) *launches = e->last_launches;
+    });
+}
+
+}  // extern "C"

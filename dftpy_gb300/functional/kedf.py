@@ -1,0 +1,129 @@
+"""Kinetic energy density functionals on the accelerated path
+(src/dftpy/functional/kedf/__init__.py:27-191): TF, vW, their combinations,
+Wang-Teter (WT) and the density-dependent k_F-node kernel (LWT family with
+the WT kernel table, used for the WGC-style workload)."""
+import copy
+
+import numpy as np
+
+from .. import _lib
+from .abstract_functional import NativeFunctional
+from .functional_output import FunctionalOutput, ZeroFunctional
+
+__all__ = ["KEDF", "KEDFEngines"]
+
+_BITS = {"TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT}
+
+# name -> engines, as the reference's KEDFEngines table (kedf/__init__.py:27-69)
+KEDFEngines = {
+    "NONE": (),
+    "TF": ("TF",),
+    "VW": ("VW",),
+    "X_TF_Y_VW": ("TF", "VW"),
+    "XTFYVW": ("TF", "VW"),
+    "TFVW": ("TF", "VW"),
+    "WT": ("TF", "VW", "WT-NL"),
+    "WT-NL": ("WT-NL",),
+    "LWT": ("TF", "VW", "LWT-NL"),
+    "LWT-NL": ("LWT-NL",),
+}
+
+
+class KEDF(NativeFunctional):
+    """KEDF(name, **options) with the reference's option names: x, y, alpha, beta,
+    rho0 (WT); nsp, delta, ratio, kdd, interp, etamax, neta, kfmin, kfmax, ldw (LWT)."""
+
+    energy_slot = _lib.E_TOTAL
+    out_name = "KEDF"
+
+    def __init__(self, name="WT", kedf=None, **kwargs):
+        self.type = "KEDF"
+        self.name = (kedf or name).upper()
+        if self.name not in KEDFEngines:
+            raise NotImplementedError("KEDF %r is not on the accelerated path (have %s)" % (self.name,
+                                                                                          sorted(KEDFEngines)))
+        self.options = dict(kwargs)
+        self.ke_kernel_saved = {"Kernel": None, "rho0": 0.0, "shape": None, "KernelTable": None, "etamax": None,
+                                "KernelDeriv": None, "MGPKernelE": None, "kfmin": None, "kfmax": None}
+        self.energies = {}
+        self._check_options()
+
+    def _check_options(self):
+        o = self.options
+        if o.get("sigma") is not None:
+            raise NotImplementedError("Gaussian smoothing of the vW term (sigma) is not supported")
+        if o.get("kerneltype", "WT") != "WT":
+            raise NotImplementedError("only the WT kernel table is supported for LWT")
+        if o.get("lumpfactor") is not None:
+            raise NotImplementedError("MGP lump factors are not supported")
+        if o.get("order", 3) != 3:
+            raise NotImplementedError("kernel tables use cubic splines (order=3) only")
+        if o.get("temperature") or o.get("temperature0"):
+            raise NotImplementedError("finite-temperature TF is not supported")
+
+    def engines(self, name=None):
+        return KEDFEngines[(name or self.name).upper()]
+
+    def configure(self, cfg, engines=None):
+        o = self.options
+        for e in (engines if engines is not None else self.engines()):
+            cfg.kedf_terms |= _BITS[e]
+        x = float(o.get("x", 1.0))
+        cfg.tf_x = x
+        cfg.vw_y = float(o.get("y", 1.0))
+        a = float(o.get("alpha", 5.0 / 6.0))
+        b = float(o.get("beta", 5.0 / 6.0))
+        cfg.wt_alpha, cfg.wt_beta, cfg.wt_x = a, b, x
+        rho0 = o.get("rho0")
+        cfg.wt_rho0 = float(rho0) if rho0 else 0.0
+        cfg.lwt_alpha, cfg.lwt_beta, cfg.lwt_x = a, b, x
+        nsp, delta = o.get("nsp"), o.get("delta")
+        cfg.lwt_nsp = int(nsp) if nsp is not None else 0
+        cfg.lwt_delta = float(delta) if (nsp is None and delta is not None) else 0.0
+        cfg.lwt_ratio = float(o.get("ratio", 1.15))
+        cfg.lwt_kdd = int(o.get("kdd", 3))
+        interp = str(o.get("interp", "linear")).lower()
+        if interp == "newton":
+            interp = "linear"
+        if interp not in ("linear", "hermite"):
+            raise NotImplementedError("interp %r is not supported" % interp)
+        cfg.lwt_interp = _lib.INTERP_HERMITE if interp == "hermite" else _lib.INTERP_LINEAR
+        cfg.lwt_etamax = float(o.get("etamax", 50.0))
+        cfg.lwt_neta = int(o.get("neta", 50000))
+        cfg.lwt_kfmin = float("nan") if o.get("kfmin") is None else float(o["kfmin"])
+        cfg.lwt_kfmax = float("nan") if o.get("kfmax") is None else float(o["kfmax"])
+        ldw = o.get("ldw")
+        cfg.lwt_ldw = 1.0 / 6.0 if ldw is None else float(ldw)
+        cfg.lwt_max_batch = int(o.get("max_batch", 0))
+
+    def prepare(self, ev, grid, dtype):
+        s = self.ke_kernel_saved
+        ev.set_kfbounds(s.get("kfmin"), s.get("kfmax"))
+
+    def finish(self, ev):
+        kmin, kmax = ev.kfbounds()
+        self.ke_kernel_saved["kfmin"] = kmin
+        self.ke_kernel_saved["kfmax"] = kmax
+
+    def compute(self, density, calcType={"E", "V"}, name=None, kedf=None, split=False, **kwargs):
+        if kedf:
+            name = kedf
+        engines = self.engines(name)
+        if not engines:
+            return ZeroFunctional.compute(density, calcType=calcType)
+        if not split:
+            if name is None or name.upper() == self.name:
+                return NativeFunctional.compute(self, density, calcType)
+            sub = KEDF(name=name, **self.options)
+            sub.ke_kernel_saved = self.ke_kernel_saved
+            return NativeFunctional.compute(sub, density, calcType)
+        out = {}
+        for e in engines:
+            sub = KEDF(name=e, **self.options)
+            sub.ke_kernel_saved = self.ke_kernel_saved
+            r = NativeFunctional.compute(sub, density, calcType)
+            r.name = e
+            out[e] = r
+            if "E" in calcType:
+                self.energies[e] = r.energy
+        return out

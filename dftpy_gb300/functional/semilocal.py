@@ -1,0 +1,72 @@
+"""XC (built-in LDA, src/dftpy/functional/xc/__init__.py:9-69 and
+xc/semilocal_xc.py:283-341) and Hartree (src/dftpy/functional/hartree.py:11-45)."""
+from .. import _lib
+from .abstract_functional import NativeFunctional
+
+__all__ = ["XC", "Hartree"]
+
+
+class XC(NativeFunctional):
+    """Exchange-correlation: the reference's built-in LDA (Slater exchange +
+    Perdew-Zunger 81 correlation, unpolarised)."""
+
+    energy_slot = _lib.E_TOTAL
+    out_name = "XC"
+
+    def __init__(self, xc=None, core_density=None, libxc=None, name=None, pseudo=None, **kwargs):
+        xc = xc or name
+        if not xc and not libxc:
+            raise ValueError("Please give a 'xc' or 'libxc'.")
+        if isinstance(libxc, (list, tuple, str)) and not xc:
+            names = [libxc] if isinstance(libxc, str) else list(libxc)
+            if sorted(n.lower() for n in names) == ["lda_c_pz", "lda_x"]:
+                xc = "LDA"
+        if not xc or xc.upper() != "LDA":
+            raise NotImplementedError("only the built-in LDA is on the accelerated path (got %r)" % (xc or libxc))
+        if core_density is not None:
+            raise NotImplementedError("non-linear core corrections are not supported")
+        self.type = "XC"
+        self.name = "LDA"
+        self.options = dict(kwargs)
+        self.pseudo = pseudo
+        self.energy = None
+
+    def configure(self, cfg):
+        cfg.xc_lda = 1
+
+    def compute(self, density, calcType={"E", "V"}, **kwargs):
+        out = NativeFunctional.compute(self, density, calcType)
+        if "E" in calcType:
+            self.energy = out.energy
+        return out
+
+    def forces(self, density, pseudo=None, **kwargs):
+        """NLCC forces: zero without core densities (xc/__init__.py:71-78)."""
+        return None
+
+
+class Hartree(NativeFunctional):
+    energy_slot = _lib.E_TOTAL
+    out_name = "Hartree"
+    _energy = None
+
+    def __init__(self, **kwargs):
+        self.type = "HARTREE"
+        self.name = "HARTREE"
+        self.options = kwargs
+
+    def __repr__(self):
+        return "HARTREE"
+
+    def configure(self, cfg):
+        cfg.hartree = 1
+
+    def compute(self, density, calcType={"E", "V"}, **kwargs):
+        out = NativeFunctional.compute(self, density, calcType)
+        if "E" in calcType:
+            Hartree._energy = out.energy
+        return out
+
+    @property
+    def energy(self):
+        return self._energy

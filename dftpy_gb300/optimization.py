@@ -1,0 +1,104 @@
+"""Density optimisation (src/dftpy/optimization/optimization.py:31-547).
+
+``Optimization.optimize_rho`` runs entirely in the native library: the
+direction (TN finite-difference Hessian CG, L-BFGS two-loop or CG-HS), the
+norm-conserving rotation phi cos(theta) + p sin(theta), the MINPACK-2 line
+search and every field operation stay on the device; only scalars cross to
+the host.
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .field import DirectField, as_field
+from .functional.abstract_functional import NativeFunctional, stream_ptr
+from .functional.total_functional import TotalFunctional
+
+__all__ = ["Optimization"]
+
+_METHODS = {"TN": _lib.OPT_TN, "LBFGS": _lib.OPT_LBFGS, "CG-HS": _lib.OPT_CGHS, "CG": _lib.OPT_CGHS}
+
+
+class Optimization:
+    def __init__(self, optimization_method="CG-HS", optimization_options=None, EnergyEvaluator=None, guess_rho=None):
+        self.rho = guess_rho
+        self.optimization_options = dict(optimization_options or {})
+        defaults = {"maxcor": 6, "ftol": 1.0e-7, "xtol": 1.0e-12, "maxfun": 50, "maxiter": 200, "maxls": 30,
+                    "econv": 1.0e-5, "c1": 1e-4, "c2": 0.2, "algorithm": "EMM", "vector": "Orthogonalization",
+                    "ncheck": 2, "h0": 1.0}
+        for k, v in defaults.items():
+            self.optimization_options.setdefault(k, v)
+        if EnergyEvaluator is None:
+            raise AttributeError("Must provide an energy evaluator")
+        self.EnergyEvaluator = EnergyEvaluator
+        if optimization_method not in _METHODS:
+            raise NotImplementedError("optimisation method %r is not on the accelerated path (have %s)"
+                                      % (optimization_method, sorted(_METHODS)))
+        o = self.optimization_options
+        if o["algorithm"] != "EMM" or o["vector"] != "Orthogonalization":
+            raise NotImplementedError("only algorithm='EMM' with vector='Orthogonalization' is supported")
+        self.optimization_method = optimization_method
+        self.verbose = False
+        self.mu = None
+        self.converged = None
+        self.phi = None
+        self.functional = None
+        self.result = None
+
+    def _total(self):
+        ev = self.EnergyEvaluator
+        if isinstance(ev, TotalFunctional):
+            if not ev._fusable():
+                raise NotImplementedError("the energy evaluator's functionals cannot be fused on the device")
+            return ev
+        if isinstance(ev, NativeFunctional):
+            return TotalFunctional(F=ev)
+        raise NotImplementedError("the energy evaluator must be built from dftpy_gb300 functionals")
+
+    def options_struct(self):
+        o = self.optimization_options
+        s = _lib.OptOptions()
+        _lib.load().ofdft_opt_default(_lib.C.byref(s))
+        s.method = _METHODS[self.optimization_method]
+        s.maxiter, s.maxfun, s.maxls = int(o["maxiter"]), int(o["maxfun"]), int(o["maxls"])
+        s.ncheck, s.maxcor = int(o["ncheck"]), int(o["maxcor"])
+        s.econv = float(o["econv"]) if o["econv"] is not None else 0.0
+        s.c1, s.c2, s.xtol = float(o["c1"]), float(o["c2"]), float(o["xtol"])
+        s.h0 = float(o["h0"]) if o["h0"] else 0.0
+        s.verbose = 1 if self.verbose else 0
+        return s
+
+    def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False, lsfun="line_search", dtype=None):
+        if guess_rho is None and self.rho is None:
+            raise AttributeError("Must provide a guess density")
+        if guess_rho is not None:
+            self.rho = guess_rho
+        if guess_phi is not None:
+            raise NotImplementedError("guess_phi is not supported")
+        total = self._total()
+        rho0 = self.rho
+        grid = rho0.grid if isinstance(rho0, DirectField) else next(
+            f.grid for f in total.funcDict.values() if getattr(f, "grid", None) is not None)
+        rho = DirectField(grid, data=rho0, dtype=dtype or (rho0.dtype if isinstance(rho0, torch.Tensor)
+                                                           else torch.float64)).clone()
+        ev = total.evaluator(grid, rho.dtype)
+        total.prepare(ev, grid, rho.dtype)
+        res = _lib.OptResult()
+        opts = self.options_struct()
+        t = rho.as_subclass(torch.Tensor)
+        _lib.check(_lib.load().ofdft_optimize(ev.h, _lib.C.c_void_p(t.data_ptr()), _lib.C.byref(opts),
+                                              _lib.C.byref(res), stream_ptr()))
+        total.finish(ev)
+        rho._N = None
+        self.result = res
+        self.converged = res.converged
+        self.mu = res.mu
+        self.rho = rho
+        self.phi = torch.sqrt(rho)
+        self.functional = total(rho, calcType={"E", "V"})
+        return rho
+
+    def __call__(self, guess_rho=None, calcType={"E", "V"}, guess_phi=None, lphi=False):
+        return self.optimize_rho(guess_rho=guess_rho, guess_phi=guess_phi, lphi=lphi)

@@ -1,0 +1,193 @@
+/*
+ * ofdft.h -- C ABI of the GB300 (sm_103a) orbital-free DFT hot path.
+ *
+ * A drop-in device backend for the energy + potential (E+V) evaluation of
+ * DFTpy's total density functional and the density optimisation built on it.
+ * Every entry point is extern "C", takes plain pointers, sizes and a CUDA
+ * stream, returns an int status (0 = OK) and never throws.  Device pointers
+ * are caller-owned (the Python layer passes torch CUDA tensors); handles own
+ * cuFFT plans, tables and scratch.  A handle is not thread-safe: use one per
+ * host thread / stream.  On error, ofdft_last_error() returns a message.
+ *
+ * Units are atomic (Hartree, Bohr); densities in e/Bohr^3.  Real fields are
+ * C-ordered (n0, n1, n2) arrays; reciprocal fields are the half-complex
+ * (n0, n1, n2/2+1) arrays of an R2C transform (the reference's default
+ * "gfull=False" grid).  Precision OFDFT_F64 computes in float64 throughout;
+ * OFDFT_F32 ("FP32-mixed") stores grids and runs FFTs and pointwise work in
+ * float32 while every energy / electron-count reduction accumulates in float64.
+ *
+ * Reference interfaces each group replaces are cited as
+ * path:line within Quantum-MultiScale/DFTpy.
+ */
+#ifndef OFDFT_H
+#define OFDFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ofdft_grid ofdft_grid;         /* grid + FFT plans + scratch   */
+typedef struct ofdft_eval ofdft_eval;         /* configured total functional  */
+typedef void* ofdft_stream;                   /* a cudaStream_t (NULL = legacy default) */
+
+enum { OFDFT_OK = 0, OFDFT_EINVAL = 1, OFDFT_ECUDA = 2, OFDFT_ECUFFT = 3, OFDFT_ENOMEM = 4,
+       OFDFT_ESTATE = 5 };
+enum { OFDFT_F64 = 0, OFDFT_F32 = 1 };
+enum { OFDFT_CALC_E = 1, OFDFT_CALC_V = 2 };
+
+/* energy slots written by ofdft_eval_compute (Hartree) */
+enum { OFDFT_E_TF = 0, OFDFT_E_VW, OFDFT_E_NL, OFDFT_E_XC, OFDFT_E_H, OFDFT_E_PP, OFDFT_E_II,
+       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_NE };
+
+/* ---------------------------------------------------------------- errors */
+const char* ofdft_last_error(void);
+const char* ofdft_version(void);
+
+/* ------------------------------------------------------------------ grid
+ * DirectGrid / ReciprocalGrid (src/dftpy/grid.py:8-60, :384-415, :480-620):
+ * lattice rows are the lattice vectors (Bohr).  G vectors are computed from
+ * the index and the reciprocal lattice on the fly, never stored. */
+int ofdft_grid_create(const int nr[3], const double lattice[9], int precision, ofdft_grid** out);
+void ofdft_grid_destroy(ofdft_grid* g);
+int ofdft_grid_info(const ofdft_grid* g, int nr[3], double* volume, double* dV, int* precision);
+
+/* DirectField.fft (src/dftpy/field.py:413-430): out = rfftn(in) * dV.
+ * ReciprocalField.ifft (field.py:779-804): out = irfftn(in) / dV.  The input of
+ * ofdft_ifft is not modified (it is copied to scratch first). */
+int ofdft_fft(ofdft_grid* g, const void* in_real, void* out_cplx, ofdft_stream s);
+int ofdft_ifft(ofdft_grid* g, const void* in_cplx, void* out_real, ofdft_stream s);
+
+/* Reductions over a real field in float64 with a fixed summation order
+ * (mp.einsum/vsum, src/dftpy/mpi/mpi.py:199-246).  out[0] = sum(a*b) (b may be
+ * NULL: sum(a)).  ofdft_dot3: sum(a*b*c). */
+int ofdft_dot(ofdft_grid* g, const void* a, const void* b, double* out, ofdft_stream s);
+int ofdft_dot3(ofdft_grid* g, const void* a, const void* b, const void* c, double* out, ofdft_stream s);
+
+/* ------------------------------------------------------ total functional
+ * Configuration of the terms of TotalFunctional (src/dftpy/functional/
+ * total_functional.py:49-146) and the KEDF dispatcher (kedf/__init__.py:27-69,
+ * :124-191).  kedf_terms is a bit set of OFDFT_KE_*. */
+enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8 };
+enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
+
+typedef struct {
+    int    kedf_terms;
+    double tf_x;              /* TF prefactor x (kedf/tf.py:66)                    */
+    double vw_y;              /* vW prefactor y (kedf/vw.py:115)                   */
+    /* Wang-Teter nonlocal term (kedf/wt.py:109-132, kernel.py:325-334)           */
+    double wt_alpha, wt_beta, wt_x;
+    double wt_rho0;           /* <= 0: mean density of each call (wt.py:112-113)   */
+    /* density-dependent kernel table, LWT family (kedf/lwt.py:82-341, :502-568)  */
+    double lwt_alpha, lwt_beta, lwt_x;
+    int    lwt_nsp;           /* > 0: nsp uniform nodes (lwt.py:174-181)          */
+    double lwt_delta;         /* > 0 and nsp <= 0: node spacing (lwt.py:182-184)  */
+    double lwt_ratio;         /* otherwise: geometric node ratio (lwt.py:185-188) */
+    int    lwt_kdd;           /* 1, 2 or 3 (derivative terms kept)                */
+    int    lwt_interp;        /* OFDFT_INTERP_*                                   */
+    double lwt_etamax;        /* table range (default 50)                         */
+    int    lwt_neta;          /* table points (default 50000)                     */
+    double lwt_kfmin, lwt_kfmax; /* fixed k_F bounds, or NaN for the adaptive rule */
+    double lwt_ldw;           /* low-density weight exponent (default 1/6)        */
+    int    lwt_max_batch;     /* nodes per batched FFT pass (0 = automatic)       */
+    int    xc_lda;            /* built-in LDA, Slater + PZ81 (xc/semilocal_xc.py:283-341) */
+    int    hartree;           /* Hartree (functional/hartree.py:24-45)             */
+    int    pseudo;            /* add the local pseudopotential set by ofdft_eval_set_vloc */
+    double ewald_energy;      /* ion-ion energy added to the total (0 = none)     */
+} ofdft_config;
+
+void ofdft_config_default(ofdft_config* c);
+
+int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out);
+void ofdft_eval_destroy(ofdft_eval* e);
+/* Copy a real-space local pseudopotential (device pointer, grid precision) into
+ * the evaluator (LocalPseudo._vreal, src/dftpy/functional/pseudo/__init__.py:219-234). */
+int ofdft_eval_set_vloc(ofdft_eval* e, const void* vloc_dev, ofdft_stream s);
+int ofdft_eval_set_ewald(ofdft_eval* e, double energy);
+
+/* TotalFunctional.compute(rho, calcType) (total_functional.py:107-146).
+ * rho: device field (not modified).  v_out: device field for the total
+ * potential (required with OFDFT_CALC_V, may be NULL otherwise).  energies:
+ * host array of OFDFT_NE doubles (per-term energies, total, electron count). */
+int ofdft_eval_compute(ofdft_eval* e, const void* rho, void* v_out, unsigned calc,
+                       double* energies, ofdft_stream s);
+
+/* Stateful parts of the evaluator that persist across calls like the
+ * reference's ke_kernel_saved (kedf/__init__.py:101-111): the k_F bound state
+ * of the LWT rule (kedf/lwt.py:36-79).  get/set allow checkpoint and restore. */
+int ofdft_eval_get_kfbounds(const ofdft_eval* e, double* kfmin, double* kfmax);
+int ofdft_eval_set_kfbounds(ofdft_eval* e, double kfmin, double kfmax);
+/* kernel time accounting of the last compute: nodes used, kernel launches */
+int ofdft_eval_last_stats(const ofdft_eval* e, int* nsp, int* launches);
+
+/* Per-kernel-class profiling with CUDA events recorded on the compute stream
+ * around each launch (no counterpart in the reference, which times whole
+ * calls with wall clocks in src/dftpy/time_data.py:94-122).  While enabled,
+ * every compute accumulates, per class, the summed event time (ms), the
+ * algorithmic bytes the launches must move, and the launch count.
+ * ofdft_profile_class_name(i) names class i (NULL past the last class). */
+int ofdft_eval_profile(ofdft_eval* e, int enable);
+int ofdft_eval_profile_read(const ofdft_eval* e, int max_classes, double* ms, double* bytes, long long* launches,
+                            int* nclasses);
+const char* ofdft_profile_class_name(int i);
+
+/* ------------------------------------------------- local pseudopotential
+ * LocalPseudo (src/dftpy/functional/pseudo/__init__.py:74-452, :505-571).
+ * Radial tables per species: v(q) on a uniform grid gp[0..npts-1] (gp[0]=0),
+ * as read from a recpot file (recpot.py:11-42).  positions: nat x 3 Cartesian
+ * (Bohr).  species: per-atom index into the tables. */
+typedef struct ofdft_pseudo ofdft_pseudo;
+
+int ofdft_pseudo_create(ofdft_grid* g, int nspecies, const int* npts, const double* const* gp,
+                        const double* const* vp, int pme, int bspline_order, ofdft_pseudo** out);
+void ofdft_pseudo_destroy(ofdft_pseudo* p);
+int ofdft_pseudo_set_ions(ofdft_pseudo* p, int nat, const double* pos, const int* species);
+/* v_loc(r) on the grid (LocalPseudo.local_PP, :237-246): PME (:437-452) or exact (:425-435) */
+int ofdft_pseudo_vloc(ofdft_pseudo* p, void* vreal_out, ofdft_stream s);
+/* LocalPseudo.forces (:260-270): PME (_ForcePME :523-571) or exact (_Force :505-521) */
+int ofdft_pseudo_forces(ofdft_pseudo* p, const void* rho, double* forces, ofdft_stream s);
+
+/* ---------------------------------------------------------------- Ewald
+ * ewald (src/dftpy/ewald.py:197-864): eta from Get_Best_eta (:256-278),
+ * real-space erfc sum on a cell list, reciprocal part by PME (B-spline
+ * order) or exact structure factors, and the G=0 / self corrections.
+ * out_energy: [total, real, reciprocal, correction]; forces nat x 3 (may be NULL). */
+int ofdft_ewald(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision,
+                int pme, int bspline_order, double* out_energy, double* forces, double* out_eta,
+                ofdft_stream s);
+
+/* ----------------------------------------------------------- optimiser
+ * Optimization.optimize_rho (src/dftpy/optimization/optimization.py:283-525):
+ * direct minimisation on phi = sqrt(rho) with the norm-conserving rotation
+ * phi cos(theta) + p sin(theta), directions TN / LBFGS / CG-HS, and the
+ * MINPACK-2 (More-Thuente) line search of scipy's line_search_wolfe1
+ * (math_utils.py:37-52).  rho is overwritten with the optimised density. */
+enum { OFDFT_OPT_TN = 0, OFDFT_OPT_LBFGS = 1, OFDFT_OPT_CGHS = 2 };
+typedef struct {
+    int method, maxiter, maxfun, maxls, ncheck, maxcor;
+    double econv, c1, c2, xtol, h0;
+    int verbose;
+} ofdft_opt_options;
+typedef struct {
+    int converged;            /* 0 converged, 1 line search failed, 2 max steps (optimization.py:444-516) */
+    int niter, nfev;
+    double energy, mu, dP;
+} ofdft_opt_result;
+
+void ofdft_opt_default(ofdft_opt_options* o);
+int ofdft_optimize(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r,
+                   ofdft_stream s);
+
+/* The scalar MINPACK-2 line search on a host callback, exposed for testing
+ * against scipy.optimize line_search_wolfe1 (scalar_search_wolfe1). */
+typedef int (*ofdft_phi_fn)(double alpha, double* f, double* g, void* ctx);
+int ofdft_linesearch(ofdft_phi_fn fn, void* ctx, double f0, double g0, double stp0, double c1, double c2,
+                     double amax, double amin, double xtol, int maxiter, double* stp_out, double* f_out,
+                     double* g_out, int* nfev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OFDFT_H */

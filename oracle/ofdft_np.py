@@ -119,13 +119,29 @@ class Grid:
         return np.pi ** 2 / (2 * spacing.max() ** 2)
 
 
+_FFT_WORKERS = None
+
+
+def set_fft_workers(n):
+    """Run the oracle's FFTs on n threads (scipy.fft) instead of numpy's single
+    thread; the transforms are the same pocketfft algorithm."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = n
+
+
 def fft(f, grid):
     """DirectField.fft: rfftn times dV (field.py:413-430)."""
+    if _FFT_WORKERS:
+        import scipy.fft as sfft
+        return sfft.rfftn(f, workers=_FFT_WORKERS) * grid.dV
     return np.fft.rfftn(f) * grid.dV
 
 
 def ifft(F, grid):
     """ReciprocalField.ifft(force_real=True): irfftn / dV (field.py:779-804)."""
+    if _FFT_WORKERS:
+        import scipy.fft as sfft
+        return sfft.irfftn(F, s=tuple(grid.nr), axes=(0, 1, 2), workers=_FFT_WORKERS) / grid.dV
     return np.fft.irfftn(F, s=tuple(grid.nr), axes=(0, 1, 2)) / grid.dV
 
 
@@ -407,9 +423,23 @@ class LWT:
         deriv = splev(eta, self.tck, der=1) * (-1.0 * eta)
         self.tckD = splrep(eta, deriv, k=self.order)
 
-    def __call__(self, rho, grid, calc=("E", "V")):
+    def timed_sample(self, rho, grid, intervals=1):
+        """Wall time of one E+V split into the part outside the node-interval loop
+        and the mean time of one interval, running only ``intervals`` of them
+        (a bounded sample of a full evaluation for CPU baselines)."""
+        import time
+        timing = {}
+        t0 = time.perf_counter()
+        self(rho, grid, ("E", "V"), max_intervals=intervals, timing=timing)
+        total = time.perf_counter() - t0
+        loop = timing.get("loop", 0.0)
+        n = max(1, timing.get("intervals", 1))
+        return total - loop, loop / n
+
+    def __call__(self, rho, grid, calc=("E", "V"), max_intervals=None, timing=None):
         """LWTPotentialEnergy (lwt.py:82-341), streamed interval by interval like the
-        reference so that memory stays O(grid)."""
+        reference so that memory stays O(grid).  ``max_intervals``/``timing`` only
+        serve timed samples (the result is then incomplete)."""
         alpha, beta = self.alpha, self.beta
         q = grid.q
         kf = 2.0 * np.cbrt(3.0 * np.pi ** 2 * rho)                     # lwt.py:106
@@ -459,7 +489,10 @@ class LWT:
         pot1[small] = p0[small] * t[small]
         if kdd > 1:
             pot2G = K0 * fft(rA * np.where(small, t, 0.0), grid)
-        for i in range(nsp - 1):                                      # lwt.py:213-306
+        import time as _time
+        _tl = _time.perf_counter()
+        n_run = nsp - 1 if max_intervals is None else min(nsp - 1, max_intervals)
+        for i in range(n_run):                                        # lwt.py:213-306
             K1, p1, KD1, m1 = node(i + 1)
             m = np.logical_and(kf > kfl[i], kf < kfl[i + 1] + 1e-18)
             u = np.where(m, rA, 0.0)
@@ -491,6 +524,9 @@ class LWT:
                         h11D = 3.0 * t2m - 2 * tm
                         pot3[m] = (h00D * p0[m] + h01D * p1[m]) / Dkf + h10D * m0[m] + h11D * m1[m]
             K0, p0, KD0, m0 = K1, p1, KD1, m1
+        if timing is not None:
+            timing["loop"] = _time.perf_counter() - _tl
+            timing["intervals"] = n_run
         if vcalc:
             pot2 = ifft(pot2G, grid) if pot2G is not None else pot1.copy()
         ldw = 1.0 / 6.0 if self.ldw is None else self.ldw            # lwt.py:315-322

@@ -1,0 +1,249 @@
+"""GPU parity of the CUDA path against the reference's golden vectors and the
+numpy oracle.  Bars (FP64): energy within 1e-10 relative (per atom scale),
+potential within 1e-9 a.u. max-abs, forces within 1e-9 Ha/Bohr."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+import dftpy_gb300 as D
+from dftpy_gb300 import synthetic as syn
+from oracle import ofdft_np as O
+
+WGC = dict(alpha=(5 + np.sqrt(5)) / 6, beta=(5 - np.sqrt(5)) / 6)
+E_RTOL = 1e-10
+V_ATOL = 1e-9
+F_ATOL = 1e-9
+
+
+def e_close(a, b, scale=1.0):
+    assert abs(a - b) <= E_RTOL * max(scale, abs(b)), (a, b, a - b)
+
+
+def v_close(v, ref, atol=V_ATOL):
+    v = v.numpy() if hasattr(v, "numpy") else np.asarray(v)
+    err = float(np.abs(v - ref).max())
+    assert err <= atol * max(1.0, float(np.abs(ref).max())), err
+
+
+def _pp(g):
+    return D.functional.RECPOT(r=g["recpot_gp"], v=g["recpot_vp"], zval=int(g["recpot_zval"]))
+
+
+def _setup(g, pre):
+    grid = D.DirectGrid(g[pre + "lattice"], g[pre + "nr"])
+    rho = D.DirectField(grid, data=g[pre + "rho"])
+    return grid, rho
+
+
+@pytest.mark.parametrize("pre", ["A_", "B_"])
+def test_local_and_fft_terms(golden, pre):
+    grid, rho = _setup(golden, pre)
+    funcs = {"TF": D.Functional(type="KEDF", name="TF"), "VW": D.Functional(type="KEDF", name="VW"),
+             "WTNL": D.Functional(type="KEDF", name="WT-NL"), "XC": D.Functional(type="XC", name="LDA"),
+             "H": D.Functional(type="HARTREE")}
+    if pre == "A_":
+        ions = D.Ions(symbols=["Al"] * 4, positions=golden["A_pos"], cell=golden["A_lattice"])
+        funcs["PPPME"] = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(golden)}, PME=True)
+        funcs["PPEX"] = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(golden)}, PME=False)
+    for k, f in funcs.items():
+        out = f(rho)
+        e_close(out.energy, float(golden[pre + "E_" + k]))
+        v_close(out.potential, golden[pre + "V_" + k])
+
+
+@pytest.mark.parametrize("tag,kw", [
+    ("A_LWT64", dict(nsp=64, kdd=3, interp="linear", **WGC)),
+    ("A_LWT8H", dict(nsp=8, kdd=3, interp="hermite", **WGC)),
+    ("A_LWTR", dict(ratio=1.15, kdd=3, interp="linear")),
+    ("A_LWT8K1", dict(nsp=8, kdd=1, interp="linear", **WGC)),
+    ("B_LWT16", dict(nsp=16, kdd=3, interp="linear", **WGC)),
+    ("B_LWT6H", dict(nsp=6, kdd=3, interp="hermite")),
+])
+def test_density_dependent_kernel(golden, tag, kw):
+    pre = tag[:2]
+    grid, rho = _setup(golden, pre)
+    out = D.Functional(type="KEDF", name="LWT-NL", **kw)(rho)
+    e_close(out.energy, float(golden[pre + "E_" + tag[2:]]))
+    v_close(out.potential, golden[pre + "V_" + tag[2:]])
+
+
+def test_density_dependent_kernel_batches(golden):
+    """Node batching (several batched FFT passes) gives the same result as one pass."""
+    grid, rho = _setup(golden, "A_")
+    ref = D.Functional(type="KEDF", name="LWT-NL", nsp=64, kdd=3, **WGC)(rho)
+    for b in (1, 7, 64):
+        out = D.Functional(type="KEDF", name="LWT-NL", nsp=64, kdd=3, max_batch=b, **WGC)(rho)
+        e_close(out.energy, ref.energy)
+        v_close(out.potential, ref.potential.numpy(), atol=1e-12)
+
+
+def test_pp_forces(golden):
+    g = golden
+    grid, rho = _setup(g, "A_")
+    ions = D.Ions(symbols=["Al"] * 4, positions=g["A_pos"], cell=g["A_lattice"])
+    for pme, key in ((True, "A_F_PPPME"), (False, "A_F_PPEX")):
+        pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(g)}, PME=pme)
+        np.testing.assert_allclose(pp.forces(rho), g[key], rtol=0, atol=F_ATOL)
+
+
+def test_ewald(golden):
+    g = golden
+    grid, _ = _setup(g, "A_")
+    ions = D.Ions(symbols=["Al"] * 4, positions=g["A_pos"], cell=g["A_lattice"], charges=3.0)
+    ew = D.ewald(ions=ions, grid=grid, PME=True)
+    e_close(ew.energy, float(g["A_ewald_E"]))
+    assert abs(ew.eta - float(g["A_ewald_eta"])) < 1e-12
+    e_close(ew.Energy_corr(), float(g["A_ewald_Ecorr"]))
+    e_close(ew.Energy_rec(), float(g["A_ewald_Erec"]))
+    np.testing.assert_allclose(ew.forces, g["A_ewald_F"], rtol=0, atol=F_ATOL)
+    ex = D.ewald(ions=ions, grid=grid, PME=False)
+    e_close(ex.energy, float(g["A_ewaldex_E"]))
+    np.testing.assert_allclose(ex.forces, g["A_ewaldex_F"], rtol=0, atol=F_ATOL)
+
+
+def test_two_species_wt_system(golden):
+    g = golden
+    grid, rho = _setup(g, "D_")
+    sp = g["D_species"]
+    sym = ["Al" if s == 0 else "Mg" for s in sp]
+    ions = D.Ions(symbols=sym, positions=g["D_pos"], cell=g["D_lattice"])
+    gb, vb = syn.analytic_vloc(2.0, 1.2)
+    with tempfile.TemporaryDirectory() as d:
+        fn = os.path.join(d, "Mg.recpot")
+        D.write_recpot(fn, gb[-1], vb)
+        pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(g), "Mg": fn}, PME=True)
+    e_close(pp(rho).energy, float(g["D_E_PP"]))
+    np.testing.assert_allclose(pp.forces(rho), g["D_F_PP"], rtol=0, atol=F_ATOL)
+    ew = pp.get_ewald()
+    e_close(ew.energy, float(g["D_ewald_E"]))
+    np.testing.assert_allclose(ew.forces, g["D_ewald_F"], rtol=0, atol=F_ATOL)
+    e_close(D.Functional(type="KEDF", name="WT")(rho).energy, float(g["D_E_WT"]))
+
+
+def test_reference_fixture(golden):
+    """The reference's own Al_fde_rho.pp fixture (examples/test/test_functional.py:23-27)."""
+    g = golden
+    grid, rho = _setup(g, "E_")
+    e_close(D.Functional(type="KEDF", name="WT")(rho).energy, float(g["E_E_WT"]))
+    ions = D.Ions(symbols=["Al"] * len(g["E_pos"]), positions=g["E_pos"], cell=g["E_lattice"])
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(
+        r=g["E_pp_al_gp"], v=g["E_pp_al_vp"], zval=int(g["E_pp_al_zval"]))}, PME=True)
+    e_close(pp(rho).energy, float(g["E_E_PP_allda"]))
+    assert np.isclose(pp(rho).energy, 1.3497046, atol=1e-4)
+    ew = pp.get_ewald()
+    e_close(ew.energy, float(g["E_ewald_E"]))
+    assert np.isclose(ew.Energy_corr(), -13.003839613564997, atol=1e-5)
+    assert np.isclose(ew.Energy_rec(), 7.606943756474895, atol=1e-5)
+    np.testing.assert_allclose(ew.forces, g["E_ewald_F"], rtol=0, atol=F_ATOL)
+
+
+def _c1(golden, kedf="TFVW", dtype=torch.float64):
+    lat, pos = syn.fcc_cell(7.60)
+    grid = D.DirectGrid(lat, (32, 32, 32))
+    ions = D.Ions(symbols=["Al"] * 4, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(golden)}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name=kedf),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    rho0 = D.DirectField(grid, dtype=dtype) + 12.0 / grid.volume
+    return grid, tot, rho0
+
+
+def test_fused_total_matches_sum_and_oracle(golden):
+    g = golden
+    grid, rho = _setup(g, "A_")
+    ions = D.Ions(symbols=["Al"] * 4, positions=g["A_pos"], cell=g["A_lattice"])
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(g)}, PME=True)
+    funcs = dict(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                 XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+    tot = D.TotalFunctional(**funcs)
+    out = tot(rho)
+    parts = tot(rho, split=True)
+    e_close(out.energy, parts["TOTAL"].energy)
+    v_close(out.potential, parts["TOTAL"].potential.numpy(), atol=1e-12)
+    e_ref = sum(float(g["A_E_" + k]) for k in ("TF", "VW", "WTNL", "XC", "H", "PPPME")) + float(g["A_ewald_E"])
+    e_close(out.energy, e_ref, scale=4.0)
+    v_ref = sum(g["A_V_" + k] for k in ("TF", "VW", "WTNL", "XC", "H", "PPPME"))
+    v_close(out.potential, v_ref)
+    # forces: PP + Ewald
+    F = tot.get_forces(rho)
+    np.testing.assert_allclose(F, g["A_F_PPPME"] + g["A_ewald_F"], rtol=0, atol=F_ATOL)
+
+
+@pytest.mark.parametrize("method", ["TN", "LBFGS", "CG-HS"])
+def test_optimizer_ground_state(golden, method):
+    grid, tot, rho0 = _c1(golden)
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method,
+                         optimization_options={"econv": 1e-11 * 4, "maxiter": 60, "maxfun": 50})
+    rho = opt.optimize_rho(guess_rho=rho0)
+    tag = "C_" + method.replace("-", "") + "_"
+    assert opt.converged == 0
+    e_close(tot.Energy(rho), float(golden[tag + "E"]), scale=4.0)
+    assert abs(opt.mu - float(golden[tag + "mu"])) < 1e-6 * abs(float(golden[tag + "mu"]))
+    assert abs(rho.integral() - 12.0) < 1e-10
+    if method == "TN":
+        np.testing.assert_allclose(rho.numpy(), golden["C_TN_rho"], rtol=2e-6, atol=0)
+        np.testing.assert_allclose(tot.get_forces(rho), golden["C_F_PP"] + golden["C_ewald_F"], rtol=0, atol=1e-6)
+
+
+def test_fft_conventions():
+    lat = np.diag([5.0, 6.0, 7.0]) + 0.3
+    grid = D.DirectGrid(lat, (12, 10, 14))
+    x = np.random.default_rng(0).normal(size=(12, 10, 14))
+    f = D.DirectField(grid, data=x)
+    F = f.fft()
+    np.testing.assert_allclose(F.numpy(), np.fft.rfftn(x) * grid.dV, rtol=1e-13, atol=1e-13)
+    back = F.ifft()
+    np.testing.assert_allclose(back.numpy(), x, rtol=0, atol=1e-13)
+    assert abs(f.integral() - x.sum() * grid.dV) < 1e-12 * abs(x).sum()
+
+
+def test_repeatable_bitwise(golden):
+    grid, rho = _setup(golden, "A_")
+    f = D.Functional(type="KEDF", name="LWT-NL", nsp=32, kdd=3, **WGC)
+    a = f(rho)
+    b = f(rho)
+    assert a.energy == b.energy
+    assert torch.equal(a.potential.as_subclass(torch.Tensor), b.potential.as_subclass(torch.Tensor))
+
+
+def test_mixed_precision_errors(golden):
+    """FP32 grids/FFTs with FP64 reductions against the FP64 path."""
+    g = golden
+    grid, rho = _setup(g, "A_")
+    ions = D.Ions(symbols=["Al"] * 4, positions=g["A_pos"], cell=g["A_lattice"])
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(g)}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="LWT", nsp=16, **WGC),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    o64 = tot(rho)
+    o32 = tot(D.DirectField(grid, data=g["A_rho"], dtype=torch.float32))
+    assert abs(o32.energy - o64.energy) / 4 < 2e-5
+    dv = float((o32.potential.as_subclass(torch.Tensor).double() - o64.potential.as_subclass(torch.Tensor)).abs().max())
+    assert dv < 1e-4 * float(o64.potential.abs().max())
+
+
+def test_gradient_consistency_128(golden):
+    """Size-independent check at 128^3 (256-atom WT system): the potential is the
+    functional derivative, (E(rho+h d) - E(rho-h d))/2h = int V d."""
+    lat, pos = syn.fcc_supercell(7.6, 4, sigma=0.1, seed=3)
+    grid = D.DirectGrid(lat, (128, 128, 128))
+    ions = D.Ions(symbols=["Al"] * len(pos), positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(golden)}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    rho = D.DirectField(grid, data=syn.smooth_density(lat, (128, 128, 128), 768.0, seed=4, amp=0.3))
+    d = D.DirectField(grid, data=syn.smooth_density(lat, (128, 128, 128), 1.0, seed=5, amp=0.5)) - 1.0 / grid.volume
+    h = 1e-4
+    out = tot(rho)
+    ep = tot(rho + h * d, calcType={"E"}).energy
+    em = tot(rho - h * d, calcType={"E"}).energy
+    fd = (ep - em) / (2 * h)
+    an = float((out.potential * d).sum()) * grid.dV
+    assert abs(fd - an) < 1e-6 * max(1.0, abs(an)), (fd, an)

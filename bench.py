@@ -173,7 +173,7 @@ def reference_arm(args):
 def config(args, nat):
     return {"workload": "fcc Al %dx%dx%d (%d atoms), %d^3 grid, TF+vW+kF-node NL kernel (nsp=%d, kdd=3, "
                         "linear, WGC alpha/beta) + LDA + Hartree + PME local PP + Ewald"
-                        % (args.reps, args.reps, args.reps, nat, args.n, args.n, args.nsp),
+                        % (args.reps, args.reps, args.reps, nat, args.n, args.nsp),
             "grid": [args.n] * 3, "atoms": nat, "nsp": args.nsp,
             "l2": "per-step working set (tens of GB) far exceeds the 126 MB L2; a 512 MB buffer is "
                   "written between timed steps",

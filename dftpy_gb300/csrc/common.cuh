@@ -81,6 +81,7 @@ struct Geo {
     long long N, Nc;
     double b[9];
     double fv[3];
+    float bf[9];  // float copies for the FP32-mixed kernels
 };
 
 __host__ __device__ inline long long freq_index(int i, int n) {
@@ -107,6 +108,31 @@ __device__ inline double gsq(const Geo& g, long long idx) {
     double gx, gy, gz, gg;
     gvec(g, idx, gx, gy, gz, gg);
     return gg;
+}
+
+// |G|^2 in the working precision M: float64 as above, or float32 arithmetic
+// for the FP32-mixed kernels (GB300 runs float64 at a small fraction of float32).
+template <typename M>
+__device__ inline M gsq_t(const Geo& g, long long idx);
+
+template <>
+__device__ inline double gsq_t<double>(const Geo& g, long long idx) {
+    return gsq(g, idx);
+}
+
+template <>
+__device__ inline float gsq_t<float>(const Geo& g, long long idx) {
+    int k = (int)(idx % g.n2h);
+    int t = (int)(idx / g.n2h);
+    int j = t % g.n1;
+    int i = t / g.n1;
+    float f0 = (float)(i < (g.n0 - 1) / 2 + 1 ? i : i - g.n0);
+    float f1 = (float)(j < (g.n1 - 1) / 2 + 1 ? j : j - g.n1);
+    float f2 = (float)k;
+    float gx = f0 * g.bf[0] + f1 * g.bf[3] + f2 * g.bf[6];
+    float gy = f0 * g.bf[1] + f1 * g.bf[4] + f2 * g.bf[7];
+    float gz = f0 * g.bf[2] + f1 * g.bf[5] + f2 * g.bf[8];
+    return gx * gx + gy * gy + gz * gz;
 }
 
 // Half-space mask that counts each +-G pair once (src/dftpy/grid.py:658-695,

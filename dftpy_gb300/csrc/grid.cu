@@ -190,7 +190,10 @@ int ofdft_grid_create(const int nr[3], const double lattice[9], int precision, o
         geo.n2h = g->n2h;
         geo.N = N;
         geo.Nc = g->Nc;
-        for (int i = 0; i < 9; ++i) geo.b[i] = g->rlattice[i];
+        for (int i = 0; i < 9; ++i) {
+            geo.b[i] = g->rlattice[i];
+            geo.bf[i] = (float)g->rlattice[i];
+        }
         for (int d = 0; d < 3; ++d) geo.fv[d] = 1.0 / ((double)nr[d] * (1.0 / (double)nr[d]));
         int dev = 0;
         cudaGetDevice(&dev);

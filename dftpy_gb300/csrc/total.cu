@@ -245,12 +245,12 @@ struct Table {
 };
 
 template <typename T>
-__device__ inline double spline_eval(const T* c, int nint, double step, double inv_step, double eta) {
+__device__ inline T spline_eval(const T* c, int nint, T step, T inv_step, T eta) {
     int l = (int)(eta * inv_step);
     l = l < 0 ? 0 : (l >= nint ? nint - 1 : l);
-    double u = eta - (double)l * step;
+    T u = eta - (T)l * step;
     const T* q = c + 4 * (long long)l;
-    return (double)q[0] + u * ((double)q[1] + u * ((double)q[2] + u * (double)q[3]));
+    return q[0] + u * (q[1] + u * (q[2] + u * q[3]));
 }
 
 struct Nodes {
@@ -258,36 +258,49 @@ struct Nodes {
     const double* invk;  // 1/k
 };
 
+// Node kernel values in the working precision T: K_j(|G|) for eta = |G|/k_j
+// below etamax (spline), the etamax value above it, 0 at G = 0.
+template <typename T>
+__device__ inline void node_kernel(const Table<T>& tab, T q, T invk, bool deriv, long long i, T& K, T& KD) {
+    const T eta = q * invk;
+    KD = (T)0;
+    if (eta < (T)tab.etamax) {
+        K = spline_eval(tab.c, tab.nint, (T)tab.step, (T)tab.inv_step, eta);
+        if (deriv) KD = spline_eval(tab.cd, tab.nint, (T)tab.step, (T)tab.inv_step, eta);
+    } else {
+        K = (T)tab.limit;
+        KD = (T)tab.limitd;
+    }
+    if (i == 0) K = KD = (T)0;
+}
+
 // X_j = K_j(G) FFT(rho^beta)/N and Y_j = K'_j(G)/k_j FFT(rho^beta)/N for the
-// chunk's nodes (LWTKernelKf, kernel.py:379-405; lwt.py:226-251)
+// chunk's nodes (LWTKernelKf, kernel.py:379-405; lwt.py:226-251).  The node
+// reciprocals of the chunk sit in shared memory.
 template <typename T>
 __global__ void k_lwt_nodes(const typename Cplx<T>::type* __restrict__ rbG, typename Cplx<T>::type* __restrict__ XY,
                             Table<T> tab, Nodes nd, int j0, int nb, int mcalc, Geo geo, double invN) {
+    extern __shared__ unsigned char smem_nodes[];
+    T* sinvk = (T*)smem_nodes;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) sinvk[t] = (T)nd.invk[j0 + t];
+    __syncthreads();
+    const T invNt = (T)invN;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
-        double q = sqrt(gsq(geo, i));
-        auto z = rbG[i];
-        double zr = (double)z.x * invN, zi = (double)z.y * invN;
+        const T q = sqrt(gsq_t<T>(geo, i));
+        const auto z = rbG[i];
+        const T zr = z.x * invNt, zi = z.y * invNt;
         for (int jj = 0; jj < nb; ++jj) {
-            const int j = j0 + jj;
-            double eta = q * nd.invk[j];
-            double K, KD = 0.0;
-            if (eta < tab.etamax) {
-                K = spline_eval(tab.c, tab.nint, tab.step, tab.inv_step, eta);
-                if (mcalc) KD = spline_eval(tab.cd, tab.nint, tab.step, tab.inv_step, eta);
-            } else {
-                K = tab.limit;
-                KD = tab.limitd;
-            }
-            if (i == 0) K = KD = 0.0;
+            T K, KD;
+            node_kernel(tab, q, sinvk[jj], mcalc != 0, i, K, KD);
             typename Cplx<T>::type o;
-            o.x = (T)(K * zr);
-            o.y = (T)(K * zi);
+            o.x = K * zr;
+            o.y = K * zi;
             XY[(long long)jj * geo.Nc + i] = o;
             if (mcalc) {
-                double kd = KD * nd.invk[j];
-                o.x = (T)(kd * zr);
-                o.y = (T)(kd * zi);
+                const T kd = KD * sinvk[jj];
+                o.x = kd * zr;
+                o.y = kd * zi;
                 XY[(long long)(nb + jj) * geo.Nc + i] = o;
             }
         }
@@ -298,39 +311,35 @@ __global__ void k_lwt_nodes(const typename Cplx<T>::type* __restrict__ rbG, type
 template <typename T>
 __global__ void k_lwt_pot2(const typename Cplx<T>::type* __restrict__ U, typename Cplx<T>::type* __restrict__ pot2G,
                            Table<T> tab, Nodes nd, int j0, int nb, int hermite, int first, Geo geo, double invN) {
+    extern __shared__ unsigned char smem_nodes[];
+    T* sinvk = (T*)smem_nodes;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) sinvk[t] = (T)nd.invk[j0 + t];
+    __syncthreads();
+    const T invNt = (T)invN;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
-        double q = sqrt(gsq(geo, i));
-        double sr = 0.0, si = 0.0;
+        const T q = sqrt(gsq_t<T>(geo, i));
+        T sr = 0, si = 0;
         if (!first) {
-            sr = (double)pot2G[i].x;
-            si = (double)pot2G[i].y;
+            sr = pot2G[i].x;
+            si = pot2G[i].y;
         }
         for (int jj = 0; jj < nb; ++jj) {
-            const int j = j0 + jj;
-            double eta = q * nd.invk[j];
-            double K, KD = 0.0;
-            if (eta < tab.etamax) {
-                K = spline_eval(tab.c, tab.nint, tab.step, tab.inv_step, eta);
-                if (hermite) KD = spline_eval(tab.cd, tab.nint, tab.step, tab.inv_step, eta);
-            } else {
-                K = tab.limit;
-                KD = tab.limitd;
-            }
-            if (i == 0) K = KD = 0.0;
-            auto u = U[(long long)jj * geo.Nc + i];
-            sr += K * invN * (double)u.x;
-            si += K * invN * (double)u.y;
+            T K, KD;
+            node_kernel(tab, q, sinvk[jj], hermite != 0, i, K, KD);
+            const auto u = U[(long long)jj * geo.Nc + i];
+            sr += K * invNt * u.x;
+            si += K * invNt * u.y;
             if (hermite) {
-                double kd = KD * nd.invk[j] * invN;
-                auto w = U[(long long)(nb + jj) * geo.Nc + i];
-                sr += kd * (double)w.x;
-                si += kd * (double)w.y;
+                const T kd = KD * sinvk[jj] * invNt;
+                const auto w = U[(long long)(nb + jj) * geo.Nc + i];
+                sr += kd * w.x;
+                si += kd * w.y;
             }
         }
         typename Cplx<T>::type o;
-        o.x = (T)sr;
-        o.y = (T)si;
+        o.x = sr;
+        o.y = si;
         pot2G[i] = o;
     }
 }
@@ -342,7 +351,11 @@ struct Member {
     bool small;
 };
 
-__device__ inline Member membership(double kf, const double* kn, const double* kup, int m) {
+// closed_interior: a point exactly on an interior node joins the interval below
+// it.  Float32 k_F values tie with interior nodes now and then (the nodes are
+// built from float32 extremes); the open test of the reference would then drop
+// the point from every interval.  Float64 keeps the reference's test exactly.
+__device__ inline Member membership(double kf, const double* kn, const double* kup, int m, bool closed_interior) {
     // c = number of nodes strictly below kf
     int lo = 0, hi = m;
     while (lo < hi) {
@@ -355,8 +368,11 @@ __device__ inline Member membership(double kf, const double* kn, const double* k
     r.ilast = -1;
     r.iprev = -1;
     int i1 = c - 1, i2 = c - 2;
-    bool in1 = (i1 >= 0 && i1 <= m - 2 && kf < kup[i1 + 1]);
-    bool in2 = (i2 >= 0 && i2 <= m - 2 && kf < kup[i2 + 1]);
+    auto below_top = [&](int i) {
+        return (closed_interior && i + 1 <= m - 2) ? kf <= kn[i + 1] : kf < kup[i + 1];
+    };
+    bool in1 = (i1 >= 0 && i1 <= m - 2 && below_top(i1));
+    bool in2 = (i2 >= 0 && i2 <= m - 2 && below_top(i2));
     if (in1) {
         r.ilast = i1;
         if (in2) r.iprev = i2;
@@ -396,7 +412,7 @@ __global__ void k_lwt_interp(InterpArgs<T> a) {
     const int j1 = a.j0 + a.nb;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < a.N; r += stride) {
         double kf = fmin((double)a.kf[r], a.kfclip);
-        Member mb = membership(kf, kn, kup, a.m);
+        Member mb = membership(kf, kn, kup, a.m, sizeof(T) == 4);
         double p1 = 0.0, p3 = 0.0;
         // weights of nodes il (lower) and il+1 (upper) of the deciding interval
         auto P = [&](int j) { return (double)a.PM[(long long)(j - a.j0) * a.N + r]; };
@@ -893,7 +909,8 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
             const int nplanes = mcalc ? 2 * nb : nb;
             // read FFT(rho^beta) once, write one complex plane per node (two with derivatives)
             timed(e, P_LWT_NODES, Ncd * 2 * s * (1 + nplanes), st, [&] {
-                k_lwt_nodes<T><<<gblk, 256, 0, st>>>(rbG, XY, tab, nd, j0, nb, mcalc, g->geo, 1.0 / (double)N);
+                k_lwt_nodes<T><<<gblk, 256, nb * sizeof(T), st>>>(rbG, XY, tab, nd, j0, nb, mcalc, g->geo,
+                                                                 1.0 / (double)N);
             });
             OFDFT_LAUNCH_CHECK();
             c2r(XY, PM, nplanes);
@@ -931,7 +948,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
                 const int upl = hermite ? 2 * nb : nb;
                 r2c(U, XY, upl);
                 timed(e, P_LWT_POT2, Ncd * 2 * s * (upl + (j0 == 0 ? 1 : 2)), st, [&] {
-                    k_lwt_pot2<T><<<gblk, 256, 0, st>>>(XY, pot2G, tab, nd, j0, nb, hermite, j0 == 0, g->geo,
+                    k_lwt_pot2<T><<<gblk, 256, nb * sizeof(T), st>>>(XY, pot2G, tab, nd, j0, nb, hermite, j0 == 0, g->geo,
                                                          1.0 / (double)N);
                 });
                 OFDFT_LAUNCH_CHECK();

@@ -92,18 +92,39 @@ def smooth_density(lattice, nr, nelec, seed=0, amp=0.3, kmax=3):
 def atomic_density(lattice, nr, positions, zvals, width=1.2, floor=0.0):
     """Superposition of periodic Gaussians of charge zvals[a] at each site plus a
     floor; normalised to sum(zvals) electrons.  Used for vacuum-like trial
-    densities where rho spans many orders of magnitude."""
+    densities where rho spans many orders of magnitude.  Orthorhombic cells use
+    separable stencils truncated at 6 widths (exp(-18) relative); other cells
+    sum over the whole grid per atom."""
     nr = tuple(int(n) for n in nr)
-    s = [np.arange(n) / n for n in nr]
-    S = np.stack(np.meshgrid(*s, indexing="ij"), axis=-1)
-    inv = np.linalg.inv(lattice)
+    lattice = np.asarray(lattice, dtype=np.float64)
     rho = np.full(nr, floor, dtype=np.float64)
-    for p, z in zip(positions, zvals):
-        f = S - (p @ inv)
-        f -= np.round(f)
-        r = f @ lattice
-        rr = (r * r).sum(-1)
-        rho += z * np.exp(-rr / (2 * width ** 2)) / (2 * np.pi * width ** 2) ** 1.5
+    norm = (2 * np.pi * width ** 2) ** 1.5
+    if np.allclose(lattice, np.diag(np.diag(lattice))):
+        L = np.diag(lattice)
+        cut = 6.0 * width
+        for p, z in zip(positions, zvals):
+            idx, val = [], []
+            for d in range(3):
+                h = L[d] / nr[d]
+                c = p[d] / h
+                w = min(int(np.ceil(cut / h)), nr[d] // 2)
+                k = np.arange(int(np.floor(c)) - w, int(np.floor(c)) + w + 1)
+                if len(k) > nr[d]:
+                    k = k[:nr[d]]
+                x = k * h - p[d]
+                idx.append(np.mod(k, nr[d]))
+                val.append(np.exp(-x * x / (2 * width ** 2)))
+            rho[np.ix_(idx[0], idx[1], idx[2])] += (z / norm) * np.einsum("i,j,k->ijk", val[0], val[1], val[2])
+    else:
+        s = [np.arange(n) / n for n in nr]
+        S = np.stack(np.meshgrid(*s, indexing="ij"), axis=-1)
+        inv = np.linalg.inv(lattice)
+        for p, z in zip(positions, zvals):
+            f = S - (p @ inv)
+            f -= np.round(f)
+            r = f @ lattice
+            rr = (r * r).sum(-1)
+            rho += z * np.exp(-rr / (2 * width ** 2)) / norm
     vol = abs(np.linalg.det(lattice))
     rho *= float(np.sum(zvals)) / (rho.sum() * vol / rho.size)
     return rho

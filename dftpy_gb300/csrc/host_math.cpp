@@ -71,6 +71,72 @@ void CubicSpline::fit(const std::vector<double>& xs, const std::vector<double>& 
     }
 }
 
+std::vector<double> CubicSpline::adjoint(const std::vector<double>& gc) const {
+    const int n = (int)x.size();
+    std::vector<double> h(n - 1);
+    for (int i = 0; i < n - 1; ++i) h[i] = x[i + 1] - x[i];
+    const int m = n - 2;
+    // the (modified) tridiagonal system of fit()
+    std::vector<double> lo(m), di(m), up(m);
+    for (int r = 0; r < m; ++r) {
+        int i = r + 1;
+        lo[r] = h[i - 1];
+        di[r] = 2.0 * (h[i - 1] + h[i]);
+        up[r] = h[i];
+    }
+    const double a = h[0] / h[1], b = h[n - 2] / h[n - 3];
+    di[0] += lo[0] * (1.0 + a);
+    up[0] -= lo[0] * a;
+    lo[0] = 0.0;
+    di[m - 1] += up[m - 1] * (1.0 + b);
+    lo[m - 1] -= up[m - 1] * b;
+    up[m - 1] = 0.0;
+    std::vector<double> gy(n, 0.0), gd(n - 1, 0.0), gM(n, 0.0);
+    // coefficients -> (y, d, M)
+    for (int i = 0; i < n - 1; ++i) {
+        const double g0 = gc[4 * i], g1 = gc[4 * i + 1], g2 = gc[4 * i + 2], g3 = gc[4 * i + 3];
+        gy[i] += g0;
+        gd[i] += g1;
+        gM[i] += -h[i] * 2.0 / 6.0 * g1 + 0.5 * g2 - g3 / (6.0 * h[i]);
+        gM[i + 1] += -h[i] / 6.0 * g1 + g3 / (6.0 * h[i]);
+    }
+    // not-a-knot end relations M_0(M_1, M_2), M_{n-1}(M_{n-2}, M_{n-3})
+    gM[1] += gM[0] * (1.0 + a);
+    gM[2] -= gM[0] * a;
+    gM[n - 2] += gM[n - 1] * (1.0 + b);
+    gM[n - 3] -= gM[n - 1] * b;
+    // interior solve: rhs adjoint = T^-T gM_interior (Thomas on the transpose)
+    std::vector<double> tl(m), td(m), tu(m), g(m);
+    for (int r = 0; r < m; ++r) {
+        td[r] = di[r];
+        tl[r] = r > 0 ? up[r - 1] : 0.0;
+        tu[r] = r < m - 1 ? lo[r + 1] : 0.0;
+        g[r] = gM[r + 1];
+    }
+    if (m == 1) {
+        g[0] /= td[0];
+    } else {
+        for (int r = 1; r < m; ++r) {
+            double w = tl[r] / td[r - 1];
+            td[r] -= w * tu[r - 1];
+            g[r] -= w * g[r - 1];
+        }
+        g[m - 1] /= td[m - 1];
+        for (int r = m - 2; r >= 0; --r) g[r] = (g[r] - tu[r] * g[r + 1]) / td[r];
+    }
+    // rhs_r = 6 (d_{r+1} - d_r)
+    for (int r = 0; r < m; ++r) {
+        gd[r + 1] += 6.0 * g[r];
+        gd[r] -= 6.0 * g[r];
+    }
+    // d_i = (y_{i+1} - y_i) / h_i
+    for (int i = 0; i < n - 1; ++i) {
+        gy[i + 1] += gd[i] / h[i];
+        gy[i] -= gd[i] / h[i];
+    }
+    return gy;
+}
+
 int CubicSpline::interval(double xv) const {
     const int n = (int)x.size();
     if (xv <= x[0]) return 0;

@@ -15,6 +15,9 @@ struct CubicSpline {
     int interval(double xv) const;
     double eval(double xv) const;
     double deriv(double xv) const;
+    // Adjoint of fit(): given dL/dc (4 per interval) return dL/dy (n values).
+    // The fit is linear in y, so this is the transpose of the data-to-coefficient map.
+    std::vector<double> adjoint(const std::vector<double>& gc) const;
 };
 
 // Inverse Lindhard function F(eta; lambda, mu) with the reference's four

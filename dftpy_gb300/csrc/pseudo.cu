@@ -153,6 +153,73 @@ __global__ void __launch_bounds__(RED_THREADS) k_pp_force_exact(const typename C
     block_sum_store<3 * kForceChunk>(acc, partials);
 }
 
+// Gradient of E_PP = int v_loc rho dV with respect to the radial table of each
+// species.  E_PP = (dV/V) sum_{G in half grid} w_G vline_s(|G|) Re(S_s(G) conj(rho(G)))
+// (w_G = 2 off the k2 = 0 / Nyquist planes, 1 on them), and vline is linear in
+// the table: a quartic in vp[0..2] below gp[1], a cubic spline of vp[1:] above.
+// Per G this kernel adds h = (dV/V) w_G Re(S conj rho) times the derivative of
+// vline with respect to the quartic's three values, or times u^p (p = 0..3) to
+// the spline interval holding |G|; the host applies the spline adjoint.
+template <typename T>
+__global__ void k_pp_grad_moments(const typename Cplx<T>::type* __restrict__ rhoG,
+                                  const typename Cplx<T>::type* __restrict__ QG, const double* bre,
+                                  const double* bim, Line L, Geo geo, double scale, double* moments,
+                                  double* quart) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        double q = sqrt(gsq(geo, i));
+        if (q >= L.gplast) continue;
+        double br = 1.0, bi = 0.0;  // no B-spline factor for exact structure factors
+        if (bre) barray(bre, bim, geo, i, br, bi);
+        const double qr = (double)QG[i].x, qi = (double)QG[i].y;
+        const double sr = qr * br - qi * bi, si = qr * bi + qi * br;
+        const int k2 = (int)(i % geo.n2h);
+        const double w = (k2 == 0 || (geo.n2 % 2 == 0 && k2 == geo.n2 / 2)) ? 1.0 : 2.0;
+        const double h = scale * w * (sr * (double)rhoG[i].x + si * (double)rhoG[i].y);
+        if (q < L.gp1) {
+            const double dx = q / L.dp, x2 = dx * dx, x4 = x2 * x2;
+            atomicAdd(&quart[0], (1.0 + (-30.0 * x2 + 6.0 * x4) / 24.0) * h);
+            atomicAdd(&quart[1], ((32.0 * x2 - 8.0 * x4) / 24.0) * h);
+            atomicAdd(&quart[2], ((-2.0 * x2 + 2.0 * x4) / 24.0) * h);
+            continue;
+        }
+        int lo = 0, hi = L.n - 1;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (L.x[mid] <= q) lo = mid;
+            else hi = mid;
+        }
+        const double u = q - L.x[lo];
+        double* mp = moments + 4 * (long long)lo;
+        atomicAdd(&mp[0], h);
+        atomicAdd(&mp[1], h * u);
+        atomicAdd(&mp[2], h * u * u);
+        atomicAdd(&mp[3], h * u * u * u);
+    }
+}
+
+// exact structure factor of one species, S_s(G) = sum_{a in s} exp(-i G.R_a), as a complex field
+template <typename T>
+__global__ void k_strf_species(typename Cplx<T>::type* S, const double* __restrict__ pos, const int* __restrict__ sel,
+                               int na, Geo geo) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        double gx, gy, gz, gg;
+        gvec(geo, i, gx, gy, gz, gg);
+        double sr = 0.0, si = 0.0;
+        for (int t = 0; t < na; ++t) {
+            const int a = sel[t];
+            double ph = gx * pos[3 * a] + gy * pos[3 * a + 1] + gz * pos[3 * a + 2];
+            double sn, cs;
+            sincos(ph, &sn, &cs);
+            sr += cs;
+            si -= sn;
+        }
+        S[i].x = (T)sr;
+        S[i].y = (T)si;
+    }
+}
+
 }  // namespace
 
 struct ofdft_pseudo {
@@ -332,9 +399,69 @@ void forces_t(ofdft_pseudo* p, const T* rho, double* F, cudaStream_t st) {
     }
 }
 
+template <typename T>
+void vloc_grad_t(ofdft_pseudo* p, const T* rho, double* grad, cudaStream_t st) {
+    ofdft_grid* g = p->g;
+    using C = typename Cplx<T>::type;
+    const size_t cb = g->cplx_bytes(), rb = g->real_bytes();
+    C* rhoG = (C*)p->sc.get("rhoG", cb);
+    C* SG = (C*)p->sc.get("QG", cb);
+    g->exec_r2c(rho, rhoG, 1, st);
+    const int gblk = blocks_for(g->Nc, 256, g->sms * 16);
+    const double scale = g->dV / g->volume;
+    size_t off = 0;
+    for (int s = 0; s < p->ns; ++s) {
+        const int n_s = p->sel_off[s + 1] - p->sel_off[s];
+        const int nint = (int)p->spl[s].x.size() - 1;
+        double* mom = (double*)p->sc.get("mom", (4 * (size_t)nint + 3) * sizeof(double));
+        OFDFT_CK(cudaMemsetAsync(mom, 0, (4 * (size_t)nint + 3) * sizeof(double), st));
+        if (n_s > 0) {
+            if (p->pme) {
+                T* Q = (T*)p->sc.get("Q", rb);
+                OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
+                k_pme_spread<T><<<n_s, 256, 0, st>>>(p->d_frac, nullptr, p->d_sel + p->sel_off[s], p->order, g->geo, Q);
+                OFDFT_LAUNCH_CHECK();
+                g->exec_r2c(Q, SG, 1, st);
+                k_pp_grad_moments<T><<<gblk, 256, 0, st>>>(rhoG, SG, p->d_bre, p->d_bim, p->line(s), g->geo, scale,
+                                                           mom, mom + 4 * (size_t)nint);
+            } else {
+                k_strf_species<T><<<gblk, 256, 0, st>>>(SG, p->d_pos, p->d_sel + p->sel_off[s], n_s, g->geo);
+                OFDFT_LAUNCH_CHECK();
+                k_pp_grad_moments<T><<<gblk, 256, 0, st>>>(rhoG, SG, nullptr, nullptr, p->line(s), g->geo, scale, mom,
+                                                           mom + 4 * (size_t)nint);
+            }
+            OFDFT_LAUNCH_CHECK();
+        }
+        std::vector<double> h(4 * (size_t)nint + 3);
+        OFDFT_CK(cudaMemcpyAsync(h.data(), mom, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+        const int np = p->npts[s];
+        double* gs = grad + off;
+        for (int k = 0; k < np; ++k) gs[k] = 0.0;
+        // spline over vp[1:]: d vline / d c_{l,p} = u^p, then the transpose of the fit
+        std::vector<double> gc(h.begin(), h.begin() + 4 * (size_t)nint);
+        std::vector<double> gy = p->spl[s].adjoint(gc);
+        for (int k = 0; k < np - 1; ++k) gs[k + 1] += gy[k];
+        // quartic near q = 0 in vp[0], vp[1], vp[2]
+        gs[0] += h[4 * nint + 0];
+        gs[1] += h[4 * nint + 1];
+        gs[2] += h[4 * nint + 2];
+        off += np;
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int ofdft_pseudo_vloc_grad(ofdft_pseudo* p, const void* rho, double* grad, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(p && rho && grad, "ofdft_pseudo_vloc_grad: null argument");
+        OFDFT_REQUIRE(p->nat > 0, "ofdft_pseudo_vloc_grad: no ions set");
+        if (p->g->prec == OFDFT_F64) vloc_grad_t<double>(p, (const double*)rho, grad, (cudaStream_t)s);
+        else vloc_grad_t<float>(p, (const float*)rho, grad, (cudaStream_t)s);
+    });
+}
 
 int ofdft_pseudo_create(ofdft_grid* g, int nspecies, const int* npts, const double* const* gp, const double* const* vp,
                         int pme, int bspline_order, ofdft_pseudo** out) {

@@ -256,6 +256,38 @@ class LocalPseudo(NativeFunctional):
         _lib.check(_lib.load().ofdft_pseudo_forces(h, _lib.C.c_void_p(t.data_ptr()), _lib.dptr(F), stream_ptr()))
         return F
 
+    def vloc_grad(self, rho):
+        """dE_PP/dvp: gradient of int v_loc rho dV with respect to every value of
+        each species' radial table (keys as PP_list), from the device adjoint."""
+        if not isinstance(rho, DirectField):
+            raise TypeError("rho must be DirectField")
+        h = self._handle(rho.dtype)
+        keys = self.species_keys
+        sizes = [len(self.readpp.gp[k]) for k in keys]
+        G = np.zeros(sum(sizes))
+        t = rho.as_subclass(torch.Tensor).contiguous()
+        _lib.check(_lib.load().ofdft_pseudo_vloc_grad(h, _lib.C.c_void_p(t.data_ptr()), _lib.dptr(G), stream_ptr()))
+        out, off = {}, 0
+        for k, n in zip(keys, sizes):
+            out[k] = G[off:off + n].copy()
+            off += n
+        return out
+
+    def set_tables(self, tables):
+        """Replace the radial tables {symbol: vp} (same grids); drops cached v_loc."""
+        for k, v in tables.items():
+            v = np.asarray(v, dtype=np.float64)
+            if v.shape != self.readpp.vp[k].shape:
+                raise ValueError("table of %s must keep its %d points" % (k, len(self.readpp.vp[k])))
+            self.readpp._vp[k] = v.copy()
+        self._native, self._vreal, self._version = {}, {}, object()
+
+    def set_positions(self, positions):
+        """Move the ions (Bohr); drops cached v_loc and the Ewald object."""
+        self._ions.positions = np.array(positions, dtype=np.float64).reshape(self._ions.nat, 3)
+        self._native, self._vreal, self._version = {}, {}, object()
+        self.ewald = None
+
     def get_ewald(self, PME=None):
         if self.ewald is None:
             from ..ewald import ewald

@@ -148,6 +148,12 @@ int ofdft_pseudo_set_ions(ofdft_pseudo* p, int nat, const double* pos, const int
 int ofdft_pseudo_vloc(ofdft_pseudo* p, void* vreal_out, ofdft_stream s);
 /* LocalPseudo.forces (:260-270): PME (_ForcePME :523-571) or exact (_Force :505-521) */
 int ofdft_pseudo_forces(ofdft_pseudo* p, const void* rho, double* forces, ofdft_stream s);
+/* Gradient of E_PP = int v_loc rho dV with respect to every value of every
+ * species' radial table vp (the v_loc(G) coefficients), by the adjoint of the
+ * spline fit and of the structure-factor path; grad holds sum(npts) doubles,
+ * species in order.  The reference has no counterpart (it offers no table
+ * derivatives); the test pins it to finite differences of the oracle. */
+int ofdft_pseudo_vloc_grad(ofdft_pseudo* p, const void* rho, double* grad, ofdft_stream s);
 
 /* ---------------------------------------------------------------- Ewald
  * ewald (src/dftpy/ewald.py:197-864): eta from Get_Best_eta (:256-278),

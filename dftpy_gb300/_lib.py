@@ -86,6 +86,7 @@ _SIGS = {
     "ofdft_pseudo_set_ions": (_I, [_P, _I, _PD, _PI]),
     "ofdft_pseudo_vloc": (_I, [_P, _P, _P]),
     "ofdft_pseudo_forces": (_I, [_P, _P, _PD, _P]),
+    "ofdft_pseudo_vloc_grad": (_I, [_P, _P, _PD, _P]),
     "ofdft_ewald": (_I, [_P, _I, _PD, _PD, _D, _I, _I, _PD, _PD, _PD, _P]),
     "ofdft_opt_default": (None, [C.POINTER(OptOptions)]),
     "ofdft_optimize": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P]),

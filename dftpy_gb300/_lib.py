@@ -69,6 +69,7 @@ _SIGS = {
     "ofdft_ifft": (_I, [_P, _P, _P, _P]),
     "ofdft_dot": (_I, [_P, _P, _P, _PD, _P]),
     "ofdft_dot3": (_I, [_P, _P, _P, _P, _PD, _P]),
+    "ofdft_dot_noalloc": (_I, [_P, _P, C.c_longlong, _I, _P, _P]),
     "ofdft_config_default": (None, [C.POINTER(Config)]),
     "ofdft_eval_create": (_I, [_P, C.POINTER(Config), C.POINTER(_P)]),
     "ofdft_eval_destroy": (None, [_P]),

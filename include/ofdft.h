@@ -66,6 +66,18 @@ int ofdft_ifft(ofdft_grid* g, const void* in_cplx, void* out_real, ofdft_stream 
 int ofdft_dot(ofdft_grid* g, const void* a, const void* b, double* out, ofdft_stream s);
 int ofdft_dot3(ofdft_grid* g, const void* a, const void* b, const void* c, double* out, ofdft_stream s);
 
+/* The same float64 reduction without a grid handle and without any allocation,
+ * for callers that cannot allocate device memory where they need it (inside
+ * an allocator or memory-pool hook, in loops that forbid allocation after
+ * start-up, or when a framework pool has reserved all device memory).  This
+ * entry point has no counterpart in the reference.  out_dev[0] = sum(a*b) (b
+ * may be NULL: sum(a)) over n elements of the given precision, written to
+ * device memory in stream order.  Its scratch is a 32 KiB static device array
+ * (4096 block partials), so n is limited to 67,108,864 (OFDFT_EINVAL beyond).
+ * The first call on a device looks the array up and should come before any
+ * stream capture; calls that overlap on the GPU share the array and race. */
+int ofdft_dot_noalloc(const void* a, const void* b, long long n, int precision, double* out_dev, ofdft_stream s);
+
 /* ------------------------------------------------------ total functional
  * Configuration of the terms of TotalFunctional (src/dftpy/functional/
  * total_functional.py:49-146) and the KEDF dispatcher (kedf/__init__.py:27-69,

@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--gs", action="store_true", help="also time the ground-state optimisation")
+    p.add_argument("--workload", default="ev", choices=["ev", "diff"],
+                   help="ev: the E+V metric (default); diff: the differentiation workload")
     return p.parse_args()
 
 
@@ -180,6 +182,25 @@ def config(args, nat):
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 
+# ------------------------------------------------------------ replicas
+def max_over_ranks(x, dist=None, device="cpu"):
+    """Slowest rank's value (the timing of a replica job is its slowest replica)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(ms_per_step_local, world, dist=None, device="cpu"):
+    """Whole-job evaluations/s of ``world`` independent replicas: every rank
+    evaluates its own system, so the job does ``world`` evaluations per step
+    of the slowest rank.  Returns (evals/s, slowest ms per step)."""
+    ms = max_over_ranks(ms_per_step_local, dist, device)
+    return world * 1e3 / ms, ms
+
+
 # --------------------------------------------------------------- GPU arm
 def gpu_arm(args):
     import torch
@@ -252,11 +273,7 @@ def gpu_arm(args):
                 "nsp_used": nsp_used, "launches": launches}
 
     def maxrank(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(x, dist, "cuda")
 
     # ---- FP32-mixed headline, with clock sampling and per-kernel events
     sampler = ClockSampler(local)
@@ -343,24 +360,125 @@ def gpu_arm(args):
         print(json.dumps(out), flush=True)
 
 
-def ground_state(D, tot, grid, rho_np, nat):
+def ground_state(D, tot, grid, rho_np, nat, method="LBFGS", econv_per_atom=1e-7):
+    """Wall time of optimize_rho from the uniform density: plain FP64, and
+    FP32-mixed followed by an FP64 refinement, both to the same econv rule."""
     import torch
-    res = {}
-    for name, dtype in (("f32_mixed", torch.float32), ("f64", torch.float64)):
-        rho0 = D.DirectField(grid, dtype=dtype) + float(rho_np.mean())
-        opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
-                             optimization_options={"econv": 1e-6 * nat, "maxiter": 200})
+    econv = econv_per_atom * nat
+    opts = {"econv": econv, "maxiter": 300, "maxfun": 50}
+    res = {"method": method, "econv_Ha": econv}
+    rho0 = D.DirectField(grid) + float(rho_np.mean())
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method, optimization_options=dict(opts))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    opt.optimize_rho(guess_rho=rho0)
+    torch.cuda.synchronize()
+    e64 = float(opt.functional.energy)
+    res["f64"] = {"seconds": time.perf_counter() - t0, "energy": e64, "converged": int(opt.converged),
+                  "niter": opt.result.niter, "nfev": opt.result.nfev, "dP": opt.result.dP}
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method, optimization_options=dict(opts))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    opt.optimize_rho_mixed(guess_rho=rho0, econv_f32=10.0 * econv)
+    torch.cuda.synchronize()
+    em = float(opt.functional.energy)
+    res["f32_mixed_then_f64"] = {"seconds": time.perf_counter() - t0, "energy": em, "converged": int(opt.converged),
+                                 "stages": opt.stages, "dP": opt.result.dP, "dE_per_atom_vs_f64": (em - e64) / nat}
+    res["speedup"] = res["f64"]["seconds"] / res["f32_mixed_then_f64"]["seconds"]
+    return res
+
+
+def diff_workload(args):
+    """Differentiation workload: 500-atom two-species random alloy (Z = 3,
+    rc = 1.0 and Z = 2, rc = 1.2; 256-point radial tables), minimum separation
+    4.0 Bohr at 0.18 e/Angstrom^3, 160^3 grid, WT KEDF + LDA + Hartree + PME PP
+    + Ewald, FP32-mixed.  Times the forward E and the adjoint (dE/drho,
+    forces dE/dR, dE/d table), checks them against central differences and the
+    FP64 adjoint, and reports the device memory the evaluation holds."""
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import synthetic as syn
+    from dftpy_gb300.autograd import energy_and_gradients, total_energy
+    from dftpy_gb300.constants import BOHR
+    torch.cuda.set_device(0)
+    n = args.n if args.n != 256 else 160
+    lat, pos, spec = syn.random_alloy(500, 0.18 * BOHR ** 3, [3.0, 2.0], 4.0, seed=500)
+    sym = ["Al" if s == 0 else "Mg" for s in spec]
+    ga, va = syn.analytic_vloc(3.0, 1.0, npts=256)
+    gb, vb = syn.analytic_vloc(2.0, 1.2, npts=256)
+    grid = D.DirectGrid(lat, (n, n, n))
+    ions = D.Ions(symbols=sym, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PME=True, PP_list={"Al": D.functional.RECPOT(r=ga, v=va, zval=3),
+                                                                "Mg": D.functional.RECPOT(r=gb, v=vb, zval=2)})
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    rho_np = syn.atomic_density(lat, (n, n, n), pos, [3.0 if s == 0 else 2.0 for s in spec], width=1.3, floor=0.003)
+    free0 = torch.cuda.mem_get_info()[0]
+    rho32 = D.DirectField(grid, data=rho_np, dtype=torch.float32)
+    keys = pp.species_keys
+    T = torch.tensor(np.concatenate([pp.readpp.vp[k] for k in keys]), requires_grad=True)
+    R = torch.tensor(pos, dtype=torch.float64, requires_grad=True)
+    # warm-up (plans, tables, Ewald forces cached per geometry)
+    E = total_energy(tot, rho32.as_subclass(torch.Tensor).clone().requires_grad_(True), R, T)
+    E.backward()
+    fw, bw = [], []
+    for _ in range(max(3, args.steps)):
+        r = rho32.as_subclass(torch.Tensor).clone().requires_grad_(True)
+        R.grad = None
+        T.grad = None
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rho = opt.optimize_rho(guess_rho=rho0)
+        E = total_energy(tot, r, R, T)
         torch.cuda.synchronize()
-        res[name] = {"seconds": time.perf_counter() - t0, "energy": float(opt.functional.energy),
-                     "converged": int(opt.converged), "niter": opt.result.niter, "nfev": opt.result.nfev}
-    return res
+        t1 = time.perf_counter()
+        E.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        fw.append(t1 - t0)
+        bw.append(t2 - t1)
+    used = free0 - torch.cuda.mem_get_info()[0]
+    # checks: central differences (h = 1e-4) in FP64, FP32 adjoint against FP64 adjoint
+    rho64 = D.DirectField(grid, data=rho_np)
+    E64, V64, dR64, dT64 = energy_and_gradients(tot, rho64)
+    E32, V32, dR32, dT32 = energy_and_gradients(tot, rho32)
+    h = 1e-4
+    fd_err = []
+    for a, c in ((0, 0), (137, 1), (411, 2)):
+        Rp = R.detach().clone()
+        Rm = R.detach().clone()
+        Rp[a, c] += h
+        Rm[a, c] -= h
+        ep = float(total_energy(tot, rho64.as_subclass(torch.Tensor), Rp, T.detach()))
+        em = float(total_energy(tot, rho64.as_subclass(torch.Tensor), Rm, T.detach()))
+        fd_err.append(abs((ep - em) / (2 * h) - dR64[a, c]))
+    pp.set_positions(pos)
+    tfd = []
+    for idx in (0, 3, 60, 256 + 7, 256 + 100):
+        Tp = T.detach().clone()
+        Tm = T.detach().clone()
+        Tp[idx] += h
+        Tm[idx] -= h
+        ep = float(total_energy(tot, rho64.as_subclass(torch.Tensor), R.detach(), Tp))
+        em = float(total_energy(tot, rho64.as_subclass(torch.Tensor), R.detach(), Tm))
+        tfd.append(abs((ep - em) / (2 * h) - dT64[idx]))
+    out = {"workload": "differentiation: 500-atom Al/Mg-like random alloy, %d^3, WT+LDA+H+PME PP, FP32-mixed" % n,
+           "box_bohr": float(lat[0, 0]), "forward_ms": 1e3 * float(np.median(fw)),
+           "backward_ms": 1e3 * float(np.median(bw)), "backward_over_forward": float(np.median(bw) / np.median(fw)),
+           "device_bytes_held": int(used), "fd_force_max_abs_err": float(max(fd_err)),
+           "fd_table_max_abs_err": float(max(tfd)),
+           "fp32_vs_fp64": {"dE_per_atom": (E32 - E64) / 500, "force_max_abs": float(np.abs(dR32 - dR64).max()),
+                            "dEdtable_max_rel": float(np.abs(dT32 - dT64).max() / np.abs(dT64).max()),
+                            "V_max_abs": float((V32.as_subclass(torch.Tensor).double()
+                                                - V64.as_subclass(torch.Tensor)).abs().max())}}
+    print(json.dumps(out), flush=True)
 
 
 def main():
     args = parse()
+    if args.workload == "diff":
+        diff_workload(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
     else:

@@ -49,6 +49,22 @@ Consts make_consts() {
 
 // PZ81 correlation parameters, unpolarised (xc/semilocal_xc.py:287-293)
 __constant__ double cPZ[7] = {0.0311, -0.048, 0.0020, -0.0116, -0.1423, 1.0529, 0.3334};
+__constant__ float cPZf[7] = {0.0311f, -0.048f, 0.0020f, -0.0116f, -0.1423f, 1.0529f, 0.3334f};
+
+// Working-precision math: float64 for the FP64 path, float32 for FP32-mixed
+// (GB300 runs float64 at a small fraction of the float32 rate).
+__device__ inline double mcbrt(double x) { return cbrt(x); }
+__device__ inline float mcbrt(float x) { return cbrtf(x); }
+__device__ inline double mlog(double x) { return log(x); }
+__device__ inline float mlog(float x) { return logf(x); }
+__device__ inline double msqrt(double x) { return sqrt(x); }
+__device__ inline float msqrt(float x) { return sqrtf(x); }
+__device__ inline double mpow(double x, double y) { return pow(x, y); }
+__device__ inline float mpow(float x, float y) { return powf(x, y); }
+template <typename M>
+__device__ inline M pz(int k) {
+    return sizeof(M) == 8 ? (M)cPZ[k] : (M)cPZf[k];
+}
 
 template <typename T>
 struct PreArgs {
@@ -70,67 +86,73 @@ struct PreArgs {
 // slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho
 constexpr int PRE_NS = 7;
 
+// Pointwise pre-pass.  All arithmetic runs in the grid precision T; the
+// per-thread energy accumulators are float64 in both precisions.
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* partials) {
+    using M = T;
     double acc[PRE_NS] = {0.0, 0.0, 0.0, 0.0, INFINITY, -INFINITY, -INFINITY};
     const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2};
+    const M cTF_E = (M)a.k.cTF_E, cTF_V = (M)a.k.cTF_V, tf_x = (M)a.tf_x;
+    const M lda_rs = (M)a.k.lda_rs, lda_ex = (M)a.k.lda_ex, lda_vx = (M)a.k.lda_vx;
+    const M threepi2 = (M)a.k.threepi2, alpha = (M)a.alpha, beta = (M)a.beta;
+    const M P0 = pz<M>(0), P1 = pz<M>(1), P2 = pz<M>(2), P3 = pz<M>(3), P4 = pz<M>(4), P5 = pz<M>(5),
+            P6 = pz<M>(6);
+    const M tiny = (M)1e-30, zero_clamp = (M)kZERO;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
-        const double r = (double)a.rho[i];
-        double v = 0.0;
-        acc[3] += r;
-        acc[6] = fmax(acc[6], r);
+        const M r = a.rho[i];
+        M v = (M)0;
+        acc[3] += (double)r;
+        acc[6] = fmax(acc[6], (double)r);
         if (a.tf) {
             // PowerInt(rho, 5, 3): repeated products then cbrt (math_utils.py:158-176)
-            double r5 = r * r;
+            M r5 = r * r;
             r5 *= r;
             r5 *= r;
             r5 *= r;
-            acc[0] += cbrt(r5) * a.k.cTF_E;
-            if (a.wantV) v += a.k.cTF_V * cbrt(r * r) * a.tf_x;
+            acc[0] += (double)(mcbrt(r5) * cTF_E);
+            if (a.wantV) v += cTF_V * mcbrt(r * r) * tf_x;
         }
         if (a.xc) {
             // built-in LDA, Slater exchange + PZ81 (xc/semilocal_xc.py:283-319)
-            double rc = cbrt(r);
-            if (rc < 1e-30) rc = 1e-30;
-            double Rs = a.k.lda_rs / rc;
-            double ex, vx;
-            if (Rs < 1.0) {
-                double lr = log(Rs);
-                ex = a.k.lda_ex * rc + (cPZ[0] * lr + cPZ[1] + cPZ[2] * Rs * lr + cPZ[3] * Rs);
-                vx = a.k.lda_vx * rc +
-                     (lr * (cPZ[0] + 2.0 / 3 * cPZ[2] * Rs) + cPZ[1] - 1.0 / 3 * cPZ[0] +
-                      1.0 / 3 * (2 * cPZ[3] - cPZ[2]) * Rs);
+            M rc = mcbrt(r);
+            if (rc < tiny) rc = tiny;
+            const M Rs = lda_rs / rc;
+            M ex, vx;
+            if (Rs < (M)1) {
+                const M lr = mlog(Rs);
+                ex = lda_ex * rc + (P0 * lr + P1 + P2 * Rs * lr + P3 * Rs);
+                vx = lda_vx * rc +
+                     (lr * (P0 + (M)(2.0 / 3) * P2 * Rs) + P1 - (M)(1.0 / 3) * P0 + (M)(1.0 / 3) * (2 * P3 - P2) * Rs);
             } else {
-                double s = sqrt(Rs);
-                double den = 1.0 + cPZ[5] * s + cPZ[6] * Rs;
-                ex = a.k.lda_ex * rc + cPZ[4] / den;
-                vx = a.k.lda_vx * rc +
-                     (cPZ[4] + (7.0 / 6.0 * cPZ[4] * cPZ[5]) * s + (4.0 / 3.0 * cPZ[4] * cPZ[6] * Rs)) / (den * den);
+                const M sRs = msqrt(Rs);
+                const M den = (M)1 + P5 * sRs + P6 * Rs;
+                ex = lda_ex * rc + P4 / den;
+                vx = lda_vx * rc +
+                     (P4 + ((M)(7.0 / 6.0) * P4 * P5) * sRs + ((M)(4.0 / 3.0) * P4 * P6 * Rs)) / (den * den);
             }
-            acc[1] += ex * r;
+            acc[1] += (double)(ex * r);
             v += vx;
         }
         if (a.pp) {
-            double vl = (double)a.vloc[i];
-            acc[2] += vl * r;
+            const M vl = a.vloc[i];
+            acc[2] += (double)(vl * r);
             v += vl;
         }
-        if (a.vw) a.sq[i] = (T)sqrt(r > 0.0 ? r : 1e-30);  // kedf/vw.py:34-44
+        if (a.vw) a.sq[i] = msqrt(r > (M)0 ? r : tiny);  // kedf/vw.py:34-44
         if (a.nl) {
-            double rc = a.nl_is_lwt ? (r > 0.0 ? r : 1e-30) : (r < kZERO ? kZERO : r);
-            double pb = pow(rc, a.beta);
-            a.rb[i] = (T)pb;
-            if (!a.same_ab) a.ra[i] = (T)pow(rc, a.alpha);
+            const M rc = a.nl_is_lwt ? (r > (M)0 ? r : tiny) : (r < zero_clamp ? zero_clamp : r);
+            a.rb[i] = mpow(rc, beta);
+            if (!a.same_ab) a.ra[i] = mpow(rc, alpha);
         }
         if (a.lwt) {
-            double kf = 2.0 * cbrt(a.k.threepi2 * r);  // kedf/lwt.py:106
-            a.kf[i] = (T)kf;
-            double kfr = (double)(T)kf;
-            acc[4] = fmin(acc[4], kfr);
-            acc[5] = fmax(acc[5], kfr);
+            const M kf = (M)2 * mcbrt(threepi2 * r);  // kedf/lwt.py:106
+            a.kf[i] = kf;
+            acc[4] = fmin(acc[4], (double)kf);
+            acc[5] = fmax(acc[5], (double)kf);
         }
-        if (a.wantV) a.V[i] = (T)v;
+        if (a.wantV) a.V[i] = v;
     }
     block_reduce_store<PRE_NS>(acc, kinds, partials);
 }
@@ -174,42 +196,44 @@ __device__ inline double lindhard_dev(double eta, double lbda, double mu) {
 
 template <typename T>
 __global__ void k_gspace(GArgs<T> a) {
+    using M = T;  // working precision of the multipliers
     const long long stride = (long long)gridDim.x * blockDim.x;
     const bool recompute = a.wtK && a.wtstate[1] != 0.0;
+    const M invN = (M)a.invN, fourpi = (M)(4.0 * M_PI), half = (M)0.5;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.geo.Nc; i += stride) {
-        double gg = gsq(a.geo, i);
+        const M gg = gsq_t<M>(a.geo, i);
         if (a.rhoG) {  // Hartree: 4 pi / G^2, G=0 -> 0 (hartree.py:33-35, grid.py:532-541)
-            double f = (i == 0) ? 0.0 : 4.0 * M_PI / gg * a.invN;
+            const M f = (i == 0) ? (M)0 : fourpi / gg * invN;
             auto z = a.rhoG[i];
-            z.x = (T)(z.x * f);
-            z.y = (T)(z.y * f);
+            z.x = z.x * f;
+            z.y = z.y * f;
             a.rhoG[i] = z;
         }
         if (a.sqG) {  // vW: G^2 (vw.py:45-51) with the 1/2 folded in
-            double f = 0.5 * gg * a.invN;
+            const M f = half * gg * invN;
             auto z = a.sqG[i];
-            z.x = (T)(z.x * f);
-            z.y = (T)(z.y * f);
+            z.x = z.x * f;
+            z.y = z.y * f;
             a.sqG[i] = z;
         }
-        if (a.wtK) {  // Wang-Teter kernel (kernel.py:325-334), cached per rho0
-            double K;
+        if (a.wtK) {  // Wang-Teter kernel (kernel.py:325-334), cached per rho0, built in float64
+            M K;
             if (recompute) {
-                double q = sqrt(gg);
-                K = lindhard_dev(q / a.wtstate[2], a.wt_x, 1.0) * a.wtstate[3];
-                a.wtK[i] = (T)K;
+                const double q = sqrt(gsq(a.geo, i));
+                K = (M)(lindhard_dev(q / a.wtstate[2], a.wt_x, 1.0) * a.wtstate[3]);
+                a.wtK[i] = K;
             } else {
-                K = (double)a.wtK[i];
+                K = a.wtK[i];
             }
-            double f = K * a.invN;
+            const M f = K * invN;
             auto z = a.rbG[i];
-            z.x = (T)(z.x * f);
-            z.y = (T)(z.y * f);
+            z.x = z.x * f;
+            z.y = z.y * f;
             a.rbG[i] = z;
             if (a.raG) {
                 auto w = a.raG[i];
-                w.x = (T)(w.x * f);
-                w.y = (T)(w.y * f);
+                w.x = w.x * f;
+                w.y = w.y * f;
                 a.raG[i] = w;
             }
         }
@@ -244,13 +268,22 @@ struct Table {
     double limit, limitd;  // values at etamax
 };
 
+// one interval's four coefficients in a single vector load (rows are 16 B
+// aligned for float32, 32 B for float64; the table is read through L2)
+__device__ inline float4 coef4(const float* c, int l) { return __ldg(reinterpret_cast<const float4*>(c) + l); }
+__device__ inline double4 coef4(const double* c, int l) {
+    const double2* p = reinterpret_cast<const double2*>(c) + 2 * (long long)l;
+    double2 a = __ldg(p), b = __ldg(p + 1);
+    return make_double4(a.x, a.y, b.x, b.y);
+}
+
 template <typename T>
 __device__ inline T spline_eval(const T* c, int nint, T step, T inv_step, T eta) {
     int l = (int)(eta * inv_step);
     l = l < 0 ? 0 : (l >= nint ? nint - 1 : l);
     T u = eta - (T)l * step;
-    const T* q = c + 4 * (long long)l;
-    return q[0] + u * (q[1] + u * (q[2] + u * q[3]));
+    const auto q = coef4(c, l);
+    return q.x + u * (q.y + u * (q.z + u * q.w));
 }
 
 struct Nodes {
@@ -400,6 +433,7 @@ struct InterpArgs {
 
 template <typename T>
 __global__ void k_lwt_interp(InterpArgs<T> a) {
+    using M = T;  // working precision of the weights; membership tests stay float64
     extern __shared__ double sh[];
     double* kn = sh;
     double* kup = sh + a.m;
@@ -410,93 +444,91 @@ __global__ void k_lwt_interp(InterpArgs<T> a) {
     __syncthreads();
     const long long stride = (long long)gridDim.x * blockDim.x;
     const int j1 = a.j0 + a.nb;
+    // interval coordinate t = (kf - k_i) / (k_{i+1} - k_i), as the reference divides
+    auto tcoord = [&](double kf, int i) { return (M)(kf - kn[i]) / (M)(kn[i + 1] - kn[i]); };
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < a.N; r += stride) {
-        double kf = fmin((double)a.kf[r], a.kfclip);
-        Member mb = membership(kf, kn, kup, a.m, sizeof(T) == 4);
-        double p1 = 0.0, p3 = 0.0;
-        // weights of nodes il (lower) and il+1 (upper) of the deciding interval
-        auto P = [&](int j) { return (double)a.PM[(long long)(j - a.j0) * a.N + r]; };
-        auto M = [&](int j) { return (double)a.PM[(long long)(a.nb + j - a.j0) * a.N + r]; };
+        const double kf = fmin((double)a.kf[r], a.kfclip);
+        const Member mb = membership(kf, kn, kup, a.m, sizeof(T) == 4);
+        M p1 = (M)0, p3 = (M)0;
+        auto P = [&](int j) { return a.PM[(long long)(j - a.j0) * a.N + r]; };
+        auto Md = [&](int j) { return a.PM[(long long)(a.nb + j - a.j0) * a.N + r]; };
         if (mb.ilast >= 0) {
             const int i = mb.ilast;
-            const double D = kn[i + 1] - kn[i];
-            const double t = (kf - kn[i]) / D;
+            const M D = (M)(kn[i + 1] - kn[i]);
+            const M t = tcoord(kf, i);
             if (!a.hermite) {
-                const double t0 = 1.0 - t;
+                const M t0 = (M)1 - t;
                 if (i >= a.j0 && i < j1) {
                     p1 += P(i) * t0;
-                    if (a.kdd == 3) p3 += M(i) * t0;
+                    if (a.kdd == 3) p3 += Md(i) * t0;
                 }
                 if (i + 1 >= a.j0 && i + 1 < j1) {
                     p1 += P(i + 1) * t;
-                    if (a.kdd == 3) p3 += M(i + 1) * t;
+                    if (a.kdd == 3) p3 += Md(i + 1) * t;
                 }
             } else {
-                const double t2 = t * t, t3 = t2 * t;
-                const double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = t3 - 2.0 * t2 + t, h01 = 1.0 - h00,
-                             h11 = t3 - t2;
-                const double h00D = 6.0 * t2 - 6 * t, h10D = 3.0 * t2 - 4 * t + 1.0, h01D = -h00D,
-                             h11D = 3.0 * t2 - 2 * t;
+                const M t2 = t * t, t3 = t2 * t;
+                const M h00 = (M)2 * t3 - (M)3 * t2 + (M)1, h10 = t3 - (M)2 * t2 + t, h01 = (M)1 - h00,
+                        h11 = t3 - t2;
+                const M h00D = (M)6 * t2 - 6 * t, h10D = (M)3 * t2 - 4 * t + (M)1, h01D = -h00D,
+                        h11D = (M)3 * t2 - 2 * t;
                 if (i >= a.j0 && i < j1) {
-                    p1 += h00 * P(i) + D * h10 * M(i);
-                    if (a.kdd == 3) p3 += h00D * P(i) / D + h10D * M(i);
+                    p1 += h00 * P(i) + D * h10 * Md(i);
+                    if (a.kdd == 3) p3 += h00D * P(i) / D + h10D * Md(i);
                 }
                 if (i + 1 >= a.j0 && i + 1 < j1) {
-                    p1 += h01 * P(i + 1) + D * h11 * M(i + 1);
-                    if (a.kdd == 3) p3 += h01D * P(i + 1) / D + h11D * M(i + 1);
+                    p1 += h01 * P(i + 1) + D * h11 * Md(i + 1);
+                    if (a.kdd == 3) p3 += h01D * P(i + 1) / D + h11D * Md(i + 1);
                 }
             }
         } else if (mb.small) {
-            const double ts = (kf - kn[0]) / kn[0];
+            const M ts = (M)(kf - kn[0]) / (M)kn[0];
             if (a.j0 == 0) p1 += P(0) * ts;
         }
         if (a.first) {
-            a.pot1[r] = (T)p1;
-            if (a.kdd == 3) a.pot3[r] = (T)p3;
+            a.pot1[r] = p1;
+            if (a.kdd == 3) a.pot3[r] = p3;
         } else {
-            a.pot1[r] = (T)((double)a.pot1[r] + p1);
-            if (a.kdd == 3) a.pot3[r] = (T)((double)a.pot3[r] + p3);
+            a.pot1[r] = a.pot1[r] + p1;
+            if (a.kdd == 3) a.pot3[r] = a.pot3[r] + p3;
         }
         if (a.kdd > 1) {
-            // hat weights W_j (and WD_j for hermite) of every containing interval
-            const double rA = (double)a.rA[r];
-            int ints[2] = {mb.ilast, mb.iprev};
-            double w[4] = {0, 0, 0, 0};  // weights for nodes base, base+1 (W) and (WD)
-            int base = mb.ilast >= 0 ? (mb.iprev >= 0 ? mb.iprev : mb.ilast) : 0;
-            // up to three distinct nodes: base, base+1, base+2
-            double W[3] = {0, 0, 0}, WD[3] = {0, 0, 0};
+            // hat weights W_j (and WD_j for hermite) of every containing interval;
+            // at most three distinct nodes: base, base+1, base+2
+            const M rA = a.rA[r];
+            const int ints[2] = {mb.ilast, mb.iprev};
+            const int base = mb.ilast >= 0 ? (mb.iprev >= 0 ? mb.iprev : mb.ilast) : 0;
+            M W[3] = {0, 0, 0}, WD[3] = {0, 0, 0};
             for (int q = 0; q < 2; ++q) {
                 const int i = ints[q];
                 if (i < 0) continue;
-                const double D = kn[i + 1] - kn[i];
-                const double t = (kf - kn[i]) / D;
+                const M t = tcoord(kf, i);
                 if (!a.hermite) {
-                    W[i - base] += 1.0 - t;
+                    W[i - base] += (M)1 - t;
                     W[i + 1 - base] += t;
                 } else {
-                    const double t2 = t * t, t3 = t2 * t;
-                    const double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = t3 - 2.0 * t2 + t, h01 = 1.0 - h00,
-                                 h11 = t3 - t2;
+                    const M D = (M)(kn[i + 1] - kn[i]);
+                    const M t2 = t * t, t3 = t2 * t;
+                    const M h00 = (M)2 * t3 - (M)3 * t2 + (M)1, h10 = t3 - (M)2 * t2 + t, h01 = (M)1 - h00,
+                            h11 = t3 - t2;
                     W[i - base] += h00;
                     W[i + 1 - base] += h01;
                     WD[i - base] += D * h10;
                     WD[i + 1 - base] += D * h11;
                 }
             }
-            (void)w;
-            double ws0 = 0.0;
-            if (mb.small) ws0 = (kf - kn[0]) / kn[0];
+            const M ws0 = mb.small ? (M)(kf - kn[0]) / (M)kn[0] : (M)0;
             for (int jj = 0; jj < a.nb; ++jj) {
                 const int j = a.j0 + jj;
-                double wj = 0.0, wdj = 0.0;
+                M wj = (M)0, wdj = (M)0;
                 const int d = j - base;
                 if (mb.ilast >= 0 && d >= 0 && d < 3) {
                     wj = W[d];
                     wdj = WD[d];
                 }
                 if (j == 0) wj += ws0;
-                a.u[(long long)jj * a.N + r] = (T)(rA * wj);
-                if (a.hermite) a.u[(long long)(a.nb + jj) * a.N + r] = (T)(rA * wdj);
+                a.u[(long long)jj * a.N + r] = rA * wj;
+                if (a.hermite) a.u[(long long)(a.nb + jj) * a.N + r] = rA * wdj;
             }
         }
     }
@@ -531,59 +563,63 @@ constexpr int POST_NS = 3;
 
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double* partials) {
+    using M = T;  // working precision; energies accumulate in float64
     double acc[POST_NS] = {0.0, 0.0, 0.0};
+    const M alpha = (M)a.alpha, beta = (M)a.beta, vw_y = (M)a.vw_y, ld = (M)a.ld, rhomax = (M)a.rhomax;
+    const M kfclip = (M)a.kfclip, tiny = (M)1e-30, zero_clamp = (M)kZERO;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
-        const double r = (double)a.rho[i];
-        double v = a.wantV ? (double)a.V[i] : 0.0;
+        const M r = a.rho[i];
+        M v = a.wantV ? a.V[i] : (M)0;
         if (a.vw) {
-            double s = (double)a.sq[i];
-            if (fabs(s) < 1e-30) s = 1e-30;
-            double pw = (double)a.lap[i] / s;
-            if (r > 0.0) acc[0] += r * pw;
-            v += pw * a.vw_y;
+            M s = a.sq[i];
+            if (fabs(s) < tiny) s = tiny;
+            const M pw = a.lap[i] / s;
+            if (r > (M)0) acc[0] += (double)(r * pw);
+            v += pw * vw_y;
         }
         if (a.h) {
-            double vh = (double)a.vH[i];
-            acc[1] += vh * r;
+            const M vh = a.vH[i];
+            acc[1] += (double)(vh * r);
             v += vh;
         }
         if (a.wt) {
-            double rc = r < kZERO ? kZERO : r;
-            double pb = (double)a.rb[i];
-            double c1 = (double)a.nl1[i];
+            const M rc = r < zero_clamp ? zero_clamp : r;
+            const M pb = a.rb[i];
+            const M c1 = a.nl1[i];
             if (a.same_ab) {
-                double pot = 2.0 * a.alpha * (pb / rc) * c1;  // wt.py:19-23
+                const M pot = (M)2 * alpha * (pb / rc) * c1;  // wt.py:19-23
                 if (a.wantV) {
-                    acc[2] += pot * r / (2.0 * a.alpha);      // wt.py:124-125
+                    acc[2] += (double)(pot * r / ((M)2 * alpha));  // wt.py:124-125
                     v += pot;
                 } else {
-                    acc[2] += c1 * pb;                        // wt.py:44-56
+                    acc[2] += (double)(c1 * pb);  // wt.py:44-56
                 }
             } else {
-                double pa = (double)a.ra[i];
-                acc[2] += c1 * pa;
-                if (a.wantV) v += a.alpha * (pa / rc) * c1 + a.beta * (pb / rc) * (double)a.nl2[i];
+                const M pa = a.ra[i];
+                acc[2] += (double)(c1 * pa);
+                if (a.wantV) v += alpha * (pa / rc) * c1 + beta * (pb / rc) * a.nl2[i];
             }
         }
         if (a.lwt) {
             // low-density factor (lwt.py:315-322) and the final combination (:324-339)
-            double f = 1.0;
-            if (r < 1e-6) f = pow(fabs(r), a.ld) / pow(a.rhomax, a.ld);
-            if (r < 0.0) f = 0.0;
-            double rc = r > 0.0 ? r : 1e-30;
-            double pa = a.same_ab ? (double)a.rb[i] : (double)a.ra[i];
-            double p1 = (double)a.pot1[i] * f;
-            acc[2] += pa * p1;
+            M f = (M)1;
+            if (r < (M)1e-6) f = mpow(fabs(r), ld) / mpow(rhomax, ld);
+            if (r < (M)0) f = (M)0;
+            const M rc = r > (M)0 ? r : tiny;
+            const M pa = a.same_ab ? a.rb[i] : a.ra[i];
+            const M p1 = a.pot1[i] * f;
+            acc[2] += (double)(pa * p1);
             if (a.wantV) {
-                double pb = (double)a.rb[i];
-                double p2 = (a.kdd > 1 ? (double)a.pot2[i] : (double)a.pot1[i]) * f;
-                double p3 = (a.kdd == 3 ? (double)a.pot3[i] : 0.0) * f;
-                double kf = fmin((double)a.kf[i], a.kfclip);
-                v += a.alpha * (pa / rc) * p1 + (a.beta * (pb / rc) * p2 + (kf / 3.0) * (pa / rc) * p3);
+                const M pb = a.rb[i];
+                const M p2 = (a.kdd > 1 ? a.pot2[i] : a.pot1[i]) * f;
+                const M p3 = (a.kdd == 3 ? a.pot3[i] : (M)0) * f;
+                const M kfv = a.kf[i];
+                const M kf = kfv < kfclip ? kfv : kfclip;
+                v += alpha * (pa / rc) * p1 + (beta * (pb / rc) * p2 + (kf / (M)3) * (pa / rc) * p3);
             }
         }
-        if (a.wantV) a.V[i] = (T)v;
+        if (a.wantV) a.V[i] = v;
     }
     block_sum_store<POST_NS>(acc, partials);
 }

@@ -100,5 +100,50 @@ class Optimization:
         self.functional = total(rho, calcType={"E", "V"})
         return rho
 
+    def optimize_rho_mixed(self, guess_rho=None, econv_f32=None, f32_method=None, refine_method=None,
+                           refine_maxiter=None):
+        """FP32-mixed ground state with a final FP64 refinement.
+
+        Stage 1 optimises in FP32-mixed (float32 fields and FFTs, float64
+        reductions) until the energy changes by less than ``econv_f32``
+        (default 10x the FP64 econv) or the line search can make no progress.
+        Stage 2 continues in FP64 from that density with the FP64 econv, so the
+        converged energy and density are those of the FP64 functional.
+        Returns the FP64 density; ``self.stages`` records both stages."""
+        if guess_rho is not None:
+            self.rho = guess_rho
+        o = dict(self.optimization_options)
+        econv64 = o["econv"]
+        stages = []
+        m32 = f32_method or ("LBFGS" if self.optimization_method == "TN" else self.optimization_method)
+        o32 = dict(o, econv=econv_f32 if econv_f32 is not None else 10.0 * econv64)
+        opt32 = Optimization(m32, o32, self.EnergyEvaluator)
+        opt32.verbose = self.verbose
+        rho32 = opt32.optimize_rho(guess_rho=self.rho, dtype=torch.float32)
+        stages.append({"precision": "f32", "method": m32, "niter": opt32.result.niter,
+                       "nfev": opt32.result.nfev, "converged": opt32.converged, "energy": opt32.result.energy})
+        o64 = dict(o)
+        if refine_maxiter is not None:
+            o64["maxiter"] = refine_maxiter
+        opt64 = Optimization(refine_method or self.optimization_method, o64, self.EnergyEvaluator)
+        opt64.verbose = self.verbose
+        # float32 fields keep the electron count only to ~1e-7; the FP64 stage
+        # conserves whatever count it starts from, so restore the guess's count
+        guess = self.rho if isinstance(self.rho, DirectField) else DirectField(rho32.grid, data=self.rho)
+        n_target = DirectField(rho32.grid, data=guess, dtype=torch.float64).integral()
+        rho_start = rho32.as_subclass(torch.Tensor).double()
+        n32 = DirectField(rho32.grid, data=rho_start).integral()
+        rho = opt64.optimize_rho(guess_rho=rho_start * (n_target / n32), dtype=torch.float64)
+        stages.append({"precision": "f64", "method": opt64.optimization_method, "niter": opt64.result.niter,
+                       "nfev": opt64.result.nfev, "converged": opt64.converged, "energy": opt64.result.energy})
+        self.stages = stages
+        self.result = opt64.result
+        self.converged = opt64.converged
+        self.mu = opt64.mu
+        self.rho = rho
+        self.phi = opt64.phi
+        self.functional = opt64.functional
+        return rho
+
     def __call__(self, guess_rho=None, calcType={"E", "V"}, guess_phi=None, lphi=False):
         return self.optimize_rho(guess_rho=guess_rho, guess_phi=guess_phi, lphi=lphi)

@@ -266,7 +266,31 @@ struct Table {
     int nint;        // neta - 1
     double step, inv_step, etamax;
     double limit, limitd;  // values at etamax
+    double factor, lbda;   // table = factor * F(eta; lbda, 1); closed form used above eta_series
+    double eta_series;     // FP32 path: closed-form large-eta series at and above this eta
 };
+
+// Large-eta branch of the inverse Lindhard function (kernel.py:79-133) with
+// mu = 1: F = -lbda - 0.6 + sum_k c_k eta^{-2k}, and -eta dF/deta = sum_k 2k c_k
+// eta^{-2k}.  The 50000-point spline of the table reproduces this smooth
+// series to ~1e-12 for eta >= 4, so the FP32 path evaluates it in registers.
+__constant__ float cLargeF[15] = {-0.13714285714285712f, -6.39999999999999875e-2f, -3.77825602968460128e-2f,
+                                  -2.51824061652633074e-2f, -1.80879839616166146e-2f, -1.36715733124818332e-2f,
+                                  -1.07236045520990083e-2f, -8.65192783339199453e-3f, -7.1372762502456763e-3f,
+                                  -5.9945117538835746e-3f, -5.10997527675418131e-3f, -4.41060829979912465e-3f,
+                                  -3.84763737842981233e-3f, -3.38745061493813488e-3f, -3.00624946457977689e-3f};
+
+__device__ inline void large_eta_series(float eta, float factor, float lbda, bool deriv, float& K, float& KD) {
+    const float inv2 = 1.0f / (eta * eta);
+    float f = cLargeF[14], d = 30.0f * cLargeF[14];
+#pragma unroll
+    for (int k = 13; k >= 0; --k) {
+        f = fmaf(f, inv2, cLargeF[k]);
+        if (deriv) d = fmaf(d, inv2, (float)(2 * (k + 1)) * cLargeF[k]);
+    }
+    K = factor * (-lbda - 0.6f + f * inv2);
+    KD = deriv ? factor * d * inv2 : 0.0f;
+}
 
 // one interval's four coefficients in a single vector load (rows are 16 B
 // aligned for float32, 32 B for float64; the table is read through L2)
@@ -298,8 +322,15 @@ __device__ inline void node_kernel(const Table<T>& tab, T q, T invk, bool deriv,
     const T eta = q * invk;
     KD = (T)0;
     if (eta < (T)tab.etamax) {
-        K = spline_eval(tab.c, tab.nint, (T)tab.step, (T)tab.inv_step, eta);
-        if (deriv) KD = spline_eval(tab.cd, tab.nint, (T)tab.step, (T)tab.inv_step, eta);
+        if (sizeof(T) == 4 && eta >= (T)tab.eta_series) {
+            float k, kd;
+            large_eta_series((float)eta, (float)tab.factor, (float)tab.lbda, deriv, k, kd);
+            K = (T)k;
+            KD = (T)kd;
+        } else {
+            K = spline_eval(tab.c, tab.nint, (T)tab.step, (T)tab.inv_step, eta);
+            if (deriv) KD = spline_eval(tab.cd, tab.nint, (T)tab.step, (T)tab.inv_step, eta);
+        }
     } else {
         K = (T)tab.limit;
         KD = (T)tab.limitd;
@@ -757,6 +788,9 @@ Table<T> table_of(const ofdft_eval* e) {
     t.etamax = e->cfg.lwt_etamax;
     t.limit = e->tab_limit;
     t.limitd = e->tab_limitd;
+    t.factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
+    t.lbda = e->cfg.lwt_x;
+    t.eta_series = 4.0;
     return t;
 }
 

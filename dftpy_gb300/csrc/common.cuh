@@ -55,6 +55,21 @@ struct Error {
 
 #define OFDFT_LAUNCH_CHECK() OFDFT_CK(cudaGetLastError())
 
+// Setup-time copies made without a caller stream (tables, ion lists).  A plain
+// cudaMemcpy from pageable memory may return before its DMA lands and is not
+// ordered before kernels on non-blocking streams, so these copies go through
+// the calling thread's default stream and are waited for: when they return,
+// kernels launched afterwards on any stream see the data.
+inline void upload_now(void* dst, const void* src, size_t bytes) {
+    OFDFT_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, cudaStreamPerThread));
+    OFDFT_CK(cudaStreamSynchronize(cudaStreamPerThread));
+}
+
+inline void zero_now(void* dst, size_t bytes) {
+    OFDFT_CK(cudaMemsetAsync(dst, 0, bytes, cudaStreamPerThread));
+    OFDFT_CK(cudaStreamSynchronize(cudaStreamPerThread));
+}
+
 // Run a body and convert exceptions into the int status of the C ABI.
 template <class F>
 int guard(F&& f) {

@@ -278,7 +278,8 @@ void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, d
     OFDFT_CK(cudaStreamSynchronize(st));
     const double e_real = g->h_results[0] / 2.0;
     std::vector<double> Freal(3 * (size_t)nat);
-    OFDFT_CK(cudaMemcpy(Freal.data(), d_Fr, 3 * (size_t)nat * sizeof(double), cudaMemcpyDeviceToHost));
+    OFDFT_CK(cudaMemcpyAsync(Freal.data(), d_Fr, 3 * (size_t)nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+    OFDFT_CK(cudaStreamSynchronize(st));
 
     // ---- reciprocal space
     double e_rec = 0.0;

@@ -316,8 +316,8 @@ void bspline_tables(const ofdft_grid* g, int order, double** d_re, double** d_im
     }
     OFDFT_CK(cudaMalloc(d_re, re.size() * sizeof(double)));
     OFDFT_CK(cudaMalloc(d_im, im.size() * sizeof(double)));
-    OFDFT_CK(cudaMemcpy(*d_re, re.data(), re.size() * sizeof(double), cudaMemcpyHostToDevice));
-    OFDFT_CK(cudaMemcpy(*d_im, im.data(), im.size() * sizeof(double), cudaMemcpyHostToDevice));
+    upload_now(*d_re, re.data(), re.size() * sizeof(double));
+    upload_now(*d_im, im.data(), im.size() * sizeof(double));
 }
 }  // namespace ofdft
 
@@ -498,14 +498,14 @@ int ofdft_pseudo_create(ofdft_grid* g, int nspecies, const int* npts, const doub
                 OFDFT_CK(cudaMalloc(&dc, S.c.size() * sizeof(double)));
                 p->d_x.push_back(dx);
                 p->d_c.push_back(dc);
-                OFDFT_CK(cudaMemcpy(dx, S.x.data(), S.x.size() * sizeof(double), cudaMemcpyHostToDevice));
-                OFDFT_CK(cudaMemcpy(dc, S.c.data(), S.c.size() * sizeof(double), cudaMemcpyHostToDevice));
+                upload_now(dx, S.x.data(), S.x.size() * sizeof(double));
+                upload_now(dc, S.c.data(), S.c.size() * sizeof(double));
             }
             bspline_tables(g, bspline_order, &p->d_bre, &p->d_bim);
             double inv[9];
             lattice_inverse(g->lattice, inv);
             OFDFT_CK(cudaMalloc(&p->d_cinv, 9 * sizeof(double)));
-            OFDFT_CK(cudaMemcpy(p->d_cinv, inv, 9 * sizeof(double), cudaMemcpyHostToDevice));
+            upload_now(p->d_cinv, inv, 9 * sizeof(double));
         } catch (...) {
             ofdft_pseudo_destroy(p);
             throw;
@@ -561,11 +561,11 @@ int ofdft_pseudo_set_ions(ofdft_pseudo* p, int nat, const double* pos, const int
         OFDFT_CK(cudaMalloc(&p->d_spec, (size_t)nat * sizeof(int)));
         OFDFT_CK(cudaMalloc(&p->d_sel, (size_t)nat * sizeof(int)));
         OFDFT_CK(cudaMalloc(&p->d_scale, (size_t)nat * sizeof(double)));
-        OFDFT_CK(cudaMemcpy(p->d_pos, pos, 3 * (size_t)nat * sizeof(double), cudaMemcpyHostToDevice));
-        OFDFT_CK(cudaMemcpy(p->d_frac, p->frac.data(), 3 * (size_t)nat * sizeof(double), cudaMemcpyHostToDevice));
-        OFDFT_CK(cudaMemcpy(p->d_spec, species, (size_t)nat * sizeof(int), cudaMemcpyHostToDevice));
-        OFDFT_CK(cudaMemcpy(p->d_sel, sel.data(), (size_t)nat * sizeof(int), cudaMemcpyHostToDevice));
-        OFDFT_CK(cudaMemcpy(p->d_scale, scale.data(), (size_t)nat * sizeof(double), cudaMemcpyHostToDevice));
+        upload_now(p->d_pos, pos, 3 * (size_t)nat * sizeof(double));
+        upload_now(p->d_frac, p->frac.data(), 3 * (size_t)nat * sizeof(double));
+        upload_now(p->d_spec, species, (size_t)nat * sizeof(int));
+        upload_now(p->d_sel, sel.data(), (size_t)nat * sizeof(int));
+        upload_now(p->d_scale, scale.data(), (size_t)nat * sizeof(double));
     });
 }
 

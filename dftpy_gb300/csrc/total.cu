@@ -769,8 +769,8 @@ void build_table(ofdft_eval* e) {
     }
     OFDFT_CK(cudaMalloc(&e->tab_c, hc.size() * sizeof(T)));
     OFDFT_CK(cudaMalloc(&e->tab_cd, hcd.size() * sizeof(T)));
-    OFDFT_CK(cudaMemcpy(e->tab_c, hc.data(), hc.size() * sizeof(T), cudaMemcpyHostToDevice));
-    OFDFT_CK(cudaMemcpy(e->tab_cd, hcd.data(), hcd.size() * sizeof(T), cudaMemcpyHostToDevice));
+    upload_now(e->tab_c, hc.data(), hc.size() * sizeof(T));
+    upload_now(e->tab_cd, hcd.data(), hcd.size() * sizeof(T));
     e->tab_nint = nint;
     e->tab_step = step;
     e->tab_limit = S.eval(etamax);
@@ -1146,7 +1146,7 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
         e->k = make_consts();
         try {
             OFDFT_CK(cudaMalloc(&e->wtstate, 8 * sizeof(double)));
-            OFDFT_CK(cudaMemset(e->wtstate, 0, 8 * sizeof(double)));
+            zero_now(e->wtstate, 8 * sizeof(double));
             if (c.kedf_terms & OFDFT_KE_LWT) {
                 if (g->prec == OFDFT_F64) build_table<double>(e);
                 else build_table<float>(e);

@@ -50,9 +50,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--gs", action="store_true", help="also time the ground-state optimisation")
-    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch"],
-                   help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems")
-    p.add_argument("--threads", type=int, default=16, help="concurrent systems for --workload batch")
+    p.add_argument("--workload", default="ev", choices=["ev", "diff"],
+                   help="ev: the E+V metric (default); diff: differentiation")
     return p.parse_args()
 
 
@@ -475,81 +474,10 @@ def diff_workload(args):
     print(json.dumps(out), flush=True)
 
 
-def batch_workload(args):
-    """64 independent Al-like cells (sc/bcc/fcc, 4-108 atoms, a in [7.3, 7.9]
-    Bohr, sigma = 0.1 Bohr, grids from {48, 64, 72, 80, 96}^3), TF + vW + LDA +
-    Hartree + PME local PP + Ewald, ground states from the uniform density:
-    all systems concurrently in FP32-mixed (+ FP64 refinement) against the
-    same systems solved one after another in plain FP64."""
-    import torch
-    import dftpy_gb300 as D
-    from dftpy_gb300 import synthetic as syn
-    from dftpy_gb300.batch import optimize_many
-    torch.cuda.set_device(0)
-    systems = syn.batch_systems(64, seed=5)
-    gp, vp = syn.analytic_vloc(3.0, 1.0)
-
-    def build():
-        totals, guesses, nats = [], [], []
-        for lat, pos, nr in systems:
-            grid = D.DirectGrid(lat, nr)
-            ions = D.Ions(symbols=["Al"] * len(pos), positions=pos, cell=lat)
-            pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)})
-            totals.append(D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="TFVW"),
-                                            XCFunctional=D.Functional(type="XC", name="LDA"),
-                                            HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp))
-            guesses.append(D.DirectField(grid) + 3.0 * len(pos) / grid.volume)
-            nats.append(len(pos))
-        return totals, guesses, nats
-
-    opts = {"econv": None, "maxiter": 300}
-    totals, guesses, nats = build()
-    # plain FP64, one system after another
-    seq = []
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for tot, g, nat in zip(totals, guesses, nats):
-        o = dict(opts, econv=1e-7 * nat)
-        r, _ = optimize_many([tot], [g], "LBFGS", o, threads=1)
-        seq.append(r[0])
-    t_seq = time.perf_counter() - t0
-    # all systems at once: FP32-mixed then FP64 refinement
-    totals, guesses, nats = build()
-    res = [None] * len(totals)
-    from concurrent.futures import ThreadPoolExecutor
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-
-    # econv is per system (1e-7 Ha/atom); every system runs on its own stream
-    def one(i):
-        r, _ = optimize_many([totals[i]], [guesses[i]], "LBFGS", dict(opts, econv=1e-7 * nats[i]), mixed=True,
-                             threads=1)
-        res[i] = r[0]
-
-    with ThreadPoolExecutor(max_workers=args.threads) as ex:
-        list(ex.map(one, range(len(totals))))
-    torch.cuda.synchronize()
-    t_batch = time.perf_counter() - t0
-    de = [abs(b["energy"] - s["energy"]) / n for b, s, n in zip(res, seq, nats)]
-    out = {"workload": "64 Al-like cells (sc/bcc/fcc, 4-108 atoms), grids {48..96}^3, TF+vW+LDA+H+PME PP+Ewald",
-           "systems": len(systems), "atoms_total": int(sum(nats)),
-           "sequential_fp64": {"seconds": t_seq, "systems_per_s": len(systems) / t_seq,
-                               "per_system_s": t_seq / len(systems),
-                               "converged": sum(1 for r in seq if r["converged"] == 0)},
-           "concurrent_mixed": {"seconds": t_batch, "systems_per_s": len(systems) / t_batch,
-                                "per_system_s": t_batch / len(systems), "threads": args.threads,
-                                "converged": sum(1 for r in res if r["converged"] == 0)},
-           "speedup": t_seq / t_batch, "max_dE_per_atom": max(de), "mean_dE_per_atom": float(np.mean(de))}
-    print(json.dumps(out), flush=True)
-
-
 def main():
     args = parse()
     if args.workload == "diff":
         diff_workload(args)
-        return
-    if args.workload == "batch":
-        batch_workload(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -58,33 +58,6 @@ def random_alloy(nat, density_e_per_bohr3, zvals, min_sep, seed=0, max_tries=2_0
     return np.eye(3) * L, pos, species
 
 
-_CELLS = {"sc": np.zeros((1, 3)), "bcc": np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]]),
-          "fcc": np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])}
-# repetitions giving 4..108 atoms: sc 2,3,4 (8, 27, 64), bcc 2,3 (16, 54), fcc 1,2,3 (4, 32, 108)
-_REPS = {"sc": (2, 3, 4), "bcc": (2, 3), "fcc": (1, 2, 3)}
-
-
-def batch_systems(count=64, seed=5, grids=(48, 64, 72, 80, 96), alat=(7.3, 7.9), sigma=0.1):
-    """Independent Al-like cells of uneven size: a random cubic cell type
-    (sc/bcc/fcc), repetitions giving 4..108 atoms, lattice constant uniform in
-    ``alat`` (Bohr), Gaussian displacements ``sigma`` and a grid drawn from
-    ``grids``.  Returns a list of (lattice, positions, nr)."""
-    rng = np.random.default_rng(seed)
-    out = []
-    kinds = sorted(_CELLS)
-    for _ in range(count):
-        kind = kinds[rng.integers(len(kinds))]
-        reps = _REPS[kind][rng.integers(len(_REPS[kind]))]
-        a = rng.uniform(*alat)
-        lat = np.eye(3) * a
-        pos = _CELLS[kind] @ lat
-        lat, pos = supercell(lat, pos, (reps, reps, reps))
-        pos = pos + rng.normal(0.0, sigma, size=pos.shape)
-        n = int(grids[rng.integers(len(grids))])
-        out.append((lat, pos, (n, n, n)))
-    return out
-
-
 def analytic_vloc(Z, rc, A=15.0, npts=4096, gmax=40.0):
     """Radial local pseudopotential in G space on a uniform grid [0, gmax]:
     v(G) = -4 pi Z/G^2 exp(-G^2 rc^2/4) + A exp(-G^2 rc^2/4), with the finite

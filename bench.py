@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--gs", action="store_true", help="also time the ground-state optimisation")
+    p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused"],
+                   help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
     p.add_argument("--workload", default="ev", choices=["ev", "diff"],
                    help="ev: the E+V metric (default); diff: differentiation")
     return p.parse_args()
@@ -221,7 +223,8 @@ def gpu_arm(args):
     grid = D.DirectGrid(lat, (args.n,) * 3)
     ions = D.Ions(symbols=["Al"] * nat, positions=pos, cell=lat)
     pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
-    ke = D.Functional(type="KEDF", name="LWT", nsp=args.nsp, kdd=3, interp="linear", **WGC)
+    ke = D.Functional(type="KEDF", name="LWT", nsp=args.nsp, kdd=3, interp="linear", pipeline=args.lwt_pipeline,
+                      **WGC)
     tot = D.TotalFunctional(KineticEnergyFunctional=ke, XCFunctional=D.Functional(type="XC", name="LDA"),
                             HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -260,11 +263,11 @@ def gpu_arm(args):
         ms = t0.elapsed_time(t1)
         prof = None
         if profile:
-            ms_c = (_lib.C.c_double * 8)()
-            by_c = (_lib.C.c_double * 8)()
-            la_c = (_lib.C.c_longlong * 8)()
+            ms_c = (_lib.C.c_double * 16)()
+            by_c = (_lib.C.c_double * 16)()
+            la_c = (_lib.C.c_longlong * 16)()
             ncls = _lib.C.c_int()
-            _lib.check(lib.ofdft_eval_profile_read(ev.h, 8, ms_c, by_c, la_c, _lib.C.byref(ncls)))
+            _lib.check(lib.ofdft_eval_profile_read(ev.h, 16, ms_c, by_c, la_c, _lib.C.byref(ncls)))
             _lib.check(lib.ofdft_eval_profile(ev.h, 0))
             prof = {lib.ofdft_profile_class_name(i).decode(): {"ms": ms_c[i], "bytes": by_c[i], "launches": la_c[i]}
                     for i in range(ncls.value)}

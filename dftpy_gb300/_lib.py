@@ -18,6 +18,7 @@ CALC_E, CALC_V = 1, 2
 E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, NE = range(10)
 KE_TF, KE_VW, KE_WT, KE_LWT = 1, 2, 4, 8
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
+LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
 OPT_TN, OPT_LBFGS, OPT_CGHS = 0, 1, 2
 
 
@@ -35,6 +36,7 @@ class Config(C.Structure):
         ("lwt_kdd", C.c_int), ("lwt_interp", C.c_int), ("lwt_etamax", C.c_double), ("lwt_neta", C.c_int),
         ("lwt_kfmin", C.c_double), ("lwt_kfmax", C.c_double), ("lwt_ldw", C.c_double), ("lwt_max_batch", C.c_int),
         ("xc_lda", C.c_int), ("hartree", C.c_int), ("pseudo", C.c_int), ("ewald_energy", C.c_double),
+        ("lwt_pipeline", C.c_int),
     ]
 
 

@@ -135,12 +135,8 @@ __device__ inline double gsq_t<double>(const Geo& g, long long idx) {
     return gsq(g, idx);
 }
 
-template <>
-__device__ inline float gsq_t<float>(const Geo& g, long long idx) {
-    int k = (int)(idx % g.n2h);
-    int t = (int)(idx / g.n2h);
-    int j = t % g.n1;
-    int i = t / g.n1;
+// float32 |G|^2 of half-grid indices (i, j, k)
+__device__ inline float gsq_f(const Geo& g, int i, int j, int k) {
     float f0 = (float)(i < (g.n0 - 1) / 2 + 1 ? i : i - g.n0);
     float f1 = (float)(j < (g.n1 - 1) / 2 + 1 ? j : j - g.n1);
     float f2 = (float)k;
@@ -148,6 +144,15 @@ __device__ inline float gsq_t<float>(const Geo& g, long long idx) {
     float gy = f0 * g.bf[1] + f1 * g.bf[4] + f2 * g.bf[7];
     float gz = f0 * g.bf[2] + f1 * g.bf[5] + f2 * g.bf[8];
     return gx * gx + gy * gy + gz * gz;
+}
+
+template <>
+__device__ inline float gsq_t<float>(const Geo& g, long long idx) {
+    int k = (int)(idx % g.n2h);
+    int t = (int)(idx / g.n2h);
+    int j = t % g.n1;
+    int i = t / g.n1;
+    return gsq_f(g, i, j, k);
 }
 
 // Half-space mask that counts each +-G pair once (src/dftpy/grid.py:658-695,

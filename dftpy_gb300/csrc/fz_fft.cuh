@@ -1,0 +1,191 @@
+// Float32 tile FFTs for the fused density-dependent-kernel pipeline.
+//
+// A line of N complex points is held by T = N/E threads with E points each:
+// thread t holds element t + T*e in register e.  The transform is a Stockham
+// auto-sort FFT (decimation in time): passes of radix E (one butterfly per
+// thread) followed by at most one smaller radix (E/R butterflies per thread),
+// exchanging through shared memory between passes.  On return register e holds
+// output element t + T*e, the distribution of the input, so a line is loaded
+// from and stored to the same addresses.  Twiddles come from a table of
+// exp(-2 pi i k/N) computed on the host in float64; inverse transforms use its
+// conjugate.  Transforms are unnormalised, as cuFFT's are.
+//
+// Real transforms along the contiguous axis use the half-length complex
+// transform: z[m] = x[2m] + i x[2m+1] with the usual pre/post-processing of
+// the pairs (k, H-k), H = n/2.  The C2R drops the imaginary parts of X[0] and
+// X[H], as numpy's irfftn does.
+#pragma once
+#include "common.cuh"
+
+namespace ofdft {
+namespace fz {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+// a * (S i) with S = -1 (forward) or +1 (inverse)
+template <int S>
+__device__ __forceinline__ float2 mul_si(float2 a) {
+    return S < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+// a * (c + S s i)
+template <int S>
+__device__ __forceinline__ float2 mul_cs(float2 a, float c, float s) {
+    const float ss = S < 0 ? -s : s;
+    return make_float2(a.x * c - a.y * ss, a.x * ss + a.y * c);
+}
+
+constexpr float kC1 = 0.923879532511286756f;  // cos(pi/8)
+constexpr float kS1 = 0.382683432365089772f;  // sin(pi/8)
+constexpr float kH = 0.707106781186547524f;   // cos(pi/4)
+
+// In-register DFTs, natural order in and out; X[k] = sum_n x[n] exp(S 2 pi i nk/R)
+template <int S>
+__device__ __forceinline__ void dft2(float2* v) {
+    const float2 a = v[0];
+    v[0] = cadd(a, v[1]);
+    v[1] = csub(a, v[1]);
+}
+
+template <int S>
+__device__ __forceinline__ void dft4(float2* v) {
+    const float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    const float2 a2 = cadd(v[1], v[3]), a3 = mul_si<S>(csub(v[1], v[3]));
+    v[0] = cadd(a0, a2);
+    v[2] = csub(a0, a2);
+    v[1] = cadd(a1, a3);
+    v[3] = csub(a1, a3);
+}
+
+// 8 and 16 points: radix-2 split, X[k] = E[k] + W^k O[k], X[k + R/2] = E[k] - W^k O[k]
+template <int S>
+__device__ __forceinline__ void dft8(float2* v) {
+    float2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    dft4<S>(e);
+    dft4<S>(o);
+    const float2 w1 = mul_cs<S>(o[1], kH, kH), w2 = mul_si<S>(o[2]), w3 = mul_cs<S>(o[3], -kH, kH);
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], w1);
+    v[5] = csub(e[1], w1);
+    v[2] = cadd(e[2], w2);
+    v[6] = csub(e[2], w2);
+    v[3] = cadd(e[3], w3);
+    v[7] = csub(e[3], w3);
+}
+
+template <int S>
+__device__ __forceinline__ void dft16(float2* v) {
+    float2 e[8], o[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        e[k] = v[2 * k];
+        o[k] = v[2 * k + 1];
+    }
+    dft8<S>(e);
+    dft8<S>(o);
+    float2 w[8];
+    w[0] = o[0];
+    w[1] = mul_cs<S>(o[1], kC1, kS1);
+    w[2] = mul_cs<S>(o[2], kH, kH);
+    w[3] = mul_cs<S>(o[3], kS1, kC1);
+    w[4] = mul_si<S>(o[4]);
+    w[5] = mul_cs<S>(o[5], -kS1, kC1);
+    w[6] = mul_cs<S>(o[6], -kH, kH);
+    w[7] = mul_cs<S>(o[7], -kC1, kS1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = cadd(e[k], w[k]);
+        v[k + 8] = csub(e[k], w[k]);
+    }
+}
+
+template <int R, int S>
+__device__ __forceinline__ void dft(float2* v) {
+    if constexpr (R == 2) dft2<S>(v);
+    else if constexpr (R == 4) dft4<S>(v);
+    else if constexpr (R == 8) dft8<S>(v);
+    else {
+        static_assert(R == 16, "radix must be 2, 4, 8 or 16");
+        dft16<S>(v);
+    }
+}
+
+// Shared-memory placement of element n of a line.
+// Column tiles: 16 lines side by side, element-major, one pad slot per 16 elements.
+struct ColIdx {
+    __device__ __forceinline__ int operator()(int n) const { return n * 16 + (n >> 4); }
+};
+// Row tiles: one line per row buffer, one pad slot per 8 elements.
+struct RowIdx {
+    __device__ __forceinline__ int operator()(int n) const { return n + (n >> 3); }
+};
+// slots a line of n elements occupies
+__host__ __device__ constexpr int col_slots(int n) { return n * 16 + (n >> 4) + 16; }
+__host__ __device__ constexpr int row_slots(int n) { return n + (n >> 3) + 1; }
+
+// radix of the pass that starts at sub-transform length NS
+template <int N, int E, int NS>
+struct PassRadix {
+    static constexpr int R = (N / NS >= E) ? E : N / NS;
+};
+
+// One Stockham pass and, recursively, the passes after it.  sm must be free
+// (every thread done with it) on entry; on return the last pass has read sm.
+template <int N, int E, int S, int NS, class Idx>
+struct Stockham {
+    static constexpr int T = N / E;
+    static constexpr int R = PassRadix<N, E, NS>::R;
+    static constexpr int NB = E / R;
+    static constexpr bool LAST = NS * R == N;
+    static_assert(E % R == 0, "radix must divide the points per thread");
+
+    __device__ __forceinline__ static void run(float2 (&v)[E], float2* sm, Idx ix, int t,
+                                               const float2* __restrict__ tw) {
+        if constexpr (NS > 1) {
+            __syncthreads();  // the previous pass's outputs are in sm
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = sm[ix(t + T * e)];
+            if constexpr (!LAST) __syncthreads();  // every input read before sm is overwritten
+        }
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            const int j = t + T * b;
+            const int jm = j & (NS - 1);
+            float2 u[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) u[r] = v[b + r * NB];
+            if constexpr (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    const float2 w = __ldg(tw + r * jm * (N / (NS * R)));
+                    u[r] = S < 0 ? cmul(u[r], w) : cmulc(u[r], w);
+                }
+            }
+            dft<R, S>(u);
+            if constexpr (LAST) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[b + r * NB] = u[r];
+            } else {
+                const int idxD = (j / NS) * NS * R + jm;
+#pragma unroll
+                for (int r = 0; r < R; ++r) sm[ix(idxD + r * NS)] = u[r];
+            }
+        }
+        if constexpr (!LAST) Stockham<N, E, S, NS * R, Idx>::run(v, sm, ix, t, tw);
+    }
+};
+
+template <int N, int E, int S, class Idx>
+__device__ __forceinline__ void line_fft(float2 (&v)[E], float2* sm, Idx ix, int t, const float2* __restrict__ tw) {
+    Stockham<N, E, S, 1, Idx>::run(v, sm, ix, t, tw);
+}
+
+}  // namespace fz
+}  // namespace ofdft

@@ -18,6 +18,7 @@
 #include "host_math.h"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 
 using namespace ofdft;
@@ -663,6 +664,8 @@ __global__ void k_zero(T* p, long long n) {
 
 }  // namespace
 
+#include "lwt_fused.cuh"
+
 // ------------------------------------------------------------------ handle
 struct ofdft_eval {
     ofdft_grid* g = nullptr;
@@ -679,11 +682,12 @@ struct ofdft_eval {
     double tab_step = 0, tab_limit = 0, tab_limitd = 0;
     double* d_nodes = nullptr;  // [k (kMaxNodes), 1/k, k+1e-18]
     double* h_nodes = nullptr;  // pinned staging
+    float2* fz_tw = nullptr;    // twiddle tables of the fused k_F-node pipeline
     bool kf_set_min = false, kf_set_max = false;
     double kf_st_min = 0, kf_st_max = 0;
     int last_nsp = 0, last_launches = 0;
     // per-kernel-class CUDA-event profiling
-    static constexpr int kClasses = 8;
+    static constexpr int kClasses = 10;
     bool prof = false;
     std::vector<cudaEvent_t> evs;   // pool, two per recorded launch
     std::vector<int> rec_cls;       // class of each recorded launch
@@ -697,9 +701,20 @@ ofdft_grid* e_grid(ofdft_eval* e) { return e->g; }
 
 namespace {
 
-enum ProfClass { P_PREPASS = 0, P_GSPACE, P_LWT_NODES, P_LWT_INTERP, P_LWT_POT2, P_POSTPASS, P_REDUCE, P_CUFFT };
-const char* kProfNames[ofdft_eval::kClasses] = {"prepass", "gspace", "lwt_nodes", "lwt_interp",
-                                                 "lwt_pot2", "postpass", "reduce", "cufft"};
+enum ProfClass {
+    P_PREPASS = 0,
+    P_GSPACE,
+    P_LWT_NODES,
+    P_LWT_INTERP,
+    P_LWT_POT2,
+    P_POSTPASS,
+    P_REDUCE,
+    P_CUFFT,
+    P_FZ_AXIS1,
+    P_FZ_HAT
+};
+const char* kProfNames[ofdft_eval::kClasses] = {"prepass", "gspace",   "lwt_nodes", "lwt_interp", "lwt_pot2",
+                                                 "postpass", "reduce", "cufft",     "fz_axis1",   "fz_hat"};
 
 // Record a start event for one launch of class cls moving `bytes` algorithmic bytes.
 int prof_begin(ofdft_eval* e, int cls, double bytes, cudaStream_t st) {
@@ -799,6 +814,193 @@ struct LwtPlan {
     std::vector<double> nodes;
     double kfclip = INFINITY;
 };
+
+// ------------------------------------------------ fused k_F-node pipeline (host)
+constexpr int kFzMaxNodes = 1024;  // node lists (2 doubles each) staged in shared memory
+constexpr int kFzMaxBatch = 256;   // node reciprocals staged in shared memory
+
+bool fz_applies(const ofdft_grid* g, bool hermite, int m) {
+    auto p2 = [](int n, int lo, int hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; };
+    return g->prec == OFDFT_F32 && !hermite && m <= kFzMaxNodes && p2(g->nr[0], 32, 256) &&
+           p2(g->nr[1], 32, 256) && p2(g->nr[2], 32, 512);
+}
+
+// column lengths (axes 0 and 1)
+template <class F>
+void with_col(int n, F&& f) {
+    switch (n) {
+        case 32: f(std::integral_constant<int, 32>()); break;
+        case 64: f(std::integral_constant<int, 64>()); break;
+        case 128: f(std::integral_constant<int, 128>()); break;
+        case 256: f(std::integral_constant<int, 256>()); break;
+        default: OFDFT_REQUIRE(false, "tile FFT: no column transform of length %d", n);
+    }
+}
+
+// half lengths of the contiguous axis
+template <class F>
+void with_row(int h, F&& f) {
+    switch (h) {
+        case 16: f(std::integral_constant<int, 16>()); break;
+        case 32: f(std::integral_constant<int, 32>()); break;
+        case 64: f(std::integral_constant<int, 64>()); break;
+        case 128: f(std::integral_constant<int, 128>()); break;
+        case 256: f(std::integral_constant<int, 256>()); break;
+        default: OFDFT_REQUIRE(false, "tile FFT: no row transform of half length %d", h);
+    }
+}
+
+// exp(-2 pi i k/n) tables for n0, n1, n2/2 and the n2 real-transform twiddles,
+// from float64 host trigonometry
+void fz_tables(ofdft_eval* e) {
+    if (e->fz_tw) return;
+    const ofdft_grid* g = e->g;
+    const int n0 = g->nr[0], n1 = g->nr[1], n2 = g->nr[2], H = n2 / 2;
+    std::vector<float2> h((size_t)n0 + n1 + 2 * (size_t)H);
+    auto fill = [&](size_t off, int count, int n) {
+        for (int k = 0; k < count; ++k) {
+            const double a = -2.0 * M_PI * (double)k / (double)n;
+            h[off + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+    };
+    fill(0, n0, n0);
+    fill((size_t)n0, n1, n1);
+    fill((size_t)n0 + n1, H, H);
+    fill((size_t)n0 + n1 + H, H, n2);
+    OFDFT_CK(cudaMalloc(&e->fz_tw, h.size() * sizeof(float2)));
+    upload_now(e->fz_tw, h.data(), h.size() * sizeof(float2));
+}
+
+struct FzRun {
+    const float2* rbG;  // FFT(rho^beta), half grid
+    const float* kf;
+    const float* rA;    // rho^alpha
+    float* pot1;
+    float* pot3;
+    float2* pot2G;
+    Table<float> tab;
+    Nodes nd;
+    int m, kdd;
+    double kfclip;
+};
+
+// Runs every node batch of the fused pipeline; returns the number of launches.
+int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
+    ofdft_grid* g = e->g;
+    const ofdft_config& c = e->cfg;
+    const int n0 = g->nr[0], n1 = g->nr[1], n2 = g->nr[2], H = n2 / 2;
+    fz_tables(e);
+    FzDims d;
+    d.n0 = n0;
+    d.n1 = n1;
+    d.n2 = n2;
+    d.H = H;
+    d.nyq = (long long)n0 * n1 * H;
+    d.plane = g->Nc;
+    FzTw tw;
+    tw.t0 = e->fz_tw;
+    tw.t1 = e->fz_tw + n0;
+    tw.th = e->fz_tw + n0 + n1;
+    tw.tr = e->fz_tw + n0 + n1 + H;
+    const size_t cb = g->cplx_bytes();
+    const bool mc = r.kdd == 3;  // M planes feed pot3 only
+    const int per_node = mc ? 2 : 1;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    int B = c.lwt_max_batch > 0 ? c.lwt_max_batch : 64;
+    B = std::min(B, kFzMaxBatch);
+    const long long fit = (long long)(0.5 * (double)freeb) / (long long)(per_node * cb);
+    if (fit < B) B = (int)std::max(1LL, fit);
+    B = std::min(B, r.m);
+    float2* XY = (float2*)e->sc.get("lwtXY", (size_t)per_node * B * cb);
+    const double Ncd = (double)g->Nc, Nd = (double)g->N, invN = 1.0 / Nd;
+    const int tiles0 = n1 * (H / kFzLines) + n1 / kFzLines;
+    const int tiles1 = n0 * (H / kFzLines) + n0 / kFzLines;
+    int launches = 0;
+    for (int j0 = 0; j0 < r.m; j0 += B) {
+        const int nb = std::min(B, r.m - j0);
+        const int nplanes = mc ? 2 * nb : nb;
+        const bool first = j0 == 0;
+        // ---- C2R: axis 0 with the node kernels applied on load
+        with_col(n0, [&](auto c0) {
+            constexpr int N0 = decltype(c0)::value;
+            const size_t smem = fz::col_slots(N0) * sizeof(float2) + (size_t)nb * sizeof(float);
+            timed(e, P_LWT_NODES, Ncd * 8.0 * (1 + nplanes), st, [&] {
+                k_fz_nodes<N0><<<tiles0, N0, smem, st>>>(r.rbG, XY, r.tab, r.nd, j0, nb, mc ? 1 : 0, g->geo, d,
+                                                          tw.t0, invN);
+            });
+        });
+        OFDFT_LAUNCH_CHECK();
+        // ---- axis 1
+        with_col(n1, [&](auto c1) {
+            constexpr int N1 = decltype(c1)::value;
+            const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
+            timed(e, P_FZ_AXIS1, Ncd * 16.0 * nplanes, st,
+                  [&] { k_fz_axis1<N1, +1><<<tiles1 * nplanes, N1, smem, st>>>(XY, d, tw.t1); });
+        });
+        OFDFT_LAUNCH_CHECK();
+        // ---- axis 2 C2R with the interpolation into pot1 (pot3)
+        FzRowArgs ra;
+        ra.kf = r.kf;
+        ra.rA = r.rA;
+        ra.XY = XY;
+        ra.pot1 = r.pot1;
+        ra.pot3 = r.pot3;
+        ra.kn = e->d_nodes;
+        ra.kup = e->d_nodes + 2 * kMaxNodes;
+        ra.m = r.m;
+        ra.j0 = j0;
+        ra.nb = nb;
+        ra.nplanes = nplanes;
+        ra.kdd = r.kdd;
+        ra.first = first ? 1 : 0;
+        ra.kfclip = r.kfclip;
+        ra.d = d;
+        ra.tw = tw;
+        with_row(H, [&](auto ch) {
+            constexpr int HH = decltype(ch)::value;
+            constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
+            const size_t smem = 2 * (size_t)r.m * sizeof(double) + ROWS * fz::row_slots(HH) * sizeof(float2);
+            const int grid = (int)((long long)n0 * n1 / ROWS);
+            const int accs = 1 + (r.kdd == 3);
+            timed(e, P_LWT_INTERP, Ncd * 8.0 * nplanes + Nd * 4.0 * (1 + accs * (first ? 1 : 2)), st,
+                  [&] { k_fz_c2r_rows<HH><<<grid, kFzRowThreads, smem, st>>>(ra); });
+        });
+        OFDFT_LAUNCH_CHECK();
+        launches += 3;
+        if (r.kdd > 1) {
+            // ---- R2C: hat-weighted rho^alpha along axis 2, then axis 1, then axis 0 into pot2(G)
+            ra.nplanes = nb;
+            with_row(H, [&](auto ch) {
+                constexpr int HH = decltype(ch)::value;
+                constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
+                const size_t smem = 2 * (size_t)r.m * sizeof(double) + ROWS * fz::row_slots(HH) * sizeof(float2);
+                const int grid = (int)((long long)n0 * n1 / ROWS);
+                timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st,
+                      [&] { k_fz_r2c_rows<HH><<<grid, kFzRowThreads, smem, st>>>(ra); });
+            });
+            OFDFT_LAUNCH_CHECK();
+            with_col(n1, [&](auto c1) {
+                constexpr int N1 = decltype(c1)::value;
+                const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
+                timed(e, P_FZ_AXIS1, Ncd * 16.0 * nb, st,
+                      [&] { k_fz_axis1<N1, -1><<<tiles1 * nb, N1, smem, st>>>(XY, d, tw.t1); });
+            });
+            OFDFT_LAUNCH_CHECK();
+            with_col(n0, [&](auto c0) {
+                constexpr int N0 = decltype(c0)::value;
+                const size_t smem = fz::col_slots(N0) * sizeof(float2) + (size_t)nb * sizeof(float);
+                timed(e, P_LWT_POT2, Ncd * 8.0 * (nb + (first ? 1 : 2)), st, [&] {
+                    k_fz_pot2<N0><<<tiles0, N0, smem, st>>>(XY, r.pot2G, r.tab, r.nd, j0, nb, first ? 1 : 0, g->geo,
+                                                             d, tw.t0, invN);
+                });
+            });
+            OFDFT_LAUNCH_CHECK();
+            launches += 3;
+        }
+    }
+    return launches;
+}
 
 template <typename T>
 void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energies, cudaStream_t st) {
@@ -954,75 +1156,102 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         const int m = (int)lp.nodes.size();
         const bool hermite = c.lwt_interp == OFDFT_INTERP_HERMITE;
         const bool mcalc = kdd > 1 || hermite;
-        // nodes per batched pass from the free memory: per node 2 complex + 2 real + (1|2) real planes
-        size_t per_node = 2 * cb + 2 * rb + (hermite ? 2 : 1) * rb;
-        size_t freeb = 0, totalb = 0;
-        cudaMemGetInfo(&freeb, &totalb);
-        int B = c.lwt_max_batch > 0 ? c.lwt_max_batch : 64;
-        long long fit = (long long)(0.5 * (double)freeb) / (long long)per_node;
-        if (fit < B) B = (int)std::max(1LL, fit);
-        B = std::min(B, m);
         pot1 = (T*)e->sc.get("pot1", rb);
         if (kdd == 3) pot3 = (T*)e->sc.get("pot3", rb);
         C* pot2G = kdd > 1 ? (C*)e->sc.get("pot2G", cb) : nullptr;
-        C* XY = (C*)e->sc.get("lwtXY", (size_t)2 * B * cb);
-        T* PM = (T*)e->sc.get("lwtPM", (size_t)2 * B * rb);
-        T* U = kdd > 1 ? (T*)e->sc.get("lwtU", (size_t)(hermite ? 2 : 1) * B * rb) : nullptr;
         Nodes nd;
         nd.k = e->d_nodes;
         nd.invk = e->d_nodes + kMaxNodes;
-        Table<T> tab = table_of<T>(e);
-        const int gblk = blocks_for(Nc, 256, g->sms * 16);
-        const int rblk = blocks_for(N, 256, g->sms * 16);
-        for (int j0 = 0; j0 < m; j0 += B) {
-            const int nb = std::min(B, m - j0);
-            const int nplanes = mcalc ? 2 * nb : nb;
-            // read FFT(rho^beta) once, write one complex plane per node (two with derivatives)
-            timed(e, P_LWT_NODES, Ncd * 2 * s * (1 + nplanes), st, [&] {
-                k_lwt_nodes<T><<<gblk, 256, nb * sizeof(T), st>>>(rbG, XY, tab, nd, j0, nb, mcalc, g->geo,
-                                                                 1.0 / (double)N);
-            });
-            OFDFT_LAUNCH_CHECK();
-            c2r(XY, PM, nplanes);
-            InterpArgs<T> ia;
-            ia.kf = kfv;
-            ia.rA = same_ab ? rbp : rap;
-            ia.PM = PM;
-            ia.pot1 = pot1;
-            ia.pot3 = pot3;
-            ia.u = U;
-            ia.kn = e->d_nodes;
-            ia.kup = e->d_nodes + 2 * kMaxNodes;
-            ia.m = m;
-            ia.j0 = j0;
-            ia.nb = nb;
-            ia.kdd = kdd;
-            ia.hermite = hermite;
-            ia.mcalc = mcalc;
-            ia.first = j0 == 0;
-            ia.kfclip = lp.kfclip;
-            ia.N = N;
-            {
-                // read k_F and rho^alpha; gather the two (four with derivatives) node values of each
-                // point; write pot1 (+pot3), reading them back after the first pass; write the hat planes
-                const int upl = kdd > 1 ? (hermite ? 2 * nb : nb) : 0;
-                const int gat = kdd == 3 || hermite ? 4 : 2;
-                const int accs = 1 + (kdd == 3);
-                double b = Nd * s * (2 + gat + accs * (j0 == 0 ? 1 : 2) + upl);
-                timed(e, P_LWT_INTERP, b, st,
-                      [&] { k_lwt_interp<T><<<rblk, 256, 2 * m * sizeof(double), st>>>(ia); });
+        bool fused = false;
+        if (c.lwt_pipeline != OFDFT_LWT_PIPE_CUFFT) {
+            fused = fz_applies(g, hermite, m);
+            OFDFT_REQUIRE(fused || c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED,
+                          "fused k_F-node pipeline: needs a float32 grid, linear interpolation, at most %d nodes and "
+                          "power-of-two axes (32..256, the last 32..512)",
+                          kFzMaxNodes);
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (fused) {
+                FzRun fr;
+                fr.rbG = rbG;
+                fr.kf = kfv;
+                fr.rA = same_ab ? rbp : rap;
+                fr.pot1 = pot1;
+                fr.pot3 = pot3;
+                fr.pot2G = pot2G;
+                fr.tab = table_of<float>(e);
+                fr.nd = nd;
+                fr.m = m;
+                fr.kdd = kdd;
+                fr.kfclip = lp.kfclip;
+                launches += fz_run(e, fr, st);
             }
-            OFDFT_LAUNCH_CHECK();
-            launches += 2;
-            if (kdd > 1) {
-                const int upl = hermite ? 2 * nb : nb;
-                r2c(U, XY, upl);
-                timed(e, P_LWT_POT2, Ncd * 2 * s * (upl + (j0 == 0 ? 1 : 2)), st, [&] {
-                    k_lwt_pot2<T><<<gblk, 256, nb * sizeof(T), st>>>(XY, pot2G, tab, nd, j0, nb, hermite, j0 == 0, g->geo,
-                                                         1.0 / (double)N);
+        }
+        if (!fused) {
+            // nodes per batched pass from the free memory: per node 2 complex + 2 real + (1|2) real planes
+            size_t per_node = 2 * cb + 2 * rb + (hermite ? 2 : 1) * rb;
+            size_t freeb = 0, totalb = 0;
+            cudaMemGetInfo(&freeb, &totalb);
+            int B = c.lwt_max_batch > 0 ? c.lwt_max_batch : 64;
+            long long fit = (long long)(0.5 * (double)freeb) / (long long)per_node;
+            if (fit < B) B = (int)std::max(1LL, fit);
+            B = std::min(B, m);
+            C* XY = (C*)e->sc.get("lwtXY", (size_t)2 * B * cb);
+            T* PM = (T*)e->sc.get("lwtPM", (size_t)2 * B * rb);
+            T* U = kdd > 1 ? (T*)e->sc.get("lwtU", (size_t)(hermite ? 2 : 1) * B * rb) : nullptr;
+            Table<T> tab = table_of<T>(e);
+            const int gblk = blocks_for(Nc, 256, g->sms * 16);
+            const int rblk = blocks_for(N, 256, g->sms * 16);
+            for (int j0 = 0; j0 < m; j0 += B) {
+                const int nb = std::min(B, m - j0);
+                const int nplanes = mcalc ? 2 * nb : nb;
+                // read FFT(rho^beta) once, write one complex plane per node (two with derivatives)
+                timed(e, P_LWT_NODES, Ncd * 2 * s * (1 + nplanes), st, [&] {
+                    k_lwt_nodes<T><<<gblk, 256, nb * sizeof(T), st>>>(rbG, XY, tab, nd, j0, nb, mcalc, g->geo,
+                                                                     1.0 / (double)N);
                 });
                 OFDFT_LAUNCH_CHECK();
-                launches += 1;
+                c2r(XY, PM, nplanes);
+                InterpArgs<T> ia;
+                ia.kf = kfv;
+                ia.rA = same_ab ? rbp : rap;
+                ia.PM = PM;
+                ia.pot1 = pot1;
+                ia.pot3 = pot3;
+                ia.u = U;
+                ia.kn = e->d_nodes;
+                ia.kup = e->d_nodes + 2 * kMaxNodes;
+                ia.m = m;
+                ia.j0 = j0;
+                ia.nb = nb;
+                ia.kdd = kdd;
+                ia.hermite = hermite;
+                ia.mcalc = mcalc;
+                ia.first = j0 == 0;
+                ia.kfclip = lp.kfclip;
+                ia.N = N;
+                {
+                    // read k_F and rho^alpha; gather the two (four with derivatives) node values of each
+                    // point; write pot1 (+pot3), reading them back after the first pass; write the hat planes
+                    const int upl = kdd > 1 ? (hermite ? 2 * nb : nb) : 0;
+                    const int gat = kdd == 3 || hermite ? 4 : 2;
+                    const int accs = 1 + (kdd == 3);
+                    double b = Nd * s * (2 + gat + accs * (j0 == 0 ? 1 : 2) + upl);
+                    timed(e, P_LWT_INTERP, b, st,
+                          [&] { k_lwt_interp<T><<<rblk, 256, 2 * m * sizeof(double), st>>>(ia); });
+                }
+                OFDFT_LAUNCH_CHECK();
+                launches += 2;
+                if (kdd > 1) {
+                    const int upl = hermite ? 2 * nb : nb;
+                    r2c(U, XY, upl);
+                    timed(e, P_LWT_POT2, Ncd * 2 * s * (upl + (j0 == 0 ? 1 : 2)), st, [&] {
+                        k_lwt_pot2<T><<<gblk, 256, nb * sizeof(T), st>>>(XY, pot2G, tab, nd, j0, nb, hermite, j0 == 0, g->geo,
+                                                             1.0 / (double)N);
+                    });
+                    OFDFT_LAUNCH_CHECK();
+                    launches += 1;
+                }
             }
         }
         if (kdd > 1) {
@@ -1170,6 +1399,7 @@ void ofdft_eval_destroy(ofdft_eval* e) {
     if (e->tab_cd) cudaFree(e->tab_cd);
     if (e->d_nodes) cudaFree(e->d_nodes);
     if (e->h_nodes) cudaFreeHost(e->h_nodes);
+    if (e->fz_tw) cudaFree(e->fz_tw);
     for (auto ev : e->evs) cudaEventDestroy(ev);
     delete e;
 }

@@ -84,6 +84,13 @@ int ofdft_dot_noalloc(const void* a, const void* b, long long n, int precision, 
  * :124-191).  kedf_terms is a bit set of OFDFT_KE_*. */
 enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8 };
 enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
+/* k_F-node kernel pipeline: AUTO takes FUSED where it applies (float32 grid,
+ * linear interpolation, every axis a power of two in 32..256, the last axis
+ * up to 512) and CUFFT otherwise; FUSED fails with OFDFT_EINVAL where it does
+ * not apply.  FUSED folds the node kernel, the interpolation and the pot2 sum
+ * into the library's own tile FFTs; CUFFT runs them as separate passes around
+ * batched cuFFT transforms.  Both compute the same quantities. */
+enum { OFDFT_LWT_PIPE_AUTO = 0, OFDFT_LWT_PIPE_CUFFT = 1, OFDFT_LWT_PIPE_FUSED = 2 };
 
 typedef struct {
     int    kedf_terms;
@@ -108,6 +115,7 @@ typedef struct {
     int    hartree;           /* Hartree (functional/hartree.py:24-45)             */
     int    pseudo;            /* add the local pseudopotential set by ofdft_eval_set_vloc */
     double ewald_energy;      /* ion-ion energy added to the total (0 = none)     */
+    int    lwt_pipeline;      /* OFDFT_LWT_PIPE_*: how the k_F-node kernel runs   */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

@@ -17,6 +17,8 @@
 #pragma once
 #include "common.cuh"
 
+#include <type_traits>
+
 namespace ofdft {
 namespace fz {
 
@@ -185,6 +187,83 @@ struct Stockham {
 template <int N, int E, int S, class Idx>
 __device__ __forceinline__ void line_fft(float2 (&v)[E], float2* sm, Idx ix, int t, const float2* __restrict__ tw) {
     Stockham<N, E, S, 1, Idx>::run(v, sm, ix, t, tw);
+}
+
+// Row placement for lines of 128 or more elements: an XOR swizzle inside each
+// group of 16 slots.  The loads of every pass (16 consecutive elements per
+// half-warp) and the stores of the radix-8 passes then fall in distinct
+// banks, with no padding.
+struct RowSwz {
+    __device__ __forceinline__ int operator()(int n) const { return n ^ ((n >> 3) & 15); }
+};
+// Row placement for shorter lines: one pad slot per 16 elements.
+struct RowPad16 {
+    __device__ __forceinline__ int operator()(int n) const { return n + (n >> 4); }
+};
+template <int N>
+struct RowLayout {
+    using Idx = typename std::conditional<(N >= 128), RowSwz, RowPad16>::type;
+    static constexpr int slots = N >= 128 ? N : N + (N >> 4) + 1;
+};
+
+// The Stockham passes with two exchange buffers used in turn: pass p stores
+// into buffer p & 1 and pass p + 1 reads it after one barrier, so a pass needs
+// one barrier instead of two.  Entry: buffer 0 is free.  Exit: both buffers are
+// free for the next transform (a trailing barrier is added when the number of
+// exchanges is odd, because the last reads then come from buffer 0).
+template <int N, int E, int S, int NS, int PASS, class Idx>
+struct StockhamPP {
+    static constexpr int T = N / E;
+    static constexpr int R = PassRadix<N, E, NS>::R;
+    static constexpr int NB = E / R;
+    static constexpr bool LAST = NS * R == N;
+    static_assert(E % R == 0, "radix must divide the points per thread");
+
+    __device__ __forceinline__ static void run(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
+                                               const float2* __restrict__ tw) {
+        if constexpr (NS > 1) {
+            const float2* src = ((PASS - 1) & 1) ? b1 : b0;
+            __syncthreads();  // the previous pass's outputs are in src
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = src[ix(t + T * e)];
+        }
+        float2* dst = (PASS & 1) ? b1 : b0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            const int j = t + T * b;
+            const int jm = j & (NS - 1);
+            float2 u[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) u[r] = v[b + r * NB];
+            if constexpr (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    const float2 w = __ldg(tw + r * jm * (N / (NS * R)));
+                    u[r] = S < 0 ? cmul(u[r], w) : cmulc(u[r], w);
+                }
+            }
+            dft<R, S>(u);
+            if constexpr (LAST) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[b + r * NB] = u[r];
+            } else {
+                const int idxD = (j / NS) * NS * R + jm;
+#pragma unroll
+                for (int r = 0; r < R; ++r) dst[ix(idxD + r * NS)] = u[r];
+            }
+        }
+        if constexpr (!LAST) {
+            StockhamPP<N, E, S, NS * R, PASS + 1, Idx>::run(v, b0, b1, ix, t, tw);
+        } else if constexpr ((PASS & 1) == 1) {
+            __syncthreads();  // odd number of exchanges: the last reads were from buffer 0
+        }
+    }
+};
+
+template <int N, int E, int S, class Idx>
+__device__ __forceinline__ void line_fft_pp(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
+                                            const float2* __restrict__ tw) {
+    StockhamPP<N, E, S, 1, 0, Idx>::run(v, b0, b1, ix, t, tw);
 }
 
 }  // namespace fz

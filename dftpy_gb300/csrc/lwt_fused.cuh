@@ -18,6 +18,12 @@
 // Intermediate planes hold k2 < n2/2 as [n0][n1][n2/2] followed by the
 // Nyquist column k2 = n2/2 as [n0][n1]; pot2(G) and FFT(rho^beta) use the
 // R2C half-grid layout [n0][n1][n2/2+1].
+//
+// Nothing in these kernels runs on the float64 pipe inside a node loop: the
+// kernel-table parameters come in float32 (FzTab), and the interval
+// membership of each point is decided in float32 against node bounds rounded
+// outward (__double2float_rd/_ru), which reproduces the float64 comparisons of
+// the reference exactly for float32 k_F values.
 #pragma once
 #include "fz_fft.cuh"
 
@@ -41,6 +47,80 @@ constexpr int kFzColE = 16;   // points per thread along a column
 constexpr int kFzRowE = 8;    // complex points per thread along a row
 constexpr int kFzRowThreads = 256;
 
+// float32 copy of the kernel-table parameters
+struct FzTab {
+    const float* c;   // K(eta) cubic pieces
+    const float* cd;  // -eta K'(eta) cubic pieces
+    int nint;
+    float step, inv_step, etamax, limit, limitd, factor, kconst, eta_series;  // kconst = -lbda - 0.6
+};
+
+FzTab fz_tab(const Table<float>& t) {
+    FzTab f;
+    f.c = t.c;
+    f.cd = t.cd;
+    f.nint = t.nint;
+    f.step = (float)t.step;
+    f.inv_step = (float)t.inv_step;
+    f.etamax = (float)t.etamax;
+    f.limit = (float)t.limit;
+    f.limitd = (float)t.limitd;
+    f.factor = (float)t.factor;
+    f.kconst = (float)(-t.lbda - 0.6);
+    f.eta_series = (float)t.eta_series;
+    return f;
+}
+
+// Coefficients c_k of the large-eta series of the inverse Lindhard function
+// with mu = 1 (kernel.py:79-133): F = -lbda - 0.6 + sum_k c_k eta^{-2(k+1)}.
+// For eta >= 4 the terms after k = 7 are below 1e-12 of F, so eight terms
+// reproduce the table to float32 precision.
+__device__ __forceinline__ constexpr float fz_series_c(int k) {
+    return k == 0   ? -0.13714285714285712f
+           : k == 1 ? -6.39999999999999875e-2f
+           : k == 2 ? -3.77825602968460128e-2f
+           : k == 3 ? -2.51824061652633074e-2f
+           : k == 4 ? -1.80879839616166146e-2f
+           : k == 5 ? -1.36715733124818332e-2f
+           : k == 6 ? -1.07236045520990083e-2f
+                    : -8.65192783339199453e-3f;
+}
+
+__device__ __forceinline__ float fz_spline(const float* c, int nint, float step, float inv_step, float eta) {
+    int l = (int)(eta * inv_step);
+    l = l < 0 ? 0 : (l >= nint ? nint - 1 : l);
+    const float u = eta - (float)l * step;
+    const float4 q = __ldg(reinterpret_cast<const float4*>(c) + l);
+    return q.x + u * (q.y + u * (q.z + u * q.w));
+}
+
+// K_j(|G|) and (DERIV) -eta K_j'(eta) at eta = q/k_j: the table limit at and
+// above etamax, the series at and above eta_series (u = eta^-2 = k_j^2/q^2),
+// the spline below.  G = 0 is handled by the callers.
+template <bool DERIV>
+__device__ __forceinline__ void fz_node_kernel(const FzTab& tb, float q, float ik, float iq2, float kj2, float& K,
+                                               float& KD) {
+    const float eta = q * ik;
+    if (eta >= tb.etamax) {
+        K = tb.limit;
+        KD = tb.limitd;
+    } else if (eta >= tb.eta_series) {
+        const float u = iq2 * kj2;
+        float f = fz_series_c(7);
+        float d = 16.0f * fz_series_c(7);
+#pragma unroll
+        for (int k = 6; k >= 0; --k) {
+            f = fmaf(f, u, fz_series_c(k));
+            if (DERIV) d = fmaf(d, u, (float)(2 * (k + 1)) * fz_series_c(k));
+        }
+        K = tb.factor * fmaf(f, u, tb.kconst);
+        KD = DERIV ? tb.factor * (d * u) : 0.0f;
+    } else {
+        K = fz_spline(tb.c, tb.nint, tb.step, tb.inv_step, eta);
+        KD = DERIV ? fz_spline(tb.cd, tb.nint, tb.step, tb.inv_step, eta) : 0.0f;
+    }
+}
+
 // Column tile of the axis-0 passes: main tiles (k1, 16 consecutive k2 < H) then
 // Nyquist tiles (16 consecutive k1, k2 = H).  Sets k1, k2 of this thread's line,
 // the offset/stride in a plane and the offset/stride in the half-grid layout.
@@ -63,57 +143,75 @@ __device__ __forceinline__ void fz_axis0_tile(const FzDims& d, int tile, int l, 
     gstride = (long long)d.n1 * (d.H + 1);
 }
 
-// X_j, Y_j of a batch of nodes, inverse-transformed along axis 0.
-template <int N0>
-__global__ void __launch_bounds__(kFzLines * (N0 / kFzColE))
-    k_fz_nodes(const float2* __restrict__ rbG, float2* __restrict__ XY, Table<float> tab, Nodes nd, int j0, int nb,
-               int mcalc, Geo geo, FzDims d, const float2* __restrict__ tw, double invN) {
-    constexpr int E = kFzColE, T = N0 / E;
+// Shared-memory size of k_fz_nodes / k_fz_pot2 for column length n0 and nb nodes.
+inline size_t fz_col_smem(int n0, int nb, bool with_b) {
+    const size_t pts = (size_t)n0 * kFzLines;
+    return fz::col_slots(n0) * sizeof(float2) + pts * (2 * sizeof(float) + (with_b ? sizeof(float2) : 0)) +
+           2 * (size_t)nb * sizeof(float);
+}
+
+// X_j = K_j FFT(rho^beta)/N (DERIV false) or Y_j = K'_j/k_j FFT(rho^beta)/N
+// (DERIV true) of the block's share of a batch of nodes, inverse-transformed
+// along axis 0 into plane `plane0 + jj`.  Block b handles tile b % tiles and
+// node share b / tiles of nsplit.  The tile's FFT(rho^beta)/N, |G| and 1/|G|^2
+// sit in shared memory for the whole node loop; FFT(rho^beta) at G = 0 is
+// zeroed there, which is K_j(0) = 0.
+template <int N0, bool DERIV>
+__global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
+    k_fz_nodes(const float2* __restrict__ rbG, float2* __restrict__ XY, FzTab tb, const double* __restrict__ knode,
+               const double* __restrict__ invk, int j0, int nb, int plane0, int tiles, int nsplit, Geo geo,
+               FzDims d, const float2* __restrict__ tw, float invN) {
+    constexpr int E = kFzColE, T = N0 / E, L = kFzLines;
     extern __shared__ float2 fz_sm[];
-    float* sinvk = reinterpret_cast<float*>(fz_sm + fz::col_slots(N0));
-    for (int q = threadIdx.x; q < nb; q += blockDim.x) sinvk[q] = (float)nd.invk[j0 + q];
-    __syncthreads();
-    const int l = threadIdx.x % kFzLines, t = threadIdx.x / kFzLines;
+    float2* sm = fz_sm;
+    float2* sz = fz_sm + fz::col_slots(N0);
+    float* sq = reinterpret_cast<float*>(sz + N0 * L);
+    float* siq = sq + N0 * L;
+    float* sik = siq + N0 * L;
+    float* sk2 = sik + nb;
+    const int tile = blockIdx.x % tiles, part = blockIdx.x / tiles;
+    const int per = (nb + nsplit - 1) / nsplit;
+    const int s0 = part * per, s1 = min(nb, s0 + per);
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        const double k = knode[j0 + q];
+        sik[q] = (float)invk[j0 + q];
+        sk2[q] = (float)(k * k);
+    }
+    const int l = threadIdx.x % L, t = threadIdx.x / L;
     int k1, k2;
     long long pbase, pstride, gbase, gstride;
-    fz_axis0_tile(d, blockIdx.x, l, k1, k2, pbase, pstride, gbase, gstride);
-    const float invNt = (float)invN;
-    float2 z[E];
-    float q[E];
-#pragma unroll
+    fz_axis0_tile(d, tile, l, k1, k2, pbase, pstride, gbase, gstride);
+#pragma unroll 4
     for (int e = 0; e < E; ++e) {
         const int k0 = t + T * e;
-        const float2 a = rbG[gbase + k0 * gstride];
-        z[e] = make_float2(a.x * invNt, a.y * invNt);
-        q[e] = sqrtf(gsq_f(geo, k0, k1, k2));
+        const int s = k0 * L + l;
+        float2 a = __ldg(rbG + gbase + k0 * gstride);
+        a = make_float2(a.x * invN, a.y * invN);
+        const float q2 = gsq_f(geo, k0, k1, k2);
+        if (k0 == 0 && k1 == 0 && k2 == 0) a = make_float2(0.0f, 0.0f);
+        sz[s] = a;
+        sq[s] = sqrtf(q2);
+        siq[s] = q2 > 0.0f ? 1.0f / q2 : 0.0f;
     }
-    const bool g0 = (t == 0 && k1 == 0 && k2 == 0);  // G = 0 sits in register 0 of thread t = 0
-    float2* sm = fz_sm + l;
-    for (int jj = 0; jj < nb; ++jj) {
-        const float ik = sinvk[jj];
+    __syncthreads();
+    for (int jj = s0; jj < s1; ++jj) {
+        const float ik = sik[jj], kj2 = sk2[jj];
         float2 v[E];
-        float kd[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
+            const int s = (t + T * e) * L + l;
             float K, KD;
-            node_kernel<float>(tab, q[e], ik, mcalc != 0, (g0 && e == 0) ? 0 : 1, K, KD);
-            v[e] = make_float2(K * z[e].x, K * z[e].y);
-            kd[e] = KD * ik;
+            fz_node_kernel<DERIV>(tb, sq[s], ik, siq[s], kj2, K, KD);
+            const float f = DERIV ? KD * ik : K;
+            const float2 z = sz[s];
+            v[e] = make_float2(f * z.x, f * z.y);
         }
-        __syncthreads();
-        fz::line_fft<N0, E, +1>(v, sm, fz::ColIdx(), t, tw);
-        float2* outp = XY + (long long)jj * d.plane + pbase;
+        __syncthreads();  // the exchange buffer is free
+        fz::line_fft<N0, E, +1>(v, sm + l, fz::ColIdx(), t, tw);
+        float2* outp = XY + (long long)(plane0 + jj) * d.plane + pbase + t * pstride;
+        const long long step = (long long)T * pstride;
 #pragma unroll
-        for (int e = 0; e < E; ++e) outp[(t + T * e) * pstride] = v[e];
-        if (mcalc) {
-#pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = make_float2(kd[e] * z[e].x, kd[e] * z[e].y);
-            __syncthreads();
-            fz::line_fft<N0, E, +1>(v, sm, fz::ColIdx(), t, tw);
-            float2* outm = XY + (long long)(nb + jj) * d.plane + pbase;
-#pragma unroll
-            for (int e = 0; e < E; ++e) outm[(t + T * e) * pstride] = v[e];
-        }
+        for (int e = 0; e < E; ++e) __stcs(outp + e * step, v[e]);
     }
 }
 
@@ -136,19 +234,19 @@ __global__ void __launch_bounds__(kFzLines * (N1 / kFzColE))
         const int i0 = tile / per_row, k2 = (tile % per_row) * kFzLines + l;
         float2* line = base + (long long)i0 * N1 * d.H + k2;
 #pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = line[(long long)(t + T * e) * d.H];
+        for (int e = 0; e < E; ++e) v[e] = __ldcs(line + (long long)(t + T * e) * d.H);
         fz::line_fft<N1, E, S>(v, fz_sm + l, fz::ColIdx(), t, tw);
 #pragma unroll
-        for (int e = 0; e < E; ++e) line[(long long)(t + T * e) * d.H] = v[e];
+        for (int e = 0; e < E; ++e) __stcs(line + (long long)(t + T * e) * d.H, v[e]);
     } else {
         const int t = threadIdx.x % T, l = threadIdx.x / T;
         const int i0 = (tile - tiles_main) * kFzLines + l;
         float2* line = base + d.nyq + (long long)i0 * N1;
 #pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = line[t + T * e];
+        for (int e = 0; e < E; ++e) v[e] = __ldcs(line + t + T * e);
         fz::line_fft<N1, E, S>(v, fz_sm + l * fz::row_slots(N1), fz::RowIdx(), t, tw);
 #pragma unroll
-        for (int e = 0; e < E; ++e) line[t + T * e] = v[e];
+        for (int e = 0; e < E; ++e) __stcs(line + t + T * e, v[e]);
     }
 }
 
@@ -160,260 +258,329 @@ struct FzRowArgs {
     float* pot3;
     const double* kn;
     const double* kup;
-    int m, j0, nb, nplanes, kdd, first;
+    int m, j0, nb, first;
     double kfclip;
     FzDims d;
     FzTw tw;
 };
 
-// per-point interval state for the interpolation (lwt.py:252-306 with the
-// float32 closed-interior membership): ir >= 0 interval index with coordinate
-// tr; ir = -1 small-k_F branch of node 0 with coordinate tr; ir = -2 nothing.
-__device__ __forceinline__ void fz_point_state(double kf, const double* kn, const double* kup, int m, int& ir,
-                                               float& tr) {
-    const Member mb = membership(kf, kn, kup, m, true);
-    if (mb.ilast >= 0) {
-        const int i = mb.ilast;
-        ir = i;
-        tr = (float)(kf - kn[i]) / (float)(kn[i + 1] - kn[i]);
-    } else if (mb.small) {
-        ir = -1;
-        tr = (float)(kf - kn[0]) / (float)kn[0];
-    } else {
-        ir = -2;
-        tr = 0.0f;
+// Node bounds of the interval search in float32, staged per block (5 m floats):
+//   kdn  = kn rounded down:  kn < kf  <=> kdn < kf,  kf <= kn <=> kf <= kdn
+//   kupu = kup rounded up:   kf < kup <=> kf < kupu
+//   khi + klo = kn (two floats), iw = 1/(kn[i+1] - kn[i])
+// for float32 kf.  iw[m-1] holds 1/kn[0] (the small-k_F coordinate).
+struct FzNodeSm {
+    const float *kdn, *kupu, *khi, *klo, *iw;
+};
+
+__device__ __forceinline__ FzNodeSm fz_stage_nodes(const FzRowArgs& a, float* s) {
+    const int m = a.m;
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        const double k = a.kn[q];
+        const float hi = __double2float_rn(k);
+        s[q] = __double2float_rd(k);
+        s[m + q] = __double2float_ru(a.kup[q]);
+        s[2 * m + q] = hi;
+        s[3 * m + q] = __double2float_rn(k - (double)hi);
+        s[4 * m + q] = __double2float_rn(q + 1 < m ? 1.0 / (a.kn[q + 1] - k) : 1.0 / a.kn[0]);
     }
+    FzNodeSm n;
+    n.kdn = s;
+    n.kupu = s + m;
+    n.khi = s + 2 * m;
+    n.klo = s + 3 * m;
+    n.iw = s + 4 * m;
+    return n;
 }
 
-template <int H>
-__device__ __forceinline__ void fz_load_nodes(const FzRowArgs& a, double* kn, double* kup) {
-    for (int q = threadIdx.x; q < a.m; q += blockDim.x) {
-        kn[q] = a.kn[q];
-        kup[q] = a.kup[q];
+// Interval membership of the reference (lwt.py:252-306) in float32 with the
+// closed-interior rule of the float32 path (a point exactly on an interior node
+// joins the interval below it): il = containing interval or -1, small = the
+// small-k_F branch of node 0, with their coordinates.  At most one interval
+// contains a point under this rule.
+__device__ __forceinline__ void fz_member(float kf, const FzNodeSm& n, int m, int& il, float& til, bool& small,
+                                          float& tsm) {
+    int lo = 0, hi = m;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (n.kdn[mid] < kf) lo = mid + 1;
+        else hi = mid;
     }
+    const int i1 = lo - 1, i2 = lo - 2;
+    auto below_top = [&](int i) { return (i + 1 <= m - 2) ? kf <= n.kdn[i + 1] : kf < n.kupu[i + 1]; };
+    const bool in1 = i1 >= 0 && i1 <= m - 2 && below_top(i1);
+    const bool in2 = i2 >= 0 && i2 <= m - 2 && below_top(i2);
+    il = in1 ? i1 : (in2 ? i2 : -1);
+    til = il >= 0 ? ((kf - n.khi[il]) - n.klo[il]) * n.iw[il] : 0.0f;
+    small = kf < n.kupu[0];
+    tsm = ((kf - n.khi[0]) - n.klo[0]) * n.iw[m - 1];
 }
 
-// Axis-2 C2R of every plane of the batch, row by row, with the interpolation
-// of the P (and M) values into pot1 (pot3) at every point of the row.
+// The same for a k_F clipped to kfclip (float64 value; only with a user bound).
+__device__ __noinline__ void fz_member_clip(const FzRowArgs& a, int& il, float& til, bool& small, float& tsm) {
+    const double kf = a.kfclip;
+    const Member mb = membership(kf, a.kn, a.kup, a.m, true);
+    il = mb.ilast;
+    til = il >= 0 ? (float)(kf - a.kn[il]) / (float)(a.kn[il + 1] - a.kn[il]) : 0.0f;
+    small = mb.small;
+    tsm = (float)(kf - a.kn[0]) / (float)a.kn[0];
+}
+
+// Per-point interval of the interpolation: node fi gets 1 - tr and node fi + 1
+// gets tr, both as max(0, 1 - |(j - fi) - tr|) for node j; fi = -2 when the
+// point lies in no interval.  The small-k_F branch (node 0 only) is added
+// separately at j = 0 (fz_small_weight).
+__device__ __forceinline__ void fz_interval_state(float kf, const FzRowArgs& a, const FzNodeSm& n, float clipdn,
+                                                  float& fi, float& tr) {
+    int il;
+    float til, tsm;
+    bool small;
+    if (kf > clipdn) fz_member_clip(a, il, til, small, tsm);
+    else fz_member(kf, n, a.m, il, til, small, tsm);
+    fi = il >= 0 ? (float)il : -2.0f;
+    tr = il >= 0 ? til : 0.0f;
+}
+
+// Weight of node 0 from the small-k_F branch: pot1 takes it only at points in
+// no interval (lwt.py:252-263); the hat planes add it to node 0 (lwt.py:266-296).
+__device__ __forceinline__ float fz_small_weight(float kf, const FzRowArgs& a, const FzNodeSm& n, float clipdn,
+                                                 bool only_outside) {
+    int il;
+    float til, tsm;
+    bool small;
+    if (kf > clipdn) fz_member_clip(a, il, til, small, tsm);
+    else fz_member(kf, n, a.m, il, til, small, tsm);
+    return (small && !(only_outside && il >= 0)) ? tsm : 0.0f;
+}
+
+__device__ __forceinline__ float fz_hat(float jf, float fi, float tr) {
+    return fmaxf(0.0f, 1.0f - fabsf((jf - fi) - tr));
+}
+
+// Row of plane `src` pre-processed for the half-length complex C2R:
+// Z[k] = (X[k] + conj X[H-k]) + i w^k (X[k] - conj X[H-k]), w = exp(+2 pi i/n2),
+// the imaginary parts of X[0] and X[H] dropped.
 template <int H>
-__global__ void __launch_bounds__(kFzRowThreads) k_fz_c2r_rows(FzRowArgs a) {
-    constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
-    constexpr int RS = fz::row_slots(H);
-    extern __shared__ double fz_rsm[];
-    double* kn = fz_rsm;
-    double* kup = fz_rsm + a.m;
-    float2* rows = reinterpret_cast<float2*>(fz_rsm + 2 * a.m);
-    fz_load_nodes<H>(a, kn, kup);
-    __syncthreads();
-    const int t = threadIdx.x % T, l = threadIdx.x / T;
-    const long long row = (long long)blockIdx.x * ROWS + l;
-    const int n2 = 2 * H;
-    float2* sm = rows + l * RS;
-    const fz::RowIdx ix;
-    int ir[P];
-    float tr[P], acc1[P], acc3[P];
+__device__ __forceinline__ void fz_c2r_load(const float2* __restrict__ src, long long row, long long nyq, int t,
+                                            const float2* __restrict__ twr, float2 (&v)[kFzRowE]) {
+    constexpr int E = kFzRowE, T = H / E;
+    const float2* r = src + row * H;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-        const int mm = t + T * e;
-        const float2 kk = *reinterpret_cast<const float2*>(a.kf + row * n2 + 2 * mm);
-        fz_point_state(fmin((double)kk.x, a.kfclip), kn, kup, a.m, ir[2 * e], tr[2 * e]);
-        fz_point_state(fmin((double)kk.y, a.kfclip), kn, kup, a.m, ir[2 * e + 1], tr[2 * e + 1]);
-    }
-#pragma unroll
-    for (int q = 0; q < P; ++q) acc1[q] = acc3[q] = 0.0f;
-    for (int p = 0; p < a.nplanes; ++p) {
-        const bool isM = p >= a.nb;
-        const int j = a.j0 + (isM ? p - a.nb : p);
-        const float2* src = a.XY + (long long)p * a.d.plane;
-        __syncthreads();  // sm free
-#pragma unroll
-        for (int e = 0; e < E; ++e) sm[ix(t + T * e)] = src[row * H + t + T * e];
-        if (t == 0) sm[ix(H)] = src[a.d.nyq + row];
-        __syncthreads();
-        float2 v[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int k = t + T * e;
-            float2 X = sm[ix(k)], Y = sm[ix(H - k)];
+        const int k = t + T * e;
+        float2 X = __ldg(r + k);
+        float2 Y;
+        if (e == 0) {
+            Y = k == 0 ? __ldg(src + nyq + row) : __ldg(r + H - k);
             if (k == 0) {
                 X.y = 0.0f;
                 Y.y = 0.0f;
             }
-            // Z = (X + conj Y) + i w^k (X - conj Y), w = exp(+2 pi i/n2)
-            const float2 A = make_float2(X.x + Y.x, X.y - Y.y);
-            const float2 B = make_float2(X.x - Y.x, X.y + Y.y);
-            const float2 wB = fz::cmulc(B, __ldg(a.tw.tr + k));
-            v[e] = make_float2(A.x - wB.y, A.y + wB.x);
+        } else {
+            Y = __ldg(r + H - k);
         }
-        __syncthreads();  // every pair read before the transform writes sm
-        fz::line_fft<H, E, +1>(v, sm, ix, t, a.tw.th);
-#pragma unroll
-        for (int q = 0; q < P; ++q) {
-            const float val = (q & 1) ? v[q >> 1].y : v[q >> 1].x;
-            if (!isM) {
-                if (ir[q] >= 0) {
-                    if (j == ir[q]) acc1[q] += val * (1.0f - tr[q]);
-                    else if (j == ir[q] + 1) acc1[q] += val * tr[q];
-                } else if (ir[q] == -1 && j == 0) {
-                    acc1[q] += val * tr[q];
-                }
-            } else if (a.kdd == 3 && ir[q] >= 0) {
-                if (j == ir[q]) acc3[q] += val * (1.0f - tr[q]);
-                else if (j == ir[q] + 1) acc3[q] += val * tr[q];
-            }
-        }
-    }
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const long long r = row * n2 + 2 * (t + T * e);
-        float2 o1 = make_float2(acc1[2 * e], acc1[2 * e + 1]);
-        if (!a.first) {
-            const float2 old = *reinterpret_cast<const float2*>(a.pot1 + r);
-            o1 = make_float2(old.x + o1.x, old.y + o1.y);
-        }
-        *reinterpret_cast<float2*>(a.pot1 + r) = o1;
-        if (a.kdd == 3) {
-            float2 o3 = make_float2(acc3[2 * e], acc3[2 * e + 1]);
-            if (!a.first) {
-                const float2 old = *reinterpret_cast<const float2*>(a.pot3 + r);
-                o3 = make_float2(old.x + o3.x, old.y + o3.y);
-            }
-            *reinterpret_cast<float2*>(a.pot3 + r) = o3;
-        }
+        const float2 A = make_float2(X.x + Y.x, X.y - Y.y);
+        const float2 B = make_float2(X.x - Y.x, X.y + Y.y);
+        const float2 wB = fz::cmulc(B, __ldg(twr + k));
+        v[e] = make_float2(A.x - wB.y, A.y + wB.x);
     }
 }
 
-// hat weights of one point (lwt.py:266-296, linear): up to three nodes
-// base..base+2 with weights rA*W[d]; the small-k_F weight of node 0 is folded
-// into W[0] (node 0 is then always the base).
-__device__ __forceinline__ void fz_hat_state(double kf, float rA, const double* kn, const double* kup, int m,
-                                             int& base, float (&rw)[3]) {
-    const Member mb = membership(kf, kn, kup, m, true);
-    const int ints[2] = {mb.ilast, mb.iprev};
-    base = mb.ilast >= 0 ? (mb.iprev >= 0 ? mb.iprev : mb.ilast) : 0;
-    float W[3] = {0.0f, 0.0f, 0.0f};
-    if (mb.ilast >= 0) {
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const int i = ints[s];
-            if (i < 0) continue;
-            const float tt = (float)(kf - kn[i]) / (float)(kn[i + 1] - kn[i]);
-            W[i - base] += 1.0f - tt;
-            W[i + 1 - base] += tt;
-        }
-    }
-    if (mb.small && base == 0) W[0] += (float)(kf - kn[0]) / (float)kn[0];
-#pragma unroll
-    for (int s = 0; s < 3; ++s) rw[s] = rA * W[s];
+inline size_t fz_row_smem(int H, int m) {
+    const int T = H / kFzRowE, ROWS = kFzRowThreads / T;
+    const size_t nodes = ((size_t)5 * m * sizeof(float) + 15) / 16 * 16;
+    return nodes + 2 * (size_t)ROWS * (H >= 128 ? H : H + (H >> 4) + 1) * sizeof(float2);
 }
 
-// rho^alpha W_j of every node of the batch, R2C along axis 2, row by row.
-template <int H>
-__global__ void __launch_bounds__(kFzRowThreads) k_fz_r2c_rows(FzRowArgs a) {
+// Axis-2 C2R of the batch's planes plane0 .. plane0 + nb - 1 (node j0 + jj),
+// row by row, interpolated into `pot` at every point of the row: pot1 from the
+// P planes, pot3 from the M planes (SMALL: the small-k_F branch of node 0
+// counts, which it does for pot1 only).
+template <int H, bool SMALL>
+__global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, int plane0, float* __restrict__ pot) {
     constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
-    constexpr int RS = fz::row_slots(H);
-    extern __shared__ double fz_rsm[];
-    double* kn = fz_rsm;
-    double* kup = fz_rsm + a.m;
-    float2* rows = reinterpret_cast<float2*>(fz_rsm + 2 * a.m);
-    fz_load_nodes<H>(a, kn, kup);
+    using Lay = fz::RowLayout<H>;
+    extern __shared__ float4 fz_rsm4[];
+    float* fs = reinterpret_cast<float*>(fz_rsm4);
+    const FzNodeSm nodes = fz_stage_nodes(a, fs);
+    float2* buf0 = reinterpret_cast<float2*>(fs + ((5 * a.m + 3) & ~3));
+    float2* buf1 = buf0 + ROWS * Lay::slots;
     __syncthreads();
     const int t = threadIdx.x % T, l = threadIdx.x / T;
     const long long row = (long long)blockIdx.x * ROWS + l;
     const int n2 = 2 * H;
-    float2* sm = rows + l * RS;
-    const fz::RowIdx ix;
-    int base[P];
-    float rw[P][3];
+    float2* b0 = buf0 + l * Lay::slots;
+    float2* b1 = buf1 + l * Lay::slots;
+    const typename Lay::Idx ix;
+    const float clipdn = __double2float_rd(a.kfclip);
+    const float2* kfrow = reinterpret_cast<const float2*>(a.kf + row * n2) + t;
+    float fi[P], tr[P], acc[P];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-        const int mm = t + T * e;
-        const float2 kk = *reinterpret_cast<const float2*>(a.kf + row * n2 + 2 * mm);
-        const float2 ra = *reinterpret_cast<const float2*>(a.rA + row * n2 + 2 * mm);
-        fz_hat_state(fmin((double)kk.x, a.kfclip), ra.x, kn, kup, a.m, base[2 * e], rw[2 * e]);
-        fz_hat_state(fmin((double)kk.y, a.kfclip), ra.y, kn, kup, a.m, base[2 * e + 1], rw[2 * e + 1]);
+        const float2 kk = __ldg(kfrow + T * e);
+        fz_interval_state(kk.x, a, nodes, clipdn, fi[2 * e], tr[2 * e]);
+        fz_interval_state(kk.y, a, nodes, clipdn, fi[2 * e + 1], tr[2 * e + 1]);
+        acc[2 * e] = acc[2 * e + 1] = 0.0f;
     }
     for (int jj = 0; jj < a.nb; ++jj) {
         const int j = a.j0 + jj;
         float2 v[E];
+        fz_c2r_load<H>(a.XY + (long long)(plane0 + jj) * a.d.plane, row, a.d.nyq, t, a.tw.tr, v);
+        fz::line_fft_pp<H, E, +1>(v, b0, b1, ix, t, a.tw.th);
+        const float jf = (float)j;
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            float u[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int q = 2 * e + h;
-                const int dd = j - base[q];
-                u[h] = dd == 0 ? rw[q][0] : (dd == 1 ? rw[q][1] : (dd == 2 ? rw[q][2] : 0.0f));
-            }
-            v[e] = make_float2(u[0], u[1]);
+        for (int q = 0; q < P; ++q) {
+            const float pv = (q & 1) ? v[q >> 1].y : v[q >> 1].x;
+            acc[q] = fmaf(fz_hat(jf, fi[q], tr[q]), pv, acc[q]);
         }
-        __syncthreads();  // sm free
-        fz::line_fft<H, E, -1>(v, sm, ix, t, a.tw.th);
-        __syncthreads();  // the transform's last reads done
+        if (SMALL && j == 0) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) sm[ix(t + T * e)] = v[e];
-        __syncthreads();
+            for (int e = 0; e < E; ++e) {
+                const float2 kk = __ldg(kfrow + T * e);
+                acc[2 * e] = fmaf(fz_small_weight(kk.x, a, nodes, clipdn, true), v[e].x, acc[2 * e]);
+                acc[2 * e + 1] = fmaf(fz_small_weight(kk.y, a, nodes, clipdn, true), v[e].y, acc[2 * e + 1]);
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        float2* p = reinterpret_cast<float2*>(pot + row * n2) + t + T * e;
+        float2 o = make_float2(acc[2 * e], acc[2 * e + 1]);
+        if (!a.first) {
+            const float2 old = *p;
+            o = make_float2(old.x + o.x, old.y + o.y);
+        }
+        *p = o;
+    }
+}
+
+// rho^alpha W_j of every node of the batch, R2C along axis 2, row by row.
+// The post-processing pairs (k, H-k) are exchanged between the row's threads
+// with shuffles: element H-k of thread t's slot e sits in thread (T - t) % T,
+// slot E-1-e (t > 0) or in thread 0, slot (E-e) % E (t = 0).
+template <int H>
+__global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
+    constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
+    static_assert(T <= 32, "a row must fit in one warp");
+    using Lay = fz::RowLayout<H>;
+    extern __shared__ float4 fz_rsm4[];
+    float* fs = reinterpret_cast<float*>(fz_rsm4);
+    const FzNodeSm nodes = fz_stage_nodes(a, fs);
+    float2* buf0 = reinterpret_cast<float2*>(fs + ((5 * a.m + 3) & ~3));
+    float2* buf1 = buf0 + ROWS * Lay::slots;
+    __syncthreads();
+    const int t = threadIdx.x % T, l = threadIdx.x / T;
+    const long long row = (long long)blockIdx.x * ROWS + l;
+    const int n2 = 2 * H;
+    float2* b0 = buf0 + l * Lay::slots;
+    float2* b1 = buf1 + l * Lay::slots;
+    const typename Lay::Idx ix;
+    const float clipdn = __double2float_rd(a.kfclip);
+    const int lane = threadIdx.x & 31;
+    const int partner = (lane & ~(T - 1)) | ((T - t) & (T - 1));
+    const float2* kfrow = reinterpret_cast<const float2*>(a.kf + row * n2) + t;
+    const float2* rarow = reinterpret_cast<const float2*>(a.rA + row * n2) + t;
+    float fi[P], tr[P], ra[P];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const float2 kk = __ldg(kfrow + T * e);
+        const float2 rr = __ldg(rarow + T * e);
+        fz_interval_state(kk.x, a, nodes, clipdn, fi[2 * e], tr[2 * e]);
+        fz_interval_state(kk.y, a, nodes, clipdn, fi[2 * e + 1], tr[2 * e + 1]);
+        ra[2 * e] = rr.x;
+        ra[2 * e + 1] = rr.y;
+    }
+    for (int jj = 0; jj < a.nb; ++jj) {
+        const int j = a.j0 + jj;
+        const float jf = (float)j;
+        float2 v[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            v[e] = make_float2(ra[2 * e] * fz_hat(jf, fi[2 * e], tr[2 * e]),
+                               ra[2 * e + 1] * fz_hat(jf, fi[2 * e + 1], tr[2 * e + 1]));
+        if (j == 0) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const float2 kk = __ldg(kfrow + T * e);
+                v[e].x = fmaf(ra[2 * e], fz_small_weight(kk.x, a, nodes, clipdn, false), v[e].x);
+                v[e].y = fmaf(ra[2 * e + 1], fz_small_weight(kk.y, a, nodes, clipdn, false), v[e].y);
+            }
+        }
+        fz::line_fft_pp<H, E, -1>(v, b0, b1, ix, t, a.tw.th);
         float2* dst = a.XY + (long long)jj * a.d.plane;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int k = t + T * e;
-            const float2 Zk = sm[ix(k)], Zc = sm[ix((H - k) & (H - 1))];
+            const float2 Zk = v[e];
+            float2 Zc;
+            Zc.x = __shfl_sync(0xffffffffu, v[E - 1 - e].x, partner);
+            Zc.y = __shfl_sync(0xffffffffu, v[E - 1 - e].y, partner);
+            if (t == 0) Zc = v[(E - e) % E];
             // X = (Zk + conj Zc)/2 - i w^-k (Zk - conj Zc)/2, w^-k = exp(-2 pi i k/n2)
             const float2 A = make_float2(0.5f * (Zk.x + Zc.x), 0.5f * (Zk.y - Zc.y));
             const float2 B = make_float2(0.5f * (Zk.x - Zc.x), 0.5f * (Zk.y + Zc.y));
             const float2 wB = fz::cmul(B, __ldg(a.tw.tr + k));
-            dst[row * H + k] = make_float2(A.x + wB.y, A.y - wB.x);
+            __stcs(dst + row * H + k, make_float2(A.x + wB.y, A.y - wB.x));
         }
-        if (t == 0) {
-            const float2 Z0 = sm[ix(0)];
-            dst[a.d.nyq + row] = make_float2(Z0.x - Z0.y, 0.0f);
-        }
+        if (t == 0) __stcs(dst + a.d.nyq + row, make_float2(v[0].x - v[0].y, 0.0f));
     }
 }
 
 // Axis-0 forward transform of the batch's planes, K_j(G)/N applied and summed
 // into pot2(G) (lwt.py:266-296; the sum starts from the previous batches').
+// K_j(0) = 0: the G = 0 element keeps its starting value.
 template <int N0>
-__global__ void __launch_bounds__(kFzLines * (N0 / kFzColE))
-    k_fz_pot2(const float2* __restrict__ XY, float2* __restrict__ pot2G, Table<float> tab, Nodes nd, int j0, int nb,
-              int first, Geo geo, FzDims d, const float2* __restrict__ tw, double invN) {
-    constexpr int E = kFzColE, T = N0 / E;
+__global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
+    k_fz_pot2(const float2* __restrict__ XY, float2* __restrict__ pot2G, FzTab tb, const double* __restrict__ knode,
+              const double* __restrict__ invk, int j0, int nb, int first, Geo geo, FzDims d,
+              const float2* __restrict__ tw, float invN) {
+    constexpr int E = kFzColE, T = N0 / E, L = kFzLines;
     extern __shared__ float2 fz_sm[];
-    float* sinvk = reinterpret_cast<float*>(fz_sm + fz::col_slots(N0));
-    for (int q = threadIdx.x; q < nb; q += blockDim.x) sinvk[q] = (float)nd.invk[j0 + q];
-    __syncthreads();
-    const int l = threadIdx.x % kFzLines, t = threadIdx.x / kFzLines;
+    float2* sm = fz_sm;
+    float* sq = reinterpret_cast<float*>(fz_sm + fz::col_slots(N0));
+    float* siq = sq + N0 * L;
+    float* sik = siq + N0 * L;
+    float* sk2 = sik + nb;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        const double k = knode[j0 + q];
+        sik[q] = (float)invk[j0 + q];
+        sk2[q] = (float)(k * k);
+    }
+    const int l = threadIdx.x % L, t = threadIdx.x / L;
     int k1, k2;
     long long pbase, pstride, gbase, gstride;
     fz_axis0_tile(d, blockIdx.x, l, k1, k2, pbase, pstride, gbase, gstride);
-    const float invNt = (float)invN;
-    float q[E];
     float2 acc[E];
-#pragma unroll
+#pragma unroll 4
     for (int e = 0; e < E; ++e) {
         const int k0 = t + T * e;
-        q[e] = sqrtf(gsq_f(geo, k0, k1, k2));
+        const int s = k0 * L + l;
+        const float q2 = gsq_f(geo, k0, k1, k2);
+        sq[s] = sqrtf(q2);
+        siq[s] = q2 > 0.0f ? 1.0f / q2 : 0.0f;
         acc[e] = first ? make_float2(0.0f, 0.0f) : pot2G[gbase + k0 * gstride];
     }
     const bool g0 = (t == 0 && k1 == 0 && k2 == 0);
-    float2* sm = fz_sm + l;
+    const float2 acc00 = acc[0];
     for (int jj = 0; jj < nb; ++jj) {
-        const float ik = sinvk[jj];
         const float2* inp = XY + (long long)jj * d.plane + pbase;
         float2 v[E];
 #pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = inp[(t + T * e) * pstride];
-        __syncthreads();
-        fz::line_fft<N0, E, -1>(v, sm, fz::ColIdx(), t, tw);
+        for (int e = 0; e < E; ++e) v[e] = __ldcs(inp + (t + T * e) * pstride);
+        __syncthreads();  // the exchange buffer is free; the node and |G| tables are staged
+        fz::line_fft<N0, E, -1>(v, sm + l, fz::ColIdx(), t, tw);
+        const float ik = sik[jj], kj2 = sk2[jj];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
+            const int s = (t + T * e) * L + l;
             float K, KD;
-            node_kernel<float>(tab, q[e], ik, false, (g0 && e == 0) ? 0 : 1, K, KD);
-            const float f = K * invNt;
-            acc[e].x += f * v[e].x;
-            acc[e].y += f * v[e].y;
+            fz_node_kernel<false>(tb, sq[s], ik, siq[s], kj2, K, KD);
+            const float f = K * invN;
+            acc[e].x = fmaf(f, v[e].x, acc[e].x);
+            acc[e].y = fmaf(f, v[e].y, acc[e].y);
         }
     }
+    if (g0) acc[0] = acc00;
 #pragma unroll
     for (int e = 0; e < E; ++e) pot2G[gbase + (t + T * e) * gstride] = acc[e];
 }

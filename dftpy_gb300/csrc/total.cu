@@ -816,7 +816,7 @@ struct LwtPlan {
 };
 
 // ------------------------------------------------ fused k_F-node pipeline (host)
-constexpr int kFzMaxNodes = 1024;  // node lists (2 doubles each) staged in shared memory
+constexpr int kFzMaxNodes = 1024;  // node bounds (5 floats each) staged in shared memory
 constexpr int kFzMaxBatch = 256;   // node reciprocals staged in shared memory
 
 bool fz_applies(const ofdft_grid* g, bool hermite, int m) {
@@ -884,6 +884,12 @@ struct FzRun {
     double kfclip;
 };
 
+// Dynamic shared memory above the default 48 KB needs a per-kernel opt-in.
+template <class K>
+void fz_smem_optin(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) OFDFT_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
 // Runs every node batch of the fused pipeline; returns the number of launches.
 int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     ofdft_grid* g = e->g;
@@ -902,6 +908,7 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     tw.t1 = e->fz_tw + n0;
     tw.th = e->fz_tw + n0 + n1;
     tw.tr = e->fz_tw + n0 + n1 + H;
+    const FzTab tb = fz_tab(r.tab);
     const size_t cb = g->cplx_bytes();
     const bool mc = r.kdd == 3;  // M planes feed pot3 only
     const int per_node = mc ? 2 : 1;
@@ -913,24 +920,35 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     if (fit < B) B = (int)std::max(1LL, fit);
     B = std::min(B, r.m);
     float2* XY = (float2*)e->sc.get("lwtXY", (size_t)per_node * B * cb);
-    const double Ncd = (double)g->Nc, Nd = (double)g->N, invN = 1.0 / Nd;
+    const double Ncd = (double)g->Nc, Nd = (double)g->N;
+    const float invN = (float)(1.0 / Nd);
     const int tiles0 = n1 * (H / kFzLines) + n1 / kFzLines;
     const int tiles1 = n0 * (H / kFzLines) + n0 / kFzLines;
+    const double* knode = r.nd.k;
+    const double* invk = r.nd.invk;
     int launches = 0;
     for (int j0 = 0; j0 < r.m; j0 += B) {
         const int nb = std::min(B, r.m - j0);
         const int nplanes = mc ? 2 * nb : nb;
         const bool first = j0 == 0;
-        // ---- C2R: axis 0 with the node kernels applied on load
+        // ---- C2R: axis 0 with the node kernels applied on load (P planes, then M
+        // planes); nodes split over blocks when the tile count alone leaves a long
+        // last wave
+        const int nsplit = (nb >= 16 && tiles0 < 8 * g->sms) ? 2 : 1;
         with_col(n0, [&](auto c0) {
             constexpr int N0 = decltype(c0)::value;
-            const size_t smem = fz::col_slots(N0) * sizeof(float2) + (size_t)nb * sizeof(float);
-            timed(e, P_LWT_NODES, Ncd * 8.0 * (1 + nplanes), st, [&] {
-                k_fz_nodes<N0><<<tiles0, N0, smem, st>>>(r.rbG, XY, r.tab, r.nd, j0, nb, mc ? 1 : 0, g->geo, d,
-                                                          tw.t0, invN);
-            });
+            const size_t smem = fz_col_smem(N0, nb, true);
+            auto launch = [&](auto kern, int plane0) {
+                fz_smem_optin(kern, smem);
+                timed(e, P_LWT_NODES, Ncd * 8.0 * (nsplit + nb), st, [&] {
+                    kern<<<tiles0 * nsplit, kFzLines * (N0 / kFzColE), smem, st>>>(
+                        r.rbG, XY, tb, knode, invk, j0, nb, plane0, tiles0, nsplit, g->geo, d, tw.t0, invN);
+                });
+                OFDFT_LAUNCH_CHECK();
+            };
+            launch(k_fz_nodes<N0, false>, 0);
+            if (mc) launch(k_fz_nodes<N0, true>, nb);
         });
-        OFDFT_LAUNCH_CHECK();
         // ---- axis 1
         with_col(n1, [&](auto c1) {
             constexpr int N1 = decltype(c1)::value;
@@ -951,8 +969,6 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         ra.m = r.m;
         ra.j0 = j0;
         ra.nb = nb;
-        ra.nplanes = nplanes;
-        ra.kdd = r.kdd;
         ra.first = first ? 1 : 0;
         ra.kfclip = r.kfclip;
         ra.d = d;
@@ -960,22 +976,26 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         with_row(H, [&](auto ch) {
             constexpr int HH = decltype(ch)::value;
             constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
-            const size_t smem = 2 * (size_t)r.m * sizeof(double) + ROWS * fz::row_slots(HH) * sizeof(float2);
+            const size_t smem = fz_row_smem(HH, r.m);
             const int grid = (int)((long long)n0 * n1 / ROWS);
-            const int accs = 1 + (r.kdd == 3);
-            timed(e, P_LWT_INTERP, Ncd * 8.0 * nplanes + Nd * 4.0 * (1 + accs * (first ? 1 : 2)), st,
-                  [&] { k_fz_c2r_rows<HH><<<grid, kFzRowThreads, smem, st>>>(ra); });
+            auto launch = [&](auto kern, int plane0, float* pot) {
+                fz_smem_optin(kern, smem);
+                timed(e, P_LWT_INTERP, Ncd * 8.0 * nb + Nd * 4.0 * (1 + (first ? 1 : 2)), st,
+                      [&] { kern<<<grid, kFzRowThreads, smem, st>>>(ra, plane0, pot); });
+                OFDFT_LAUNCH_CHECK();
+            };
+            launch(k_fz_c2r_rows<HH, true>, 0, r.pot1);
+            if (mc) launch(k_fz_c2r_rows<HH, false>, nb, r.pot3);
         });
-        OFDFT_LAUNCH_CHECK();
-        launches += 3;
+        launches += mc ? 5 : 3;
         if (r.kdd > 1) {
             // ---- R2C: hat-weighted rho^alpha along axis 2, then axis 1, then axis 0 into pot2(G)
-            ra.nplanes = nb;
             with_row(H, [&](auto ch) {
                 constexpr int HH = decltype(ch)::value;
                 constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
-                const size_t smem = 2 * (size_t)r.m * sizeof(double) + ROWS * fz::row_slots(HH) * sizeof(float2);
+                const size_t smem = fz_row_smem(HH, r.m);
                 const int grid = (int)((long long)n0 * n1 / ROWS);
+                fz_smem_optin(k_fz_r2c_rows<HH>, smem);
                 timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st,
                       [&] { k_fz_r2c_rows<HH><<<grid, kFzRowThreads, smem, st>>>(ra); });
             });
@@ -989,10 +1009,11 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
             OFDFT_LAUNCH_CHECK();
             with_col(n0, [&](auto c0) {
                 constexpr int N0 = decltype(c0)::value;
-                const size_t smem = fz::col_slots(N0) * sizeof(float2) + (size_t)nb * sizeof(float);
+                const size_t smem = fz_col_smem(N0, nb, false);
+                fz_smem_optin(k_fz_pot2<N0>, smem);
                 timed(e, P_LWT_POT2, Ncd * 8.0 * (nb + (first ? 1 : 2)), st, [&] {
-                    k_fz_pot2<N0><<<tiles0, N0, smem, st>>>(XY, r.pot2G, r.tab, r.nd, j0, nb, first ? 1 : 0, g->geo,
-                                                             d, tw.t0, invN);
+                    k_fz_pot2<N0><<<tiles0, kFzLines * (N0 / kFzColE), smem, st>>>(
+                        XY, r.pot2G, tb, knode, invk, j0, nb, first ? 1 : 0, g->geo, d, tw.t0, invN);
                 });
             });
             OFDFT_LAUNCH_CHECK();

@@ -150,6 +150,7 @@ struct Stockham {
 
     __device__ __forceinline__ static void run(float2 (&v)[E], float2* sm, Idx ix, int t,
                                                const float2* __restrict__ tw) {
+        __builtin_assume(t >= 0 && t < T);
         if constexpr (NS > 1) {
             __syncthreads();  // the previous pass's outputs are in sm
 #pragma unroll
@@ -221,6 +222,7 @@ struct StockhamPP {
 
     __device__ __forceinline__ static void run(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
                                                const float2* __restrict__ tw) {
+        __builtin_assume(t >= 0 && t < T);
         if constexpr (NS > 1) {
             const float2* src = ((PASS - 1) & 1) ? b1 : b0;
             __syncthreads();  // the previous pass's outputs are in src
@@ -259,6 +261,44 @@ struct StockhamPP {
         }
     }
 };
+
+// ---- 1-D bulk asynchronous copies (TMA) into shared memory, completed on an
+// mbarrier.  Sources and destinations are 16-byte aligned, sizes multiples of 16.
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// makes initialised mbarriers visible to the copy engine
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+// orders this thread's earlier shared-memory accesses before later copies into it
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// Waits for the phase of `parity` to complete, polling at most 2^22 times;
+// false when it did not (the caller records an error instead of hanging).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_addr(bar);
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 template <int N, int E, int S, class Idx>
 __device__ __forceinline__ void line_fft_pp(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,

@@ -94,31 +94,31 @@ __device__ __forceinline__ float fz_spline(const float* c, int nint, float step,
     return q.x + u * (q.y + u * (q.z + u * q.w));
 }
 
-// K_j(|G|) and (DERIV) -eta K_j'(eta) at eta = q/k_j: the table limit at and
-// above etamax, the series at and above eta_series (u = eta^-2 = k_j^2/q^2),
-// the spline below.  G = 0 is handled by the callers.
+// K_j(|G|) (DERIV false) or -eta K_j'(eta) (DERIV true) at eta = q/k_j: the
+// table limit at and above etamax, the series at and above eta_series
+// (u = eta^-2 = k_j^2/q^2), the spline below.  The series and the limit are
+// selected without branching; only the spline (points near G = 0) branches.
+// G = 0 is handled by the callers.
 template <bool DERIV>
-__device__ __forceinline__ void fz_node_kernel(const FzTab& tb, float q, float ik, float iq2, float kj2, float& K,
-                                               float& KD) {
+__device__ __forceinline__ float fz_node_kernel(const FzTab& tb, float q, float ik, float iq2, float kj2) {
     const float eta = q * ik;
-    if (eta >= tb.etamax) {
-        K = tb.limit;
-        KD = tb.limitd;
-    } else if (eta >= tb.eta_series) {
-        const float u = iq2 * kj2;
-        float f = fz_series_c(7);
+    const float u = iq2 * kj2;
+    float r;
+    if constexpr (DERIV) {
         float d = 16.0f * fz_series_c(7);
 #pragma unroll
-        for (int k = 6; k >= 0; --k) {
-            f = fmaf(f, u, fz_series_c(k));
-            if (DERIV) d = fmaf(d, u, (float)(2 * (k + 1)) * fz_series_c(k));
-        }
-        K = tb.factor * fmaf(f, u, tb.kconst);
-        KD = DERIV ? tb.factor * (d * u) : 0.0f;
+        for (int k = 6; k >= 0; --k) d = fmaf(d, u, (float)(2 * (k + 1)) * fz_series_c(k));
+        r = tb.factor * (d * u);
+        r = eta >= tb.etamax ? tb.limitd : r;
     } else {
-        K = fz_spline(tb.c, tb.nint, tb.step, tb.inv_step, eta);
-        KD = DERIV ? fz_spline(tb.cd, tb.nint, tb.step, tb.inv_step, eta) : 0.0f;
+        float f = fz_series_c(7);
+#pragma unroll
+        for (int k = 6; k >= 0; --k) f = fmaf(f, u, fz_series_c(k));
+        r = tb.factor * fmaf(f, u, tb.kconst);
+        r = eta >= tb.etamax ? tb.limit : r;
     }
+    if (eta < tb.eta_series) r = fz_spline(DERIV ? tb.cd : tb.c, tb.nint, tb.step, tb.inv_step, eta);
+    return r;
 }
 
 // Column tile of the axis-0 passes: main tiles (k1, 16 consecutive k2 < H) then
@@ -200,9 +200,8 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int s = (t + T * e) * L + l;
-            float K, KD;
-            fz_node_kernel<DERIV>(tb, sq[s], ik, siq[s], kj2, K, KD);
-            const float f = DERIV ? KD * ik : K;
+            const float kv = fz_node_kernel<DERIV>(tb, sq[s], ik, siq[s], kj2);
+            const float f = DERIV ? kv * ik : kv;
             const float2 z = sz[s];
             v[e] = make_float2(f * z.x, f * z.y);
         }
@@ -262,6 +261,7 @@ struct FzRowArgs {
     double kfclip;
     FzDims d;
     FzTw tw;
+    unsigned* err;  // set to 1 when a copy into shared memory did not complete in time
 };
 
 // Node bounds of the interval search in float32, staged per block (5 m floats):
@@ -357,27 +357,24 @@ __device__ __forceinline__ float fz_hat(float jf, float fi, float tr) {
     return fmaxf(0.0f, 1.0f - fabsf((jf - fi) - tr));
 }
 
-// Row of plane `src` pre-processed for the half-length complex C2R:
+// Row l of a staged block (ROWS rows of H complex, then their ROWS Nyquist
+// values) pre-processed for the half-length complex C2R:
 // Z[k] = (X[k] + conj X[H-k]) + i w^k (X[k] - conj X[H-k]), w = exp(+2 pi i/n2),
 // the imaginary parts of X[0] and X[H] dropped.
 template <int H>
-__device__ __forceinline__ void fz_c2r_load(const float2* __restrict__ src, long long row, long long nyq, int t,
-                                            const float2* __restrict__ twr, float2 (&v)[kFzRowE]) {
-    constexpr int E = kFzRowE, T = H / E;
-    const float2* r = src + row * H;
+__device__ __forceinline__ void fz_c2r_pre(const float2* st, int l, int t, const float2* __restrict__ twr,
+                                           float2 (&v)[kFzRowE]) {
+    constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T;
+    const float2* r = st + l * H;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const int k = t + T * e;
-        float2 X = __ldg(r + k);
-        float2 Y;
-        if (e == 0) {
-            Y = k == 0 ? __ldg(src + nyq + row) : __ldg(r + H - k);
-            if (k == 0) {
-                X.y = 0.0f;
-                Y.y = 0.0f;
-            }
-        } else {
-            Y = __ldg(r + H - k);
+        float2 X = r[k];
+        float2 Y = r[(H - k) & (H - 1)];
+        if (e == 0 && k == 0) {
+            Y = st[ROWS * H + l];
+            X.y = 0.0f;
+            Y.y = 0.0f;
         }
         const float2 A = make_float2(X.x + Y.x, X.y - Y.y);
         const float2 B = make_float2(X.x - Y.x, X.y + Y.y);
@@ -386,28 +383,50 @@ __device__ __forceinline__ void fz_c2r_load(const float2* __restrict__ src, long
     }
 }
 
-inline size_t fz_row_smem(int H, int m) {
+// shared memory of k_fz_c2r_rows (with_stages) and k_fz_r2c_rows
+inline size_t fz_row_smem(int H, int m, bool with_stages) {
     const int T = H / kFzRowE, ROWS = kFzRowThreads / T;
-    const size_t nodes = ((size_t)5 * m * sizeof(float) + 15) / 16 * 16;
-    return nodes + 2 * (size_t)ROWS * (H >= 128 ? H : H + (H >> 4) + 1) * sizeof(float2);
+    const size_t slots = H >= 128 ? H : H + (H >> 4) + 1;
+    size_t b = 16 + 2 * (size_t)ROWS * slots * sizeof(float2) + (size_t)5 * m * sizeof(float);
+    if (with_stages) b += 2 * (size_t)(ROWS * H + ROWS) * sizeof(float2);
+    return b;
 }
 
 // Axis-2 C2R of the batch's planes plane0 .. plane0 + nb - 1 (node j0 + jj),
 // row by row, interpolated into `pot` at every point of the row: pot1 from the
 // P planes, pot3 from the M planes (SMALL: the small-k_F branch of node 0
-// counts, which it does for pot1 only).
+// counts, which it does for pot1 only).  The block's rows of each plane (16 KB
+// at n2 = 256) arrive by bulk copy two planes ahead of their use.
 template <int H, bool SMALL>
 __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, int plane0, float* __restrict__ pot) {
     constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
+    constexpr int STAGE = ROWS * H + ROWS;  // float2: the block's rows, then their Nyquist values
     using Lay = fz::RowLayout<H>;
     extern __shared__ float4 fz_rsm4[];
-    float* fs = reinterpret_cast<float*>(fz_rsm4);
-    const FzNodeSm nodes = fz_stage_nodes(a, fs);
-    float2* buf0 = reinterpret_cast<float2*>(fs + ((5 * a.m + 3) & ~3));
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(fz_rsm4);
+    float2* stage = reinterpret_cast<float2*>(fz_rsm4 + 1);
+    float2* buf0 = stage + 2 * STAGE;
     float2* buf1 = buf0 + ROWS * Lay::slots;
+    float* fs = reinterpret_cast<float*>(buf1 + ROWS * Lay::slots);
+    const long long row0 = (long long)blockIdx.x * ROWS;
+    auto issue = [&](int jj) {  // one thread: plane jj into stage jj & 1
+        const int s = jj & 1;
+        const float2* src = a.XY + (long long)(plane0 + jj) * a.d.plane;
+        fz::mbar_expect_tx(&bar[s], STAGE * (unsigned)sizeof(float2));
+        fz::bulk_load(stage + s * STAGE, src + row0 * H, ROWS * H * (unsigned)sizeof(float2), &bar[s]);
+        fz::bulk_load(stage + s * STAGE + ROWS * H, src + a.d.nyq + row0, ROWS * (unsigned)sizeof(float2), &bar[s]);
+    };
+    if (threadIdx.x == 0) {
+        fz::mbar_init(&bar[0], 1);
+        fz::mbar_init(&bar[1], 1);
+        fz::mbar_fence_init();
+        issue(0);
+        if (a.nb > 1) issue(1);
+    }
+    const FzNodeSm nodes = fz_stage_nodes(a, fs);
     __syncthreads();
     const int t = threadIdx.x % T, l = threadIdx.x / T;
-    const long long row = (long long)blockIdx.x * ROWS + l;
+    const long long row = row0 + l;
     const int n2 = 2 * H;
     float2* b0 = buf0 + l * Lay::slots;
     float2* b1 = buf1 + l * Lay::slots;
@@ -424,9 +443,16 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
     }
     for (int jj = 0; jj < a.nb; ++jj) {
         const int j = a.j0 + jj;
+        const int s = jj & 1;
+        if (!fz::mbar_wait(&bar[s], (jj >> 1) & 1)) atomicOr(a.err, 1u);
         float2 v[E];
-        fz_c2r_load<H>(a.XY + (long long)(plane0 + jj) * a.d.plane, row, a.d.nyq, t, a.tw.tr, v);
+        fz_c2r_pre<H>(stage + s * STAGE, l, t, a.tw.tr, v);
         fz::line_fft_pp<H, E, +1>(v, b0, b1, ix, t, a.tw.th);
+        // every thread has passed the transform's first barrier, so stage s is read
+        if (threadIdx.x == 0 && jj + 2 < a.nb) {
+            fz::fence_proxy_async();
+            issue(jj + 2);
+        }
         const float jf = (float)j;
 #pragma unroll
         for (int q = 0; q < P; ++q) {
@@ -464,10 +490,10 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
     static_assert(T <= 32, "a row must fit in one warp");
     using Lay = fz::RowLayout<H>;
     extern __shared__ float4 fz_rsm4[];
-    float* fs = reinterpret_cast<float*>(fz_rsm4);
-    const FzNodeSm nodes = fz_stage_nodes(a, fs);
-    float2* buf0 = reinterpret_cast<float2*>(fs + ((5 * a.m + 3) & ~3));
+    float2* buf0 = reinterpret_cast<float2*>(fz_rsm4 + 1);
     float2* buf1 = buf0 + ROWS * Lay::slots;
+    float* fs = reinterpret_cast<float*>(buf1 + ROWS * Lay::slots);
+    const FzNodeSm nodes = fz_stage_nodes(a, fs);
     __syncthreads();
     const int t = threadIdx.x % T, l = threadIdx.x / T;
     const long long row = (long long)blockIdx.x * ROWS + l;
@@ -573,9 +599,7 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int s = (t + T * e) * L + l;
-            float K, KD;
-            fz_node_kernel<false>(tb, sq[s], ik, siq[s], kj2, K, KD);
-            const float f = K * invN;
+            const float f = fz_node_kernel<false>(tb, sq[s], ik, siq[s], kj2) * invN;
             acc[e].x = fmaf(f, v[e].x, acc[e].x);
             acc[e].y = fmaf(f, v[e].y, acc[e].y);
         }

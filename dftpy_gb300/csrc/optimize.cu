@@ -201,22 +201,54 @@ bool wolfe1(Phi&& phi, double f0, double g0, double stp0, double c1, double c2, 
 }
 
 // ------------------------------------------------------------- field ops
+// Element arithmetic runs in the grid precision T (GB300 runs float64 at a
+// small fraction of the float32 rate); sums run per thread in RunSum<T> and
+// across threads in float64.
+template <typename T>
+struct RunSum;
+template <>
+struct RunSum<double> {
+    double s = 0.0;
+    __device__ void add(double x) { s += x; }
+    __device__ double get() const { return s; }
+};
+template <>
+struct RunSum<float> {
+    float s = 0.0f, c = 0.0f;
+    __device__ void add(float x) {  // Kahan-compensated
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ double get() const { return (double)s - (double)c; }
+};
+
 template <typename T>
 __global__ void k_lincomb(long long n, T* out, double a0, const T* x0, double a1, const T* x1, double a2,
                           const T* x2) {
+    const T b0 = (T)a0, b1 = (T)a1, b2 = (T)a2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double v = a0 * (double)x0[i];
-        if (x1) v += a1 * (double)x1[i];
-        if (x2) v += a2 * (double)x2[i];
-        out[i] = (T)v;
+        T v = b0 * x0[i];
+        if (x1) v += b1 * x1[i];
+        if (x2) v += b2 * x2[i];
+        out[i] = v;
     }
 }
+
+// sqrt(rho), 1e-300 where rho <= 0 (0 in float32, where 1e-300 underflows)
+template <typename T>
+__device__ inline T phi_floor();
+template <>
+__device__ inline double phi_floor<double>() { return 1e-300; }
+template <>
+__device__ inline float phi_floor<float>() { return 0.0f; }
 
 template <typename T>
 __global__ void k_phi_init(long long n, const T* rho, T* phi) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double r = (double)rho[i];
-        phi[i] = (T)(r > 0 ? sqrt(r) : 1e-300);
+        const T r = rho[i];
+        phi[i] = r > (T)0 ? sqrt(r) : phi_floor<T>();
     }
 }
 
@@ -224,50 +256,56 @@ __global__ void k_phi_init(long long n, const T* rho, T* phi) {
 template <typename T>
 __global__ void k_square(long long n, const T* x, T* out) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double v = (double)x[i];
-        out[i] = (T)(v * v);
+        const T v = x[i];
+        out[i] = v * v;
     }
 }
 
 // newphi = phi cos + p sin, rho = newphi^2
 template <typename T>
 __global__ void k_rotate(long long n, const T* phi, const T* p, double c, double s, T* newphi, T* rho) {
+    const T cw = (T)c, sw = (T)s;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double v = (double)phi[i] * c + (double)p[i] * s;
-        newphi[i] = (T)v;
-        rho[i] = (T)(v * v);
+        const T v = phi[i] * cw + p[i] * sw;
+        newphi[i] = v;
+        rho[i] = v * v;
     }
 }
 
 // out = (V - mu) phi
 template <typename T>
 __global__ void k_resid(long long n, const T* V, double mu, const T* phi, T* out) {
+    const T m = (T)mu;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = (T)(((double)V[i] - mu) * (double)phi[i]);
+        out[i] = (V[i] - m) * phi[i];
 }
 
 // Ap = ((V1 - mu) phi1 - res0) / eps
 template <typename T>
 __global__ void k_tn_ap(long long n, const T* V1, double mu, const T* phi1, const T* res0, double eps, T* Ap) {
+    const T m = (T)mu, ep = (T)eps;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        Ap[i] = (T)((((double)V1[i] - mu) * (double)phi1[i] - (double)res0[i]) / eps);
+        Ap[i] = ((V1[i] - m) * phi1[i] - res0[i]) / ep;
 }
 
 // sum V * newphi * (p cos - phi sin)
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_dtheta(long long n, const T* V, const T* nphi, const T* p,
                                                         const T* phi, double c, double s, double* partials) {
-    double acc[1] = {0.0};
+    const T cw = (T)c, sw = (T)s;
+    RunSum<T> sum;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        acc[0] += (double)V[i] * (double)nphi[i] * ((double)p[i] * c - (double)phi[i] * s);
+        sum.add(V[i] * nphi[i] * (p[i] * cw - phi[i] * sw));
+    double acc[1] = {sum.get()};
     block_sum_store<1>(acc, partials);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_dot2(long long n, const T* a, const T* b, double* partials) {
-    double acc[1] = {0.0};
+    RunSum<T> sum;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        acc[0] += (double)a[i] * (double)b[i];
+        sum.add(a[i] * b[i]);
+    double acc[1] = {sum.get()};
     block_sum_store<1>(acc, partials);
 }
 

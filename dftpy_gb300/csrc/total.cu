@@ -87,12 +87,37 @@ struct PreArgs {
 // slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho
 constexpr int PRE_NS = 7;
 
-// Pointwise pre-pass.  All arithmetic runs in the grid precision T; the
-// per-thread energy accumulators are float64 in both precisions.
+// Per-thread running sum of a field reduction: float64 in the FP64 path; in the
+// FP32 path a float32 Kahan-compensated sum over the thread's points (GB300
+// runs float64 at a small fraction of the float32 rate), handed to the float64
+// block and grid reductions at the end.
+template <typename T>
+struct RunSum;
+template <>
+struct RunSum<double> {
+    double s = 0.0;
+    __device__ void add(double x) { s += x; }
+    __device__ double get() const { return s; }
+};
+template <>
+struct RunSum<float> {
+    float s = 0.0f, c = 0.0f;
+    __device__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ double get() const { return (double)s - (double)c; }
+};
+
+// Pointwise pre-pass.  All arithmetic runs in the grid precision T; sums run
+// per thread in RunSum<T> and across threads in float64.
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* partials) {
     using M = T;
-    double acc[PRE_NS] = {0.0, 0.0, 0.0, 0.0, INFINITY, -INFINITY, -INFINITY};
+    RunSum<M> sum[4];
+    M kfmin = (M)INFINITY, kfmax = -(M)INFINITY, rmax = -(M)INFINITY;
     const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2};
     const M cTF_E = (M)a.k.cTF_E, cTF_V = (M)a.k.cTF_V, tf_x = (M)a.tf_x;
     const M lda_rs = (M)a.k.lda_rs, lda_ex = (M)a.k.lda_ex, lda_vx = (M)a.k.lda_vx;
@@ -104,15 +129,15 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
         const M r = a.rho[i];
         M v = (M)0;
-        acc[3] += (double)r;
-        acc[6] = fmax(acc[6], (double)r);
+        sum[3].add(r);
+        rmax = r > rmax ? r : rmax;
         if (a.tf) {
             // PowerInt(rho, 5, 3): repeated products then cbrt (math_utils.py:158-176)
             M r5 = r * r;
             r5 *= r;
             r5 *= r;
             r5 *= r;
-            acc[0] += (double)(mcbrt(r5) * cTF_E);
+            sum[0].add(mcbrt(r5) * cTF_E);
             if (a.wantV) v += cTF_V * mcbrt(r * r) * tf_x;
         }
         if (a.xc) {
@@ -133,12 +158,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
                 vx = lda_vx * rc +
                      (P4 + ((M)(7.0 / 6.0) * P4 * P5) * sRs + ((M)(4.0 / 3.0) * P4 * P6 * Rs)) / (den * den);
             }
-            acc[1] += (double)(ex * r);
+            sum[1].add(ex * r);
             v += vx;
         }
         if (a.pp) {
             const M vl = a.vloc[i];
-            acc[2] += (double)(vl * r);
+            sum[2].add(vl * r);
             v += vl;
         }
         if (a.vw) a.sq[i] = msqrt(r > (M)0 ? r : tiny);  // kedf/vw.py:34-44
@@ -150,11 +175,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
         if (a.lwt) {
             const M kf = (M)2 * mcbrt(threepi2 * r);  // kedf/lwt.py:106
             a.kf[i] = kf;
-            acc[4] = fmin(acc[4], (double)kf);
-            acc[5] = fmax(acc[5], (double)kf);
+            kfmin = kf < kfmin ? kf : kfmin;
+            kfmax = kf > kfmax ? kf : kfmax;
         }
         if (a.wantV) a.V[i] = v;
     }
+    double acc[PRE_NS] = {sum[0].get(), sum[1].get(), sum[2].get(), sum[3].get(), (double)kfmin, (double)kfmax,
+                          (double)rmax};
     block_reduce_store<PRE_NS>(acc, kinds, partials);
 }
 
@@ -595,8 +622,8 @@ constexpr int POST_NS = 3;
 
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double* partials) {
-    using M = T;  // working precision; energies accumulate in float64
-    double acc[POST_NS] = {0.0, 0.0, 0.0};
+    using M = T;  // working precision; sums run in RunSum<T>, then float64
+    RunSum<M> sum[POST_NS];
     const M alpha = (M)a.alpha, beta = (M)a.beta, vw_y = (M)a.vw_y, ld = (M)a.ld, rhomax = (M)a.rhomax;
     const M kfclip = (M)a.kfclip, tiny = (M)1e-30, zero_clamp = (M)kZERO;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -607,12 +634,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
             M s = a.sq[i];
             if (fabs(s) < tiny) s = tiny;
             const M pw = a.lap[i] / s;
-            if (r > (M)0) acc[0] += (double)(r * pw);
+            if (r > (M)0) sum[0].add(r * pw);
             v += pw * vw_y;
         }
         if (a.h) {
             const M vh = a.vH[i];
-            acc[1] += (double)(vh * r);
+            sum[1].add(vh * r);
             v += vh;
         }
         if (a.wt) {
@@ -622,14 +649,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
             if (a.same_ab) {
                 const M pot = (M)2 * alpha * (pb / rc) * c1;  // wt.py:19-23
                 if (a.wantV) {
-                    acc[2] += (double)(pot * r / ((M)2 * alpha));  // wt.py:124-125
+                    sum[2].add(pot * r / ((M)2 * alpha));  // wt.py:124-125
                     v += pot;
                 } else {
-                    acc[2] += (double)(c1 * pb);  // wt.py:44-56
+                    sum[2].add(c1 * pb);  // wt.py:44-56
                 }
             } else {
                 const M pa = a.ra[i];
-                acc[2] += (double)(c1 * pa);
+                sum[2].add(c1 * pa);
                 if (a.wantV) v += alpha * (pa / rc) * c1 + beta * (pb / rc) * a.nl2[i];
             }
         }
@@ -641,7 +668,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
             const M rc = r > (M)0 ? r : tiny;
             const M pa = a.same_ab ? a.rb[i] : a.ra[i];
             const M p1 = a.pot1[i] * f;
-            acc[2] += (double)(pa * p1);
+            sum[2].add(pa * p1);
             if (a.wantV) {
                 const M pb = a.rb[i];
                 const M p2 = (a.kdd > 1 ? a.pot2[i] : a.pot1[i]) * f;
@@ -653,6 +680,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
         }
         if (a.wantV) a.V[i] = v;
     }
+    double acc[POST_NS] = {sum[0].get(), sum[1].get(), sum[2].get()};
     block_sum_store<POST_NS>(acc, partials);
 }
 
@@ -683,6 +711,9 @@ struct ofdft_eval {
     double* d_nodes = nullptr;  // [k (kMaxNodes), 1/k, k+1e-18]
     double* h_nodes = nullptr;  // pinned staging
     float2* fz_tw = nullptr;    // twiddle tables of the fused k_F-node pipeline
+    unsigned* d_fz_err = nullptr;  // fused pipeline: nonzero after a bulk copy that did not complete
+    unsigned* h_fz_err = nullptr;  // pinned mirror
+    bool fz_ran = false;           // the last evaluation ran the fused pipeline
     bool kf_set_min = false, kf_set_max = false;
     double kf_st_min = 0, kf_st_max = 0;
     int last_nsp = 0, last_launches = 0;
@@ -869,6 +900,10 @@ void fz_tables(ofdft_eval* e) {
     fill((size_t)n0 + n1 + H, H, n2);
     OFDFT_CK(cudaMalloc(&e->fz_tw, h.size() * sizeof(float2)));
     upload_now(e->fz_tw, h.data(), h.size() * sizeof(float2));
+    OFDFT_CK(cudaMalloc(&e->d_fz_err, sizeof(unsigned)));
+    OFDFT_CK(cudaMallocHost(&e->h_fz_err, sizeof(unsigned)));
+    *e->h_fz_err = 0;
+    upload_now(e->d_fz_err, e->h_fz_err, sizeof(unsigned));
 }
 
 struct FzRun {
@@ -973,10 +1008,11 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         ra.kfclip = r.kfclip;
         ra.d = d;
         ra.tw = tw;
+        ra.err = e->d_fz_err;
         with_row(H, [&](auto ch) {
             constexpr int HH = decltype(ch)::value;
             constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
-            const size_t smem = fz_row_smem(HH, r.m);
+            const size_t smem = fz_row_smem(HH, r.m, true);
             const int grid = (int)((long long)n0 * n1 / ROWS);
             auto launch = [&](auto kern, int plane0, float* pot) {
                 fz_smem_optin(kern, smem);
@@ -993,7 +1029,7 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
             with_row(H, [&](auto ch) {
                 constexpr int HH = decltype(ch)::value;
                 constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
-                const size_t smem = fz_row_smem(HH, r.m);
+                const size_t smem = fz_row_smem(HH, r.m, false);
                 const int grid = (int)((long long)n0 * n1 / ROWS);
                 fz_smem_optin(k_fz_r2c_rows<HH>, smem);
                 timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st,
@@ -1206,6 +1242,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
                 fr.kdd = kdd;
                 fr.kfclip = lp.kfclip;
                 launches += fz_run(e, fr, st);
+                e->fz_ran = true;
             }
         }
         if (!fused) {
@@ -1325,8 +1362,17 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     OFDFT_LAUNCH_CHECK();
     launches += 2;
     OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 24 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (e->fz_ran) OFDFT_CK(cudaMemcpyAsync(e->h_fz_err, e->d_fz_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     OFDFT_CK(cudaStreamSynchronize(st));
     if (e->prof) prof_collect(e);
+    if (e->fz_ran) {
+        e->fz_ran = false;
+        if (*e->h_fz_err) {
+            *e->h_fz_err = 0;
+            upload_now(e->d_fz_err, e->h_fz_err, sizeof(unsigned));
+            OFDFT_REQUIRE(false, "fused k_F-node pipeline: a bulk copy into shared memory did not complete");
+        }
+    }
     const double* R = g->h_results;
     const double dV = g->dV;
     double* E = energies;
@@ -1421,6 +1467,8 @@ void ofdft_eval_destroy(ofdft_eval* e) {
     if (e->d_nodes) cudaFree(e->d_nodes);
     if (e->h_nodes) cudaFreeHost(e->h_nodes);
     if (e->fz_tw) cudaFree(e->fz_tw);
+    if (e->d_fz_err) cudaFree(e->d_fz_err);
+    if (e->h_fz_err) cudaFreeHost(e->h_fz_err);
     for (auto ev : e->evs) cudaEventDestroy(ev);
     delete e;
 }

@@ -37,11 +37,24 @@ METRIC = "E+V evals/s & time-to-ground-state at 256^3 WGC: FP32-mixed vs FP64 on
 WGC = dict(alpha=(5 + 5 ** 0.5) / 6, beta=(5 - 5 ** 0.5) / 6)
 HBM_FALLBACK = 6800.0
 
+# DRAM traffic per algorithmic byte of each kernel class, from one ncu capture of
+# the same kernels on the 256^3 grid with 16 nodes (dram__bytes_read.sum +
+# dram__bytes_write.sum over the bytes the launch must move); a launch at 64
+# nodes moves 4x the planes of that capture, so its traffic scales with them.
+TRAFFIC_SOURCE = "profiles/fused_kernels_256cube_nsp16.md (ncu, 256^3, 16 nodes, scaled by planes per launch)"
+TRAFFIC_RATIO = {
+    "fz_axis1": (2.164457 + 2.104394) / (32 * 2 * 67633152 / 1e9),
+    "lwt_nodes": (0.072036 + 1.020640) / ((16 + 1) * 67633152 / 1e9),
+    "lwt_interp": (1.149727 + 0.063654) / ((16 * 67633152 + 2 * 4 * 16777216) / 1e9),
+    "lwt_pot2": (1.083230 + 0.013175) / ((16 + 1) * 67633152 / 1e9),
+    "fz_hat": (0.134320 + 1.020322) / ((16 * 67633152 + 2 * 4 * 16777216) / 1e9),
+}
+
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=256, help="grid points per axis")
@@ -52,8 +65,8 @@ def parse():
     p.add_argument("--gs", action="store_true", help="also time the ground-state optimisation")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
-    p.add_argument("--workload", default="ev", choices=["ev", "diff"],
-                   help="ev: the E+V metric (default); diff: differentiation")
+    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch"],
+                   help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems")
     return p.parse_args()
 
 
@@ -76,7 +89,8 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []   # (arrival time, line)
+        self.window = None
 
     def start(self):
         try:
@@ -90,7 +104,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, t0, t1):
+        """Keep only the samples that arrived while [t0, t1] (host clock) ran."""
+        self.window = (t0, t1)
 
     def stop(self):
         if self.proc is None:
@@ -102,7 +120,14 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
+        lines = self.lines
+        if self.window is not None:
+            t0, t1 = self.window
+            inside = [l for t, l in lines if t0 <= t <= t1 + 0.25]
+            lines = inside if inside else [l for _, l in lines[-1:]]
+        else:
+            lines = [l for _, l in lines]
+        for l in lines:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue
@@ -240,14 +265,14 @@ def gpu_arm(args):
         tot.prepare(ev, grid, dtype)
         V = torch.empty_like(rho.as_subclass(torch.Tensor))
         calc = _lib.CALC_E | _lib.CALC_V
+        if sampler:
+            sampler.start()  # started before the warm-up so that it samples the whole timed region
         for _ in range(warmup):
             E, _ = ev.compute(rho, calc, out=V)
         lib = _lib.load()
         if profile:
             _lib.check(lib.ofdft_eval_profile(ev.h, 1))
         barrier()
-        if sampler:
-            sampler.start()
         st = torch.cuda.current_stream()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
@@ -258,7 +283,10 @@ def gpu_arm(args):
             E, _ = ev.compute(rho, calc, out=V)
         t1.record(st)
         barrier()
-        wall = time.perf_counter() - w0
+        w1 = time.perf_counter()
+        wall = w1 - w0
+        if sampler:
+            sampler.mark(w0, w1)
         clocks = sampler.stop() if sampler else None
         ms = t0.elapsed_time(t1)
         prof = None
@@ -295,8 +323,10 @@ def gpu_arm(args):
     per_launch_bytes = d["bytes"] / d["launches"]
     per_launch_ms = d["ms"] / d["launches"]
     ach = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+    ratio = TRAFFIC_RATIO.get(dom)
     out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
-                       "frac": ach / peak, "traffic": None, "peak_source": src,
+                       "frac": ach / peak, "traffic": per_launch_bytes * ratio if ratio else None,
+                       "traffic_source": TRAFFIC_SOURCE if ratio else None, "peak_source": src,
                        "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
     tot_ms = sum(v["ms"] for v in r32["prof"].values())
     out["kernels"] = {k: {"share": v["ms"] / tot_ms if tot_ms else 0.0, "ms_per_step": v["ms"] / args.steps,
@@ -312,11 +342,14 @@ def gpu_arm(args):
                                 "note": "(2*n_FFT+3)*s*N with n_FFT=198, s=4"}
     # ---- FP64 path
     if not args.no_fp64:
-        k64 = max(2, args.steps // 3)
-        r64 = run(torch.float64, k64, 1)
+        k64 = min(5, max(2, args.steps // 3))
+        r64 = run(torch.float64, k64, 1, profile=True)
         ms64 = maxrank(r64["ms_total"]) / k64
+        tot64 = sum(v["ms"] for v in r64["prof"].values())
         out["fp64"] = {"value": world * 1e3 / ms64, "unit": "evals/s", "ms_per_step": ms64, "steps": k64,
-                       "energy": r64["E"]}
+                       "energy": r64["E"],
+                       "kernels": {k: {"share": v["ms"] / tot64 if tot64 else 0.0, "ms_per_step": v["ms"] / k64}
+                                   for k, v in r64["prof"].items() if v["launches"] > 0}}
         out["fp32_vs_fp64"] = {"speedup": ms64 / ms32, "dE_per_atom": (r32["E"] - r64["E"]) / nat}
     # ---- end to end through the public API from pinned host memory
     rho_h = torch.from_numpy(rho_np.astype(np.float32)).pin_memory()
@@ -477,10 +510,69 @@ def diff_workload(args):
     print(json.dumps(out), flush=True)
 
 
+def batch_workload(args):
+    """Batching workload: 64 independent systems of uneven size (fcc/bcc/sc Al
+    cells of 4-108 atoms, a uniform in [7.3, 7.9] Bohr, displacements sigma =
+    0.1 Bohr, grids from {48, 64, 72, 80, 96}^3), TF + vW + LDA + Hartree + PME
+    local PP, each optimised from the uniform density with L-BFGS to econv =
+    1e-7 Ha/atom: FP32-mixed with the FP64 refinement, and plain FP64, one
+    system after another on one stream.  Reports systems/s of both and the
+    largest |dE| per atom between them."""
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import synthetic as syn
+    torch.cuda.set_device(0)
+    systems = syn.batch_systems(64, seed=64)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    rows = []
+    t_mix = t_64 = 0.0
+    for sd in systems:
+        lat, pos, nr = sd["lattice"], sd["positions"], sd["nr"]
+        nat = len(pos)
+        grid = D.DirectGrid(lat, nr)
+        ions = D.Ions(symbols=["Al"] * nat, positions=pos, cell=lat)
+        pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+        tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="TFVW"),
+                                XCFunctional=D.Functional(type="XC", name="LDA"),
+                                HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+        rho0 = D.DirectField(grid) + 3.0 * nat / grid.volume
+        opts = {"econv": 1e-7 * nat, "maxiter": 500, "maxfun": 50}
+        tot(rho0)  # setup outside the timed solves: plans, v_loc, Ewald
+        tot(D.DirectField(grid, data=rho0.numpy(), dtype=torch.float32))
+        res = {}
+        for mode in ("f64", "mixed"):
+            opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS", optimization_options=dict(opts))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mode == "f64":
+                opt.optimize_rho(guess_rho=rho0)
+            else:
+                opt.optimize_rho_mixed(guess_rho=rho0, econv_f32=opts["econv"])
+            torch.cuda.synchronize()
+            res[mode] = (time.perf_counter() - t0, float(opt.functional.energy), int(opt.converged))
+        t_64 += res["f64"][0]
+        t_mix += res["mixed"][0]
+        rows.append({"kind": sd["kind"], "atoms": nat, "grid": nr[0], "t_f64_s": res["f64"][0],
+                     "t_mixed_s": res["mixed"][0], "dE_per_atom": (res["mixed"][1] - res["f64"][1]) / nat,
+                     "converged": [res["f64"][2], res["mixed"][2]]})
+    out = {"workload": "batching: 64 systems (fcc/bcc/sc Al, 4-108 atoms, grids {48..96}^3), TF+vW+LDA+Hartree+PME "
+                       "PP, L-BFGS from the uniform density to econv 1e-7 Ha/atom, sequential on one stream",
+           "systems": len(rows), "mixed_systems_per_s": len(rows) / t_mix, "f64_systems_per_s": len(rows) / t_64,
+           "mixed_s": t_mix, "f64_s": t_64, "speedup": t_64 / t_mix,
+           "max_abs_dE_per_atom": max(abs(r["dE_per_atom"]) for r in rows),
+           "median_t_mixed_s": float(np.median([r["t_mixed_s"] for r in rows])),
+           "median_t_f64_s": float(np.median([r["t_f64_s"] for r in rows])),
+           "not_converged": sum(1 for r in rows if r["converged"] != [0, 0]), "systems_detail": rows}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "diff":
         diff_workload(args)
+        return
+    if args.workload == "batch":
+        batch_workload(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -14,6 +14,18 @@ def fcc_cell(a):
     return lattice, frac @ lattice
 
 
+def bcc_cell(a):
+    """Conventional cubic bcc cell: lattice (rows) and the 2 Cartesian sites."""
+    lattice = np.eye(3) * a
+    frac = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]])
+    return lattice, frac @ lattice
+
+
+def sc_cell(a):
+    """Simple cubic cell: lattice (rows) and the single site."""
+    return np.eye(3) * a, np.zeros((1, 3))
+
+
 def supercell(lattice, positions, reps):
     """Repeat a cell reps=(r0, r1, r2) times; returns (lattice, positions)."""
     reps = np.asarray(reps, dtype=np.int64)
@@ -128,3 +140,28 @@ def atomic_density(lattice, nr, positions, zvals, width=1.2, floor=0.0):
     vol = abs(np.linalg.det(lattice))
     rho *= float(np.sum(zvals)) / (rho.sum() * vol / rho.size)
     return rho
+
+
+# (cell builder, repetitions) pairs whose supercells hold 4 to 108 atoms
+_BATCH_SHAPES = [(fcc_cell, 1), (fcc_cell, 2), (fcc_cell, 3), (bcc_cell, 2), (bcc_cell, 3), (sc_cell, 2),
+                 (sc_cell, 3), (sc_cell, 4)]
+_BATCH_GRIDS = (48, 64, 72, 80, 96)
+
+
+def batch_systems(count=64, seed=64, sigma=0.1, a_range=(7.3, 7.9)):
+    """Independent systems of uneven size for batched ground states: fcc, bcc or
+    sc cells repeated to 4-108 atoms, lattice constant uniform in a_range,
+    seeded Gaussian displacements of width sigma, grids drawn from
+    {48, 64, 72, 80, 96}^3.  Returns a list of dicts (lattice, positions, nr, kind)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        build, reps = _BATCH_SHAPES[int(rng.integers(len(_BATCH_SHAPES)))]
+        a = float(rng.uniform(*a_range))
+        lat, pos = build(a)
+        lat, pos = supercell(lat, pos, (reps, reps, reps))
+        pos = pos + rng.normal(0.0, sigma, size=pos.shape)
+        n = int(_BATCH_GRIDS[int(rng.integers(len(_BATCH_GRIDS)))])
+        out.append({"lattice": lat, "positions": pos, "nr": (n, n, n),
+                    "kind": "%s %dx%dx%d" % (build.__name__.replace("_cell", ""), reps, reps, reps)})
+    return out

@@ -14,7 +14,8 @@
  * (n0, n1, n2/2+1) arrays of an R2C transform (the reference's default
  * "gfull=False" grid).  Precision OFDFT_F64 computes in float64 throughout;
  * OFDFT_F32 ("FP32-mixed") stores grids and runs FFTs and pointwise work in
- * float32 while every energy / electron-count reduction accumulates in float64.
+ * float32; energy / electron-count / dot-product sums run per thread in
+ * compensated (Kahan) float32 and across threads in float64.
  *
  * Reference interfaces each group replaces are cited as
  * path:line within Quantum-MultiScale/DFTpy.

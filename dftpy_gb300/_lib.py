@@ -93,6 +93,7 @@ _SIGS = {
     "ofdft_ewald": (_I, [_P, _I, _PD, _PD, _D, _I, _I, _PD, _PD, _PD, _P]),
     "ofdft_opt_default": (None, [C.POINTER(OptOptions)]),
     "ofdft_optimize": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P]),
+    "ofdft_optimize_v": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P, _P]),
     "ofdft_linesearch": (_I, [PHI_FN, _P, _D, _D, _D, _D, _D, _D, _D, _D, _I, _PD, _PD, _PD, _PI]),
 }
 

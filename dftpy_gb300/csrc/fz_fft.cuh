@@ -262,6 +262,115 @@ struct StockhamPP {
     }
 };
 
+// ---- twiddles held in registers
+// Every pass after the first multiplies by twiddles that depend only on the
+// thread index, so a thread can load them once and keep them for all the
+// lines it transforms.  tw_count<N, E>() is the number of such twiddles per
+// thread; pass p's twiddle (b, r) sits at its offset + b * (R - 1) + r - 1.
+template <int N, int E>
+__host__ __device__ constexpr int tw_count() {
+    int c = 0;
+    for (int ns = 1; ns < N;) {
+        const int r = (N / ns >= E) ? E : N / ns;
+        if (ns > 1) c += (E / r) * (r - 1);
+        ns *= r;
+    }
+    return c;
+}
+
+template <int N, int E, int NS, int OFF>
+struct TwFill {
+    static constexpr int T = N / E;
+    static constexpr int R = PassRadix<N, E, NS>::R;
+    static constexpr int NB = E / R;
+    static constexpr bool LAST = NS * R == N;
+    __device__ __forceinline__ static void run(float2* w, int t, const float2* __restrict__ tw) {
+        constexpr int HERE = NS > 1 ? NB * (R - 1) : 0;
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const int jm = (t + T * b) & (NS - 1);
+#pragma unroll
+                for (int r = 1; r < R; ++r) w[OFF + b * (R - 1) + r - 1] = __ldg(tw + r * jm * (N / (NS * R)));
+            }
+        }
+        if constexpr (!LAST) TwFill<N, E, NS * R, OFF + HERE>::run(w, t, tw);
+    }
+};
+
+// loads this thread's twiddles of an N-point line transform (t < N / E)
+template <int N, int E>
+__device__ __forceinline__ void tw_load(float2 (&w)[tw_count<N, E>()], int t, const float2* __restrict__ tw) {
+    TwFill<N, E, 1, 0>::run(w, t, tw);
+}
+
+// The Stockham passes with register twiddles (OFF: this pass's first twiddle)
+// and one exchange buffer (PP false: two barriers per exchange) or two used in
+// turn (PP true: one barrier per exchange, as StockhamPP).
+template <int N, int E, int S, int NS, int PASS, int OFF, bool PP, class Idx>
+struct StockhamR {
+    static constexpr int T = N / E;
+    static constexpr int R = PassRadix<N, E, NS>::R;
+    static constexpr int NB = E / R;
+    static constexpr bool LAST = NS * R == N;
+    static_assert(E % R == 0, "radix must divide the points per thread");
+
+    __device__ __forceinline__ static void run(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
+                                               const float2* w) {
+        __builtin_assume(t >= 0 && t < T);
+        constexpr int HERE = NS > 1 ? NB * (R - 1) : 0;
+        const float2* src = (PP && ((PASS - 1) & 1)) ? b1 : b0;
+        float2* dst = (PP && (PASS & 1)) ? b1 : b0;
+        if constexpr (NS > 1) {
+            __syncthreads();  // the previous pass's outputs are in src
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = src[ix(t + T * e)];
+            if constexpr (!PP && !LAST) __syncthreads();  // every input read before the buffer is overwritten
+        }
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            const int j = t + T * b;
+            const int jm = j & (NS - 1);
+            float2 u[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) u[r] = v[b + r * NB];
+            if constexpr (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    const float2 tw = w[OFF + b * (R - 1) + r - 1];
+                    u[r] = S < 0 ? cmul(u[r], tw) : cmulc(u[r], tw);
+                }
+            }
+            dft<R, S>(u);
+            if constexpr (LAST) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[b + r * NB] = u[r];
+            } else {
+                const int idxD = (j / NS) * NS * R + jm;
+#pragma unroll
+                for (int r = 0; r < R; ++r) dst[ix(idxD + r * NS)] = u[r];
+            }
+        }
+        if constexpr (!LAST) {
+            StockhamR<N, E, S, NS * R, PASS + 1, OFF + HERE, PP, Idx>::run(v, b0, b1, ix, t, w);
+        } else if constexpr (PP && (PASS & 1) == 1) {
+            __syncthreads();  // odd number of exchanges: the last reads were from buffer 0
+        }
+    }
+};
+
+// single exchange buffer `sm`, free on entry; the last pass has read it on return
+template <int N, int E, int S, class Idx>
+__device__ __forceinline__ void line_fft_r(float2 (&v)[E], float2* sm, Idx ix, int t, const float2* w) {
+    StockhamR<N, E, S, 1, 0, 0, false, Idx>::run(v, sm, sm, ix, t, w);
+}
+// two exchange buffers used in turn (entry: b0 free; exit: both free)
+template <int N, int E, int S, class Idx>
+__device__ __forceinline__ void line_fft_ppr(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
+                                             const float2* w) {
+    StockhamR<N, E, S, 1, 0, 0, true, Idx>::run(v, b0, b1, ix, t, w);
+}
+
 // ---- 1-D bulk asynchronous copies (TMA) into shared memory, completed on an
 // mbarrier.  Sources and destinations are 16-byte aligned, sizes multiples of 16.
 __device__ __forceinline__ unsigned smem_addr(const void* p) {

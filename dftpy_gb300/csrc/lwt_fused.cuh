@@ -193,6 +193,8 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
         sq[s] = sqrtf(q2);
         siq[s] = q2 > 0.0f ? 1.0f / q2 : 0.0f;
     }
+    float2 twr[fz::tw_count<N0, E>()];
+    fz::tw_load<N0, E>(twr, t, tw);
     __syncthreads();
     for (int jj = s0; jj < s1; ++jj) {
         const float ik = sik[jj], kj2 = sk2[jj];
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
             v[e] = make_float2(f * z.x, f * z.y);
         }
         __syncthreads();  // the exchange buffer is free
-        fz::line_fft<N0, E, +1>(v, sm + l, fz::ColIdx(), t, tw);
+        fz::line_fft_r<N0, E, +1>(v, sm + l, fz::ColIdx(), t, twr);
         float2* outp = XY + (long long)(plane0 + jj) * d.plane + pbase + t * pstride;
         const long long step = (long long)T * pstride;
 #pragma unroll
@@ -441,13 +443,15 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
         fz_interval_state(kk.y, a, nodes, clipdn, fi[2 * e + 1], tr[2 * e + 1]);
         acc[2 * e] = acc[2 * e + 1] = 0.0f;
     }
+    float2 twr[fz::tw_count<H, E>()];
+    fz::tw_load<H, E>(twr, t, a.tw.th);
     for (int jj = 0; jj < a.nb; ++jj) {
         const int j = a.j0 + jj;
         const int s = jj & 1;
         if (!fz::mbar_wait(&bar[s], (jj >> 1) & 1)) atomicOr(a.err, 1u);
         float2 v[E];
         fz_c2r_pre<H>(stage + s * STAGE, l, t, a.tw.tr, v);
-        fz::line_fft_pp<H, E, +1>(v, b0, b1, ix, t, a.tw.th);
+        fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, t, twr);
         // every thread has passed the transform's first barrier, so stage s is read
         if (threadIdx.x == 0 && jj + 2 < a.nb) {
             fz::fence_proxy_async();
@@ -516,6 +520,8 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
         ra[2 * e] = rr.x;
         ra[2 * e + 1] = rr.y;
     }
+    float2 twr[fz::tw_count<H, E>()];
+    fz::tw_load<H, E>(twr, t, a.tw.th);
     for (int jj = 0; jj < a.nb; ++jj) {
         const int j = a.j0 + jj;
         const float jf = (float)j;
@@ -532,7 +538,7 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
                 v[e].y = fmaf(ra[2 * e + 1], fz_small_weight(kk.y, a, nodes, clipdn, false), v[e].y);
             }
         }
-        fz::line_fft_pp<H, E, -1>(v, b0, b1, ix, t, a.tw.th);
+        fz::line_fft_ppr<H, E, -1>(v, b0, b1, ix, t, twr);
         float2* dst = a.XY + (long long)jj * a.d.plane;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -588,13 +594,15 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
     }
     const bool g0 = (t == 0 && k1 == 0 && k2 == 0);
     const float2 acc00 = acc[0];
+    float2 twr[fz::tw_count<N0, E>()];
+    fz::tw_load<N0, E>(twr, t, tw);
     for (int jj = 0; jj < nb; ++jj) {
         const float2* inp = XY + (long long)jj * d.plane + pbase;
         float2 v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = __ldcs(inp + (t + T * e) * pstride);
         __syncthreads();  // the exchange buffer is free; the node and |G| tables are staged
-        fz::line_fft<N0, E, -1>(v, sm + l, fz::ColIdx(), t, tw);
+        fz::line_fft_r<N0, E, -1>(v, sm + l, fz::ColIdx(), t, twr);
         const float ik = sik[jj], kj2 = sk2[jj];
 #pragma unroll
         for (int e = 0; e < E; ++e) {

@@ -323,9 +323,10 @@ struct Opt {
     cudaStream_t st;
     long long N;
     int eb;
-    Scratch sc;
+    // Work fields live in the grid's scratch under "opt_" names, so repeated
+    // optimisations on one grid allocate them once.
 
-    T* buf(const char* name) { return (T*)sc.get(name, g->real_bytes()); }
+    T* buf(const char* name) { return (T*)g->scratch.get(std::string("opt_") + name, g->real_bytes()); }
     double finish() {
         reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, 1, 0ull, g->d_results + 32);
         OFDFT_LAUNCH_CHECK();
@@ -369,7 +370,8 @@ struct Opt {
 };
 
 template <typename T>
-void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_result& res, cudaStream_t st) {
+void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_result& res, T* v_out,
+                cudaStream_t st) {
     Opt<T> op;
     op.e = e;
     op.g = e_grid(e);
@@ -418,7 +420,7 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
     int pool_i = 0;
     auto lb_buf = [&]() {
         std::string nm = "lb" + std::to_string(pool_i++);
-        return (T*)op.sc.get(nm, g->real_bytes());
+        return op.buf(nm.c_str());
     };
     // TN work
     T* dvec = (o.method == OFDFT_OPT_TN) ? op.buf("tn_d") : nullptr;
@@ -595,9 +597,10 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
         op.copy(dir_prev, p);
         have_dir_prev = true;
     }
-    // rho_io <- phi^2
+    // rho_io <- phi^2; the potential of the last accepted evaluation is that of rho_io
     k_square<T><<<op.eb, 256, 0, st>>>(N, phi, rho_io);
     OFDFT_LAUNCH_CHECK();
+    if (v_out) OFDFT_CK(cudaMemcpyAsync(v_out, V, g->real_bytes(), cudaMemcpyDeviceToDevice, st));
     OFDFT_CK(cudaStreamSynchronize(st));
     res.converged = converged;
     res.niter = it;
@@ -628,16 +631,21 @@ void ofdft_opt_default(ofdft_opt_options* o) {
     o->verbose = 0;
 }
 
-int ofdft_optimize(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, ofdft_stream s) {
+int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, void* v_out,
+                     ofdft_stream s) {
     return guard([&] {
         OFDFT_REQUIRE(e && rho && o && r, "ofdft_optimize: null argument");
         OFDFT_REQUIRE(o->method >= 0 && o->method <= 2, "ofdft_optimize: unknown method");
         OFDFT_REQUIRE(o->maxiter >= 1 && o->maxfun >= 1 && o->ncheck >= 1, "ofdft_optimize: bad limits");
         memset(r, 0, sizeof(*r));
         ofdft_grid* g = e_grid(e);
-        if (g->prec == OFDFT_F64) optimize_t<double>(e, (double*)rho, *o, *r, (cudaStream_t)s);
-        else optimize_t<float>(e, (float*)rho, *o, *r, (cudaStream_t)s);
+        if (g->prec == OFDFT_F64) optimize_t<double>(e, (double*)rho, *o, *r, (double*)v_out, (cudaStream_t)s);
+        else optimize_t<float>(e, (float*)rho, *o, *r, (float*)v_out, (cudaStream_t)s);
     });
+}
+
+int ofdft_optimize(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, ofdft_stream s) {
+    return ofdft_optimize_v(e, rho, o, r, nullptr, s);
 }
 
 int ofdft_linesearch(ofdft_phi_fn fn, void* ctx, double f0, double g0, double stp0, double c1, double c2, double amax,

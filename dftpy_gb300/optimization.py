@@ -14,6 +14,7 @@ import torch
 from . import _lib
 from .field import DirectField, as_field
 from .functional.abstract_functional import NativeFunctional, stream_ptr
+from .functional.functional_output import FunctionalOutput
 from .functional.total_functional import TotalFunctional
 
 __all__ = ["Optimization"]
@@ -88,8 +89,9 @@ class Optimization:
         res = _lib.OptResult()
         opts = self.options_struct()
         t = rho.as_subclass(torch.Tensor)
-        _lib.check(_lib.load().ofdft_optimize(ev.h, _lib.C.c_void_p(t.data_ptr()), _lib.C.byref(opts),
-                                              _lib.C.byref(res), stream_ptr()))
+        V = torch.empty_like(t)
+        _lib.check(_lib.load().ofdft_optimize_v(ev.h, _lib.C.c_void_p(t.data_ptr()), _lib.C.byref(opts),
+                                                _lib.C.byref(res), _lib.C.c_void_p(V.data_ptr()), stream_ptr()))
         total.finish(ev)
         rho._N = None
         self.result = res
@@ -97,19 +99,28 @@ class Optimization:
         self.mu = res.mu
         self.rho = rho
         self.phi = torch.sqrt(rho)
-        self.functional = total(rho, calcType={"E", "V"})
+        # the last accepted evaluation (optimization.py:517-523): no further evaluation
+        v = V.as_subclass(DirectField)
+        v.grid = grid
+        v._N = None
+        self.functional = FunctionalOutput(name="TOTAL", energy=float(res.energy), potential=v)
         return rho
 
     def optimize_rho_mixed(self, guess_rho=None, econv_f32=None, f32_method=None, refine_method=None,
-                           refine_maxiter=None):
+                           refine_maxiter=None, refine="optimize"):
         """FP32-mixed ground state with a final FP64 refinement.
 
         Stage 1 optimises in FP32-mixed (float32 fields and FFTs, float64
         reductions) until the energy changes by less than ``econv_f32``
         (default 10x the FP64 econv) or the line search can make no progress.
-        Stage 2 continues in FP64 from that density with the FP64 econv, so the
-        converged energy and density are those of the FP64 functional.
+        Stage 2, ``refine="optimize"``: continues in FP64 from that density with
+        the FP64 econv, so the converged energy and density are those of the
+        FP64 functional.  ``refine="evaluate"``: one FP64 E+V evaluation of the
+        stage-1 density (electron count restored in float64), whose energy and
+        potential become the result.
         Returns the FP64 density; ``self.stages`` records both stages."""
+        if refine not in ("optimize", "evaluate"):
+            raise ValueError("refine must be 'optimize' or 'evaluate'")
         if guess_rho is not None:
             self.rho = guess_rho
         o = dict(self.optimization_options)
@@ -133,6 +144,21 @@ class Optimization:
         n_target = DirectField(rho32.grid, data=guess, dtype=torch.float64).integral()
         rho_start = rho32.as_subclass(torch.Tensor).double()
         n32 = DirectField(rho32.grid, data=rho_start).integral()
+        if refine == "evaluate":
+            rho = DirectField(rho32.grid, data=rho_start * (n_target / n32))
+            total = self._total()
+            func = total(rho, calcType={"E", "V"})
+            res = opt32.result
+            stages.append({"precision": "f64", "method": "evaluate", "niter": 0, "nfev": 1,
+                           "converged": opt32.converged, "energy": func.energy})
+            self.stages = stages
+            self.result = res
+            self.converged = opt32.converged
+            self.mu = float((func.potential * rho).integral() / rho.integral())
+            self.rho = rho
+            self.phi = torch.sqrt(rho)
+            self.functional = func
+            return rho
         rho = opt64.optimize_rho(guess_rho=rho_start * (n_target / n32), dtype=torch.float64)
         stages.append({"precision": "f64", "method": opt64.optimization_method, "niter": opt64.result.niter,
                        "nfev": opt64.result.nfev, "converged": opt64.converged, "energy": opt64.result.energy})

@@ -206,6 +206,12 @@ typedef struct {
 void ofdft_opt_default(ofdft_opt_options* o);
 int ofdft_optimize(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r,
                    ofdft_stream s);
+/* The same, also writing the potential of the returned density (the one of the
+ * last accepted evaluation, the reference's `self.functional`,
+ * optimization.py:517-523) to v_out (device, grid precision; may be NULL), so
+ * the caller needs no further evaluation. */
+int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, void* v_out,
+                     ofdft_stream s);
 
 /* The scalar MINPACK-2 line search on a host callback, exposed for testing
  * against scipy.optimize line_search_wolfe1 (scalar_search_wolfe1). */

@@ -183,6 +183,10 @@ def test_optimizer_ground_state(golden, method):
     rho = opt.optimize_rho(guess_rho=rho0)
     tag = "C_" + method.replace("-", "") + "_"
     assert opt.converged == 0
+    # the optimiser hands back the energy and potential of its last accepted evaluation
+    chk = tot(rho)
+    e_close(opt.functional.energy, chk.energy, scale=4.0)
+    v_close(opt.functional.potential, chk.potential.numpy(), atol=1e-12)
     e_close(tot.Energy(rho), float(golden[tag + "E"]), scale=4.0)
     assert abs(opt.mu - float(golden[tag + "mu"])) < 1e-6 * abs(float(golden[tag + "mu"]))
     assert abs(rho.integral() - 12.0) < 1e-10

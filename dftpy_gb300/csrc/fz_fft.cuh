@@ -190,21 +190,28 @@ __device__ __forceinline__ void line_fft(float2 (&v)[E], float2* sm, Idx ix, int
     Stockham<N, E, S, 1, Idx>::run(v, sm, ix, t, tw);
 }
 
-// Row placement for lines of 128 or more elements: an XOR swizzle inside each
-// group of 16 slots.  The loads of every pass (16 consecutive elements per
-// half-warp) and the stores of the radix-8 passes then fall in distinct
-// banks, with no padding.
-struct RowSwz {
-    __device__ __forceinline__ int operator()(int n) const { return n ^ ((n >> 3) & 15); }
-};
-// Row placement for shorter lines: one pad slot per 16 elements.
+// Row placement: one pad slot per 16 elements.  With 8 points per thread the
+// loads of every pass (16 consecutive elements per half-warp) and the stores
+// of the first radix-8 pass fall in distinct banks; the second radix-8 pass of
+// a 128-point row stores with a two-way conflict.  The offsets fold to
+// immediates (thread t < 16 holds elements t + 16e), where an XOR swizzle
+// free of conflicts costs integer instructions on every access.
 struct RowPad16 {
     __device__ __forceinline__ int operator()(int n) const { return n + (n >> 4); }
 };
+// Second exchange buffer of the ping-pong row transforms: 8 pad slots per 64
+// elements.  The second radix-8 pass stores elements n and n + 64 from
+// threads t and t + 8; this places them 8 banks apart, so that store and the
+// following loads are free of conflicts for 128- and 256-point rows.
+struct RowPad8of64 {
+    __device__ __forceinline__ int operator()(int n) const { return n + 8 * (n >> 6); }
+};
 template <int N>
 struct RowLayout {
-    using Idx = typename std::conditional<(N >= 128), RowSwz, RowPad16>::type;
-    static constexpr int slots = N >= 128 ? N : N + (N >> 4) + 1;
+    using Idx = RowPad16;       // exchange buffer 0
+    using Idx1 = RowPad8of64;   // exchange buffer 1
+    static constexpr int slots = N + (N >> 4) + 1;
+    static constexpr int slots1 = N + 8 * (N >> 6) + 1;
 };
 
 // The Stockham passes with two exchange buffers used in turn: pass p stores
@@ -307,7 +314,7 @@ __device__ __forceinline__ void tw_load(float2 (&w)[tw_count<N, E>()], int t, co
 // The Stockham passes with register twiddles (OFF: this pass's first twiddle)
 // and one exchange buffer (PP false: two barriers per exchange) or two used in
 // turn (PP true: one barrier per exchange, as StockhamPP).
-template <int N, int E, int S, int NS, int PASS, int OFF, bool PP, class Idx>
+template <int N, int E, int S, int NS, int PASS, int OFF, bool PP, class Idx, class Idx1 = Idx>
 struct StockhamR {
     static constexpr int T = N / E;
     static constexpr int R = PassRadix<N, E, NS>::R;
@@ -315,16 +322,25 @@ struct StockhamR {
     static constexpr bool LAST = NS * R == N;
     static_assert(E % R == 0, "radix must divide the points per thread");
 
+    // element n of buffer 1 sits at ix1(n) (PP only; buffer 0 uses ix)
+    template <int B>
+    __device__ __forceinline__ static int at(Idx ix, Idx1 ix1, int n) {
+        if constexpr (B == 1) return ix1(n);
+        else return ix(n);
+    }
+
     __device__ __forceinline__ static void run(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
-                                               const float2* w) {
+                                               const float2* w, Idx1 ix1 = Idx1()) {
         __builtin_assume(t >= 0 && t < T);
         constexpr int HERE = NS > 1 ? NB * (R - 1) : 0;
-        const float2* src = (PP && ((PASS - 1) & 1)) ? b1 : b0;
-        float2* dst = (PP && (PASS & 1)) ? b1 : b0;
+        constexpr int SB = PP ? ((PASS - 1) & 1) : 0;  // buffer this pass reads
+        constexpr int DB = PP ? (PASS & 1) : 0;        // buffer this pass writes
+        const float2* src = SB ? b1 : b0;
+        float2* dst = DB ? b1 : b0;
         if constexpr (NS > 1) {
             __syncthreads();  // the previous pass's outputs are in src
 #pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = src[ix(t + T * e)];
+            for (int e = 0; e < E; ++e) v[e] = src[at<SB>(ix, ix1, t + T * e)];
             if constexpr (!PP && !LAST) __syncthreads();  // every input read before the buffer is overwritten
         }
 #pragma unroll
@@ -348,11 +364,11 @@ struct StockhamR {
             } else {
                 const int idxD = (j / NS) * NS * R + jm;
 #pragma unroll
-                for (int r = 0; r < R; ++r) dst[ix(idxD + r * NS)] = u[r];
+                for (int r = 0; r < R; ++r) dst[at<DB>(ix, ix1, idxD + r * NS)] = u[r];
             }
         }
         if constexpr (!LAST) {
-            StockhamR<N, E, S, NS * R, PASS + 1, OFF + HERE, PP, Idx>::run(v, b0, b1, ix, t, w);
+            StockhamR<N, E, S, NS * R, PASS + 1, OFF + HERE, PP, Idx, Idx1>::run(v, b0, b1, ix, t, w, ix1);
         } else if constexpr (PP && (PASS & 1) == 1) {
             __syncthreads();  // odd number of exchanges: the last reads were from buffer 0
         }
@@ -364,11 +380,12 @@ template <int N, int E, int S, class Idx>
 __device__ __forceinline__ void line_fft_r(float2 (&v)[E], float2* sm, Idx ix, int t, const float2* w) {
     StockhamR<N, E, S, 1, 0, 0, false, Idx>::run(v, sm, sm, ix, t, w);
 }
-// two exchange buffers used in turn (entry: b0 free; exit: both free)
-template <int N, int E, int S, class Idx>
-__device__ __forceinline__ void line_fft_ppr(float2 (&v)[E], float2* b0, float2* b1, Idx ix, int t,
+// two exchange buffers used in turn (entry: b0 free; exit: both free), laid out
+// by ix and ix1
+template <int N, int E, int S, class Idx, class Idx1>
+__device__ __forceinline__ void line_fft_ppr(float2 (&v)[E], float2* b0, float2* b1, Idx ix, Idx1 ix1, int t,
                                              const float2* w) {
-    StockhamR<N, E, S, 1, 0, 0, true, Idx>::run(v, b0, b1, ix, t, w);
+    StockhamR<N, E, S, 1, 0, 0, true, Idx, Idx1>::run(v, b0, b1, ix, t, w, ix1);
 }
 
 // ---- 1-D bulk asynchronous copies (TMA) into shared memory, completed on an

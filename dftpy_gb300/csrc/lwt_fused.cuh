@@ -96,10 +96,10 @@ __device__ __forceinline__ float fz_spline(const float* c, int nint, float step,
 
 // K_j(|G|) (DERIV false) or -eta K_j'(eta) (DERIV true) at eta = q/k_j: the
 // table limit at and above etamax, the series at and above eta_series
-// (u = eta^-2 = k_j^2/q^2), the spline below.  The series and the limit are
-// selected without branching; only the spline (points near G = 0) branches.
-// G = 0 is handled by the callers.
-template <bool DERIV>
+// (u = eta^-2 = k_j^2/q^2), the spline below (NEAR only: callers pass
+// NEAR = false when no point of the warp can have eta < eta_series, so that
+// warp runs no spline instructions at all).  G = 0 is handled by the callers.
+template <bool DERIV, bool NEAR>
 __device__ __forceinline__ float fz_node_kernel(const FzTab& tb, float q, float ik, float iq2, float kj2) {
     const float eta = q * ik;
     const float u = iq2 * kj2;
@@ -117,8 +117,15 @@ __device__ __forceinline__ float fz_node_kernel(const FzTab& tb, float q, float 
         r = tb.factor * fmaf(f, u, tb.kconst);
         r = eta >= tb.etamax ? tb.limit : r;
     }
-    if (eta < tb.eta_series) r = fz_spline(DERIV ? tb.cd : tb.c, tb.nint, tb.step, tb.inv_step, eta);
+    if constexpr (NEAR) {
+        if (eta < tb.eta_series) r = fz_spline(DERIV ? tb.cd : tb.c, tb.nint, tb.step, tb.inv_step, eta);
+    }
     return r;
+}
+
+// Smallest |G| over the 32 lanes' points (|G| >= 0, so its bits order as unsigned).
+__device__ __forceinline__ float fz_warp_min(float x) {
+    return __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(x)));
 }
 
 // Column tile of the axis-0 passes: main tiles (k1, 16 consecutive k2 < H) then
@@ -196,17 +203,26 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
     float2 twr[fz::tw_count<N0, E>()];
     fz::tw_load<N0, E>(twr, t, tw);
     __syncthreads();
+    float qmin = INFINITY;
+#pragma unroll
+    for (int e = 0; e < E; ++e) qmin = fminf(qmin, sq[(t + T * e) * L + l]);
+    qmin = fz_warp_min(qmin);
     for (int jj = s0; jj < s1; ++jj) {
         const float ik = sik[jj], kj2 = sk2[jj];
         float2 v[E];
+        auto scale = [&](auto near) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int s = (t + T * e) * L + l;
-            const float kv = fz_node_kernel<DERIV>(tb, sq[s], ik, siq[s], kj2);
-            const float f = DERIV ? kv * ik : kv;
-            const float2 z = sz[s];
-            v[e] = make_float2(f * z.x, f * z.y);
-        }
+            for (int e = 0; e < E; ++e) {
+                const int s = (t + T * e) * L + l;
+                const float kv = fz_node_kernel<DERIV, decltype(near)::value>(tb, sq[s], ik, siq[s], kj2);
+                const float f = DERIV ? kv * ik : kv;
+                const float2 z = sz[s];
+                v[e] = make_float2(f * z.x, f * z.y);
+            }
+        };
+        // warp-uniform: does any point of this warp need the spline for node j?
+        if (qmin * ik < tb.eta_series) scale(std::true_type());
+        else scale(std::false_type());
         __syncthreads();  // the exchange buffer is free
         fz::line_fft_r<N0, E, +1>(v, sm + l, fz::ColIdx(), t, twr);
         float2* outp = XY + (long long)(plane0 + jj) * d.plane + pbase + t * pstride;
@@ -388,8 +404,8 @@ __device__ __forceinline__ void fz_c2r_pre(const float2* st, int l, int t, const
 // shared memory of k_fz_c2r_rows (with_stages) and k_fz_r2c_rows
 inline size_t fz_row_smem(int H, int m, bool with_stages) {
     const int T = H / kFzRowE, ROWS = kFzRowThreads / T;
-    const size_t slots = H >= 128 ? H : H + (H >> 4) + 1;
-    size_t b = 16 + 2 * (size_t)ROWS * slots * sizeof(float2) + (size_t)5 * m * sizeof(float);
+    const size_t slots = (H + (H >> 4) + 1) + (H + 8 * (H >> 6) + 1);
+    size_t b = 16 + (size_t)ROWS * slots * sizeof(float2) + (size_t)5 * m * sizeof(float);
     if (with_stages) b += 2 * (size_t)(ROWS * H + ROWS) * sizeof(float2);
     return b;
 }
@@ -409,7 +425,7 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
     float2* stage = reinterpret_cast<float2*>(fz_rsm4 + 1);
     float2* buf0 = stage + 2 * STAGE;
     float2* buf1 = buf0 + ROWS * Lay::slots;
-    float* fs = reinterpret_cast<float*>(buf1 + ROWS * Lay::slots);
+    float* fs = reinterpret_cast<float*>(buf1 + ROWS * Lay::slots1);
     const long long row0 = (long long)blockIdx.x * ROWS;
     auto issue = [&](int jj) {  // one thread: plane jj into stage jj & 1
         const int s = jj & 1;
@@ -431,8 +447,9 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
     const long long row = row0 + l;
     const int n2 = 2 * H;
     float2* b0 = buf0 + l * Lay::slots;
-    float2* b1 = buf1 + l * Lay::slots;
+    float2* b1 = buf1 + l * Lay::slots1;
     const typename Lay::Idx ix;
+    const typename Lay::Idx1 ix1;
     const float clipdn = __double2float_rd(a.kfclip);
     const float2* kfrow = reinterpret_cast<const float2*>(a.kf + row * n2) + t;
     float fi[P], tr[P], acc[P];
@@ -451,7 +468,7 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
         if (!fz::mbar_wait(&bar[s], (jj >> 1) & 1)) atomicOr(a.err, 1u);
         float2 v[E];
         fz_c2r_pre<H>(stage + s * STAGE, l, t, a.tw.tr, v);
-        fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, t, twr);
+        fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, ix1, t, twr);
         // every thread has passed the transform's first barrier, so stage s is read
         if (threadIdx.x == 0 && jj + 2 < a.nb) {
             fz::fence_proxy_async();
@@ -496,15 +513,16 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
     extern __shared__ float4 fz_rsm4[];
     float2* buf0 = reinterpret_cast<float2*>(fz_rsm4 + 1);
     float2* buf1 = buf0 + ROWS * Lay::slots;
-    float* fs = reinterpret_cast<float*>(buf1 + ROWS * Lay::slots);
+    float* fs = reinterpret_cast<float*>(buf1 + ROWS * Lay::slots1);
     const FzNodeSm nodes = fz_stage_nodes(a, fs);
     __syncthreads();
     const int t = threadIdx.x % T, l = threadIdx.x / T;
     const long long row = (long long)blockIdx.x * ROWS + l;
     const int n2 = 2 * H;
     float2* b0 = buf0 + l * Lay::slots;
-    float2* b1 = buf1 + l * Lay::slots;
+    float2* b1 = buf1 + l * Lay::slots1;
     const typename Lay::Idx ix;
+    const typename Lay::Idx1 ix1;
     const float clipdn = __double2float_rd(a.kfclip);
     const int lane = threadIdx.x & 31;
     const int partner = (lane & ~(T - 1)) | ((T - t) & (T - 1));
@@ -538,7 +556,7 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
                 v[e].y = fmaf(ra[2 * e + 1], fz_small_weight(kk.y, a, nodes, clipdn, false), v[e].y);
             }
         }
-        fz::line_fft_ppr<H, E, -1>(v, b0, b1, ix, t, twr);
+        fz::line_fft_ppr<H, E, -1>(v, b0, b1, ix, ix1, t, twr);
         float2* dst = a.XY + (long long)jj * a.d.plane;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -596,6 +614,13 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
     const float2 acc00 = acc[0];
     float2 twr[fz::tw_count<N0, E>()];
     fz::tw_load<N0, E>(twr, t, tw);
+    float qmin = INFINITY;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int k0 = t + T * e;
+        qmin = fminf(qmin, sqrtf(gsq_f(geo, k0, k1, k2)));
+    }
+    qmin = fz_warp_min(qmin);
     for (int jj = 0; jj < nb; ++jj) {
         const float2* inp = XY + (long long)jj * d.plane + pbase;
         float2 v[E];
@@ -604,12 +629,21 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
         __syncthreads();  // the exchange buffer is free; the node and |G| tables are staged
         fz::line_fft_r<N0, E, -1>(v, sm + l, fz::ColIdx(), t, twr);
         const float ik = sik[jj], kj2 = sk2[jj];
+        float f[E];
+        auto factors = [&](auto near) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int s = (t + T * e) * L + l;
+                f[e] = fz_node_kernel<false, decltype(near)::value>(tb, sq[s], ik, siq[s], kj2) * invN;
+            }
+        };
+        // warp-uniform: does any point of this warp need the spline for node j?
+        if (qmin * ik < tb.eta_series) factors(std::true_type());
+        else factors(std::false_type());
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            const int s = (t + T * e) * L + l;
-            const float f = fz_node_kernel<false>(tb, sq[s], ik, siq[s], kj2) * invN;
-            acc[e].x = fmaf(f, v[e].x, acc[e].x);
-            acc[e].y = fmaf(f, v[e].y, acc[e].y);
+            acc[e].x = fmaf(f[e], v[e].x, acc[e].x);
+            acc[e].y = fmaf(f[e], v[e].y, acc[e].y);
         }
     }
     if (g0) acc[0] = acc00;

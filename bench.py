@@ -68,8 +68,9 @@ def parse():
     p.add_argument("--no-gs", action="store_true", help="skip the ground-state timing")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
-    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch"],
-                   help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems")
+    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2"],
+                   help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems; "
+                        "c2: 256 atoms at 128^3, FP64 against the CPU restatement")
     return p.parse_args()
 
 
@@ -591,6 +592,91 @@ def batch_workload(args):
     print(json.dumps(out), flush=True)
 
 
+def c2_workload(args):
+    """Scaled-up plain method: fcc Al 4x4x4 (256 atoms, a = 7.60 Bohr, seeded
+    displacements sigma = 0.10 Bohr), 128^3 grid, KEDF WT (TF + vW + WT,
+    alpha = beta = 5/6) + LDA + Hartree + PME local PP, FP64.  GPU: E+V evals/s
+    (rho resident, CUDA events), L-BFGS time to the ground state from the
+    uniform density (econv 1e-7 Ha/atom), PME Ewald energy+forces.  CPU (the
+    numpy restatement of the reference on this host, same inputs): one E+V, the
+    Ewald forces, and the ground state extrapolated from the GPU run's
+    evaluation count."""
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import _lib
+    from dftpy_gb300 import synthetic as syn
+    from oracle import ofdft_np as O
+    torch.cuda.set_device(0)
+    n = 128
+    lat, pos = syn.fcc_supercell(7.60, 4, sigma=0.10, seed=256)
+    nat = len(pos)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    rho_np = syn.atomic_density(lat, (n, n, n), pos, [3.0] * nat, width=1.4, floor=0.002)
+    grid = D.DirectGrid(lat, (n, n, n))
+    ions = D.Ions(symbols=["Al"] * nat, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    rho = D.DirectField(grid, data=rho_np)
+    ev = tot.evaluator(grid, torch.float64)
+    tot.prepare(ev, grid, torch.float64)
+    V = torch.empty_like(rho.as_subclass(torch.Tensor))
+    calc = _lib.CALC_E | _lib.CALC_V
+    for _ in range(max(3, args.warmup)):
+        E, _ = ev.compute(rho, calc, out=V)
+    steps = max(10, args.steps)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(steps):
+        E, _ = ev.compute(rho, calc, out=V)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms_ev = e0.elapsed_time(e1) / steps
+    e_gpu = float(E[_lib.E_TOTAL])
+    # ground state
+    rho0 = D.DirectField(grid) + 3.0 * nat / grid.volume
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
+                         optimization_options={"econv": 1e-7 * nat, "maxiter": 500, "maxfun": 50})
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    opt.optimize_rho(guess_rho=rho0)
+    torch.cuda.synchronize()
+    t_gs = time.perf_counter() - t0
+    # PME Ewald energy and forces (a fresh object per call: nothing cached)
+    t0 = time.perf_counter()
+    ew = D.ewald(ions=ions, grid=grid, PME=True)
+    F_gpu = ew.forces
+    t_ew = time.perf_counter() - t0
+    # CPU: the numpy restatement on this host
+    O.set_fft_workers(os.cpu_count() or 1)
+    g = O.Grid(lat, (n, n, n))
+    opp = O.LocalPseudo(g, pos, np.zeros(nat, dtype=int), [(gp, vp)], PME=True)
+    opp.vreal
+    wt = O.WT()
+    t0 = time.perf_counter()
+    e_cpu = 0.0
+    for f in (O.tf, O.vw, O.lda, O.hartree):
+        e_cpu += f(rho_np, g)["E"]
+    e_cpu += wt(rho_np, g)["E"] + opp(rho_np)["E"]
+    t_cpu_ev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    F_cpu = O.Ewald(g, pos, np.full(nat, 3.0), PME=True).forces()
+    t_cpu_ew = time.perf_counter() - t0
+    out = {"workload": "c2: fcc Al 4x4x4 (256 atoms), 128^3, WT+LDA+Hartree+PME PP, FP64",
+           "gpu": {"ev_per_s": 1e3 / ms_ev, "ms_per_ev": ms_ev, "ground_state_s": t_gs, "gs_niter": opt.result.niter,
+                   "gs_nfev": opt.result.nfev, "ewald_forces_s": t_ew},
+           "cpu": {"cores": os.cpu_count(), "kind": "port", "ev_s": t_cpu_ev, "ev_per_s": 1.0 / t_cpu_ev,
+                   "ewald_forces_s": t_cpu_ew, "ground_state_s_extrapolated": opt.result.nfev * t_cpu_ev},
+           "speedup": {"ev": t_cpu_ev * 1e3 / ms_ev, "ground_state": opt.result.nfev * t_cpu_ev / t_gs,
+                       "ewald_forces": t_cpu_ew / t_ew},
+           "parity": {"E_total_gpu_minus_cpu_Ha_excl_ewald": (e_gpu - float(E[_lib.E_II])) - e_cpu,
+                      "ewald_forces_max_abs": float(np.abs(F_gpu - F_cpu).max())}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "diff":
@@ -598,6 +684,9 @@ def main():
         return
     if args.workload == "batch":
         batch_workload(args)
+        return
+    if args.workload == "c2":
+        c2_workload(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -200,7 +200,7 @@ int ofdft_grid_create(const int nr[3], const double lattice[9], int precision, o
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         g->sms = sms > 0 ? sms : 152;
-        g->red_blocks = g->sms * 4;
+        g->red_blocks = g->sms * 8;  // 8 blocks of 256 threads per SM: enough loads in flight
         try {
             OFDFT_CK(cudaMalloc(&g->d_partials, (size_t)g->red_blocks * 32 * sizeof(double)));
             OFDFT_CK(cudaMalloc(&g->d_results, 64 * sizeof(double)));

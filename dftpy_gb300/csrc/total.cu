@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
             P6 = pz<M>(6);
     const M tiny = (M)1e-30, zero_clamp = (M)kZERO;
     const long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 2
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
         const M r = a.rho[i];
         M v = (M)0;
@@ -627,6 +628,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
     const M alpha = (M)a.alpha, beta = (M)a.beta, vw_y = (M)a.vw_y, ld = (M)a.ld, rhomax = (M)a.rhomax;
     const M kfclip = (M)a.kfclip, tiny = (M)1e-30, zero_clamp = (M)kZERO;
     const long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 2
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
         const M r = a.rho[i];
         M v = a.wantV ? a.V[i] : (M)0;

@@ -94,6 +94,8 @@ _SIGS = {
     "ofdft_opt_default": (None, [C.POINTER(OptOptions)]),
     "ofdft_optimize": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P]),
     "ofdft_optimize_v": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P, _P]),
+    "ofdft_optimize_batch": (_I, [_I, C.POINTER(_P), C.POINTER(_P), C.POINTER(OptOptions), C.POINTER(C.c_double),
+                                  C.POINTER(OptResult), C.POINTER(_P), _P]),
     "ofdft_linesearch": (_I, [PHI_FN, _P, _D, _D, _D, _D, _D, _D, _D, _D, _I, _PD, _PD, _PD, _PI]),
 }
 

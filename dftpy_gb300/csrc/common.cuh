@@ -213,6 +213,32 @@ __device__ inline void block_sum_store(double (&v)[NS], double* partials) {
     }
 }
 
+// The same block sum, stored at partials[slot * NS + s] (a block of a batched
+// launch stores at its position in the launch).
+template <int NS>
+__device__ inline void block_sum_store_at(double (&v)[NS], double* partials, long long slot) {
+    __shared__ double sh[NS][RED_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        double x = v[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[s][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int nw = blockDim.x / 32;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            double x = (lane < nw) ? sh[s][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) partials[slot * NS + s] = x;
+        }
+    }
+}
+
 // min/max helpers: kind 0 = sum, 1 = min, 2 = max
 __device__ inline double red_op(double a, double b, int kind) {
     return kind == 0 ? a + b : (kind == 1 ? fmin(a, b) : fmax(a, b));

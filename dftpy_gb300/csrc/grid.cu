@@ -2,6 +2,8 @@
 // float64 field reductions of the C ABI.
 #include "common.cuh"
 
+#include <algorithm>
+
 #include <cstring>
 #include <mutex>
 
@@ -200,7 +202,9 @@ int ofdft_grid_create(const int nr[3], const double lattice[9], int precision, o
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         g->sms = sms > 0 ? sms : 152;
-        g->red_blocks = g->sms * 8;  // 8 blocks of 256 threads per SM: enough loads in flight
+        // field reductions: up to 8 blocks of 256 threads per SM, fewer on small grids
+        // (about 16 points per thread), where block scheduling would dominate
+        g->red_blocks = (int)std::max(8LL, std::min((long long)g->sms * 8, (N + 4095) / 4096));
         try {
             OFDFT_CK(cudaMalloc(&g->d_partials, (size_t)g->red_blocks * 32 * sizeof(double)));
             OFDFT_CK(cudaMalloc(&g->d_results, 64 * sizeof(double)));

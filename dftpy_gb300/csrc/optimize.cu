@@ -7,6 +7,7 @@
 #include "common.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <deque>
 #include <vector>
@@ -224,16 +225,40 @@ struct RunSum<float> {
     __device__ double get() const { return (double)s - (double)c; }
 };
 
+// Rounded operations spelled out (no contraction left to the compiler), so that
+// the single-system and the batched kernels give the same bits.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// b0 x0 + b1 x1 + b2 x2 (absent terms skipped)
+template <typename T>
+__device__ __forceinline__ T lin3(T b0, const T* x0, T b1, const T* x1, T b2, const T* x2, long long i) {
+    T v = mul_rn(b0, x0[i]);
+    if (x1) v = fma_rn(b1, x1[i], v);
+    if (x2) v = fma_rn(b2, x2[i], v);
+    return v;
+}
+// phi cos + p sin
+template <typename T>
+__device__ __forceinline__ T rot(T phi, T p, T c, T s) {
+    return fma_rn(phi, c, mul_rn(p, s));
+}
+// V nphi (p cos - phi sin)
+template <typename T>
+__device__ __forceinline__ T dth_term(T V, T nphi, T p, T phi, T c, T s) {
+    return mul_rn(mul_rn(V, nphi), fma_rn(p, c, -mul_rn(phi, s)));
+}
+
 template <typename T>
 __global__ void k_lincomb(long long n, T* out, double a0, const T* x0, double a1, const T* x1, double a2,
                           const T* x2) {
     const T b0 = (T)a0, b1 = (T)a1, b2 = (T)a2;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        T v = b0 * x0[i];
-        if (x1) v += b1 * x1[i];
-        if (x2) v += b2 * x2[i];
-        out[i] = v;
-    }
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = lin3(b0, x0, b1, x1, b2, x2, i);
 }
 
 // sqrt(rho), 1e-300 where rho <= 0 (0 in float32, where 1e-300 underflows)
@@ -257,7 +282,7 @@ template <typename T>
 __global__ void k_square(long long n, const T* x, T* out) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const T v = x[i];
-        out[i] = v * v;
+        out[i] = mul_rn(v, v);
     }
 }
 
@@ -266,9 +291,9 @@ template <typename T>
 __global__ void k_rotate(long long n, const T* phi, const T* p, double c, double s, T* newphi, T* rho) {
     const T cw = (T)c, sw = (T)s;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const T v = phi[i] * cw + p[i] * sw;
+        const T v = rot(phi[i], p[i], cw, sw);
         newphi[i] = v;
-        rho[i] = v * v;
+        rho[i] = mul_rn(v, v);
     }
 }
 
@@ -277,7 +302,7 @@ template <typename T>
 __global__ void k_resid(long long n, const T* V, double mu, const T* phi, T* out) {
     const T m = (T)mu;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = (V[i] - m) * phi[i];
+        out[i] = mul_rn(sub_rn(V[i], m), phi[i]);
 }
 
 // Ap = ((V1 - mu) phi1 - res0) / eps
@@ -295,7 +320,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_dtheta(long long n, const T* V,
     const T cw = (T)c, sw = (T)s;
     RunSum<T> sum;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        sum.add(V[i] * nphi[i] * (p[i] * cw - phi[i] * sw));
+        sum.add(dth_term(V[i], nphi[i], p[i], phi[i], cw, sw));
     double acc[1] = {sum.get()};
     block_sum_store<1>(acc, partials);
 }
@@ -304,7 +329,7 @@ template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_dot2(long long n, const T* a, const T* b, double* partials) {
     RunSum<T> sum;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        sum.add(a[i] * b[i]);
+        sum.add(mul_rn(a[i], b[i]));
     double acc[1] = {sum.get()};
     block_sum_store<1>(acc, partials);
 }
@@ -313,6 +338,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot2(long long n, const T* a, c
 
 // grid of an evaluator (the evaluator struct lives in total.cu)
 ofdft_grid* e_grid(ofdft_eval* e);
+// an evaluation enqueued without waiting, and its energies after a synchronisation (total.cu)
+void eval_enqueue(ofdft_eval* e, const void* rho, void* v_out, unsigned calc, cudaStream_t st);
+void eval_collect(ofdft_eval* e, double* energies);
 
 namespace {
 
@@ -610,6 +638,654 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
     if (converged != 0) res.dP = op.dot(rsd, rsd) * dV;
 }
 
+// ------------------------------------------------------------------------
+// Lockstep L-BFGS over a batch of independent systems (uneven grids allowed).
+//
+// Every system runs the algorithm of optimize_t (L-BFGS branch) on its own
+// fields, with its own line search; the systems advance together, so each
+// vector operation is one launch over all systems (a block-to-system map in
+// device memory, per-system coefficients in the kernel arguments) and each
+// round of scalars is one device-to-host copy and one stream synchronisation
+// for the whole batch.  Evaluations stay per system (their cuFFT plans are per
+// grid) but are enqueued back to back and collected after one synchronisation.
+// The arithmetic of every operation, reductions included, is that of the
+// single-system optimiser, so each system's result is the same as a solve on
+// its own.
+
+constexpr int kBatchMax = 128;  // systems per batch (per-system arguments travel in the launch)
+constexpr int kBF = 48;         // field slots per system
+
+enum BField {
+    BF_RHOIO = 0,
+    BF_PHI,
+    BF_V,
+    BF_RSD,
+    BF_P,
+    BF_NPHI,
+    BF_NRHO,
+    BF_NV,
+    BF_OLDPHI,
+    BF_RESPREV,
+    BF_Q,
+    BF_RHO,
+    BF_LB0  // L-BFGS pair buffers from here on
+};
+
+template <typename T>
+struct BTab {
+    T* f[kBF];
+    long long N;
+    int red_blocks;  // the system grid's reduction block count
+    int boff;        // first block of the system in a reduction launch
+    int eoff, eb;    // first block and block count in an elementwise launch
+};
+
+// per-system coefficients and the active mask, passed by value
+struct BArgs {
+    double c[kBatchMax][3];
+    unsigned char act[kBatchMax];
+};
+
+template <typename T>
+__global__ void k_blincomb(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a, int o, int x0,
+                           int x1, int x2) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T b0 = (T)a.c[s][0], b1 = (T)a.c[s][1], b2 = (T)a.c[s][2];
+    T* out = t.f[o];
+    const T* X0 = t.f[x0];
+    const T* X1 = x1 >= 0 ? t.f[x1] : nullptr;
+    const T* X2 = x2 >= 0 ? t.f[x2] : nullptr;
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        out[i] = lin3(b0, X0, b1, X1, b2, X2, i);
+}
+
+template <typename T>
+__global__ void k_bsquare(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a, int x, int o) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride) {
+        const T v = t.f[x][i];
+        t.f[o][i] = mul_rn(v, v);
+    }
+}
+
+template <typename T>
+__global__ void k_bphi_init(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride) {
+        const T r = t.f[BF_RHOIO][i];
+        t.f[BF_PHI][i] = r > (T)0 ? sqrt(r) : phi_floor<T>();
+    }
+}
+
+// nphi = phi cos + p sin, nrho = nphi^2 (c[s] = {cos, sin})
+template <typename T>
+__global__ void k_brotate(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T cw = (T)a.c[s][0], sw = (T)a.c[s][1];
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride) {
+        const T v = rot(t.f[BF_PHI][i], t.f[BF_P][i], cw, sw);
+        t.f[BF_NPHI][i] = v;
+        t.f[BF_NRHO][i] = mul_rn(v, v);
+    }
+}
+
+// rsd = (V - mu) phi (c[s][0] = mu)
+template <typename T>
+__global__ void k_bresid(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T m = (T)a.c[s][0];
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        t.f[BF_RSD][i] = mul_rn(sub_rn(t.f[BF_V][i], m), t.f[BF_PHI][i]);
+}
+
+// sum a*b per system, accumulated as k_dot2 does
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_bdot2(const BTab<T>* __restrict__ tab, const int* __restrict__ bsys,
+                                                       BArgs a, int xa, int xb, double* partials) {
+    const int s = bsys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T* A = t.f[xa];
+    const T* B = t.f[xb];
+    RunSum<T> sum;
+    const long long stride = (long long)t.red_blocks * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.boff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        sum.add(mul_rn(A[i], B[i]));
+    double acc[1] = {sum.get()};
+    block_sum_store_at<1>(acc, partials, blockIdx.x);
+}
+
+// sum a per system in float64, accumulated as ofdft_dot (k_dot) does
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_bsum(const BTab<T>* __restrict__ tab, const int* __restrict__ bsys,
+                                                      BArgs a, int xa, double* partials) {
+    const int s = bsys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T* A = t.f[xa];
+    double v[1] = {0.0};
+    const long long stride = (long long)t.red_blocks * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.boff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        v[0] += (double)A[i];
+    block_sum_store_at<1>(v, partials, blockIdx.x);
+}
+
+// sum V * nphi * (p cos - phi sin) per system, as k_dtheta (c[s] = {cos, sin}; fields given)
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_bdtheta(const BTab<T>* __restrict__ tab, const int* __restrict__ bsys,
+                                                         BArgs a, int xV, int xnphi, double* partials) {
+    const int s = bsys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T cw = (T)a.c[s][0], sw = (T)a.c[s][1];
+    const T *V = t.f[xV], *nphi = t.f[xnphi], *p = t.f[BF_P], *phi = t.f[BF_PHI];
+    RunSum<T> sum;
+    const long long stride = (long long)t.red_blocks * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.boff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        sum.add(dth_term(V[i], nphi[i], p[i], phi[i], cw, sw));
+    double acc[1] = {sum.get()};
+    block_sum_store_at<1>(acc, partials, blockIdx.x);
+}
+
+// one block per system: its partials reduced with the tree of reduce_finalize
+template <typename T>
+__global__ void k_bfinalize(const BTab<T>* __restrict__ tab, BArgs a, const double* __restrict__ partials,
+                            double* out) {
+    const int s = blockIdx.x;
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    __shared__ double sh[RED_THREADS];
+    double x = 0.0;
+    for (int b = threadIdx.x; b < t.red_blocks; b += blockDim.x) x += partials[t.boff + b];
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[s] = sh[0];
+}
+
+template <typename T>
+struct Batch {
+    int S = 0;
+    std::vector<ofdft_eval*> e;
+    std::vector<ofdft_grid*> g;
+    cudaStream_t st = nullptr;
+    std::vector<BTab<T>> h_tab;
+    BTab<T>* d_tab = nullptr;
+    int *d_bsys = nullptr, *d_esys = nullptr;
+    int nb_red = 0, nb_el = 0;
+    double* d_part = nullptr;
+    double* d_out = nullptr;   // kMaxRound rows of S scalars
+    double* h_out = nullptr;   // pinned mirror
+    int rows = 0;              // scalar rows queued since the last sync
+    static constexpr int kMaxRound = 8;
+    BArgs args{};
+
+    // evaluations of a round are spread over worker streams (forked from and
+    // joined back to st), so that the small kernels of many systems overlap
+    static constexpr int kStreams = 16;
+    std::vector<cudaStream_t> ws;
+    std::vector<cudaEvent_t> wev;
+    cudaEvent_t fork_ev = nullptr;
+
+    ~Batch() {
+        for (cudaStream_t w : ws) cudaStreamDestroy(w);
+        for (cudaEvent_t v : wev) cudaEventDestroy(v);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        cudaFree(d_tab);
+        cudaFree(d_bsys);
+        cudaFree(d_esys);
+        cudaFree(d_part);
+        cudaFree(d_out);
+        cudaFreeHost(h_out);
+    }
+
+    T* field(int s, const char* name) {
+        return (T*)g[s]->scratch.get(std::string("opt_") + name, g[s]->real_bytes());
+    }
+
+    void setup(int nsys, ofdft_eval** evs, void** rho_io, int npairs, cudaStream_t stream) {
+        S = nsys;
+        st = stream;
+        e.assign(evs, evs + S);
+        g.resize(S);
+        h_tab.resize(S);
+        std::vector<int> bsys, esys;
+        for (int s = 0; s < S; ++s) {
+            g[s] = e_grid(e[s]);
+            BTab<T>& t = h_tab[s];
+            memset(&t, 0, sizeof(t));
+            t.N = g[s]->N;
+            t.red_blocks = g[s]->red_blocks;
+            t.boff = (int)bsys.size();
+            for (int b = 0; b < t.red_blocks; ++b) bsys.push_back(s);
+            t.eb = blocks_for(t.N, 256, g[s]->sms * 16);
+            t.eoff = (int)esys.size();
+            for (int b = 0; b < t.eb; ++b) esys.push_back(s);
+            t.f[BF_RHOIO] = (T*)rho_io[s];
+            static const char* names[] = {"", "phi", "V", "res", "p", "nphi", "nrho", "nV", "old_phi", "res_prev",
+                                          "lb_q", "rho"};
+            for (int f = 1; f < BF_LB0; ++f) t.f[f] = field(s, names[f]);
+            for (int k = 0; k < npairs; ++k) t.f[BF_LB0 + k] = field(s, ("lb" + std::to_string(k)).c_str());
+        }
+        nb_red = (int)bsys.size();
+        nb_el = (int)esys.size();
+        OFDFT_CK(cudaMalloc(&d_tab, S * sizeof(BTab<T>)));
+        OFDFT_CK(cudaMalloc(&d_bsys, nb_red * sizeof(int)));
+        OFDFT_CK(cudaMalloc(&d_esys, nb_el * sizeof(int)));
+        OFDFT_CK(cudaMalloc(&d_part, (size_t)nb_red * sizeof(double)));
+        OFDFT_CK(cudaMalloc(&d_out, (size_t)kMaxRound * S * sizeof(double)));
+        OFDFT_CK(cudaMallocHost(&h_out, (size_t)kMaxRound * S * sizeof(double)));
+        OFDFT_CK(cudaMemcpyAsync(d_tab, h_tab.data(), S * sizeof(BTab<T>), cudaMemcpyHostToDevice, st));
+        OFDFT_CK(cudaMemcpyAsync(d_bsys, bsys.data(), nb_red * sizeof(int), cudaMemcpyHostToDevice, st));
+        OFDFT_CK(cudaMemcpyAsync(d_esys, esys.data(), nb_el * sizeof(int), cudaMemcpyHostToDevice, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+        const int nw = std::min(S, kStreams);
+        ws.resize(nw);
+        wev.resize(nw);
+        for (int k = 0; k < nw; ++k) {
+            OFDFT_CK(cudaStreamCreateWithFlags(&ws[k], cudaStreamNonBlocking));
+            OFDFT_CK(cudaEventCreateWithFlags(&wev[k], cudaEventDisableTiming));
+        }
+        OFDFT_CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    }
+    // fork: worker streams wait for everything queued on st so far
+    void fork() {
+        OFDFT_CK(cudaEventRecord(fork_ev, st));
+        for (cudaStream_t w : ws) OFDFT_CK(cudaStreamWaitEvent(w, fork_ev, 0));
+    }
+    cudaStream_t worker(int s) const { return ws[s % (int)ws.size()]; }
+    // join: st waits for everything queued on the worker streams
+    void join() {
+        for (size_t k = 0; k < ws.size(); ++k) {
+            OFDFT_CK(cudaEventRecord(wev[k], ws[k]));
+            OFDFT_CK(cudaStreamWaitEvent(st, wev[k], 0));
+        }
+    }
+
+    void coef(int s, double c0, double c1 = 0.0, double c2 = 0.0) {
+        args.c[s][0] = c0;
+        args.c[s][1] = c1;
+        args.c[s][2] = c2;
+    }
+    // elementwise launches over the systems marked active in args
+    void lincomb(int o, int x0, int x1 = -1, int x2 = -1) {
+        k_blincomb<T><<<nb_el, 256, 0, st>>>(d_tab, d_esys, args, o, x0, x1, x2);
+        OFDFT_LAUNCH_CHECK();
+    }
+    void copy(int o, int x) {
+        for (int s = 0; s < S; ++s) coef(s, 1.0);
+        lincomb(o, x);
+    }
+    void square(int x, int o) {
+        k_bsquare<T><<<nb_el, 256, 0, st>>>(d_tab, d_esys, args, x, o);
+        OFDFT_LAUNCH_CHECK();
+    }
+    // reductions: each queues one row of S scalars, read after sync()
+    int finish_row() {
+        OFDFT_REQUIRE(rows < kMaxRound, "batched optimiser: too many scalars queued in one round");
+        k_bfinalize<T><<<S, RED_THREADS, 0, st>>>(d_tab, args, d_part, d_out + (size_t)rows * S);
+        OFDFT_LAUNCH_CHECK();
+        return rows++;
+    }
+    int dot(int xa, int xb) {
+        k_bdot2<T><<<nb_red, RED_THREADS, 0, st>>>(d_tab, d_bsys, args, xa, xb, d_part);
+        OFDFT_LAUNCH_CHECK();
+        return finish_row();
+    }
+    int sum(int xa) {
+        k_bsum<T><<<nb_red, RED_THREADS, 0, st>>>(d_tab, d_bsys, args, xa, d_part);
+        OFDFT_LAUNCH_CHECK();
+        return finish_row();
+    }
+    int dtheta(int xV, int xnphi) {
+        k_bdtheta<T><<<nb_red, RED_THREADS, 0, st>>>(d_tab, d_bsys, args, xV, xnphi, d_part);
+        OFDFT_LAUNCH_CHECK();
+        return finish_row();
+    }
+    // one device-to-host copy of the queued rows and one synchronisation
+    void sync() {
+        if (rows) OFDFT_CK(cudaMemcpyAsync(h_out, d_out, (size_t)rows * S * sizeof(double), cudaMemcpyDeviceToHost, st));
+        const auto t0 = std::chrono::steady_clock::now();
+        OFDFT_CK(cudaStreamSynchronize(st));
+        wait_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        ++syncs;
+        rows = 0;
+    }
+    double wait_s = 0.0, enqueue_s = 0.0;  // host time waiting in sync() / enqueueing evaluations
+    long long syncs = 0, evals = 0;
+    double at(int row, int s) const { return h_out[(size_t)row * S + s]; }
+    void set_active(const std::vector<char>& act) {
+        for (int s = 0; s < S; ++s) args.act[s] = act[s] ? 1 : 0;
+    }
+};
+
+template <typename T>
+void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_options& o, const double* econv,
+                      ofdft_opt_result* res, void** v_out, cudaStream_t st) {
+    OFDFT_REQUIRE(o.method == OFDFT_OPT_LBFGS, "ofdft_optimize_batch: only L-BFGS is batched");
+    OFDFT_REQUIRE(o.maxcor >= 0 && 2 * (o.maxcor + 1) <= kBF - BF_LB0, "ofdft_optimize_batch: maxcor too large");
+    Batch<T> b;
+    const int npairs = 2 * (o.maxcor + 1);
+    b.setup(S, evs, rho_io, npairs, st);
+    std::vector<double> dV(S), E(S), mu(S), Nel(S);
+    for (int s = 0; s < S; ++s) dV[s] = b.g[s]->dV;
+    std::vector<char> run(S, 1);  // still iterating
+    std::vector<int> conv(S, 2), niter(S, 0), nfev(S, 1);
+    std::vector<std::vector<double>> Ehist(S);
+    std::vector<double> dP(S, 0.0);
+    auto active = [&](const std::vector<char>& m) { b.set_active(m); };
+    auto any = [](const std::vector<char>& m) { return std::any_of(m.begin(), m.end(), [](char c) { return c != 0; }); };
+    auto evaluate = [&](const std::vector<char>& m, int xrho, int xV) {
+        const auto t0 = std::chrono::steady_clock::now();
+        b.fork();
+        for (int s = 0; s < S; ++s)
+            if (m[s]) {
+                eval_enqueue(b.e[s], b.h_tab[s].f[xrho], b.h_tab[s].f[xV], OFDFT_CALC_E | OFDFT_CALC_V,
+                             b.worker(s));
+                ++b.evals;
+            }
+        b.join();
+        b.enqueue_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    };
+    const auto t_start = std::chrono::steady_clock::now();
+    auto collect = [&](const std::vector<char>& m, std::vector<double>& out) {
+        double En[OFDFT_NE];
+        for (int s = 0; s < S; ++s)
+            if (m[s]) {
+                eval_collect(b.e[s], En);
+                out[s] = En[OFDFT_E_TOTAL];
+            }
+    };
+    auto orth_norm = [&](const std::vector<char>& m) {
+        // OrthogonalNormalization (optimization.py:205-226)
+        active(m);
+        const int rNe = b.dot(BF_PHI, BF_PHI), rf = b.dot(BF_P, BF_PHI);
+        b.sync();
+        std::vector<double> Ne(S, 1.0);
+        for (int s = 0; s < S; ++s)
+            if (m[s]) {
+                Ne[s] = b.at(rNe, s) * dV[s];
+                b.coef(s, 1.0, -(b.at(rf, s) * dV[s] / Ne[s]));
+            }
+        b.lincomb(BF_P, BF_P, BF_PHI);
+        const int rp = b.dot(BF_P, BF_P);
+        b.sync();
+        for (int s = 0; s < S; ++s)
+            if (m[s]) b.coef(s, std::sqrt(Ne[s] / (b.at(rp, s) * dV[s])));
+        b.lincomb(BF_P, BF_P);
+    };
+    // ---- start (optimize_t: phi = sqrt(rho) renormalised, first evaluation, mu, residual)
+    active(run);
+    k_bphi_init<T><<<b.nb_el, 256, 0, st>>>(b.d_tab, b.d_esys, b.args);
+    OFDFT_LAUNCH_CHECK();
+    {
+        const int rr = b.sum(BF_RHOIO), rp = b.dot(BF_PHI, BF_PHI);
+        b.sync();
+        for (int s = 0; s < S; ++s) b.coef(s, std::sqrt(b.at(rr, s) / b.at(rp, s)));
+    }
+    b.lincomb(BF_PHI, BF_PHI);
+    b.square(BF_PHI, BF_RHO);
+    evaluate(run, BF_RHO, BF_V);
+    {
+        const int rn = b.sum(BF_RHO), rm = b.dot(BF_V, BF_RHO);
+        b.sync();
+        collect(run, E);
+        for (int s = 0; s < S; ++s) {
+            Nel[s] = b.at(rn, s) * dV[s];
+            mu[s] = b.at(rm, s) * dV[s] / Nel[s];
+            b.coef(s, mu[s]);
+            Ehist[s].push_back(E[s]);
+        }
+    }
+    k_bresid<T><<<b.nb_el, 256, 0, st>>>(b.d_tab, b.d_esys, b.args);
+    OFDFT_LAUNCH_CHECK();
+    // L-BFGS pairs: the same slots and history length for every running system
+    struct Pair {
+        int s, y;
+    };
+    std::deque<Pair> lb;
+    std::vector<std::deque<double>> lbrho(S);
+    int pool_i = 0;
+    for (int it = 1; it < o.maxiter && any(run); ++it) {
+        for (int s = 0; s < S; ++s)
+            if (run[s]) niter[s] = it;
+        active(run);
+        // ---- direction: get_direction_LBFGS (optimization.py:150-171), first loop skips i = 0
+        for (int s = 0; s < S; ++s) b.coef(s, -1.0);
+        b.lincomb(BF_Q, BF_RSD);
+        const int m = (int)lb.size();
+        std::vector<std::vector<double>> al(S, std::vector<double>(m, 0.0));
+        for (int i = m - 1; i > 0; --i) {
+            const int r = b.dot(lb[i].s, BF_Q);
+            b.sync();
+            for (int s = 0; s < S; ++s)
+                if (run[s]) {
+                    al[s][i] = lbrho[s][i] * b.at(r, s);
+                    b.coef(s, 1.0, -al[s][i]);
+                }
+            b.lincomb(BF_Q, BF_Q, lb[i].y);
+        }
+        OFDFT_REQUIRE(o.h0 != 0.0, "ofdft_optimize_batch: h0 = 0 is not batched");
+        for (int s = 0; s < S; ++s) b.coef(s, o.h0);
+        b.lincomb(BF_P, BF_Q);
+        for (int i = 0; i < m; ++i) {
+            const int r = b.dot(lb[i].y, BF_P);
+            b.sync();
+            for (int s = 0; s < S; ++s)
+                if (run[s]) b.coef(s, 1.0, al[s][i] - lbrho[s][i] * b.at(r, s));
+            b.lincomb(BF_P, BF_P, lb[i].s);
+        }
+        orth_norm(run);
+        // uphill: steepest descent (optimization.py:373-380)
+        {
+            active(run);
+            for (int s = 0; s < S; ++s) b.coef(s, 1.0, 0.0);
+            const int r = b.dtheta(BF_V, BF_PHI);
+            b.sync();
+            std::vector<char> up(S, 0);
+            for (int s = 0; s < S; ++s) up[s] = run[s] && b.at(r, s) * 2.0 > 0;
+            if (any(up)) {
+                active(up);
+                for (int s = 0; s < S; ++s) b.coef(s, -1.0);
+                b.lincomb(BF_P, BF_RSD);
+                orth_norm(up);
+            }
+        }
+        // ---- line search on theta: scalar_search_wolfe1 per system, evaluations batched
+        std::vector<double> g0(S, 0.0);
+        {
+            active(run);
+            for (int s = 0; s < S; ++s) b.coef(s, 1.0, 0.0);
+            const int r = b.dtheta(BF_V, BF_PHI);
+            b.sync();
+            for (int s = 0; s < S; ++s) g0[s] = 2.0 * b.at(r, s) * dV[s];
+        }
+        std::vector<Dcsrch> ls(S);
+        std::vector<double> stp(S, 1.0), f(S), gd(S), lastE(S, NAN), last_theta(S, NAN);
+        std::vector<int> nls(S, 0), lsit(S, 0);
+        std::vector<char> searching(S, 0), ok(S, 0);
+        std::vector<Task> task(S, FG);
+        for (int s = 0; s < S; ++s) {
+            if (!run[s]) continue;
+            Dcsrch& d = ls[s];
+            d.ftol = o.c1;
+            d.gtol = o.c2;
+            d.xtol = o.xtol;
+            d.stpmin = 0.0;
+            d.stpmax = M_PI;
+            f[s] = E[s];
+            gd[s] = g0[s];
+            task[s] = d.start(stp[s], f[s], gd[s]);
+            searching[s] = task[s] != ERR;
+            ok[s] = 0;
+        }
+        while (any(searching)) {
+            // advance each state machine to its next trial step (wolfe1)
+            std::vector<char> need(S, 0);
+            for (int s = 0; s < S; ++s) {
+                if (!searching[s]) continue;
+                if (lsit[s] >= 100) {  // wolfe1's maxiter: no further dcsrch call
+                    searching[s] = 0;
+                    continue;
+                }
+                if (lsit[s] > 0) task[s] = ls[s].iterate(stp[s], f[s], gd[s]);
+                if (!std::isfinite(stp[s])) {
+                    searching[s] = 0;
+                    continue;
+                }
+                if (task[s] != FG) {
+                    searching[s] = 0;
+                    ok[s] = task[s] == CONV;
+                    continue;
+                }
+                need[s] = 1;
+            }
+            if (!any(need)) break;
+            active(need);
+            for (int s = 0; s < S; ++s)
+                if (need[s]) b.coef(s, std::cos(stp[s]), std::sin(stp[s]));
+            k_brotate<T><<<b.nb_el, 256, 0, st>>>(b.d_tab, b.d_esys, b.args);
+            OFDFT_LAUNCH_CHECK();
+            evaluate(need, BF_NRHO, BF_NV);
+            const int r = b.dtheta(BF_NV, BF_NPHI);
+            b.sync();
+            std::vector<double> En(S, 0.0);
+            collect(need, En);
+            for (int s = 0; s < S; ++s) {
+                if (!need[s]) continue;
+                f[s] = En[s];
+                gd[s] = 2.0 * b.at(r, s) * dV[s];
+                lastE[s] = f[s];
+                last_theta[s] = stp[s];
+                ++nls[s];
+                ++lsit[s];
+            }
+        }
+        std::vector<char> acc(S, 0);
+        for (int s = 0; s < S; ++s) {
+            if (!run[s]) continue;
+            nfev[s] += nls[s];
+            if (!ok[s] || nls[s] == 0 || stp[s] != last_theta[s]) {
+                conv[s] = 1;  // "Line-Search Failed" (optimization.py:444-448)
+                run[s] = 0;
+                continue;
+            }
+            acc[s] = 1;
+        }
+        if (!any(acc)) break;
+        // ---- accept
+        active(acc);
+        b.copy(BF_OLDPHI, BF_PHI);
+        b.copy(BF_PHI, BF_NPHI);
+        b.copy(BF_V, BF_NV);
+        b.square(BF_PHI, BF_RHO);
+        {
+            const int rn = b.sum(BF_RHO), rm = b.dot(BF_V, BF_RHO);
+            b.sync();
+            for (int s = 0; s < S; ++s)
+                if (acc[s]) {
+                    E[s] = lastE[s];
+                    Nel[s] = b.at(rn, s) * dV[s];
+                    mu[s] = b.at(rm, s) * dV[s] / Nel[s];
+                }
+        }
+        b.copy(BF_RESPREV, BF_RSD);
+        for (int s = 0; s < S; ++s) b.coef(s, mu[s]);
+        k_bresid<T><<<b.nb_el, 256, 0, st>>>(b.d_tab, b.d_esys, b.args);
+        OFDFT_LAUNCH_CHECK();
+        // LBFGS.update (math_utils.py:307-325): at most maxcor+1 pairs
+        Pair pr;
+        bool popped = false;
+        if ((int)lb.size() > o.maxcor) {
+            pr = lb.front();
+            lb.pop_front();
+            popped = true;
+        } else {
+            pr.s = BF_LB0 + pool_i++;
+            pr.y = BF_LB0 + pool_i++;
+        }
+        for (int s = 0; s < S; ++s) b.coef(s, 1.0, -1.0);
+        b.lincomb(pr.s, BF_PHI, BF_OLDPHI);
+        b.lincomb(pr.y, BF_RSD, BF_RESPREV);
+        const int rys = b.dot(pr.y, pr.s), rres = b.dot(BF_RSD, BF_RSD);
+        b.sync();
+        lb.push_back(pr);
+        for (int s = 0; s < S; ++s) {
+            if (!acc[s]) continue;
+            if (popped) lbrho[s].pop_front();
+            lbrho[s].push_back(1.0 / b.at(rys, s));
+            Ehist[s].push_back(E[s]);
+            dP[s] = b.at(rres, s) * dV[s];
+            if (o.verbose)
+                fprintf(stderr, "[%d] %-8d%-24.12E%-16.6E%-16.6E%-8d\n", s, it, E[s],
+                        Ehist[s][Ehist[s].size() - 1] - Ehist[s][Ehist[s].size() - 2], dP[s], nls[s]);
+            // check_converge (optimization.py:527-540)
+            const std::vector<double>& H = Ehist[s];
+            bool cv = false;
+            if ((int)H.size() - 1 >= o.ncheck) {
+                cv = true;
+                const double ec = econv ? econv[s] : o.econv;
+                for (int i = 0; i < o.ncheck; ++i)
+                    if (std::fabs(H[H.size() - 2 - i] - E[s]) > ec) cv = false;
+            }
+            if (cv) {
+                conv[s] = 0;
+                run[s] = 0;
+            }
+        }
+    }
+    for (int s = 0; s < S; ++s)
+        if (run[s]) niter[s] = o.maxiter;  // the loop ran out of iterations (conv stays 2)
+    if (o.verbose)
+        fprintf(stderr, "batch of %d: %.3f s, %lld evaluations (%.3f s enqueueing), %lld synchronisations (%.3f s "
+                "waiting)\n", S,
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count(), b.evals,
+                b.enqueue_s, b.syncs, b.wait_s);
+    // rho_io <- phi^2, the potential of the last accepted evaluation, results
+    std::vector<char> all(S, 1);
+    active(all);
+    b.square(BF_PHI, BF_RHOIO);
+    for (int s = 0; s < S; ++s)
+        if (v_out && v_out[s])
+            OFDFT_CK(cudaMemcpyAsync(v_out[s], b.h_tab[s].f[BF_V], b.g[s]->real_bytes(), cudaMemcpyDeviceToDevice, st));
+    std::vector<char> need_dp(S, 0);
+    for (int s = 0; s < S; ++s) need_dp[s] = conv[s] != 0;
+    int rdp = -1;
+    if (any(need_dp)) {
+        active(need_dp);
+        rdp = b.dot(BF_RSD, BF_RSD);
+    }
+    b.sync();
+    for (int s = 0; s < S; ++s) {
+        ofdft_opt_result& r = res[s];
+        memset(&r, 0, sizeof(r));
+        r.converged = conv[s];
+        r.niter = niter[s];
+        r.nfev = nfev[s];
+        r.energy = E[s];
+        r.mu = mu[s];
+        r.dP = (conv[s] != 0 && rdp >= 0) ? b.at(rdp, s) * dV[s] : dP[s];
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -646,6 +1322,25 @@ int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft
 
 int ofdft_optimize(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, ofdft_stream s) {
     return ofdft_optimize_v(e, rho, o, r, nullptr, s);
+}
+
+int ofdft_optimize_batch(int n, ofdft_eval** evs, void** rho, const ofdft_opt_options* o, const double* econv,
+                         ofdft_opt_result* r, void** v_out, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(n >= 1 && n <= kBatchMax, "ofdft_optimize_batch: 1..%d systems", kBatchMax);
+        OFDFT_REQUIRE(evs && rho && o && r, "ofdft_optimize_batch: null argument");
+        OFDFT_REQUIRE(o->maxiter >= 1 && o->maxfun >= 1 && o->ncheck >= 1, "ofdft_optimize_batch: bad limits");
+        const int prec = e_grid(evs[0])->prec;
+        for (int i = 0; i < n; ++i) {
+            OFDFT_REQUIRE(evs[i] && rho[i], "ofdft_optimize_batch: null system %d", i);
+            OFDFT_REQUIRE(e_grid(evs[i])->prec == prec, "ofdft_optimize_batch: mixed precisions");
+            for (int j = 0; j < i; ++j)
+                OFDFT_REQUIRE(e_grid(evs[j]) != e_grid(evs[i]), "ofdft_optimize_batch: systems %d and %d share a grid",
+                              j, i);
+        }
+        if (prec == OFDFT_F64) optimize_batch_t<double>(n, evs, rho, *o, econv, r, v_out, (cudaStream_t)s);
+        else optimize_batch_t<float>(n, evs, rho, *o, econv, r, v_out, (cudaStream_t)s);
+    });
 }
 
 int ofdft_linesearch(ofdft_phi_fn fn, void* ctx, double f0, double g0, double stp0, double c1, double c2, double amax,

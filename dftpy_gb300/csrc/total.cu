@@ -716,6 +716,11 @@ struct ofdft_eval {
     unsigned* d_fz_err = nullptr;  // fused pipeline: nonzero after a bulk copy that did not complete
     unsigned* h_fz_err = nullptr;  // pinned mirror
     bool fz_ran = false;           // the last evaluation ran the fused pipeline
+    // terms of an evaluation whose energies have not been collected yet
+    struct Pending {
+        bool tf, vw, wt, lwt, xc, h, pp, lp_active;
+        int launches;
+    } pend{};
     bool kf_set_min = false, kf_set_max = false;
     double kf_st_min = 0, kf_st_max = 0;
     int last_nsp = 0, last_launches = 0;
@@ -731,6 +736,20 @@ struct ofdft_eval {
 };
 
 ofdft_grid* e_grid(ofdft_eval* e) { return e->g; }
+
+namespace {
+template <typename T>
+void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energies, cudaStream_t st);
+void collect_energies(ofdft_eval* e, double* energies);
+}  // namespace
+
+// For the batched optimiser: enqueue an evaluation without waiting, and read its
+// energies once the stream has been synchronised.
+void eval_enqueue(ofdft_eval* e, const void* rho, void* v_out, unsigned calc, cudaStream_t st) {
+    if (e->g->prec == OFDFT_F64) compute_t<double>(e, (const double*)rho, (double*)v_out, calc, nullptr, st);
+    else compute_t<float>(e, (const float*)rho, (float*)v_out, calc, nullptr, st);
+}
+void eval_collect(ofdft_eval* e, double* energies) { collect_energies(e, energies); }
 
 namespace {
 
@@ -1061,6 +1080,12 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     return launches;
 }
 
+void collect_energies(ofdft_eval* e, double* energies);
+
+// Enqueues one evaluation on st.  With energies != NULL it waits for the
+// stream and writes them; with NULL it returns after enqueueing the copy of
+// the sums to the grid's pinned results, and collect_energies() reads them
+// once the caller has synchronised the stream.
 template <typename T>
 void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energies, cudaStream_t st) {
     ofdft_grid* g = e->g;
@@ -1365,7 +1390,24 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     launches += 2;
     OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 24 * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (e->fz_ran) OFDFT_CK(cudaMemcpyAsync(e->h_fz_err, e->d_fz_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    e->pend.tf = tf;
+    e->pend.vw = vw;
+    e->pend.wt = wt;
+    e->pend.lwt = lwt;
+    e->pend.xc = xc;
+    e->pend.h = h;
+    e->pend.pp = pp;
+    e->pend.lp_active = lwt && lp.active;
+    e->pend.launches = launches;
+    if (!energies) return;
     OFDFT_CK(cudaStreamSynchronize(st));
+    collect_energies(e, energies);
+}
+
+// Energies of the last enqueued evaluation, after its stream has been synchronised.
+void collect_energies(ofdft_eval* e, double* energies) {
+    const ofdft_config& c = e->cfg;
+    const ofdft_eval::Pending& p = e->pend;
     if (e->prof) prof_collect(e);
     if (e->fz_ran) {
         e->fz_ran = false;
@@ -1375,22 +1417,22 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
             OFDFT_REQUIRE(false, "fused k_F-node pipeline: a bulk copy into shared memory did not complete");
         }
     }
-    const double* R = g->h_results;
-    const double dV = g->dV;
+    const double* R = e->g->h_results;
+    const double dV = e->g->dV;
     double* E = energies;
     for (int i = 0; i < OFDFT_NE; ++i) E[i] = 0.0;
-    E[OFDFT_E_TF] = tf ? R[0] * dV * c.tf_x : 0.0;
-    E[OFDFT_E_XC] = xc ? R[1] * dV : 0.0;
-    E[OFDFT_E_PP] = pp ? R[2] * dV : 0.0;
+    E[OFDFT_E_TF] = p.tf ? R[0] * dV * c.tf_x : 0.0;
+    E[OFDFT_E_XC] = p.xc ? R[1] * dV : 0.0;
+    E[OFDFT_E_PP] = p.pp ? R[2] * dV : 0.0;
     E[OFDFT_E_NELEC] = R[3] * dV;
-    E[OFDFT_E_VW] = vw ? R[16] * dV * c.vw_y : 0.0;
-    E[OFDFT_E_H] = h ? R[17] * dV / 2.0 : 0.0;
-    if (wt) E[OFDFT_E_NL] = R[18] * dV;
-    if (lwt) E[OFDFT_E_NL] = lp.active ? R[18] * dV : 0.0;
+    E[OFDFT_E_VW] = p.vw ? R[16] * dV * c.vw_y : 0.0;
+    E[OFDFT_E_H] = p.h ? R[17] * dV / 2.0 : 0.0;
+    if (p.wt) E[OFDFT_E_NL] = R[18] * dV;
+    if (p.lwt) E[OFDFT_E_NL] = p.lp_active ? R[18] * dV : 0.0;
     E[OFDFT_E_II] = c.ewald_energy;
     E[OFDFT_E_TOTAL] = E[OFDFT_E_TF] + E[OFDFT_E_VW] + E[OFDFT_E_NL] + E[OFDFT_E_XC] + E[OFDFT_E_H] + E[OFDFT_E_PP] +
                        E[OFDFT_E_II];
-    e->last_launches = launches;
+    e->last_launches = p.launches;
 }
 
 }  // namespace

@@ -17,7 +17,7 @@ from .functional.abstract_functional import NativeFunctional, stream_ptr
 from .functional.functional_output import FunctionalOutput
 from .functional.total_functional import TotalFunctional
 
-__all__ = ["Optimization"]
+__all__ = ["Optimization", "optimize_rho_batch"]
 
 _METHODS = {"TN": _lib.OPT_TN, "LBFGS": _lib.OPT_LBFGS, "CG-HS": _lib.OPT_CGHS, "CG": _lib.OPT_CGHS}
 
@@ -173,3 +173,93 @@ class Optimization:
 
     def __call__(self, guess_rho=None, calcType={"E", "V"}, guess_phi=None, lphi=False):
         return self.optimize_rho(guess_rho=guess_rho, guess_phi=guess_phi, lphi=lphi)
+
+
+_BATCH_MAX = 128
+
+
+def optimize_rho_batch(optimizations, guess_rhos, dtype=None, refine=None):
+    """Ground states of many independent systems together.
+
+    ``optimizations`` are ``Optimization`` objects (L-BFGS, one per system, each
+    with its own energy evaluator and grid; options equal except ``econv``).
+    All systems run the L-BFGS of ``optimize_rho`` in lockstep on the device
+    (``ofdft_optimize_batch``): every vector operation is one launch for the
+    whole batch and every round of scalars one synchronisation, instead of one
+    per system.  Each system's result is the one ``optimize_rho`` gives it.
+
+    ``dtype``: field precision of the optimisation (default float64).
+    ``refine="evaluate"``: after a float32 optimisation, evaluate every density
+    once in FP64 (electron count restored in float64), as
+    ``optimize_rho_mixed(refine="evaluate")`` does for one system.
+    Returns the densities; each ``Optimization`` gets ``rho``, ``mu``,
+    ``converged``, ``result`` and ``functional``."""
+    opts = list(optimizations)
+    guesses = list(guess_rhos)
+    if len(opts) != len(guesses):
+        raise ValueError("one guess density per optimisation")
+    if not opts:
+        return []
+    dtype = dtype or torch.float64
+    base = opts[0].options_struct()
+    for o in opts:
+        if o.optimization_method != "LBFGS":
+            raise NotImplementedError("optimize_rho_batch runs L-BFGS only")
+        s = o.options_struct()
+        for f, _ in _lib.OptOptions._fields_:
+            if f != "econv" and getattr(s, f) != getattr(base, f):
+                raise ValueError("batched optimisations must share every option but econv (%s differs)" % f)
+    lib = _lib.load()
+    out = []
+    for c0 in range(0, len(opts), _BATCH_MAX):
+        chunk = list(zip(opts[c0:c0 + _BATCH_MAX], guesses[c0:c0 + _BATCH_MAX]))
+        n = len(chunk)
+        totals, evs, rhos, vs, grids = [], [], [], [], []
+        for o, guess in chunk:
+            total = o._total()
+            grid = guess.grid if isinstance(guess, DirectField) else next(
+                f.grid for f in total.funcDict.values() if getattr(f, "grid", None) is not None)
+            rho = DirectField(grid, data=guess, dtype=dtype).clone()
+            ev = total.evaluator(grid, rho.dtype)
+            total.prepare(ev, grid, rho.dtype)
+            totals.append((total, ev))
+            evs.append(ev.h)
+            rhos.append(rho)
+            vs.append(torch.empty_like(rho.as_subclass(torch.Tensor)))
+            grids.append(grid)
+        P = _lib.C.c_void_p
+        ev_arr = (P * n)(*[P(h.value if hasattr(h, "value") else h) for h in evs])
+        rho_arr = (P * n)(*[P(r.as_subclass(torch.Tensor).data_ptr()) for r in rhos])
+        v_arr = (P * n)(*[P(v.data_ptr()) for v in vs])
+        econv = (_lib.C.c_double * n)(*[float(o.optimization_options["econv"] or 0.0) for o, _ in chunk])
+        res = (_lib.OptResult * n)()
+        _lib.check(lib.ofdft_optimize_batch(n, ev_arr, rho_arr, _lib.C.byref(base), econv, res, v_arr, stream_ptr()))
+        for i, (o, _) in enumerate(chunk):
+            total, ev = totals[i]
+            total.finish(ev)
+            rho = rhos[i]
+            rho._N = None
+            r = res[i]
+            o.result = r
+            o.converged = r.converged
+            o.mu = r.mu
+            v = vs[i].as_subclass(DirectField)
+            v.grid = grids[i]
+            v._N = None
+            o.functional = FunctionalOutput(name="TOTAL", energy=float(r.energy), potential=v)
+            if refine == "evaluate" and rho.dtype != torch.float64:
+                n_target = DirectField(grids[i], data=chunk[i][1], dtype=torch.float64).integral()
+                r64 = DirectField(grids[i], data=rho.as_subclass(torch.Tensor).double())
+                r64 = DirectField(grids[i], data=r64 * (n_target / r64.integral()))
+                func = total(r64, calcType={"E", "V"})
+                o.stages = [{"precision": "f32", "method": "LBFGS", "niter": r.niter, "nfev": r.nfev,
+                             "converged": r.converged, "energy": r.energy},
+                            {"precision": "f64", "method": "evaluate", "niter": 0, "nfev": 1,
+                             "converged": r.converged, "energy": func.energy}]
+                o.functional = func
+                o.mu = float((func.potential * r64).integral() / r64.integral())
+                rho = r64
+            o.rho = rho
+            o.phi = torch.sqrt(rho)
+            out.append(rho)
+    return out

@@ -213,6 +213,19 @@ int ofdft_optimize(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_o
 int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, void* v_out,
                      ofdft_stream s);
 
+/* Lockstep L-BFGS over n independent systems (n <= 128), each with its own
+ * evaluator on its own grid (uneven grids allowed; one precision): the same
+ * algorithm and result per system as ofdft_optimize, with every vector
+ * operation launched once for the whole batch and one stream synchronisation
+ * per round of scalars instead of one per system.  There is no counterpart
+ * in the reference (which solves one system per call); it serves the
+ * batched ground states of many small systems.  o->method must be L-BFGS;
+ * econv (may be NULL: o->econv for all) gives each system its own energy
+ * tolerance.  rho[i] is overwritten with system i's density, r[i] receives
+ * its result, v_out[i] (v_out or its entries may be NULL) its final potential. */
+int ofdft_optimize_batch(int n, ofdft_eval** evs, void** rho, const ofdft_opt_options* o, const double* econv,
+                         ofdft_opt_result* r, void** v_out, ofdft_stream s);
+
 /* The scalar MINPACK-2 line search on a host callback, exposed for testing
  * against scipy.optimize line_search_wolfe1 (scalar_search_wolfe1). */
 typedef int (*ofdft_phi_fn)(double alpha, double* f, double* g, void* ctx);

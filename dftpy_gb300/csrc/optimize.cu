@@ -341,6 +341,7 @@ ofdft_grid* e_grid(ofdft_eval* e);
 // an evaluation enqueued without waiting, and its energies after a synchronisation (total.cu)
 void eval_enqueue(ofdft_eval* e, const void* rho, void* v_out, unsigned calc, cudaStream_t st);
 void eval_collect(ofdft_eval* e, double* energies);
+bool eval_capturable(const ofdft_eval* e);
 
 namespace {
 
@@ -845,7 +846,13 @@ struct Batch {
     std::vector<cudaEvent_t> wev;
     cudaEvent_t fork_ev = nullptr;
 
+    // the line-search evaluation (nrho -> nV) of each system, captured once as
+    // a CUDA graph and replayed: one launch instead of a dozen per evaluation
+    std::vector<cudaGraphExec_t> gexec;
+
     ~Batch() {
+        for (cudaGraphExec_t x : gexec)
+            if (x) cudaGraphExecDestroy(x);
         for (cudaStream_t w : ws) cudaStreamDestroy(w);
         for (cudaEvent_t v : wev) cudaEventDestroy(v);
         if (fork_ev) cudaEventDestroy(fork_ev);
@@ -905,6 +912,30 @@ struct Batch {
             OFDFT_CK(cudaEventCreateWithFlags(&wev[k], cudaEventDisableTiming));
         }
         OFDFT_CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        gexec.assign(S, nullptr);
+    }
+    // the line-search evaluation of system s on its worker stream, captured on
+    // first use (the evaluation's buffers and plans exist by then: the starting
+    // evaluation ran uncaptured)
+    void eval_ls(int s) {
+        cudaStream_t w = worker(s);
+        if (!gexec[s] && eval_capturable(e[s])) {
+            cudaGraph_t graph = nullptr;
+            OFDFT_CK(cudaStreamBeginCapture(w, cudaStreamCaptureModeThreadLocal));
+            try {
+                eval_enqueue(e[s], h_tab[s].f[BF_NRHO], h_tab[s].f[BF_NV], OFDFT_CALC_E | OFDFT_CALC_V, w);
+            } catch (...) {
+                cudaStreamEndCapture(w, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            OFDFT_CK(cudaStreamEndCapture(w, &graph));
+            const cudaError_t rc = cudaGraphInstantiate(&gexec[s], graph, 0);
+            cudaGraphDestroy(graph);
+            OFDFT_CK(rc);
+        }
+        if (gexec[s]) OFDFT_CK(cudaGraphLaunch(gexec[s], w));
+        else eval_enqueue(e[s], h_tab[s].f[BF_NRHO], h_tab[s].f[BF_NV], OFDFT_CALC_E | OFDFT_CALC_V, w);
     }
     // fork: worker streams wait for everything queued on st so far
     void fork() {
@@ -998,8 +1029,9 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         b.fork();
         for (int s = 0; s < S; ++s)
             if (m[s]) {
-                eval_enqueue(b.e[s], b.h_tab[s].f[xrho], b.h_tab[s].f[xV], OFDFT_CALC_E | OFDFT_CALC_V,
-                             b.worker(s));
+                if (xrho == BF_NRHO && xV == BF_NV) b.eval_ls(s);
+                else eval_enqueue(b.e[s], b.h_tab[s].f[xrho], b.h_tab[s].f[xV], OFDFT_CALC_E | OFDFT_CALC_V,
+                                  b.worker(s));
                 ++b.evals;
             }
         b.join();

@@ -750,6 +750,9 @@ void eval_enqueue(ofdft_eval* e, const void* rho, void* v_out, unsigned calc, cu
     else compute_t<float>(e, (const float*)rho, (float*)v_out, calc, nullptr, st);
 }
 void eval_collect(ofdft_eval* e, double* energies) { collect_energies(e, energies); }
+// an evaluation that waits on the host mid-way (the k_F-node kernel reads its
+// k_F bounds back) cannot be captured into a CUDA graph
+bool eval_capturable(const ofdft_eval* e) { return !(e->cfg.kedf_terms & OFDFT_KE_LWT); }
 
 namespace {
 

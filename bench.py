@@ -310,10 +310,14 @@ def gpu_arm(args):
     def maxrank(x):
         return max_over_ranks(x, dist, "cuda")
 
-    # ---- FP32-mixed headline, with clock sampling and per-kernel events
+    # ---- FP32-mixed headline, with clock sampling; then a shorter run with
+    # per-kernel events (the library serialises its two k_F-node chains while
+    # profiling, so that each kernel's events time that kernel alone)
     sampler = ClockSampler(local)
-    r32 = run(torch.float32, args.steps, args.warmup, profile=True, sampler=sampler)
+    r32 = run(torch.float32, args.steps, args.warmup, sampler=sampler)
     ms32 = maxrank(r32["ms_total"]) / args.steps
+    ksteps = max(3, min(args.steps, 10))
+    r32p = run(torch.float32, ksteps, 1, profile=True)
     out = {"metric": METRIC, "value": world * 1e3 / ms32, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 (f64 reductions)", "data": "synthetic (seeded)",
@@ -321,7 +325,7 @@ def gpu_arm(args):
            "gpu_launches": r32["launches"] * args.steps}
     # ---- roofline of the dominant own kernel
     peak, src = hbm_peak()
-    own = {k: v for k, v in r32["prof"].items() if k != "cufft" and v["launches"] > 0}
+    own = {k: v for k, v in r32p["prof"].items() if k != "cufft" and v["launches"] > 0}
     dom = max(own, key=lambda k: own[k]["ms"])
     d = own[dom]
     per_launch_bytes = d["bytes"] / d["launches"]
@@ -332,11 +336,14 @@ def gpu_arm(args):
                        "frac": ach / peak, "traffic": per_launch_bytes * ratio if ratio else None,
                        "traffic_source": TRAFFIC_SOURCE if ratio else None, "peak_source": src,
                        "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
-    tot_ms = sum(v["ms"] for v in r32["prof"].values())
-    out["kernels"] = {k: {"share": v["ms"] / tot_ms if tot_ms else 0.0, "ms_per_step": v["ms"] / args.steps,
+    tot_ms = sum(v["ms"] for v in r32p["prof"].values())
+    out["kernels"] = {k: {"share": v["ms"] / tot_ms if tot_ms else 0.0, "ms_per_step": v["ms"] / ksteps,
                           "GBps": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None,
-                          "launches_per_step": v["launches"] / args.steps}
-                      for k, v in r32["prof"].items()}
+                          "launches_per_step": v["launches"] / ksteps}
+                      for k, v in r32p["prof"].items()}
+    out["kernels_note"] = ("per-kernel CUDA events over %d profiled steps with the two k_F-node chains serialised "
+                           "(%.2f ms per step); the headline runs them concurrently on two streams" %
+                           (ksteps, r32p["ms_total"] / ksteps))
     s32 = 4
     n3 = args.n ** 3
     algo_bytes = (2 * 198 + 3) * s32 * n3 if args.nsp == 64 else None

@@ -714,6 +714,8 @@ struct ofdft_eval {
     double* h_nodes = nullptr;  // pinned staging
     float2* fz_tw = nullptr;    // twiddle tables of the fused k_F-node pipeline
     unsigned* d_fz_err = nullptr;  // fused pipeline: nonzero after a bulk copy that did not complete
+    cudaStream_t fz_st2 = nullptr;     // fused pipeline: the R2C chain runs here, beside the C2R chain
+    cudaEvent_t fz_fork = nullptr, fz_join = nullptr;
     unsigned* h_fz_err = nullptr;  // pinned mirror
     bool fz_ran = false;           // the last evaluation ran the fused pipeline
     // terms of an evaluation whose energies have not been collected yet
@@ -928,6 +930,9 @@ void fz_tables(ofdft_eval* e) {
     OFDFT_CK(cudaMallocHost(&e->h_fz_err, sizeof(unsigned)));
     *e->h_fz_err = 0;
     upload_now(e->d_fz_err, e->h_fz_err, sizeof(unsigned));
+    OFDFT_CK(cudaStreamCreateWithFlags(&e->fz_st2, cudaStreamNonBlocking));
+    OFDFT_CK(cudaEventCreateWithFlags(&e->fz_fork, cudaEventDisableTiming));
+    OFDFT_CK(cudaEventCreateWithFlags(&e->fz_join, cudaEventDisableTiming));
 }
 
 struct FzRun {
@@ -970,7 +975,9 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     const FzTab tb = fz_tab(r.tab);
     const size_t cb = g->cplx_bytes();
     const bool mc = r.kdd == 3;  // M planes feed pot3 only
-    const int per_node = mc ? 2 : 1;
+    // planes per node: P (and M) for the C2R chain, one more for the R2C chain,
+    // which runs on a second stream at the same time and needs its own planes
+    const int per_node = (mc ? 2 : 1) + (r.kdd > 1 ? 1 : 0);
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     int B = c.lwt_max_batch > 0 ? c.lwt_max_batch : 64;
@@ -978,7 +985,18 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     const long long fit = (long long)(0.5 * (double)freeb) / (long long)(per_node * cb);
     if (fit < B) B = (int)std::max(1LL, fit);
     B = std::min(B, r.m);
-    float2* XY = (float2*)e->sc.get("lwtXY", (size_t)per_node * B * cb);
+    float2* XY = (float2*)e->sc.get("lwtXY", (size_t)(mc ? 2 : 1) * B * cb);
+    float2* XY2 = r.kdd > 1 ? (float2*)e->sc.get("lwtXY2", (size_t)B * cb) : nullptr;
+    // the R2C chain (hat planes -> pot2) does not depend on the C2R chain (node
+    // planes -> pot1/pot3): fork it onto the second stream, join before return.
+    // With per-kernel profiling on, both chains stay on st so that each
+    // kernel's events time that kernel alone.
+    const bool two = r.kdd > 1 && !e->prof;
+    cudaStream_t st2 = two ? e->fz_st2 : st;
+    if (two) {
+        OFDFT_CK(cudaEventRecord(e->fz_fork, st));
+        OFDFT_CK(cudaStreamWaitEvent(st2, e->fz_fork, 0));
+    }
     const double Ncd = (double)g->Nc, Nd = (double)g->N;
     const float invN = (float)(1.0 / Nd);
     const int tiles0 = n1 * (H / kFzLines) + n1 / kFzLines;
@@ -1049,36 +1067,43 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         });
         launches += mc ? 5 : 3;
         if (r.kdd > 1) {
-            // ---- R2C: hat-weighted rho^alpha along axis 2, then axis 1, then axis 0 into pot2(G)
+            // ---- R2C on the second stream: hat-weighted rho^alpha along axis 2, then axis 1,
+            // then axis 0 into pot2(G)
+            FzRowArgs ra2 = ra;
+            ra2.XY = XY2;
             with_row(H, [&](auto ch) {
                 constexpr int HH = decltype(ch)::value;
                 constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
                 const size_t smem = fz_row_smem(HH, r.m, false);
                 const int grid = (int)((long long)n0 * n1 / ROWS);
                 fz_smem_optin(k_fz_r2c_rows<HH>, smem);
-                timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st,
-                      [&] { k_fz_r2c_rows<HH><<<grid, kFzRowThreads, smem, st>>>(ra); });
+                timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st2,
+                      [&] { k_fz_r2c_rows<HH><<<grid, kFzRowThreads, smem, st2>>>(ra2); });
             });
             OFDFT_LAUNCH_CHECK();
             with_col(n1, [&](auto c1) {
                 constexpr int N1 = decltype(c1)::value;
                 const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
-                timed(e, P_FZ_AXIS1, Ncd * 16.0 * nb, st,
-                      [&] { k_fz_axis1<N1, -1><<<tiles1 * nb, N1, smem, st>>>(XY, d, tw.t1); });
+                timed(e, P_FZ_AXIS1, Ncd * 16.0 * nb, st2,
+                      [&] { k_fz_axis1<N1, -1><<<tiles1 * nb, N1, smem, st2>>>(XY2, d, tw.t1); });
             });
             OFDFT_LAUNCH_CHECK();
             with_col(n0, [&](auto c0) {
                 constexpr int N0 = decltype(c0)::value;
                 const size_t smem = fz_col_smem(N0, nb, false);
                 fz_smem_optin(k_fz_pot2<N0>, smem);
-                timed(e, P_LWT_POT2, Ncd * 8.0 * (nb + (first ? 1 : 2)), st, [&] {
-                    k_fz_pot2<N0><<<tiles0, kFzLines * (N0 / kFzColE), smem, st>>>(
-                        XY, r.pot2G, tb, knode, invk, j0, nb, first ? 1 : 0, g->geo, d, tw.t0, invN);
+                timed(e, P_LWT_POT2, Ncd * 8.0 * (nb + (first ? 1 : 2)), st2, [&] {
+                    k_fz_pot2<N0><<<tiles0, kFzLines * (N0 / kFzColE), smem, st2>>>(
+                        XY2, r.pot2G, tb, knode, invk, j0, nb, first ? 1 : 0, g->geo, d, tw.t0, invN);
                 });
             });
             OFDFT_LAUNCH_CHECK();
             launches += 3;
         }
+    }
+    if (two) {
+        OFDFT_CK(cudaEventRecord(e->fz_join, st2));
+        OFDFT_CK(cudaStreamWaitEvent(st, e->fz_join, 0));
     }
     return launches;
 }
@@ -1514,6 +1539,9 @@ void ofdft_eval_destroy(ofdft_eval* e) {
     if (e->d_nodes) cudaFree(e->d_nodes);
     if (e->h_nodes) cudaFreeHost(e->h_nodes);
     if (e->fz_tw) cudaFree(e->fz_tw);
+    if (e->fz_st2) cudaStreamDestroy(e->fz_st2);
+    if (e->fz_fork) cudaEventDestroy(e->fz_fork);
+    if (e->fz_join) cudaEventDestroy(e->fz_join);
     if (e->d_fz_err) cudaFree(e->d_fz_err);
     if (e->h_fz_err) cudaFreeHost(e->h_fz_err);
     for (auto ev : e->evs) cudaEventDestroy(ev);

@@ -679,6 +679,7 @@ struct BTab {
     int red_blocks;  // the system grid's reduction block count
     int boff;        // first block of the system in a reduction launch
     int eoff, eb;    // first block and block count in an elementwise launch
+    double dV;
 };
 
 // per-system coefficients and the active mask, passed by value
@@ -686,6 +687,61 @@ struct BArgs {
     double c[kBatchMax][3];
     unsigned char act[kBatchMax];
 };
+
+// Device-resident scalars of the batch, kSc rows of kBatchMax: dot results,
+// L-BFGS coefficients and the per-system coefficients of the next field update,
+// so that the two-loop recursion and the normalisations run without the host.
+constexpr int kHist = kBF;  // alpha_i of the two-loop, by pair position
+enum ScRow { SC_D0 = 0, SC_D1, SC_NE, SC_MU, SC_NEL, SC_C0, SC_C1, SC_C2, SC_AL0, SC_LBRHO0 = SC_AL0 + kHist,
+             kSc = SC_LBRHO0 + kBF };
+
+__device__ __forceinline__ double* scrow(double* sc, int r) { return sc + (size_t)r * kBatchMax; }
+
+// one thread per system; op selects the scalar update (the same float64
+// operations, in the same order, as the host code of optimize_t)
+enum ScOp { OP_AL, OP_B, OP_LBRHO, OP_ORTH_F, OP_ORTH_N, OP_MU };
+template <typename T>
+__global__ void k_bscalar(const BTab<T>* __restrict__ tab, BArgs a, double* sc, int S, int op, int i, int slot) {
+    const int s = threadIdx.x;
+    if (s >= S || !a.act[s]) return;
+    const double dV = tab[s].dV;
+    const double d0 = scrow(sc, SC_D0)[s], d1 = scrow(sc, SC_D1)[s];
+    double c0 = 1.0, c1 = 0.0;
+    switch (op) {
+        case OP_AL: {  // alpha_i = rho_i (s_i . q); q -= alpha_i y_i
+            const double al = __dmul_rn(scrow(sc, SC_LBRHO0 + slot)[s], d0);
+            scrow(sc, SC_AL0 + i)[s] = al;
+            c1 = -al;
+            break;
+        }
+        case OP_B:  // beta = rho_i (y_i . p); p += (alpha_i - beta) s_i
+            c1 = __dsub_rn(scrow(sc, SC_AL0 + i)[s], __dmul_rn(scrow(sc, SC_LBRHO0 + slot)[s], d0));
+            break;
+        case OP_LBRHO:  // rho = 1 / (y . s)
+            scrow(sc, SC_LBRHO0 + slot)[s] = 1.0 / d0;
+            return;
+        case OP_ORTH_F: {  // Ne = (phi.phi) dV; p -= ((p.phi) dV / Ne) phi
+            const double ne = __dmul_rn(d0, dV);
+            scrow(sc, SC_NE)[s] = ne;
+            c1 = -(__dmul_rn(d1, dV) / ne);
+            break;
+        }
+        case OP_ORTH_N:  // p *= sqrt(Ne / ((p.p) dV))
+            c0 = sqrt(scrow(sc, SC_NE)[s] / __dmul_rn(d0, dV));
+            break;
+        case OP_MU: {  // Nel = sum(rho) dV; mu = (V.rho) dV / Nel
+            const double nel = __dmul_rn(d0, dV);
+            const double mu = __dmul_rn(d1, dV) / nel;
+            scrow(sc, SC_NEL)[s] = nel;
+            scrow(sc, SC_MU)[s] = mu;
+            c0 = mu;
+            break;
+        }
+    }
+    scrow(sc, SC_C0)[s] = c0;
+    scrow(sc, SC_C1)[s] = c1;
+    scrow(sc, SC_C2)[s] = 0.0;
+}
 
 template <typename T>
 __global__ void k_blincomb(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a, int o, int x0,
@@ -749,6 +805,35 @@ __global__ void k_bresid(const BTab<T>* __restrict__ tab, const int* __restrict_
     if (!a.act[s]) return;
     const BTab<T>& t = tab[s];
     const T m = (T)a.c[s][0];
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        t.f[BF_RSD][i] = mul_rn(sub_rn(t.f[BF_V][i], m), t.f[BF_PHI][i]);
+}
+
+// k_blincomb with the coefficients read from the device scalars
+template <typename T>
+__global__ void k_blincomb_dc(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a,
+                              const double* __restrict__ sc, int o, int x0, int x1) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T b0 = (T)sc[SC_C0 * kBatchMax + s], b1 = (T)sc[SC_C1 * kBatchMax + s];
+    T* out = t.f[o];
+    const T* X0 = t.f[x0];
+    const T* X1 = x1 >= 0 ? t.f[x1] : nullptr;
+    const long long stride = (long long)t.eb * blockDim.x;
+    for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
+        out[i] = lin3(b0, X0, b1, X1, (T)0, (const T*)nullptr, i);
+}
+
+// rsd = (V - mu) phi with mu from the device scalars
+template <typename T>
+__global__ void k_bresid_dc(const BTab<T>* __restrict__ tab, const int* __restrict__ esys, BArgs a,
+                            const double* __restrict__ sc) {
+    const int s = esys[blockIdx.x];
+    if (!a.act[s]) return;
+    const BTab<T>& t = tab[s];
+    const T m = (T)sc[SC_MU * kBatchMax + s];
     const long long stride = (long long)t.eb * blockDim.x;
     for (long long i = (long long)(blockIdx.x - t.eoff) * blockDim.x + threadIdx.x; i < t.N; i += stride)
         t.f[BF_RSD][i] = mul_rn(sub_rn(t.f[BF_V][i], m), t.f[BF_PHI][i]);
@@ -861,6 +946,7 @@ struct Batch {
         cudaFree(d_esys);
         cudaFree(d_part);
         cudaFree(d_out);
+        cudaFree(d_sc);
         cudaFreeHost(h_out);
     }
 
@@ -887,6 +973,7 @@ struct Batch {
             t.eoff = (int)esys.size();
             for (int b = 0; b < t.eb; ++b) esys.push_back(s);
             t.f[BF_RHOIO] = (T*)rho_io[s];
+            t.dV = g[s]->dV;
             static const char* names[] = {"", "phi", "V", "res", "p", "nphi", "nrho", "nV", "old_phi", "res_prev",
                                           "lb_q", "rho"};
             for (int f = 1; f < BF_LB0; ++f) t.f[f] = field(s, names[f]);
@@ -900,6 +987,8 @@ struct Batch {
         OFDFT_CK(cudaMalloc(&d_part, (size_t)nb_red * sizeof(double)));
         OFDFT_CK(cudaMalloc(&d_out, (size_t)kMaxRound * S * sizeof(double)));
         OFDFT_CK(cudaMallocHost(&h_out, (size_t)kMaxRound * S * sizeof(double)));
+        OFDFT_CK(cudaMalloc(&d_sc, (size_t)kSc * kBatchMax * sizeof(double)));
+        OFDFT_CK(cudaMemsetAsync(d_sc, 0, (size_t)kSc * kBatchMax * sizeof(double), st));
         OFDFT_CK(cudaMemcpyAsync(d_tab, h_tab.data(), S * sizeof(BTab<T>), cudaMemcpyHostToDevice, st));
         OFDFT_CK(cudaMemcpyAsync(d_bsys, bsys.data(), nb_red * sizeof(int), cudaMemcpyHostToDevice, st));
         OFDFT_CK(cudaMemcpyAsync(d_esys, esys.data(), nb_el * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -991,6 +1080,40 @@ struct Batch {
         OFDFT_LAUNCH_CHECK();
         return finish_row();
     }
+    // device-only reductions: the result stays in device scalar row `row`
+    double* d_sc = nullptr;  // kSc x kBatchMax
+    void fin_dev(int row) {
+        k_bfinalize<T><<<S, RED_THREADS, 0, st>>>(d_tab, args, d_part, d_sc + (size_t)row * kBatchMax);
+        OFDFT_LAUNCH_CHECK();
+    }
+    void dot_dev(int xa, int xb, int row) {
+        k_bdot2<T><<<nb_red, RED_THREADS, 0, st>>>(d_tab, d_bsys, args, xa, xb, d_part);
+        OFDFT_LAUNCH_CHECK();
+        fin_dev(row);
+    }
+    void sum_dev(int xa, int row) {
+        k_bsum<T><<<nb_red, RED_THREADS, 0, st>>>(d_tab, d_bsys, args, xa, d_part);
+        OFDFT_LAUNCH_CHECK();
+        fin_dev(row);
+    }
+    void scalar(int op, int i = 0, int slot = 0) {
+        k_bscalar<T><<<1, kBatchMax, 0, st>>>(d_tab, args, d_sc, S, op, i, slot);
+        OFDFT_LAUNCH_CHECK();
+    }
+    void lincomb_dc(int o, int x0, int x1 = -1) {
+        k_blincomb_dc<T><<<nb_el, 256, 0, st>>>(d_tab, d_esys, args, d_sc, o, x0, x1);
+        OFDFT_LAUNCH_CHECK();
+    }
+    // OrthogonalNormalization (optimization.py:205-226) without the host
+    void orth_norm_dev() {
+        dot_dev(BF_PHI, BF_PHI, SC_D0);
+        dot_dev(BF_P, BF_PHI, SC_D1);
+        scalar(OP_ORTH_F);
+        lincomb_dc(BF_P, BF_P, BF_PHI);
+        dot_dev(BF_P, BF_P, SC_D0);
+        scalar(OP_ORTH_N);
+        lincomb_dc(BF_P, BF_P);
+    }
     // one device-to-host copy of the queued rows and one synchronisation
     void sync() {
         if (rows) OFDFT_CK(cudaMemcpyAsync(h_out, d_out, (size_t)rows * S * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1022,6 +1145,7 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
     std::vector<int> conv(S, 2), niter(S, 0), nfev(S, 1);
     std::vector<std::vector<double>> Ehist(S);
     std::vector<double> dP(S, 0.0);
+    std::vector<char> accepted_any(S, 0);  // mu then lives in the device scalars
     auto active = [&](const std::vector<char>& m) { b.set_active(m); };
     auto any = [](const std::vector<char>& m) { return std::any_of(m.begin(), m.end(), [](char c) { return c != 0; }); };
     auto evaluate = [&](const std::vector<char>& m, int xrho, int xV) {
@@ -1045,24 +1169,6 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
                 eval_collect(b.e[s], En);
                 out[s] = En[OFDFT_E_TOTAL];
             }
-    };
-    auto orth_norm = [&](const std::vector<char>& m) {
-        // OrthogonalNormalization (optimization.py:205-226)
-        active(m);
-        const int rNe = b.dot(BF_PHI, BF_PHI), rf = b.dot(BF_P, BF_PHI);
-        b.sync();
-        std::vector<double> Ne(S, 1.0);
-        for (int s = 0; s < S; ++s)
-            if (m[s]) {
-                Ne[s] = b.at(rNe, s) * dV[s];
-                b.coef(s, 1.0, -(b.at(rf, s) * dV[s] / Ne[s]));
-            }
-        b.lincomb(BF_P, BF_P, BF_PHI);
-        const int rp = b.dot(BF_P, BF_P);
-        b.sync();
-        for (int s = 0; s < S; ++s)
-            if (m[s]) b.coef(s, std::sqrt(Ne[s] / (b.at(rp, s) * dV[s])));
-        b.lincomb(BF_P, BF_P);
     };
     // ---- start (optimize_t: phi = sqrt(rho) renormalised, first evaluation, mu, residual)
     active(run);
@@ -1094,62 +1200,55 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         int s, y;
     };
     std::deque<Pair> lb;
-    std::vector<std::deque<double>> lbrho(S);
     int pool_i = 0;
     for (int it = 1; it < o.maxiter && any(run); ++it) {
         for (int s = 0; s < S; ++s)
             if (run[s]) niter[s] = it;
         active(run);
-        // ---- direction: get_direction_LBFGS (optimization.py:150-171), first loop skips i = 0
+        // ---- direction: get_direction_LBFGS (optimization.py:150-171), first loop skips i = 0;
+        // the dot products and coefficients stay on the device
         for (int s = 0; s < S; ++s) b.coef(s, -1.0);
         b.lincomb(BF_Q, BF_RSD);
         const int m = (int)lb.size();
-        std::vector<std::vector<double>> al(S, std::vector<double>(m, 0.0));
         for (int i = m - 1; i > 0; --i) {
-            const int r = b.dot(lb[i].s, BF_Q);
-            b.sync();
-            for (int s = 0; s < S; ++s)
-                if (run[s]) {
-                    al[s][i] = lbrho[s][i] * b.at(r, s);
-                    b.coef(s, 1.0, -al[s][i]);
-                }
-            b.lincomb(BF_Q, BF_Q, lb[i].y);
+            b.dot_dev(lb[i].s, BF_Q, SC_D0);
+            b.scalar(OP_AL, i, lb[i].s - BF_LB0);
+            b.lincomb_dc(BF_Q, BF_Q, lb[i].y);
         }
         OFDFT_REQUIRE(o.h0 != 0.0, "ofdft_optimize_batch: h0 = 0 is not batched");
         for (int s = 0; s < S; ++s) b.coef(s, o.h0);
         b.lincomb(BF_P, BF_Q);
         for (int i = 0; i < m; ++i) {
-            const int r = b.dot(lb[i].y, BF_P);
-            b.sync();
-            for (int s = 0; s < S; ++s)
-                if (run[s]) b.coef(s, 1.0, al[s][i] - lbrho[s][i] * b.at(r, s));
-            b.lincomb(BF_P, BF_P, lb[i].s);
+            b.dot_dev(lb[i].y, BF_P, SC_D0);
+            b.scalar(OP_B, i, lb[i].s - BF_LB0);
+            b.lincomb_dc(BF_P, BF_P, lb[i].s);
         }
-        orth_norm(run);
-        // uphill: steepest descent (optimization.py:373-380)
+        b.orth_norm_dev();
+        // uphill: steepest descent (optimization.py:373-380); otherwise this dtheta is g0
+        std::vector<double> g0(S, 0.0);
         {
-            active(run);
             for (int s = 0; s < S; ++s) b.coef(s, 1.0, 0.0);
             const int r = b.dtheta(BF_V, BF_PHI);
             b.sync();
             std::vector<char> up(S, 0);
-            for (int s = 0; s < S; ++s) up[s] = run[s] && b.at(r, s) * 2.0 > 0;
+            for (int s = 0; s < S; ++s) {
+                up[s] = run[s] && b.at(r, s) * 2.0 > 0;
+                g0[s] = 2.0 * b.at(r, s) * dV[s];
+            }
             if (any(up)) {
                 active(up);
                 for (int s = 0; s < S; ++s) b.coef(s, -1.0);
                 b.lincomb(BF_P, BF_RSD);
-                orth_norm(up);
+                b.orth_norm_dev();
+                for (int s = 0; s < S; ++s) b.coef(s, 1.0, 0.0);
+                const int r2 = b.dtheta(BF_V, BF_PHI);
+                b.sync();
+                for (int s = 0; s < S; ++s)
+                    if (up[s]) g0[s] = 2.0 * b.at(r2, s) * dV[s];
+                active(run);
             }
         }
         // ---- line search on theta: scalar_search_wolfe1 per system, evaluations batched
-        std::vector<double> g0(S, 0.0);
-        {
-            active(run);
-            for (int s = 0; s < S; ++s) b.coef(s, 1.0, 0.0);
-            const int r = b.dtheta(BF_V, BF_PHI);
-            b.sync();
-            for (int s = 0; s < S; ++s) g0[s] = 2.0 * b.at(r, s) * dV[s];
-        }
         std::vector<Dcsrch> ls(S);
         std::vector<double> stp(S, 1.0), f(S), gd(S), lastE(S, NAN), last_theta(S, NAN);
         std::vector<int> nls(S, 0), lsit(S, 0);
@@ -1221,6 +1320,7 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
                 continue;
             }
             acc[s] = 1;
+            accepted_any[s] = 1;
         }
         if (!any(acc)) break;
         // ---- accept
@@ -1229,27 +1329,19 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         b.copy(BF_PHI, BF_NPHI);
         b.copy(BF_V, BF_NV);
         b.square(BF_PHI, BF_RHO);
-        {
-            const int rn = b.sum(BF_RHO), rm = b.dot(BF_V, BF_RHO);
-            b.sync();
-            for (int s = 0; s < S; ++s)
-                if (acc[s]) {
-                    E[s] = lastE[s];
-                    Nel[s] = b.at(rn, s) * dV[s];
-                    mu[s] = b.at(rm, s) * dV[s] / Nel[s];
-                }
-        }
+        for (int s = 0; s < S; ++s)
+            if (acc[s]) E[s] = lastE[s];
+        b.sum_dev(BF_RHO, SC_D0);
+        b.dot_dev(BF_V, BF_RHO, SC_D1);
+        b.scalar(OP_MU);
         b.copy(BF_RESPREV, BF_RSD);
-        for (int s = 0; s < S; ++s) b.coef(s, mu[s]);
-        k_bresid<T><<<b.nb_el, 256, 0, st>>>(b.d_tab, b.d_esys, b.args);
+        k_bresid_dc<T><<<b.nb_el, 256, 0, st>>>(b.d_tab, b.d_esys, b.args, b.d_sc);
         OFDFT_LAUNCH_CHECK();
         // LBFGS.update (math_utils.py:307-325): at most maxcor+1 pairs
         Pair pr;
-        bool popped = false;
         if ((int)lb.size() > o.maxcor) {
             pr = lb.front();
             lb.pop_front();
-            popped = true;
         } else {
             pr.s = BF_LB0 + pool_i++;
             pr.y = BF_LB0 + pool_i++;
@@ -1257,13 +1349,13 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         for (int s = 0; s < S; ++s) b.coef(s, 1.0, -1.0);
         b.lincomb(pr.s, BF_PHI, BF_OLDPHI);
         b.lincomb(pr.y, BF_RSD, BF_RESPREV);
-        const int rys = b.dot(pr.y, pr.s), rres = b.dot(BF_RSD, BF_RSD);
+        b.dot_dev(pr.y, pr.s, SC_D0);
+        b.scalar(OP_LBRHO, 0, pr.s - BF_LB0);
+        const int rres = b.dot(BF_RSD, BF_RSD);
         b.sync();
         lb.push_back(pr);
         for (int s = 0; s < S; ++s) {
             if (!acc[s]) continue;
-            if (popped) lbrho[s].pop_front();
-            lbrho[s].push_back(1.0 / b.at(rys, s));
             Ehist[s].push_back(E[s]);
             dP[s] = b.at(rres, s) * dV[s];
             if (o.verbose)
@@ -1305,7 +1397,12 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         active(need_dp);
         rdp = b.dot(BF_RSD, BF_RSD);
     }
+    std::vector<double> mu_dev(kBatchMax, 0.0);
+    OFDFT_CK(cudaMemcpyAsync(mu_dev.data(), b.d_sc + (size_t)SC_MU * kBatchMax, kBatchMax * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
     b.sync();
+    for (int s = 0; s < S; ++s)
+        if (accepted_any[s]) mu[s] = mu_dev[s];
     for (int s = 0; s < S; ++s) {
         ofdft_opt_result& r = res[s];
         memset(&r, 0, sizeof(r));

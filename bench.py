@@ -411,6 +411,19 @@ def gpu_arm(args):
         print(json.dumps(out), flush=True)
 
 
+def warm_optimizer(D, tot, rho0, method="LBFGS"):
+    """One-iteration solves in FP64 and FP32 before any timed solve: the CUDA
+    runtime loads each kernel on its first launch (lazy module loading, about a
+    second for the optimiser's kernels on a fresh process), a one-time cost
+    that belongs to setup, not to a solve."""
+    import torch
+    for dtype in (torch.float64, torch.float32):
+        o = D.Optimization(EnergyEvaluator=tot, optimization_method=method,
+                           optimization_options={"econv": 1e-30, "maxiter": 1, "maxfun": 50})
+        o.optimize_rho(guess_rho=rho0, dtype=dtype)
+    torch.cuda.synchronize()
+
+
 def ground_state(D, tot, grid, rho_np, nat, method="LBFGS", econv_per_atom=1e-7, f32_factor=1.0):
     """Wall time of optimize_rho from the uniform density: plain FP64, and
     FP32-mixed (to the same econv rule) followed by either one FP64 E+V
@@ -422,6 +435,7 @@ def ground_state(D, tot, grid, rho_np, nat, method="LBFGS", econv_per_atom=1e-7,
     opts = {"econv": econv, "maxiter": 300, "maxfun": 50}
     res = {"method": method, "econv_Ha": econv, "econv_f32_Ha": f32_factor * econv}
     rho0 = D.DirectField(grid) + float(rho_np.mean())
+    warm_optimizer(D, tot, rho0, method)
     opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method, optimization_options=dict(opts))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -626,10 +640,11 @@ def c2_workload(args):
     displacements sigma = 0.10 Bohr), 128^3 grid, KEDF WT (TF + vW + WT,
     alpha = beta = 5/6) + LDA + Hartree + PME local PP, FP64.  GPU: E+V evals/s
     (rho resident, CUDA events), L-BFGS time to the ground state from the
-    uniform density (econv 1e-7 Ha/atom), PME Ewald energy+forces.  CPU (the
-    numpy restatement of the reference on this host, same inputs): one E+V, the
-    Ewald forces, and the ground state extrapolated from the GPU run's
-    evaluation count."""
+    uniform density (econv 1e-7 Ha/atom), PME Ewald energy+forces, and the
+    stress tensor of every term (TotalFunctional.get_stress, PME PP and Ewald).
+    CPU (the numpy restatement of the reference on this host, same inputs): one
+    E+V, the Ewald forces, the stress, and the ground state extrapolated from
+    the GPU run's evaluation count."""
     import torch
     import dftpy_gb300 as D
     from dftpy_gb300 import _lib
@@ -667,6 +682,7 @@ def c2_workload(args):
     e_gpu = float(E[_lib.E_TOTAL])
     # ground state
     rho0 = D.DirectField(grid) + 3.0 * nat / grid.volume
+    warm_optimizer(D, tot, rho0)
     opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
                          optimization_options={"econv": 1e-7 * nat, "maxiter": 500, "maxfun": 50})
     torch.cuda.synchronize()
@@ -679,6 +695,13 @@ def c2_workload(args):
     ew = D.ewald(ions=ions, grid=grid, PME=True)
     F_gpu = ew.forces
     t_ew = time.perf_counter() - t0
+    # stress of every term at the same density (warm once: plans, v_loc)
+    tot.get_stress(rho)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    S_gpu = tot.get_stress(rho, split=True)
+    torch.cuda.synchronize()
+    t_st = time.perf_counter() - t0
     # CPU: the numpy restatement on this host
     O.set_fft_workers(os.cpu_count() or 1)
     g = O.Grid(lat, (n, n, n))
@@ -694,15 +717,26 @@ def c2_workload(args):
     t0 = time.perf_counter()
     F_cpu = O.Ewald(g, pos, np.full(nat, 3.0), PME=True).forces()
     t_cpu_ew = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xc = O.lda(rho_np, g)
+    S_cpu = {"KEDF-TF": O.tf_stress(g, O.tf(rho_np, g, calc=("E",))["E"]), "KEDF-VW": O.vw_stress(rho_np, g),
+             "KEDF-NL": O.wt_stress(rho_np, g, wt(rho_np, g, calc=("E",))["E"]),
+             "XC": O.lda_stress(rho_np, g, xc["E"], xc["V"]),
+             "HARTREE": O.hartree_stress(rho_np, g, O.hartree(rho_np, g, calc=("E",))["E"]),
+             "PSEUDO": O.pp_stress(opp, rho_np), "II": O.ewald_stress(O.Ewald(g, pos, np.full(nat, 3.0), PME=True))}
+    t_cpu_st = time.perf_counter() - t0
+    st_err = max(float(np.abs(S_gpu[k] - v).max()) for k, v in S_cpu.items())
     out = {"workload": "c2: fcc Al 4x4x4 (256 atoms), 128^3, WT+LDA+Hartree+PME PP, FP64",
            "gpu": {"ev_per_s": 1e3 / ms_ev, "ms_per_ev": ms_ev, "ground_state_s": t_gs, "gs_niter": opt.result.niter,
-                   "gs_nfev": opt.result.nfev, "ewald_forces_s": t_ew},
+                   "gs_nfev": opt.result.nfev, "ewald_forces_s": t_ew, "stress_s": t_st},
            "cpu": {"cores": os.cpu_count(), "kind": "port", "ev_s": t_cpu_ev, "ev_per_s": 1.0 / t_cpu_ev,
-                   "ewald_forces_s": t_cpu_ew, "ground_state_s_extrapolated": opt.result.nfev * t_cpu_ev},
+                   "ewald_forces_s": t_cpu_ew, "stress_s": t_cpu_st,
+                   "ground_state_s_extrapolated": opt.result.nfev * t_cpu_ev},
            "speedup": {"ev": t_cpu_ev * 1e3 / ms_ev, "ground_state": opt.result.nfev * t_cpu_ev / t_gs,
-                       "ewald_forces": t_cpu_ew / t_ew},
+                       "ewald_forces": t_cpu_ew / t_ew, "stress": t_cpu_st / t_st},
            "parity": {"E_total_gpu_minus_cpu_Ha_excl_ewald": (e_gpu - float(E[_lib.E_II])) - e_cpu,
-                      "ewald_forces_max_abs": float(np.abs(F_gpu - F_cpu).max())}}
+                      "ewald_forces_max_abs": float(np.abs(F_gpu - F_cpu).max()),
+                      "stress_max_abs_Ha_per_Bohr3": st_err}}
     print(json.dumps(out), flush=True)
 
 

@@ -16,6 +16,7 @@ OK, EINVAL, ECUDA, ECUFFT, ENOMEM, ESTATE = range(6)
 F64, F32 = 0, 1
 CALC_E, CALC_V = 1, 2
 E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, NE = range(10)
+S_TF, S_VW, S_NL, S_XC, S_H, NS = range(6)
 KE_TF, KE_VW, KE_WT, KE_LWT = 1, 2, 4, 8
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
 LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
@@ -78,6 +79,7 @@ _SIGS = {
     "ofdft_eval_set_vloc": (_I, [_P, _P, _P]),
     "ofdft_eval_set_ewald": (_I, [_P, _D]),
     "ofdft_eval_compute": (_I, [_P, _P, _P, C.c_uint, _PD, _P]),
+    "ofdft_eval_stress": (_I, [_P, _P, _PD, _PD, _P]),
     "ofdft_eval_get_kfbounds": (_I, [_P, _PD, _PD]),
     "ofdft_eval_set_kfbounds": (_I, [_P, _D, _D]),
     "ofdft_eval_last_stats": (_I, [_P, _PI, _PI]),
@@ -89,8 +91,10 @@ _SIGS = {
     "ofdft_pseudo_set_ions": (_I, [_P, _I, _PD, _PI]),
     "ofdft_pseudo_vloc": (_I, [_P, _P, _P]),
     "ofdft_pseudo_forces": (_I, [_P, _P, _PD, _P]),
+    "ofdft_pseudo_stress": (_I, [_P, _P, _D, _PD, _P]),
     "ofdft_pseudo_vloc_grad": (_I, [_P, _P, _PD, _P]),
     "ofdft_ewald": (_I, [_P, _I, _PD, _PD, _D, _I, _I, _PD, _PD, _PD, _P]),
+    "ofdft_ewald_stress": (_I, [_P, _I, _PD, _PD, _D, _I, _I, _PD, _PD, _P]),
     "ofdft_opt_default": (None, [C.POINTER(OptOptions)]),
     "ofdft_optimize": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P]),
     "ofdft_optimize_v": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P, _P]),

@@ -5,6 +5,8 @@
 //   reciprocal smooth PME (Energy_rec_PME :786-807, Forces_rec_PME :810-864)
 //              or exact structure factors (Energy_rec :449-466, Forces_rec :580-607)
 //   correction Energy_corr (:468-482), on the host
+//   stress     Stress_real (:609-662) with the real-space sum; Stress_rec_PME
+//              (:915-968) or Stress_rec (:719-763) over the mask, G = 0 term
 #include "common.cuh"
 #include "host_math.h"
 #include "pme.cuh"
@@ -31,12 +33,14 @@ struct CellList {
 };
 
 // one thread per atom: sum over the (2K+1)^3 neighbour cells (unwrapped, so
-// each periodic image of each atom is visited exactly once)
+// each periodic image of each atom is visited exactly once).  Partials: the
+// energy sum, then the six sums of Stress_real (:645-654),
+// q_i q_j (2 sqrt(eta/pi) exp(-eta d^2) + erfc(sqrt(eta) d)/d) R_a R_b / d^2.
 __global__ void __launch_bounds__(RED_THREADS) k_ewald_real(const double* __restrict__ pos,
                                                             const double* __restrict__ q, int nat,
                                                             const double* __restrict__ lat, CellList cl, double Rcut,
                                                             double eta, double* F, double* partials) {
-    double acc[1] = {0.0};
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nat) {
         const double es = sqrt(eta);
@@ -45,6 +49,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_ewald_real(const double* __rest
         const int c = cl.cellof[i];
         const int c0 = c / (cl.nc[1] * cl.nc[2]), c1 = (c / cl.nc[2]) % cl.nc[1], c2 = c % cl.nc[2];
         double e = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+        double s6[6] = {0, 0, 0, 0, 0, 0};
+        const double sp2 = 2.0 * es / sqrt(M_PI);
         for (int d0 = -cl.K[0]; d0 <= cl.K[0]; ++d0)
             for (int d1 = -cl.K[1]; d1 <= cl.K[1]; ++d1)
                 for (int d2 = -cl.K[2]; d2 <= cl.K[2]; ++d2) {
@@ -69,16 +75,24 @@ __global__ void __launch_bounds__(RED_THREADS) k_ewald_real(const double* __rest
                             fx += dx * w;
                             fy += dy * w;
                             fz += dz * w;
+                            const double ws = q[j] * (sp2 * exp(-eta * d * d) + ec / d) / (d * d);
+                            s6[0] += ws * dx * dx;
+                            s6[1] += ws * dx * dy;
+                            s6[2] += ws * dx * dz;
+                            s6[3] += ws * dy * dy;
+                            s6[4] += ws * dy * dz;
+                            s6[5] += ws * dz * dz;
                         }
                     }
                 }
         acc[0] = q[i] * e;
+        for (int k = 0; k < 6; ++k) acc[1 + k] = q[i] * s6[k];
         const double e3 = es * es * es;
         F[3 * i] = q[i] * fx * e3;
         F[3 * i + 1] = q[i] * fy * e3;
         F[3 * i + 2] = q[i] * fz * e3;
     }
-    block_sum_store<1>(acc, partials);
+    block_sum_store<7>(acc, partials);
 }
 
 // PME reciprocal energy partials and the force convolution input:
@@ -136,6 +150,42 @@ __global__ void __launch_bounds__(RED_THREADS) k_ewald_rec_exact(const double* _
     block_sum_store<1>(acc, partials);
 }
 
+// Reciprocal stress sums over the mask (Stress_rec_PME :937-950, Stress_rec
+// :733-751): |S(G)|^2 exp(-G^2/4 eta)/G^2 (2 g_i g_j/G^2 (1 + G^2/4 eta) - delta_ij)
+// with S = FFT(Q) B (PME, raw transform) or the exact structure factor.
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_ewald_stress_rec(const typename Cplx<T>::type* __restrict__ QG,
+                                                                  const double* __restrict__ S, const double* bre,
+                                                                  const double* bim, Geo geo, double eta,
+                                                                  double* partials) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        if (!half_mask(geo, i)) continue;
+        double gx, gy, gz, gg;
+        gvec(geo, i, gx, gy, gz, gg);
+        double sr, si;
+        if (QG) {
+            double br, bi;
+            barray(bre, bim, geo, i, br, bi);
+            const double qr = (double)QG[i].x, qi = (double)QG[i].y;
+            sr = qr * br - qi * bi;
+            si = qr * bi + qi * br;
+        } else {
+            sr = S[2 * i];
+            si = S[2 * i + 1];
+        }
+        const double inv = (i == 0) ? 0.0 : 1.0 / gg;
+        const double w = (sr * sr + si * si) * exp(-gg / (4.0 * eta)) * inv;
+        const double f = 2.0 * inv * (1.0 + gg / (4.0 * eta));
+        const double g[3] = {gx, gy, gz};
+        int k = 0;
+        for (int a = 0; a < 3; ++a)
+            for (int b = a; b < 3; ++b, ++k) acc[k] += w * (g[a] * g[b] * f - (a == b ? 1.0 : 0.0));
+    }
+    block_sum_store<6>(acc, partials);
+}
+
 constexpr int kChunk = 8;
 
 // exact reciprocal forces for a chunk of atoms:
@@ -186,7 +236,7 @@ double best_eta(double precision, double gmax, const std::vector<double>& q) {
 
 template <typename T>
 void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision, int pme, int order,
-             double* out_energy, double* forces, double* out_eta, cudaStream_t st) {
+             double* out_energy, double* forces, double* out_eta, double* stress, cudaStream_t st) {
     using C = typename Cplx<T>::type;
     std::vector<double> q(charges, charges + nat);
     // gmax = sqrt(2 ecut), ecut from the grid spacing (grid.py:363-366, :722-723)
@@ -272,17 +322,20 @@ void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, d
     OFDFT_REQUIRE(ablk <= g->red_blocks * 32, "Ewald: too many atoms for the reduction buffer");
     k_ewald_real<<<ablk, RED_THREADS, 0, st>>>(d_pos, d_q, nat, d_lat, cl, Rcut, eta, d_Fr, g->d_partials);
     OFDFT_LAUNCH_CHECK();
-    reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, ablk, 1, 0ull, g->d_results);
+    reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, ablk, 7, 0ull, g->d_results);
     OFDFT_LAUNCH_CHECK();
-    OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, sizeof(double), cudaMemcpyDeviceToHost, st));
+    OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
     OFDFT_CK(cudaStreamSynchronize(st));
     const double e_real = g->h_results[0] / 2.0;
+    double s_real[6];
+    for (int k = 0; k < 6; ++k) s_real[k] = g->h_results[1 + k] * (-0.5 / g->volume);
     std::vector<double> Freal(3 * (size_t)nat);
     OFDFT_CK(cudaMemcpyAsync(Freal.data(), d_Fr, 3 * (size_t)nat * sizeof(double), cudaMemcpyDeviceToHost, st));
     OFDFT_CK(cudaStreamSynchronize(st));
 
     // ---- reciprocal space
     double e_rec = 0.0;
+    double s_rec[6] = {0, 0, 0, 0, 0, 0};
     std::vector<double> Frec(3 * (size_t)nat, 0.0);
     const size_t cb = g->cplx_bytes(), rb = g->real_bytes();
     if (pme) {
@@ -304,6 +357,15 @@ void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, d
         OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, sizeof(double), cudaMemcpyDeviceToHost, st));
         OFDFT_CK(cudaStreamSynchronize(st));
         e_rec = 4.0 * M_PI * g->h_results[0] / g->volume;
+        if (stress) {
+            k_ewald_stress_rec<T><<<g->red_blocks, RED_THREADS, 0, st>>>(QG, nullptr, bre, bim, g->geo, eta,
+                                                                         g->d_partials);
+            OFDFT_LAUNCH_CHECK();
+            reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, 6, 0ull, g->d_results);
+            OFDFT_LAUNCH_CHECK();
+            OFDFT_CK(cudaMemcpyAsync(s_rec, g->d_results, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            OFDFT_CK(cudaStreamSynchronize(st));
+        }
         if (forces) {
             T* conv = (T*)sc.get("conv", rb);
             g->exec_c2r(X, conv, 1, st);
@@ -329,6 +391,15 @@ void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, d
         OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, sizeof(double), cudaMemcpyDeviceToHost, st));
         OFDFT_CK(cudaStreamSynchronize(st));
         e_rec = 4.0 * M_PI * g->h_results[0] / g->volume;
+        if (stress) {
+            k_ewald_stress_rec<T><<<g->red_blocks, RED_THREADS, 0, st>>>(nullptr, S, nullptr, nullptr, g->geo, eta,
+                                                                         g->d_partials);
+            OFDFT_LAUNCH_CHECK();
+            reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, 6, 0ull, g->d_results);
+            OFDFT_LAUNCH_CHECK();
+            OFDFT_CK(cudaMemcpyAsync(s_rec, g->d_results, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            OFDFT_CK(cudaStreamSynchronize(st));
+        }
         if (forces) {
             for (int a0 = 0; a0 < nat; a0 += kChunk) {
                 const int na = std::min(kChunk, nat - a0);
@@ -352,34 +423,63 @@ void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, d
     out_energy[3] = e_corr;
     if (forces)
         for (size_t k = 0; k < 3 * (size_t)nat; ++k) forces[k] = Freal[k] + Frec[k];
+    if (stress) {
+        // both reciprocal forms reduce to 4 pi / V^2 times the mask sums (the PME
+        // form's 2 x 2 pi / V^2 / dV^2 with the dV^2 of its transforms); the G = 0
+        // term (sum q)^2 4 pi / (8 eta V^2) sits on the diagonal
+        const double V2 = g->volume * g->volume;
+        const double sg0 = qs * qs * 4.0 * M_PI * (1.0 / (4.0 * eta * V2) / 2.0);
+        static const int I[6] = {0, 0, 0, 1, 1, 2}, J[6] = {0, 1, 2, 1, 2, 2};
+        for (int k = 0; k < 6; ++k) {
+            double v = s_real[k] + s_rec[k] * 4.0 * M_PI / V2;
+            if (I[k] == J[k]) v += sg0;
+            stress[3 * I[k] + J[k]] = stress[3 * J[k] + I[k]] = v;
+        }
+    }
 }
 
 }  // namespace
 
+// both precisions run the Ewald sums in float64: an FP32 grid gets a float64
+// twin for the PME mesh, built for this call only
+static void ewald_any(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision, int pme,
+               int bspline_order, double* out_energy, double* forces, double* out_eta, double* stress,
+               cudaStream_t st) {
+    OFDFT_REQUIRE(g && pos && charges && nat >= 1, "ofdft_ewald: bad argument");
+    OFDFT_REQUIRE(precision > 0.0 && precision < 1.0, "ofdft_ewald: precision must be in (0, 1)");
+    OFDFT_REQUIRE(!pme || (bspline_order >= 3 && bspline_order <= kMaxOrder), "B-spline order must be 3..%d",
+                  kMaxOrder);
+    if (g->prec == OFDFT_F64) {
+        ewald_t<double>(g, nat, pos, charges, precision, pme, bspline_order, out_energy, forces, out_eta, stress, st);
+        return;
+    }
+    ofdft_grid* gd = nullptr;
+    int rc = ofdft_grid_create(g->nr, g->lattice, OFDFT_F64, &gd);
+    if (rc != OFDFT_OK) throw Error{rc};
+    try {
+        ewald_t<double>(gd, nat, pos, charges, precision, pme, bspline_order, out_energy, forces, out_eta, stress, st);
+    } catch (...) {
+        ofdft_grid_destroy(gd);
+        throw;
+    }
+    ofdft_grid_destroy(gd);
+}
+
 extern "C" int ofdft_ewald(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision, int pme,
                            int bspline_order, double* out_energy, double* forces, double* out_eta, ofdft_stream s) {
     return guard([&] {
-        OFDFT_REQUIRE(g && pos && charges && out_energy && nat >= 1, "ofdft_ewald: bad argument");
-        OFDFT_REQUIRE(precision > 0.0 && precision < 1.0, "ofdft_ewald: precision must be in (0, 1)");
-        OFDFT_REQUIRE(!pme || (bspline_order >= 3 && bspline_order <= kMaxOrder), "B-spline order must be 3..%d",
-                      kMaxOrder);
-        // Ewald sums are float64 in both precisions: an FP32 grid gets a float64
-        // twin for the PME mesh, built for this call only.
-        if (g->prec == OFDFT_F64) {
-            ewald_t<double>(g, nat, pos, charges, precision, pme, bspline_order, out_energy, forces, out_eta,
-                            (cudaStream_t)s);
-        } else {
-            ofdft_grid* gd = nullptr;
-            int rc = ofdft_grid_create(g->nr, g->lattice, OFDFT_F64, &gd);
-            if (rc != OFDFT_OK) throw Error{rc};
-            try {
-                ewald_t<double>(gd, nat, pos, charges, precision, pme, bspline_order, out_energy, forces, out_eta,
-                                (cudaStream_t)s);
-            } catch (...) {
-                ofdft_grid_destroy(gd);
-                throw;
-            }
-            ofdft_grid_destroy(gd);
-        }
+        OFDFT_REQUIRE(out_energy, "ofdft_ewald: null energy output");
+        ewald_any(g, nat, pos, charges, precision, pme, bspline_order, out_energy, forces, out_eta, nullptr,
+                  (cudaStream_t)s);
+    });
+}
+
+extern "C" int ofdft_ewald_stress(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision,
+                                  int pme, int bspline_order, double* stress, double* out_eta, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(stress, "ofdft_ewald_stress: null stress output");
+        double energy[4];
+        ewald_any(g, nat, pos, charges, precision, pme, bspline_order, energy, nullptr, out_eta, stress,
+                  (cudaStream_t)s);
     });
 }

@@ -198,6 +198,92 @@ __global__ void k_pp_grad_moments(const typename Cplx<T>::type* __restrict__ rho
     }
 }
 
+// dv_s/dq: the derivative of the species' spline (splev der=1) below max(gp),
+// 0 above (_PP_Derivative_One, pseudo/__init__.py:454-460).  Unlike the
+// potential lines this uses the spline down to q = 0 (its first piece extended
+// below gp[1]); the quartic near q = 0 is not differentiated.
+__device__ inline double vline_deriv(const Line& L, double q) {
+    if (!(q < L.gplast)) return 0.0;
+    int lo = 0, hi = L.n - 1;  // largest i with x[i] <= q, clamped to [0, n-2]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (L.x[mid] <= q) lo = mid;
+        else hi = mid;
+    }
+    const double u = q - L.x[lo];
+    const double* c = L.c + 4 * (long long)lo;
+    return c[1] + u * (2.0 * c[2] + u * 3.0 * c[3]);
+}
+
+__device__ __forceinline__ void sym6(double gx, double gy, double gz, double (&t)[6]) {
+    t[0] = gx * gx;
+    t[1] = gx * gy;
+    t[2] = gx * gz;
+    t[3] = gy * gy;
+    t[4] = gy * gz;
+    t[5] = gz * gz;
+}
+
+// PME stress sums of one species over the mask (_StressPME :590-600, raw
+// transforms): g_i g_j Re(conj(rho(G)) B(G) Q_s(G)) v_s'(|G|) / |G|
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pp_stress_pme(const typename Cplx<T>::type* __restrict__ rhoG,
+                                                               const typename Cplx<T>::type* __restrict__ QG, Line L,
+                                                               const double* bre, const double* bim, Geo geo,
+                                                               double* partials) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        if (!half_mask(geo, i)) continue;
+        double gx, gy, gz, gg;
+        gvec(geo, i, gx, gy, gz, gg);
+        const double q = sqrt(gg);
+        const double invq = (i == 0) ? 0.0 : 1.0 / q;
+        double br, bi;
+        barray(bre, bim, geo, i, br, bi);
+        const double rr = (double)rhoG[i].x, ri = (double)rhoG[i].y;
+        const double xr = rr * br + ri * bi, xi = rr * bi - ri * br;  // conj(rho) B
+        const double re = (xr * (double)QG[i].x - xi * (double)QG[i].y) * vline_deriv(L, q) * invq;
+        double t[6];
+        sym6(gx, gy, gz, t);
+        for (int k = 0; k < 6; ++k) acc[k] += t[k] * re;
+    }
+    block_sum_store<6>(acc, partials);
+}
+
+// exact stress sums over the mask (_Stress :479-503, _PP_Derivative :462-477):
+// g_i g_j Re(rho(G) sum_a v_{s(a)}'(|G|) e^{i G.R_a}) / |G|
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pp_stress_exact(const typename Cplx<T>::type* __restrict__ rhoG,
+                                                                 Lines LS, const double* __restrict__ pos,
+                                                                 const int* __restrict__ spec, int nat, Geo geo,
+                                                                 double* partials) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        if (!half_mask(geo, i)) continue;
+        double gx, gy, gz, gg;
+        gvec(geo, i, gx, gy, gz, gg);
+        const double q = sqrt(gg);
+        const double invq = (i == 0) ? 0.0 : 1.0 / q;
+        double dv[kMaxSpecies];
+        for (int s = 0; s < LS.ns; ++s) dv[s] = vline_deriv(LS.s[s], q);
+        double vr = 0.0, vi = 0.0;
+        for (int a = 0; a < nat; ++a) {
+            const double ph = gx * pos[3 * a] + gy * pos[3 * a + 1] + gz * pos[3 * a + 2];
+            double sn, cs;
+            sincos(ph, &sn, &cs);
+            vr += dv[spec[a]] * cs;
+            vi += dv[spec[a]] * sn;
+        }
+        const double re = ((double)rhoG[i].x * vr - (double)rhoG[i].y * vi) * invq;
+        double t[6];
+        sym6(gx, gy, gz, t);
+        for (int k = 0; k < 6; ++k) acc[k] += t[k] * re;
+    }
+    block_sum_store<6>(acc, partials);
+}
+
 // exact structure factor of one species, S_s(G) = sum_{a in s} exp(-i G.R_a), as a complex field
 template <typename T>
 __global__ void k_strf_species(typename Cplx<T>::type* S, const double* __restrict__ pos, const int* __restrict__ sel,
@@ -400,6 +486,61 @@ void forces_t(ofdft_pseudo* p, const T* rho, double* F, cudaStream_t st) {
 }
 
 template <typename T>
+void stress_t(ofdft_pseudo* p, const T* rho, double energy, double* S, cudaStream_t st) {
+    ofdft_grid* g = p->g;
+    using C = typename Cplx<T>::type;
+    const size_t cb = g->cplx_bytes(), rb = g->real_bytes();
+    const double V = g->volume, dV = g->dV;
+    if (std::isnan(energy)) {  // E_PP = int v_loc rho dV (LocalPseudo.__call__)
+        T* v = (T*)p->sc.get("st_v", rb);
+        vloc_t<T>(p, v, st);
+        double d = 0.0;
+        const int rc = ofdft_dot(g, v, rho, &d, st);
+        if (rc != OFDFT_OK) throw Error{rc};
+        energy = d * dV;
+    }
+    C* rhoG = (C*)p->sc.get("rhoG", cb);
+    g->exec_r2c(rho, rhoG, 1, st);
+    double sum6[6] = {0, 0, 0, 0, 0, 0};
+    auto fetch6 = [&] {
+        reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, 6, 0ull, g->d_results);
+        OFDFT_LAUNCH_CHECK();
+        OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+        for (int k = 0; k < 6; ++k) sum6[k] += g->h_results[k];
+    };
+    double scale;
+    if (p->pme) {
+        T* Q = (T*)p->sc.get("Q", rb);
+        C* QG = (C*)p->sc.get("QG", cb);
+        for (int s = 0; s < p->ns; ++s) {
+            const int n_s = p->sel_off[s + 1] - p->sel_off[s];
+            if (n_s == 0) continue;
+            OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
+            k_pme_spread<T><<<n_s, 256, 0, st>>>(p->d_frac, nullptr, p->d_sel + p->sel_off[s], p->order, g->geo, Q);
+            OFDFT_LAUNCH_CHECK();
+            g->exec_r2c(Q, QG, 1, st);
+            k_pp_stress_pme<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rhoG, QG, p->line(s), p->d_bre, p->d_bim,
+                                                                      g->geo, g->d_partials);
+            OFDFT_LAUNCH_CHECK();
+            fetch6();
+        }
+        // rho and Q in the reference carry dV each; times 2 nnrR, over V^2 (:598-603)
+        scale = -2.0 * (double)g->N * dV * dV / (V * V);
+    } else {
+        k_pp_stress_exact<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rhoG, p->lines(), p->d_pos, p->d_spec, p->nat,
+                                                                    g->geo, g->d_partials);
+        OFDFT_LAUNCH_CHECK();
+        fetch6();
+        scale = -2.0 * dV / V;  // rho carries dV; -2/V (:498-499)
+    }
+    static const int I[6] = {0, 0, 0, 1, 1, 2}, J[6] = {0, 1, 2, 1, 2, 2};
+    for (int k = 0; k < 6; ++k) S[3 * I[k] + J[k]] = S[3 * J[k] + I[k]] = sum6[k] * scale;
+    for (int d = 0; d < 3; ++d) S[4 * d] -= energy;
+    for (int k = 0; k < 9; ++k) S[k] /= V;
+}
+
+template <typename T>
 void vloc_grad_t(ofdft_pseudo* p, const T* rho, double* grad, cudaStream_t st) {
     ofdft_grid* g = p->g;
     using C = typename Cplx<T>::type;
@@ -575,6 +716,15 @@ int ofdft_pseudo_vloc(ofdft_pseudo* p, void* vreal_out, ofdft_stream s) {
         OFDFT_REQUIRE(p->nat > 0, "ofdft_pseudo_vloc: no ions set");
         if (p->g->prec == OFDFT_F64) vloc_t<double>(p, (double*)vreal_out, (cudaStream_t)s);
         else vloc_t<float>(p, (float*)vreal_out, (cudaStream_t)s);
+    });
+}
+
+int ofdft_pseudo_stress(ofdft_pseudo* p, const void* rho, double energy, double* stress, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(p && rho && stress, "ofdft_pseudo_stress: null argument");
+        OFDFT_REQUIRE(p->nat > 0, "ofdft_pseudo_stress: no ions set");
+        if (p->g->prec == OFDFT_F64) stress_t<double>(p, (const double*)rho, energy, stress, (cudaStream_t)s);
+        else stress_t<float>(p, (const float*)rho, energy, stress, (cudaStream_t)s);
     });
 }
 

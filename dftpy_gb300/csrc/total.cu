@@ -67,6 +67,38 @@ __device__ inline M pz(int k) {
     return sizeof(M) == 8 ? (M)cPZ[k] : (M)cPZf[k];
 }
 
+// Constants of the built-in LDA in the working precision M
+template <typename M>
+struct LdaC {
+    M rs, ex, vx, tiny;
+    M P[7];
+    __device__ explicit LdaC(const Consts& k)
+        : rs((M)k.lda_rs), ex((M)k.lda_ex), vx((M)k.lda_vx), tiny((M)1e-30) {
+        for (int i = 0; i < 7; ++i) P[i] = pz<M>(i);
+    }
+};
+
+// Slater exchange + PZ81 correlation energy per electron ex and potential vx
+// at density r (xc/semilocal_xc.py:283-319)
+template <typename M>
+__device__ __forceinline__ void lda_point(M r, const LdaC<M>& c, M& ex, M& vx) {
+    M rc = mcbrt(r);
+    if (rc < c.tiny) rc = c.tiny;
+    const M Rs = c.rs / rc;
+    const M* P = c.P;
+    if (Rs < (M)1) {
+        const M lr = mlog(Rs);
+        ex = c.ex * rc + (P[0] * lr + P[1] + P[2] * Rs * lr + P[3] * Rs);
+        vx = c.vx * rc +
+             (lr * (P[0] + (M)(2.0 / 3) * P[2] * Rs) + P[1] - (M)(1.0 / 3) * P[0] + (M)(1.0 / 3) * (2 * P[3] - P[2]) * Rs);
+    } else {
+        const M sRs = msqrt(Rs);
+        const M den = (M)1 + P[5] * sRs + P[6] * Rs;
+        ex = c.ex * rc + P[4] / den;
+        vx = c.vx * rc + (P[4] + ((M)(7.0 / 6.0) * P[4] * P[5]) * sRs + ((M)(4.0 / 3.0) * P[4] * P[6] * Rs)) / (den * den);
+    }
+}
+
 template <typename T>
 struct PreArgs {
     const T* rho;
@@ -120,10 +152,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
     M kfmin = (M)INFINITY, kfmax = -(M)INFINITY, rmax = -(M)INFINITY;
     const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2};
     const M cTF_E = (M)a.k.cTF_E, cTF_V = (M)a.k.cTF_V, tf_x = (M)a.tf_x;
-    const M lda_rs = (M)a.k.lda_rs, lda_ex = (M)a.k.lda_ex, lda_vx = (M)a.k.lda_vx;
+    const LdaC<M> lc(a.k);
     const M threepi2 = (M)a.k.threepi2, alpha = (M)a.alpha, beta = (M)a.beta;
-    const M P0 = pz<M>(0), P1 = pz<M>(1), P2 = pz<M>(2), P3 = pz<M>(3), P4 = pz<M>(4), P5 = pz<M>(5),
-            P6 = pz<M>(6);
     const M tiny = (M)1e-30, zero_clamp = (M)kZERO;
     const long long stride = (long long)gridDim.x * blockDim.x;
 #pragma unroll 2
@@ -142,23 +172,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
             if (a.wantV) v += cTF_V * mcbrt(r * r) * tf_x;
         }
         if (a.xc) {
-            // built-in LDA, Slater exchange + PZ81 (xc/semilocal_xc.py:283-319)
-            M rc = mcbrt(r);
-            if (rc < tiny) rc = tiny;
-            const M Rs = lda_rs / rc;
             M ex, vx;
-            if (Rs < (M)1) {
-                const M lr = mlog(Rs);
-                ex = lda_ex * rc + (P0 * lr + P1 + P2 * Rs * lr + P3 * Rs);
-                vx = lda_vx * rc +
-                     (lr * (P0 + (M)(2.0 / 3) * P2 * Rs) + P1 - (M)(1.0 / 3) * P0 + (M)(1.0 / 3) * (2 * P3 - P2) * Rs);
-            } else {
-                const M sRs = msqrt(Rs);
-                const M den = (M)1 + P5 * sRs + P6 * Rs;
-                ex = lda_ex * rc + P4 / den;
-                vx = lda_vx * rc +
-                     (P4 + ((M)(7.0 / 6.0) * P4 * P5) * sRs + ((M)(4.0 / 3.0) * P4 * P6 * Rs)) / (den * den);
-            }
+            lda_point(r, lc, ex, vx);
             sum[1].add(ex * r);
             v += vx;
         }
@@ -1463,6 +1478,262 @@ void collect_energies(ofdft_eval* e, double* energies) {
     e->last_launches = p.launches;
 }
 
+// ------------------------------------------------------------------ stress
+// Stress tensors of the evaluator's terms (TotalFunctional.get_stress,
+// total_functional.py:176-208): TF (kedf/tf.py:52-63), vW (kedf/vw.py:97-111),
+// WT (kedf/wt.py:75-106), LDA (xc/semilocal_xc.py:343-346) and Hartree
+// (hartree.py:67-90).  Components k = 0..5 are (0,0) (0,1) (0,2) (1,1) (1,2)
+// (2,2), the reference's loop order.
+
+// LindhardDerivative(eta, mu) * eta (kedf/kernel.py:197-211); the two
+// boundary values eta = 1e-10 and |eta - 1| = 1e-10 fall in no branch (0).
+__device__ inline double lindhard_deriv_eta(double eta, double mu) {
+    const double atol = 1.0e-10;
+    double ld = 0.0;
+    if (eta > atol && fabs(eta - 1.0) > atol) {
+        const double A = log(fabs((1.0 + eta) / (1.0 - eta)));
+        const double den = 0.5 + 0.25 * (1.0 - eta * eta) / eta * A;
+        ld = (0.5 / eta - 0.25 * (eta * eta + 1.0) / (eta * eta) * A) / (den * den) + 6.0 * eta * mu;
+    } else if (eta < atol) {
+        ld = -2.0 * eta * (1.0 / 3.0 - 3.0 * mu);
+    } else if (fabs(eta - 1.0) < atol) {
+        ld = -48.0;
+    }
+    return ld * eta;
+}
+
+template <typename T>
+struct StressPointArgs {
+    const T* rho;
+    T* ra;  // rho^alpha (WT), or nullptr
+    T* rb;  // rho^beta (WT, alpha != beta), or nullptr
+    long long N;
+    double alpha, beta;
+    int xc;
+    Consts k;
+};
+
+// rho^alpha, rho^beta as the reference's stress raises them (no clamp), the
+// LDA sum of v_xc(rho) rho and the sum of rho (two float64 partials per block)
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_stress_point(StressPointArgs<T> a, double* partials) {
+    using M = T;
+    RunSum<M> vr, rs;
+    const LdaC<M> lc(a.k);
+    const M alpha = (M)a.alpha, beta = (M)a.beta;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += stride) {
+        const M r = a.rho[i];
+        rs.add(r);
+        if (a.ra) a.ra[i] = mpow(r, alpha);
+        if (a.rb) a.rb[i] = mpow(r, beta);
+        if (a.xc) {
+            M ex, vx;
+            lda_point(r, lc, ex, vx);
+            vr.add(vx * r);
+        }
+    }
+    double acc[2] = {vr.get(), rs.get()};
+    block_sum_store<2>(acc, partials);
+}
+
+__device__ __forceinline__ void sym6(double gx, double gy, double gz, double (&t)[6]) {
+    t[0] = gx * gx;
+    t[1] = gx * gy;
+    t[2] = gx * gz;
+    t[3] = gy * gy;
+    t[4] = gy * gz;
+    t[5] = gz * gz;
+}
+
+// Sums over the half-space mask: [0..5] g_i g_j |rho(G)|^2 / G^4 (Hartree),
+// [6..11] (g_i g_j / G^2 - delta_ij / 3) L'(|G| / tkf) Re(A conj B) (WT,
+// A = FFT(rho^alpha), B = FFT(rho^beta)); raw transforms.
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_stress_gspace(const typename Cplx<T>::type* __restrict__ rhoG,
+                                                               const typename Cplx<T>::type* __restrict__ aG,
+                                                               const typename Cplx<T>::type* __restrict__ bG, Geo geo,
+                                                               double tkf, double mu, double* partials) {
+    double acc[12];
+    for (int k = 0; k < 12; ++k) acc[k] = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < geo.Nc; i += stride) {
+        if (!half_mask(geo, i)) continue;
+        double gx, gy, gz, gg;
+        gvec(geo, i, gx, gy, gz, gg);
+        const double inv = (i == 0) ? 0.0 : 1.0 / gg;
+        double t[6];
+        sym6(gx, gy, gz, t);
+        if (rhoG) {
+            const double rr = (double)rhoG[i].x, ri = (double)rhoG[i].y;
+            const double w = (rr * rr + ri * ri) * inv * inv;
+            for (int k = 0; k < 6; ++k) acc[k] += t[k] * w;
+        }
+        if (aG) {
+            const double ar = (double)aG[i].x, ai = (double)aG[i].y;
+            const double br = (double)bG[i].x, bi = (double)bG[i].y;
+            const double w = lindhard_deriv_eta(sqrt(gg) / tkf, mu) * (ar * br + ai * bi);
+            for (int k = 0; k < 6; ++k) {
+                const double f = (k == 0 || k == 3 || k == 5) ? 1.0 / 3.0 : 0.0;
+                acc[6 + k] += (t[k] * inv - f) * w;
+            }
+        }
+    }
+    block_sum_store<12>(acc, partials);
+}
+
+// X_d = i g_d FFT(rho) / N for d = 0, 1, 2 (three planes, one after the
+// other).  The reference transforms these with numpy's irfftn, which keeps
+// only the Hermitian part of the k2 = 0 and k2 = n2/2 planes; on those planes
+// a Nyquist frequency index therefore counts as zero here, so that any C2R
+// gives numpy's result.
+template <typename T>
+__global__ void k_stress_grad(const typename Cplx<T>::type* __restrict__ rhoG, typename Cplx<T>::type* X, Geo geo,
+                              double invN) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < geo.Nc; idx += stride) {
+        const int k = (int)(idx % geo.n2h);
+        const long long t = idx / geo.n2h;
+        const int j = (int)(t % geo.n1);
+        const int i = (int)(t / geo.n1);
+        const bool edge = k == 0 || (geo.n2 % 2 == 0 && k == geo.n2 / 2);
+        double f0 = (double)freq_index(i, geo.n0), f1 = (double)freq_index(j, geo.n1), f2 = (double)k;
+        if (edge) {
+            if (geo.n0 % 2 == 0 && i == geo.n0 / 2) f0 = 0.0;
+            if (geo.n1 % 2 == 0 && j == geo.n1 / 2) f1 = 0.0;
+            if (geo.n2 % 2 == 0 && k == geo.n2 / 2) f2 = 0.0;
+        }
+        f0 *= geo.fv[0];
+        f1 *= geo.fv[1];
+        f2 *= geo.fv[2];
+        const double g[3] = {f0 * geo.b[0] + f1 * geo.b[3] + f2 * geo.b[6], f0 * geo.b[1] + f1 * geo.b[4] + f2 * geo.b[7],
+                             f0 * geo.b[2] + f1 * geo.b[5] + f2 * geo.b[8]};
+        const double rr = (double)rhoG[idx].x * invN, ri = (double)rhoG[idx].y * invN;
+        for (int d = 0; d < 3; ++d) {
+            X[d * geo.Nc + idx].x = (T)(-g[d] * ri);
+            X[d * geo.Nc + idx].y = (T)(g[d] * rr);
+        }
+    }
+}
+
+// sum_r d_i rho d_j rho / rho over the grid (six components)
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_stress_vw(const T* __restrict__ rho, const T* __restrict__ D,
+                                                           long long N, double* partials) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += stride) {
+        const double r = (double)rho[i];
+        const double dx = (double)D[i], dy = (double)D[N + i], dz = (double)D[2 * N + i];
+        double t[6];
+        sym6(dx, dy, dz, t);
+        for (int k = 0; k < 6; ++k) acc[k] += t[k] / r;
+    }
+    block_sum_store<6>(acc, partials);
+}
+
+void put6(double* S, const double* v6, double scale) {
+    static const int I[6] = {0, 0, 0, 1, 1, 2}, J[6] = {0, 1, 2, 1, 2, 2};
+    for (int k = 0; k < 6; ++k) S[3 * I[k] + J[k]] = S[3 * J[k] + I[k]] = v6[k] * scale;
+}
+
+template <typename T>
+void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cudaStream_t st) {
+    using C = typename Cplx<T>::type;
+    ofdft_grid* g = e->g;
+    const ofdft_config& c = e->cfg;
+    OFDFT_REQUIRE(!(c.kedf_terms & OFDFT_KE_LWT), "'LWT' has not implemented.");
+    double E[OFDFT_NE];
+    if (energies) std::copy(energies, energies + OFDFT_NE, E);
+    else compute_t<T>(e, rho, nullptr, OFDFT_CALC_E, E, st);
+    for (int i = 0; i < OFDFT_NS * 9; ++i) S[i] = 0.0;
+    const double V = g->volume, dV = g->dV, N = (double)g->N;
+    const bool vw = c.kedf_terms & OFDFT_KE_VW, wt = c.kedf_terms & OFDFT_KE_WT;
+    const bool xc = c.xc_lda != 0, h = c.hartree != 0;
+    const size_t cb = g->cplx_bytes(), rb = g->real_bytes();
+    const int gblk = blocks_for(g->Nc, 256, g->sms * 16);
+    auto fetch = [&](int nblk, int ns) {
+        reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, nblk, ns, 0ull, g->d_results);
+        OFDFT_LAUNCH_CHECK();
+        OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+    };
+    // TF: -2/3 E/V on the diagonal
+    if (c.kedf_terms & OFDFT_KE_TF)
+        for (int d = 0; d < 3; ++d) S[OFDFT_S_TF * 9 + 4 * d] = -2.0 / 3.0 * E[OFDFT_E_TF] / V;
+    // pointwise: rho^alpha / rho^beta, sum v_xc rho, sum rho
+    const bool same_ab = c.wt_alpha == c.wt_beta;
+    T* ra = wt ? (T*)e->sc.get("st_ra", rb) : nullptr;
+    T* rbeta = (wt && !same_ab) ? (T*)e->sc.get("st_rb", rb) : nullptr;
+    double rho0 = 0.0;
+    if (wt || xc) {
+        StressPointArgs<T> pa;
+        pa.rho = rho;
+        pa.ra = ra;
+        pa.rb = rbeta;
+        pa.N = g->N;
+        pa.alpha = c.wt_alpha;
+        pa.beta = c.wt_beta;
+        pa.xc = xc ? 1 : 0;
+        pa.k = e->k;
+        k_stress_point<T><<<g->red_blocks, RED_THREADS, 0, st>>>(pa, g->d_partials);
+        OFDFT_LAUNCH_CHECK();
+        fetch(g->red_blocks, 2);
+        rho0 = g->h_results[1] / N;  // rho.amean() (wt.py:77)
+        if (xc) {
+            const double P = E[OFDFT_E_XC] - g->h_results[0] * dV;
+            for (int d = 0; d < 3; ++d) S[OFDFT_S_XC * 9 + 4 * d] = P / V;
+        }
+    }
+    // G-space sums: Hartree and WT
+    C* rhoG = (h || vw) ? (C*)e->sc.get("st_rhoG", cb) : nullptr;
+    if (rhoG) g->exec_r2c(rho, rhoG, 1, st);
+    C *aG = nullptr, *bG = nullptr;
+    double tkf = 1.0;
+    if (wt) {
+        aG = (C*)e->sc.get("st_aG", cb);
+        g->exec_r2c(ra, aG, 1, st);
+        bG = aG;
+        if (!same_ab) {
+            bG = (C*)e->sc.get("st_bG", cb);
+            g->exec_r2c(rbeta, bG, 1, st);
+        }
+        tkf = 2.0 * std::pow(3.0 * rho0 * M_PI * M_PI, 1.0 / 3.0);  // wt.py:86
+    }
+    if (h || wt) {
+        k_stress_gspace<T><<<g->red_blocks, RED_THREADS, 0, st>>>(h ? rhoG : nullptr, aG, bG, g->geo, tkf, c.vw_y,
+                                                                   g->d_partials);
+        OFDFT_LAUNCH_CHECK();
+        fetch(g->red_blocks, 12);
+        const double* R = g->h_results;
+        if (h) {
+            // 8 pi / V^2 sum |rho_ref|^2 g_i g_j / G^4 with rho_ref = dV FFT(rho); -E_H/V on the diagonal
+            put6(S + OFDFT_S_H * 9, R, 8.0 * M_PI / (V * V) * dV * dV);
+            for (int d = 0; d < 3; ++d) S[OFDFT_S_H * 9 + 4 * d] -= E[OFDFT_E_H] / V;
+        }
+        if (wt) {
+            // DDrho = L' A_ref conj(B_ref) / V^2 = L' A conj(B) / N^2 (raw transforms), times
+            // pi^2 / (alpha beta rho0^(alpha+beta-2) tkf/2); -2/3 E_WT/V on the diagonal (wt.py:86-106)
+            const double pre = M_PI * M_PI /
+                               (c.wt_alpha * c.wt_beta * std::pow(rho0, c.wt_alpha + c.wt_beta - 2.0) * tkf / 2.0);
+            put6(S + OFDFT_S_NL * 9, R + 6, pre / (N * N));
+            for (int d = 0; d < 3; ++d) S[OFDFT_S_NL * 9 + 4 * d] -= 2.0 / 3.0 * E[OFDFT_E_NL] / V;
+        }
+    }
+    // vW: -(y/4) dV/V sum d_i rho d_j rho / rho
+    if (vw) {
+        C* X = (C*)e->sc.get("st_X", 3 * cb);
+        T* D = (T*)e->sc.get("st_D", 3 * rb);
+        k_stress_grad<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N);
+        OFDFT_LAUNCH_CHECK();
+        g->exec_c2r(X, D, 3, st);
+        k_stress_vw<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, D, g->N, g->d_partials);
+        OFDFT_LAUNCH_CHECK();
+        fetch(g->red_blocks, 6);
+        put6(S + OFDFT_S_VW * 9, g->h_results, -0.25 / V * dV * c.vw_y);
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1572,6 +1843,14 @@ int ofdft_eval_compute(ofdft_eval* e, const void* rho, void* v_out, unsigned cal
             compute_t<double>(e, (const double*)rho, (double*)v_out, calc, energies, (cudaStream_t)s);
         else
             compute_t<float>(e, (const float*)rho, (float*)v_out, calc, energies, (cudaStream_t)s);
+    });
+}
+
+int ofdft_eval_stress(ofdft_eval* e, const void* rho, const double* energies, double* stress, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && rho && stress, "ofdft_eval_stress: null argument");
+        if (e->g->prec == OFDFT_F64) stress_t<double>(e, (const double*)rho, energies, stress, (cudaStream_t)s);
+        else stress_t<float>(e, (const float*)rho, energies, stress, (cudaStream_t)s);
     });
 }
 

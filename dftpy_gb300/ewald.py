@@ -1,4 +1,4 @@
-"""Ewald ion-ion energy and forces (src/dftpy/ewald.py:197-864) on the device.
+"""Ewald ion-ion energy, forces and stress (src/dftpy/ewald.py:197-968) on the device.
 
 Sums are float64 in both precisions.  The real-space part is the exact image
 sum within the reference's cutoff, taken over a cell list; the reciprocal part
@@ -29,6 +29,7 @@ class ewald:
         self.PME = PME
         self._parts = None
         self._forces = None
+        self._stress = None
 
     def _run(self, want_forces):
         lib = _lib.load()
@@ -72,6 +73,22 @@ class ewald:
         if self._forces is None:
             self._run(True)
         return self._forces
+
+    @property
+    def stress(self):
+        """ewald.stress (:523-538): Stress_real + Stress_rec_PME or Stress_rec, 3x3 Ha/Bohr^3."""
+        if self._stress is None:
+            lib = _lib.load()
+            pos = np.ascontiguousarray(self.ions.positions, dtype=np.float64)
+            q = np.ascontiguousarray(self.ions.charges, dtype=np.float64)
+            S = np.zeros((3, 3))
+            eta = _lib.C.c_double()
+            _lib.check(lib.ofdft_ewald_stress(self.grid.native(_lib.F64), len(q), _lib.dptr(pos), _lib.dptr(q),
+                                              float(self.precision), 1 if self.PME else 0, int(self.order),
+                                              _lib.dptr(S), _lib.C.byref(eta), None))
+            self.eta = eta.value
+            self._stress = S
+        return self._stress
 
     def compute(self, *args, calcType={"E"}, **kwargs):
         from .functional.functional_output import FunctionalOutput

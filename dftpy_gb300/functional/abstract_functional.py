@@ -94,6 +94,24 @@ class NativeEval:
         return E.copy(), V
 
 
+    def stress(self, rho, energies=None):
+        """Stress tensors of the evaluator's terms, (NS, 3, 3) Ha/Bohr^3 (ofdft_eval_stress).
+        energies: array of NE term energies for the diagonal, or None to compute them on rho."""
+        r = rho.as_subclass(torch.Tensor) if isinstance(rho, torch.Tensor) else rho
+        if not r.is_contiguous():
+            r = r.contiguous()
+        S = np.zeros((_lib.NS, 3, 3))
+        e = None
+        if energies is not None:
+            e = np.ascontiguousarray(energies, dtype=np.float64)
+            if e.shape != (_lib.NE,):
+                raise ValueError("energies must hold %d values" % _lib.NE)
+        _lib.check(self.lib.ofdft_eval_stress(self.h, _lib.C.c_void_p(r.data_ptr()),
+                                              e.ctypes.data_as(_lib._PD) if e is not None else None,
+                                              S.ctypes.data_as(_lib._PD), stream_ptr()))
+        return S
+
+
 class AbstractFunctional(ABC):
     def __repr__(self):
         return getattr(self, "name", self.__class__.__name__)
@@ -156,6 +174,9 @@ class NativeFunctional(AbstractFunctional):
     def finish(self, ev):  # read back state after a compute
         pass
 
+    def absorb_energies(self, energies):  # state a functional keeps from an energy evaluation
+        pass
+
     def _evaluator(self, grid, dtype):
         cache = self.__dict__.setdefault("_evals", {})
         cfg = empty_config()
@@ -186,6 +207,13 @@ class NativeFunctional(AbstractFunctional):
             v._N = None
             out.potential = v
         return out
+
+    def _native_stress(self, density, energies=None):
+        """(NS, 3, 3) stress tensors of this functional's terms on density."""
+        rho = density if isinstance(density, DirectField) else as_field(self._grid_of(density), density)
+        ev = self._evaluator(rho.grid, rho.dtype)
+        self.prepare(ev, rho.grid, rho.dtype)
+        return ev.stress(rho, energies)
 
     def _grid_of(self, density):
         g = getattr(density, "grid", None) or getattr(self, "grid", None)

@@ -29,6 +29,12 @@ KEDFEngines = {
 }
 
 
+# engines with a stress (KEDFEngines_Stress, kedf/__init__.py:76-92): slot in the
+# stress and energy arrays of the native evaluator
+_STRESS = {"TF": (_lib.S_TF, _lib.E_TF), "VW": (_lib.S_VW, _lib.E_VW), "WT-NL": (_lib.S_NL, _lib.E_NL)}
+_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL")
+
+
 class KEDF(NativeFunctional):
     """KEDF(name, **options) with the reference's option names: x, y, alpha, beta,
     rho0 (WT); nsp, delta, ratio, kdd, interp, etamax, neta, kfmin, kfmax, ldw (LWT)."""
@@ -132,3 +138,31 @@ class KEDF(NativeFunctional):
             if "E" in calcType:
                 self.energies[e] = r.energy
         return out
+
+    def stress(self, density, name=None, kedf=None, split=False, **kwargs):
+        """KEDF.stress (kedf/__init__.py:193-234): per engine, ThomasFermiStress
+        (tf.py:52-63), vonWeizsackerStress (vw.py:97-111), WTStress (wt.py:75-106),
+        with the energies the functional cached by a split compute (computed on
+        this density when fewer than the engines are cached, as the reference does).
+        Names without a stress engine (the LWT family among them) raise
+        AttributeError, as the reference's name lookup does."""
+        if kedf:
+            name = kedf
+        if name is None:
+            name = self.name
+        name = name.upper()
+        if name not in _STRESS_NAMES:
+            raise AttributeError("'{}' has not implemented.".format(name))
+        engines = self.engines(name)
+        if len(self.energies) < len(engines):
+            self.compute(density, calcType={"E"}, name=name, split=True)
+        E = np.zeros(_lib.NE)
+        for e in engines:
+            E[_STRESS[e][1]] = self.energies[e]
+        sub = KEDF(name=name, **self.options)
+        sub.ke_kernel_saved = self.ke_kernel_saved
+        S = sub._native_stress(density, E)
+        out = {e: S[_STRESS[e][0]].copy() for e in engines}
+        if split:
+            return out
+        return sum(out.values(), np.zeros((3, 3)))

@@ -256,6 +256,21 @@ class LocalPseudo(NativeFunctional):
         _lib.check(_lib.load().ofdft_pseudo_forces(h, _lib.C.c_void_p(t.data_ptr()), _lib.dptr(F), stream_ptr()))
         return F
 
+    def stress(self, rho, energy=None):
+        """LocalPseudo.stress (:248-258): _StressPME (:573-611) or _Stress (:479-503);
+        energy None: E_PP = int v_loc rho dV of this density."""
+        if rho is None:
+            raise AttributeError("Must specify rho")
+        if not isinstance(rho, DirectField):
+            raise TypeError("rho must be DirectField")
+        h = self._handle(rho.dtype)
+        S = np.zeros((3, 3))
+        t = rho.as_subclass(torch.Tensor).contiguous()
+        _lib.check(_lib.load().ofdft_pseudo_stress(h, _lib.C.c_void_p(t.data_ptr()),
+                                                   float("nan") if energy is None else float(energy), _lib.dptr(S),
+                                                   stream_ptr()))
+        return S
+
     def vloc_grad(self, rho):
         """dE_PP/dvp: gradient of int v_loc rho dV with respect to every value of
         each species' radial table (keys as PP_list), from the device adjoint."""

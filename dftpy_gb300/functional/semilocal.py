@@ -1,5 +1,7 @@
 """XC (built-in LDA, src/dftpy/functional/xc/__init__.py:9-69 and
 xc/semilocal_xc.py:283-341) and Hartree (src/dftpy/functional/hartree.py:11-45)."""
+import numpy as np
+
 from .. import _lib
 from .abstract_functional import NativeFunctional
 
@@ -40,9 +42,22 @@ class XC(NativeFunctional):
             self.energy = out.energy
         return out
 
+    def absorb_energies(self, energies):
+        self.energy = float(energies[_lib.E_XC])
+
     def forces(self, density, pseudo=None, **kwargs):
         """NLCC forces: zero without core densities (xc/__init__.py:71-78)."""
         return None
+
+    def stress(self, density, pseudo=None, energy=None, **kwargs):
+        """XC.stress (xc/__init__.py:80-95) with _LDAStress (semilocal_xc.py:343-346):
+        (E - int v_xc rho dV)/V on the diagonal.  A given (nonzero) energy replaces
+        the one computed on density, as in the reference."""
+        E = None
+        if energy:
+            E = np.zeros(_lib.NE)
+            E[_lib.E_XC] = energy
+        return self._native_stress(density, E)[_lib.S_XC].copy()
 
 
 class Hartree(NativeFunctional):
@@ -67,6 +82,19 @@ class Hartree(NativeFunctional):
             Hartree._energy = out.energy
         return out
 
+    def absorb_energies(self, energies):
+        Hartree._energy = float(energies[_lib.E_H])
+
     @property
     def energy(self):
         return self._energy
+
+    def stress(self, density, **kwargs):
+        """Hartree.stress (hartree.py:51-56) with HartreeFunctionalStress (:67-90): the
+        energy is the one the class cached at its last energy evaluation, or computed
+        on density when there is none."""
+        E = None
+        if Hartree._energy is not None:
+            E = np.zeros(_lib.NE)
+            E[_lib.E_H] = Hartree._energy
+        return self._native_stress(density, E)[_lib.S_H].copy()

@@ -115,6 +115,11 @@ class TotalFunctional(AbstractFunctional):
         self.prepare(ev, rho.grid, rho.dtype)
         E, V = ev.compute(rho, calc)
         self.finish(ev)
+        if calc & _lib.CALC_E:
+            # what each functional's own energy evaluation leaves behind in the
+            # reference (the Hartree class energy, the XC energy)
+            for f in self.funcDict.values():
+                f.absorb_energies(E)
         out = FunctionalOutput(name="TOTAL", energy=float(E[_lib.E_TOTAL]) if calc & _lib.CALC_E else 0.0)
         if V is not None:
             v = V.as_subclass(DirectField)
@@ -168,3 +173,29 @@ class TotalFunctional(AbstractFunctional):
                 forces["II"] = fr
             forces["TOTAL"] = forces["TOTAL"] + fr
         return forces if split else forces["TOTAL"]
+
+    def get_stress(self, rho, split=False, **kwargs):
+        """total_functional.py:176-208: KEDF terms under "KEDF-<engine>", the other
+        functionals under their type, the Ewald stress under "II", and their sum
+        under "TOTAL"."""
+        stress = {"TOTAL": np.zeros((3, 3))}
+        for key, func in self.funcDict.items():
+            if func.type == "KEDF":
+                results = func.stress(rho, split=True)
+                for key2, v in results.items():
+                    stress["TOTAL"] = stress["TOTAL"] + v
+                    k = "KEDF-" + key2.split("-")[-1]
+                    stress[k] = stress.get(k, 0.0) + v
+            else:
+                v = func.stress(rho)
+                stress["TOTAL"] = stress["TOTAL"] + v
+                stress[func.type] = v
+        ew = self.ewald
+        if ew is not None:
+            stress["II"] = ew.stress
+            stress["TOTAL"] = stress["TOTAL"] + stress["II"]
+        T = stress["TOTAL"]
+        for i in range(1, 3):
+            for j in range(i - 1, -1, -1):
+                T[i, j] = T[j, i]
+        return stress if split else stress["TOTAL"]

@@ -42,6 +42,8 @@ enum { OFDFT_CALC_E = 1, OFDFT_CALC_V = 2 };
 /* energy slots written by ofdft_eval_compute (Hartree) */
 enum { OFDFT_E_TF = 0, OFDFT_E_VW, OFDFT_E_NL, OFDFT_E_XC, OFDFT_E_H, OFDFT_E_PP, OFDFT_E_II,
        OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_NE };
+/* stress tensors written by ofdft_eval_stress, 9 doubles (3 x 3, row-major) each */
+enum { OFDFT_S_TF = 0, OFDFT_S_VW, OFDFT_S_NL, OFDFT_S_XC, OFDFT_S_H, OFDFT_NS };
 
 /* ---------------------------------------------------------------- errors */
 const char* ofdft_last_error(void);
@@ -135,6 +137,21 @@ int ofdft_eval_set_ewald(ofdft_eval* e, double energy);
 int ofdft_eval_compute(ofdft_eval* e, const void* rho, void* v_out, unsigned calc,
                        double* energies, ofdft_stream s);
 
+/* Stress tensors (Ha/Bohr^3) of the evaluator's terms on density rho, the
+ * parts of TotalFunctional.get_stress (total_functional.py:176-208) that the
+ * evaluator owns: KEDF.stress (kedf/__init__.py:193-234) with TF
+ * (kedf/tf.py:52-63), vW (kedf/vw.py:97-111) and WT (kedf/wt.py:75-106);
+ * XC.stress with the built-in LDA (xc/__init__.py:80-95,
+ * xc/semilocal_xc.py:343-346); Hartree.stress (hartree.py:51-90).
+ * energies: the terms' energies that enter the diagonal (OFDFT_NE doubles, as
+ * ofdft_eval_compute writes them), or NULL to compute them on rho first (the
+ * reference uses the energies its functionals cached).  stress: OFDFT_NS x 9
+ * doubles, zero for terms not configured.  The local pseudopotential and Ewald
+ * terms come from ofdft_pseudo_stress and ofdft_ewald_stress.  With the
+ * density-dependent (LWT) kernel it fails with OFDFT_EINVAL, as the reference's
+ * KEDF.stress raises for 'LWT' (no stress engine, kedf/__init__.py:76-92). */
+int ofdft_eval_stress(ofdft_eval* e, const void* rho, const double* energies, double* stress, ofdft_stream s);
+
 /* Stateful parts of the evaluator that persist across calls like the
  * reference's ke_kernel_saved (kedf/__init__.py:101-111): the k_F bound state
  * of the LWT rule (kedf/lwt.py:36-79).  get/set allow checkpoint and restore. */
@@ -175,6 +192,11 @@ int ofdft_pseudo_forces(ofdft_pseudo* p, const void* rho, double* forces, ofdft_
  * species in order.  The reference has no counterpart (it offers no table
  * derivatives); the test pins it to finite differences of the oracle. */
 int ofdft_pseudo_vloc_grad(ofdft_pseudo* p, const void* rho, double* grad, ofdft_stream s);
+/* LocalPseudo.stress (:248-258): PME (_StressPME :573-611) or exact (_Stress
+ * :479-503), with the radial derivative of each species' spline
+ * (_PP_Derivative_One :454-460).  energy: E_PP = int v_loc rho dV, or NaN to
+ * compute it here.  stress: 9 doubles (3 x 3, row-major). */
+int ofdft_pseudo_stress(ofdft_pseudo* p, const void* rho, double energy, double* stress, ofdft_stream s);
 
 /* ---------------------------------------------------------------- Ewald
  * ewald (src/dftpy/ewald.py:197-864): eta from Get_Best_eta (:256-278),
@@ -184,6 +206,11 @@ int ofdft_pseudo_vloc_grad(ofdft_pseudo* p, const void* rho, double* grad, ofdft
 int ofdft_ewald(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision,
                 int pme, int bspline_order, double* out_energy, double* forces, double* out_eta,
                 ofdft_stream s);
+/* ewald.stress (ewald.py:523-538): Stress_real (:609-662) plus Stress_rec_PME
+ * (:915-968) or Stress_rec (:719-763), the G = 0 term included.  stress: 9
+ * doubles (3 x 3, row-major); out_eta may be NULL. */
+int ofdft_ewald_stress(ofdft_grid* g, int nat, const double* pos, const double* charges, double precision,
+                       int pme, int bspline_order, double* stress, double* out_eta, ofdft_stream s);
 
 /* ----------------------------------------------------------- optimiser
  * Optimization.optimize_rho (src/dftpy/optimization/optimization.py:283-525):

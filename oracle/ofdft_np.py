@@ -899,6 +899,193 @@ class Ewald:
 
 
 # --------------------------------------------------------------------------
+# stress (calcType 'S'): 3x3 tensors in Ha/Bohr^3
+# --------------------------------------------------------------------------
+_SYM6 = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+
+
+def tf_stress(grid, energy):
+    """ThomasFermiStress (kedf/tf.py:52-63): -2/3 E/V on the diagonal."""
+    return np.eye(3) * (-2.0 / 3.0 * energy / grid.volume)
+
+
+def vw_stress(rho, grid, y=1.0):
+    """vonWeizsackerStress (kedf/vw.py:97-111): -(y/4) dV/V sum d_i rho d_j rho / rho,
+    the gradients by irfftn of i g_i rho(G)."""
+    g = grid.g
+    rhoG = fft(rho, grid)
+    d = [ifft(1j * g[i] * rhoG, grid) for i in range(3)]
+    s = np.zeros((3, 3))
+    for i, j in _SYM6:
+        s[i, j] = s[j, i] = (-0.25 / grid.volume * grid.dV * np.einsum("ijk->", d[i] * d[j] / rho)).real * y
+    return s
+
+
+def lindhard_derivative(eta, mu):
+    """LindhardDerivative (kedf/kernel.py:197-211), returned times eta."""
+    eta = np.asarray(eta, dtype=np.float64)
+    out = np.zeros_like(eta)
+    atol = 1.0e-10
+    c0 = (eta > atol) & (np.abs(eta - 1.0) > atol)
+    c1 = eta < atol
+    c2 = np.abs(eta - 1.0) < atol
+    e = eta[c0]
+    A = np.log(np.abs((1.0 + e) / (1.0 - e)))
+    out[c0] = (0.5 / e - 0.25 * (e ** 2 + 1.0) / e ** 2 * A) / (0.5 + 0.25 * (1 - e ** 2) / e * A) ** 2 + 6.0 * e * mu
+    out[c1] = -2.0 * eta[c1] * (1.0 / 3.0 - 3.0 * mu)
+    out[c2] = -48
+    return out * eta
+
+
+def wt_stress(rho, grid, energy, y=1.0, alpha=5.0 / 6.0, beta=5.0 / 6.0):
+    """WTStress (kedf/wt.py:75-106) with rho0 = the mean density."""
+    rho0 = rho.sum() / grid.nnr
+    g, invgg, q, mask = grid.g, grid.invgg, grid.q, grid.mask
+    tkf = float(2.0 * (3.0 * rho0 * np.pi ** 2) ** (1.0 / 3.0))
+    rA = fft(rho ** alpha, grid) / grid.volume
+    rB = np.conjugate(fft(rho ** beta, grid)) / grid.volume
+    DD = lindhard_derivative(q / tkf, y) * rA * rB
+    s = np.zeros((3, 3))
+    for i, j in _SYM6:
+        fac = 1.0 / 3.0 if i == j else 0.0
+        den = (g[i][mask] * g[j][mask] * invgg[mask] - fac) * DD[mask]
+        s[i, j] = s[j, i] = np.einsum("i->", den).real
+    s *= np.pi ** 2 / (alpha * beta * rho0 ** (alpha + beta - 2) * tkf / 2.0)
+    for i in range(3):
+        s[i, i] -= 2.0 / 3.0 * energy / grid.volume
+    return s
+
+
+def lda_stress(rho, grid, energy, potential):
+    """_LDAStress (xc/semilocal_xc.py:343-346): (E - int v rho) / V on the diagonal."""
+    P = energy - np.sum(potential * rho) * grid.dV
+    return np.eye(3) * P / grid.volume
+
+
+def hartree_stress(rho, grid, energy):
+    """HartreeFunctionalStress (hartree.py:67-90)."""
+    g, invgg, mask = grid.g, grid.invgg, grid.mask
+    rhoG = fft(rho, grid)
+    rhoG2 = rhoG * np.conjugate(rhoG) * invgg * invgg
+    s = np.zeros((3, 3))
+    for i, j in _SYM6:
+        e = np.sum((g[i][mask] * g[j][mask]) * rhoG2[mask])
+        s[i, j] = s[j, i] = e.real * 8.0 * np.pi / grid.volume ** 2
+        if i == j:
+            s[i, j] -= energy / grid.volume
+    return s
+
+
+def vline_deriv(grid, gp, vp):
+    """_PP_Derivative_One (pseudo/__init__.py:454-460): splev(q, tck, der=1) of the
+    spline of ReadPseudo.get_vloc_interp (:689-706) below max(gp), 0 above."""
+    tck = splrep(gp[1:], vp[1:], k=3)
+    q = grid.q
+    out = np.zeros_like(q)
+    m = q < np.max(gp)
+    out[m] = splev(q[m], tck, der=1)
+    return out
+
+
+def _invq(grid):
+    q = grid.q.copy()  # grid.py:544-553: G = 0 -> 0
+    q[0, 0, 0] = 1.0
+    inv = 1.0 / q
+    inv[0, 0, 0] = 0.0
+    return inv
+
+
+def pp_stress(pp, rho, energy=None):
+    """LocalPseudo.stress (pseudo/__init__.py:248-258): _StressPME (:573-611) or
+    _Stress (:479-503).  ``pp`` is an oracle LocalPseudo."""
+    g = pp.grid
+    if energy is None:
+        energy = pp(rho, calc=("E",))["E"]
+    rhoG = fft(rho, g)
+    gv, mask, invq = g.g, g.mask, _invq(g)
+    s = np.zeros((3, 3))
+    if pp.PME:
+        rhoGB = np.conjugate(rhoG) * bspline_barray(g, pp.order)
+        frac = scaled_positions(pp.pos, g.lattice)
+        for sp_i, (gp, vp) in enumerate(pp.tables):
+            sel = pp.species == sp_i
+            if not sel.any():
+                continue
+            Q = pme_qarray(g, frac[sel], np.ones(sel.sum()), pp.order)
+            rhoGBV = rhoGB * vline_deriv(g, gp, vp) * fft(Q, g)
+            for i, j in _SYM6:
+                den = (gv[i][mask] * gv[j][mask]) * rhoGBV[mask] * invq[mask]
+                s[i, j] -= np.einsum("i->", den).real / g.volume ** 2
+        s *= 2.0 * g.nnr
+        for i in range(3):
+            for j in range(i, 3):
+                s[j, i] = s[i, j]
+            s[i, i] -= energy
+        return s / g.volume
+    v = np.zeros(tuple(g.nrG), dtype=np.complex128)
+    for sp_i, (gp, vp) in enumerate(pp.tables):
+        dv = vline_deriv(g, gp, vp)
+        for a in np.nonzero(pp.species == sp_i)[0]:
+            v += dv * np.exp(1j * np.einsum("lijk,l->ijk", gv, pp.pos[a]))
+    rGV = rhoG * v * invq
+    for i, j in _SYM6:
+        den = (gv[i][mask] * gv[j][mask]) * rGV[mask]
+        s[i, j] = s[j, i] = -np.einsum("i->", den).real / g.volume * 2.0
+        if i == j:
+            s[i, j] -= energy
+    return s / g.volume
+
+
+def _ewald_sfactor(grid, eta):
+    """The six sfactor planes of Stress_rec / Stress_rec_PME (ewald.py:738-745, :941-947)."""
+    gv, gg, invgg = grid.g, grid.gg, grid.invgg
+    out = []
+    for i, j in _SYM6:
+        f = gv[i] * gv[j] * 2.0 * invgg * (1 + gg / (4.0 * eta))
+        if i == j:
+            f = f - 1.0
+        out.append(f)
+    return out
+
+
+def ewald_stress(ew):
+    """ewald.stress (ewald.py:523-538): Stress_real (:609-662) + Stress_rec_PME
+    (:915-968) or Stress_rec (:719-763).  ``ew`` is an oracle Ewald."""
+    g = ew.grid
+    R, Rcut = ew._images()
+    es = np.sqrt(ew.eta)
+    S6 = np.zeros(6)
+    for ia in range(len(ew.pos)):
+        rj = (ew.pos[None, :, :] - R[:, None, :]).reshape(-1, 3)
+        qj = np.broadcast_to(ew.q[None, :], (len(R), len(ew.q))).ravel()
+        Rij = ew.pos[ia][None, :] - rj
+        d = np.sqrt((Rij * Rij).sum(-1))
+        m = (d < Rcut) & (d > 0.001)
+        Rij, d, qj = Rij[m], d[m], qj[m]
+        Rv = np.stack([Rij[:, i] * Rij[:, j] / d ** 2 for i, j in _SYM6], axis=1)
+        S6 += ew.q[ia] * np.einsum("i,ij->j", qj * (2 * es / np.sqrt(np.pi) * np.exp(-ew.eta * d ** 2)
+                                                    + sp.erfc(es * d) / d), Rv)
+    S6 *= -0.5 / g.volume
+    mask, gg, invgg = g.mask, g.gg, g.invgg
+    if ew.PME:
+        Q, _ = ew._qgrid()
+        strf = fft(Q, g) * bspline_barray(g, ew.order)
+        scale = 2.0 * 2.0 * np.pi / g.volume ** 2 / g.dV ** 2
+    else:
+        strf = np.zeros(tuple(g.nrG), dtype=np.complex128)
+        for a in range(len(ew.pos)):
+            strf += np.exp(-1j * np.einsum("lijk,l->ijk", g.g, ew.pos[a])) * ew.q[a]
+        scale = 4.0 * np.pi / g.volume ** 2
+    w = (np.conjugate(strf) * strf)[mask] * np.exp(-gg[mask] / (4.0 * ew.eta)) * invgg[mask]
+    rec6 = np.array([np.einsum("i,i->", w, f[mask]).real for f in _ewald_sfactor(g, ew.eta)]) * scale
+    sg0 = np.sum(ew.q) ** 2 * 4.0 * np.pi * (1.0 / (4.0 * ew.eta * g.volume ** 2) / 2.0)
+    s = np.zeros((3, 3))
+    for k, (i, j) in enumerate(_SYM6):
+        s[i, j] = s[j, i] = S6[k] + rec6[k] + (sg0 if i == j else 0.0)
+    return s
+
+
+# --------------------------------------------------------------------------
 # total functional
 # --------------------------------------------------------------------------
 class Total:

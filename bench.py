@@ -68,9 +68,9 @@ def parse():
     p.add_argument("--no-gs", action="store_true", help="skip the ground-state timing")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
-    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2"],
+    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2", "relax"],
                    help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems; "
-                        "c2: 256 atoms at 128^3, FP64 against the CPU restatement")
+                        "c2: 256 atoms at 128^3, FP64 against the CPU restatement; relax: calculator steps")
     return p.parse_args()
 
 
@@ -740,6 +740,107 @@ def c2_workload(args):
     print(json.dumps(out), flush=True)
 
 
+def relax_workload(args):
+    """Caller integration: the ASE-style calculator (dftpy_gb300.api.DFTpyCalculator)
+    relaxing fcc Al 4x4x4 (256 atoms, sigma = 0.10 Bohr, seed 256) at 128^3 with
+    WT + LDA + Hartree + PME PP in FP64 by ten steepest-descent steps.  Each step
+    moves the ions, rebuilds v_loc (PME) and the Ewald terms, re-optimises the
+    density from the previous ground state (L-BFGS, econv 1e-7 Ha/atom) and
+    evaluates energy, forces and stress; the density stays on the device.  CPU:
+    the oracle's time for the same work (E+V x evaluations of each step, PP and
+    Ewald forces and stresses, v_loc), measured once and summed over the steps."""
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import synthetic as syn
+    from dftpy_gb300.api import DFTpyCalculator
+    from dftpy_gb300.constants import BOHR
+    from oracle import ofdft_np as O
+
+    class Atoms:
+        def __init__(self, pos, cell):
+            self.pos, self.cell = pos, cell
+
+        def get_positions(self):
+            return self.pos.copy()
+
+        def get_cell(self):
+            return self.cell.copy()
+
+        def get_chemical_symbols(self):
+            return ["Al"] * len(self.pos)
+
+    torch.cuda.set_device(0)
+    n = 128
+    lat, pos = syn.fcc_supercell(7.60, 4, sigma=0.10, seed=256)
+    nat = len(pos)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    grid = D.DirectGrid(lat, (n, n, n))
+    ions = D.Ions(symbols=["Al"] * nat, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    rho0 = D.DirectField(grid) + 3.0 * nat / grid.volume
+    warm_optimizer(D, tot, rho0)
+    opts = {"econv": 1e-7 * nat, "maxiter": 500, "maxfun": 50}
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS", optimization_options=opts)
+    calc = DFTpyCalculator(evaluator=tot, rho=rho0, optimizer=opt)
+    atoms = Atoms(pos * BOHR, lat * BOHR)
+    steps = []
+    for it in range(11):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = calc.get_potential_energy(atoms)
+        f = calc.get_forces(atoms)
+        s = calc.get_stress(atoms)
+        torch.cuda.synchronize()
+        steps.append({"seconds": time.perf_counter() - t0, "energy_eV": e, "fmax_eV_per_A": float(np.abs(f).max()),
+                      "niter": opt.result.niter, "nfev": opt.result.nfev})
+        atoms.pos = atoms.pos + 0.01 * f
+    first, rest = steps[0], steps[1:]
+    t_step = float(np.mean([x["seconds"] for x in rest]))
+    nfev = float(np.mean([x["nfev"] for x in rest]))
+    # CPU: the oracle's time for one step's work on this host
+    O.set_fft_workers(os.cpu_count() or 1)
+    g = O.Grid(lat, (n, n, n))
+    rho_np = calc.dftpy_results["density"].as_subclass(torch.Tensor).double().cpu().numpy()
+    t0 = time.perf_counter()
+    opp = O.LocalPseudo(g, pos, np.zeros(nat, dtype=int), [(gp, vp)], PME=True)
+    opp.vreal
+    t_vloc = time.perf_counter() - t0
+    wt = O.WT()
+    t0 = time.perf_counter()
+    for fn in (O.tf, O.vw, O.lda, O.hartree):
+        fn(rho_np, g)
+    wt(rho_np, g)
+    opp(rho_np)
+    t_ev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    opp.forces(rho_np)
+    ew = O.Ewald(g, pos, np.full(nat, 3.0), PME=True)
+    ew.energy()
+    ew.forces()
+    xc = O.lda(rho_np, g)
+    O.tf_stress(g, O.tf(rho_np, g, calc=("E",))["E"])
+    O.vw_stress(rho_np, g)
+    O.wt_stress(rho_np, g, wt(rho_np, g, calc=("E",))["E"])
+    O.lda_stress(rho_np, g, xc["E"], xc["V"])
+    O.hartree_stress(rho_np, g, O.hartree(rho_np, g, calc=("E",))["E"])
+    O.pp_stress(opp, rho_np)
+    O.ewald_stress(ew)
+    t_fs = time.perf_counter() - t0
+    cpu_step = t_vloc + nfev * t_ev + t_fs
+    out = {"workload": "relax: calculator on fcc Al 4x4x4 (256 atoms), 128^3, WT+LDA+Hartree+PME PP, FP64, "
+                       "steepest descent 0.01 A^2/eV, 10 steps after the first from the uniform density",
+           "gpu": {"first_step_s": first["seconds"], "first_step_nfev": first["nfev"], "step_s": t_step,
+                   "step_nfev": nfev, "energy_first_eV": first["energy_eV"], "energy_last_eV": rest[-1]["energy_eV"],
+                   "fmax_first": first["fmax_eV_per_A"], "fmax_last": rest[-1]["fmax_eV_per_A"]},
+           "cpu": {"kind": "port", "cores": os.cpu_count(), "ev_s": t_ev, "vloc_s": t_vloc,
+                   "forces_stress_s": t_fs, "step_s_estimated": cpu_step},
+           "speedup_step": cpu_step / t_step, "steps": steps}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "diff":
@@ -750,6 +851,9 @@ def main():
         return
     if args.workload == "c2":
         c2_workload(args)
+        return
+    if args.workload == "relax":
+        relax_workload(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -19,3 +19,8 @@ ZERO = 1e-30
 
 LEN_CONV = {"Angstrom": {"Bohr": 1.0 / BOHR, "Angstrom": 1.0}, "Bohr": {"Angstrom": BOHR, "Bohr": 1.0}}
 ENERGY_CONV = {"Hartree": {"eV": HARTREE, "Hartree": 1.0}, "eV": {"Hartree": 1.0 / HARTREE, "eV": 1.0}}
+# ase.units: GPa = 1e9 J/m^3 in eV/Angstrom^3 (J = 1/e eV, m = 1e10 Angstrom)
+GPA = 1e9 / _e / 1e30
+FORCE_CONV = {"Ha/Bohr": {"eV/A": HARTREE / BOHR, "Ha/Bohr": 1.0}, "eV/A": {"Ha/Bohr": BOHR / HARTREE, "eV/A": 1.0}}
+STRESS_CONV = {"Ha/Bohr3": {"eV/A3": HARTREE / BOHR ** 3, "GPa": HARTREE / BOHR ** 3 / GPA, "Ha/Bohr3": 1.0},
+               "eV/A3": {"Ha/Bohr3": BOHR ** 3 / HARTREE, "GPa": 1.0 / GPA, "eV/A3": 1.0}}

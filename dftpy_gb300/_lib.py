@@ -20,6 +20,7 @@ S_TF, S_VW, S_NL, S_XC, S_H, NS = range(6)
 KE_TF, KE_VW, KE_WT, KE_LWT = 1, 2, 4, 8
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
 LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
+LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG = 0, 1, 2, 3
 OPT_TN, OPT_LBFGS, OPT_CGHS = 0, 1, 2
 
 
@@ -37,7 +38,7 @@ class Config(C.Structure):
         ("lwt_kdd", C.c_int), ("lwt_interp", C.c_int), ("lwt_etamax", C.c_double), ("lwt_neta", C.c_int),
         ("lwt_kfmin", C.c_double), ("lwt_kfmax", C.c_double), ("lwt_ldw", C.c_double), ("lwt_max_batch", C.c_int),
         ("xc_lda", C.c_int), ("hartree", C.c_int), ("pseudo", C.c_int), ("ewald_energy", C.c_double),
-        ("lwt_pipeline", C.c_int),
+        ("lwt_pipeline", C.c_int), ("lwt_kernel", C.c_int), ("lwt_maxpoints", C.c_int),
     ]
 
 

@@ -183,6 +183,47 @@ double lindhard(double eta, double lbda, double mu) {
     return out;
 }
 
+std::vector<double> mgp_kernel_table(const std::vector<double>& eta, int maxpoints, int sym) {
+    const int n = (int)eta.size();
+    if (n < 4) throw std::invalid_argument("MGP table needs >= 4 points");
+    // F(eta; 1, 1) as a cubic spline on numpy's logspace(log10(eta[1]/10), log10(eta[-1]+2), n)
+    const double a = std::log10(eta[1] / 10.0), b = std::log10(eta[n - 1] + 2.0);
+    const double step = (b - a) / (double)(n - 1);
+    std::vector<double> gp(n), f(n);
+    for (int i = 0; i < n; ++i) gp[i] = std::pow(10.0, i == n - 1 ? b : a + (double)i * step);
+    for (int i = 0; i < n; ++i) f[i] = lindhard(gp[i], 1.0, 1.0);
+    CubicSpline S;
+    S.fit(gp, f);
+    // sum over t = i/maxpoints of F(eta t^-1/3) / t^(1/6) (t^(-2/3) geometric), F
+    // extended by its end values outside the grid (splev ext=3); eta t^-1/3 grows
+    // with eta, so each pass walks the intervals forward
+    const double dt = 1.0 / (double)maxpoints;
+    std::vector<double> ker(n, 0.0);
+    for (int i = 1; i <= maxpoints; ++i) {
+        const double t = (double)i * dt;
+        const double ct = std::cbrt(t);
+        const double t16 = sym == 2 ? std::pow(t, -2.0 / 3.0) : std::pow(t, 1.0 / 6.0);
+        int l = 0;
+        for (int j = 0; j < n; ++j) {
+            double x = eta[j] / ct;
+            x = x < gp[0] ? gp[0] : (x > gp[n - 1] ? gp[n - 1] : x);
+            while (l < n - 2 && x >= gp[l + 1]) ++l;
+            const double u = x - gp[l];
+            const double* c = S.c.data() + 4 * (size_t)l;
+            ker[j] += (c[0] + u * (c[1] + u * (c[2] + u * c[3]))) / t16;
+        }
+    }
+    const double cTF = 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
+    const double coe = 4.0 / 5.0 * cTF * 5.0 / 6.0 * dt;
+    const double wt_factor = 4.0 / 5.0 * cTF;
+    for (int j = 0; j < n; ++j) {
+        if (sym == 1) ker[j] = 0.5 * (ker[j] * coe + lindhard(eta[j], 1.0, 1.0) * wt_factor);
+        else if (sym == 2) ker[j] *= 2.0 * coe;
+        else ker[j] *= coe;
+    }
+    return ker;
+}
+
 void guess_kf_bound(double kf_l, double kf_r, bool fixed_min, double kfmin_in, bool fixed_max, double kfmax_in,
                     bool& set_min, double& st_min, bool& set_max, double& st_max, double& out_min, double& out_max) {
     if (fixed_min && fixed_max) {

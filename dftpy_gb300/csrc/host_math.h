@@ -24,6 +24,10 @@ struct CubicSpline {
 // branches (src/dftpy/functional/kedf/kernel.py:14-136).
 double lindhard(double eta, double lbda, double mu);
 
+// MGP kernel table on the points eta (src/dftpy/functional/kedf/kernel.py:267-322,
+// serial): sym 0 none, 1 arithmetic (averaged with the WT table), 2 geometric.
+std::vector<double> mgp_kernel_table(const std::vector<double>& eta, int maxpoints, int sym);
+
 // k_F bound rule of the density-dependent kernel (src/dftpy/functional/kedf/lwt.py:36-79).
 // state_set/state_min/state_max carry the saved bounds between calls.
 void guess_kf_bound(double kf_l, double kf_r, bool fixed_min, double kfmin_in, bool fixed_max, double kfmax_in,

@@ -67,7 +67,8 @@ FzTab fz_tab(const Table<float>& t) {
     f.limitd = (float)t.limitd;
     f.factor = (float)t.factor;
     f.kconst = (float)(-t.lbda - 0.6);
-    f.eta_series = (float)t.eta_series;
+    // spline below eta_series; never at or above etamax, where the table limit applies
+    f.eta_series = (float)std::min(t.eta_series, t.etamax);
     return f;
 }
 

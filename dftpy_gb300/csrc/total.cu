@@ -839,9 +839,14 @@ void build_table(ofdft_eval* e) {
     const double step = etamax / (double)(neta - 1);
     for (int i = 0; i < neta; ++i) eta[i] = (double)i * step;
     eta[neta - 1] = etamax;
-    // WTKernelTable (kernel.py:344-352): F(eta; x, 1) * (4/5) * 0.3 (3 pi^2)^(2/3)
-    const double factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
-    for (int i = 0; i < neta; ++i) y[i] = lindhard(eta[i], c.lwt_x, 1.0) * factor;
+    if (c.lwt_kernel == OFDFT_LWT_KERNEL_WT) {
+        // WTKernelTable (kernel.py:344-352): F(eta; x, 1) * (4/5) * 0.3 (3 pi^2)^(2/3)
+        const double factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
+        for (int i = 0; i < neta; ++i) y[i] = lindhard(eta[i], c.lwt_x, 1.0) * factor;
+    } else {
+        const int sym = c.lwt_kernel == OFDFT_LWT_KERNEL_MGPA ? 1 : (c.lwt_kernel == OFDFT_LWT_KERNEL_MGPG ? 2 : 0);
+        y = mgp_kernel_table(eta, c.lwt_maxpoints, sym);
+    }
     CubicSpline S;
     S.fit(eta, y);
     std::vector<double> yd(neta);
@@ -877,7 +882,8 @@ Table<T> table_of(const ofdft_eval* e) {
     t.limitd = e->tab_limitd;
     t.factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
     t.lbda = e->cfg.lwt_x;
-    t.eta_series = 4.0;
+    // the large-eta series is the inverse Lindhard function's: WT tables only
+    t.eta_series = e->cfg.lwt_kernel == OFDFT_LWT_KERNEL_WT ? 4.0 : INFINITY;
     return t;
 }
 
@@ -1759,6 +1765,8 @@ void ofdft_config_default(ofdft_config* c) {
     c->lwt_kfmax = NAN;
     c->lwt_ldw = 1.0 / 6.0;
     c->lwt_max_batch = 0;
+    c->lwt_kernel = OFDFT_LWT_KERNEL_WT;
+    c->lwt_maxpoints = 1000;
     c->xc_lda = 1;
     c->hartree = 1;
     c->pseudo = 0;
@@ -1778,6 +1786,9 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
                           "lwt_interp must be linear or hermite");
             OFDFT_REQUIRE(c.lwt_nsp > 0 || c.lwt_delta > 0 || c.lwt_ratio > 1.0, "need nsp, delta or ratio > 1");
             OFDFT_REQUIRE(c.lwt_nsp != 1, "nsp must be >= 2");
+            OFDFT_REQUIRE(c.lwt_kernel >= OFDFT_LWT_KERNEL_WT && c.lwt_kernel <= OFDFT_LWT_KERNEL_MGPG,
+                          "lwt_kernel must be one of OFDFT_LWT_KERNEL_*");
+            OFDFT_REQUIRE(c.lwt_kernel == OFDFT_LWT_KERNEL_WT || c.lwt_maxpoints >= 1, "lwt_maxpoints must be >= 1");
         }
         auto* e = new ofdft_eval();
         e->g = g;

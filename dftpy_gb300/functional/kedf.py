@@ -1,7 +1,8 @@
 """Kinetic energy density functionals on the accelerated path
 (src/dftpy/functional/kedf/__init__.py:27-191): TF, vW, their combinations,
-Wang-Teter (WT) and the density-dependent k_F-node kernel (LWT family with
-the WT kernel table, used for the WGC-style workload)."""
+Wang-Teter (WT) and the density-dependent k_F-node kernel: LWT with the WT
+kernel table (the WGC-style workload) and LMGP / LMGPA / LMGPG with the MGP
+tables (kedf/lwt.py:571-578, kedf/kernel.py:267-322)."""
 import copy
 
 import numpy as np
@@ -12,7 +13,12 @@ from .functional_output import FunctionalOutput, ZeroFunctional
 
 __all__ = ["KEDF", "KEDFEngines"]
 
-_BITS = {"TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT}
+_BITS = {"TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+         "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
+# kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
+_TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
+_KERNELS = {"WT": _lib.LWT_KERNEL_WT, "MGP": _lib.LWT_KERNEL_MGP, "MGPA": _lib.LWT_KERNEL_MGPA,
+            "MGPG": _lib.LWT_KERNEL_MGPG}
 
 # name -> engines, as the reference's KEDFEngines table (kedf/__init__.py:27-69)
 KEDFEngines = {
@@ -26,6 +32,12 @@ KEDFEngines = {
     "WT-NL": ("WT-NL",),
     "LWT": ("TF", "VW", "LWT-NL"),
     "LWT-NL": ("LWT-NL",),
+    "LMGP": ("TF", "VW", "LMGP-NL"),
+    "LMGPA": ("TF", "VW", "LMGPA-NL"),
+    "LMGPG": ("TF", "VW", "LMGPG-NL"),
+    "LMGP-NL": ("LMGP-NL",),
+    "LMGPA-NL": ("LMGPA-NL",),
+    "LMGPG-NL": ("LMGPG-NL",),
 }
 
 
@@ -58,8 +70,11 @@ class KEDF(NativeFunctional):
         o = self.options
         if o.get("sigma") is not None:
             raise NotImplementedError("Gaussian smoothing of the vW term (sigma) is not supported")
-        if o.get("kerneltype", "WT") != "WT":
-            raise NotImplementedError("only the WT kernel table is supported for LWT")
+        if str(o.get("kerneltype", "WT")).upper() not in _KERNELS:
+            raise NotImplementedError("kernel tables WT, MGP, MGPA and MGPG are supported (got %r)"
+                                      % o.get("kerneltype"))
+        if o.get("symmetrization") not in (None, "None", "Arithmetic", "Geometric"):
+            raise NotImplementedError("MGP symmetrization must be None, 'Arithmetic' or 'Geometric'")
         if o.get("lumpfactor") is not None:
             raise NotImplementedError("MGP lump factors are not supported")
         if o.get("order", 3) != 3:
@@ -106,6 +121,15 @@ class KEDF(NativeFunctional):
         if pipe not in pipes:
             raise ValueError("pipeline must be one of %s" % sorted(pipes))
         cfg.lwt_pipeline = pipes[pipe]
+        # kernel table: fixed by the LMGP names, else the kerneltype option (lwt.py:535-548)
+        engines = engines if engines is not None else self.engines()
+        table = next((_TABLE_OF[e] for e in engines if e in _TABLE_OF), None)
+        if table is None:
+            table = str(o.get("kerneltype", "WT")).upper()
+        if table == "MGP" and o.get("symmetrization") in ("Arithmetic", "Geometric"):
+            table = "MGPA" if o.get("symmetrization") == "Arithmetic" else "MGPG"
+        cfg.lwt_kernel = _KERNELS[table]
+        cfg.lwt_maxpoints = int(o.get("maxpoints", 1000))
 
     def prepare(self, ev, grid, dtype):
         s = self.ke_kernel_saved

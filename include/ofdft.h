@@ -94,6 +94,10 @@ enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
  * into the library's own tile FFTs; CUFFT runs them as separate passes around
  * batched cuFFT transforms.  Both compute the same quantities. */
 enum { OFDFT_LWT_PIPE_AUTO = 0, OFDFT_LWT_PIPE_CUFFT = 1, OFDFT_LWT_PIPE_FUSED = 2 };
+/* kernel table of the k_F-node kernel (lwt.py:535-548): the WT table
+ * (kernel.py:344-352, LWT) or the MGP table (kernel.py:267-322; LMGP, and with
+ * the arithmetic / geometric symmetrisation LMGPA / LMGPG, lwt.py:571-578) */
+enum { OFDFT_LWT_KERNEL_WT = 0, OFDFT_LWT_KERNEL_MGP = 1, OFDFT_LWT_KERNEL_MGPA = 2, OFDFT_LWT_KERNEL_MGPG = 3 };
 
 typedef struct {
     int    kedf_terms;
@@ -119,6 +123,8 @@ typedef struct {
     int    pseudo;            /* add the local pseudopotential set by ofdft_eval_set_vloc */
     double ewald_energy;      /* ion-ion energy added to the total (0 = none)     */
     int    lwt_pipeline;      /* OFDFT_LWT_PIPE_*: how the k_F-node kernel runs   */
+    int    lwt_kernel;        /* OFDFT_LWT_KERNEL_*: the kernel table              */
+    int    lwt_maxpoints;     /* MGP tables: points of the t integral (default 1000) */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

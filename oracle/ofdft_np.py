@@ -326,6 +326,30 @@ def wt_kernel_table(eta, x=1.0):
     return lindhard(eta, x, 1.0) * factor
 
 
+def mgp_kernel_table(eta, maxpoints=1000, symmetrization=None):
+    """MGPKernelTable (kedf/kernel.py:267-322), serial: the MGP kernel as a sum
+    over t = i/maxpoints of F(eta t^-1/3; 1, 1) / t^(1/6) (t^(-2/3) for the
+    geometric symmetrisation), F from a cubic spline on a log grid evaluated
+    with constant extension (splev ext=3); 'Arithmetic' averages with the WT
+    table, 'Geometric' doubles."""
+    dt = 1.0 / maxpoints
+    cTF = 0.3 * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+    coe = 4.0 / 5.0 * cTF * 5.0 / 6.0 * dt
+    gp = np.logspace(np.log10(eta[1] / 10), np.log10(eta[-1] + 2), num=eta.size)
+    tck = splrep(gp, lindhard(gp, 1.0, 1.0))
+    kernel = np.zeros_like(eta)
+    for i in range(1, maxpoints + 1):
+        t = i * dt
+        Gt = splev(eta / np.cbrt(t), tck, ext=3)
+        t16 = t ** (-2.0 / 3.0) if symmetrization == "Geometric" else t ** (1.0 / 6.0)
+        kernel += Gt / t16
+    if symmetrization == "Arithmetic":
+        return 0.5 * (kernel * coe + wt_kernel_table(eta))
+    if symmetrization == "Geometric":
+        return kernel * 2.0 * coe
+    return kernel * coe
+
+
 def kernel_kf(q, kf, tck, etamax):
     """LWTKernelKf (kernel.py:379-405) for a spline table: splev(q/kf) below etamax,
     the value at etamax above it, element [0,0,0] zeroed when q there is 0."""
@@ -407,8 +431,9 @@ class LWT:
 
     def __init__(self, x=1.0, alpha=5.0 / 6.0, beta=5.0 / 6.0, etamax=50.0, neta=50000,
                  order=3, interp="linear", kdd=3, ratio=1.15, nsp=None, delta=None,
-                 kfmin=None, kfmax=None, ldw=None):
+                 kfmin=None, kfmax=None, ldw=None, kerneltype="WT", symmetrization=None, maxpoints=1000):
         self.x, self.alpha, self.beta = x, alpha, beta
+        self.kerneltype, self.symmetrization, self.maxpoints = kerneltype, symmetrization, maxpoints
         self.etamax, self.neta, self.order = etamax, neta, order
         self.interp, self.kdd, self.ratio, self.nsp, self.delta = interp, kdd, ratio, nsp, delta
         self.kfmin, self.kfmax, self.ldw = kfmin, kfmax, ldw
@@ -416,9 +441,14 @@ class LWT:
         self.tables()
 
     def tables(self):
-        """lwt.py:535-566 (kerneltype 'WT', order 3)."""
+        """lwt.py:535-566 (order 3): the WT table or an MGP table (kerneltype
+        'MGP' with its symmetrisation, 'MGPA' arithmetic, 'MGPG' geometric)."""
         eta = np.linspace(0, self.etamax, self.neta)
-        table = wt_kernel_table(eta, self.x)
+        if self.kerneltype == "WT":
+            table = wt_kernel_table(eta, self.x)
+        else:
+            sym = {"MGP": self.symmetrization, "MGPA": "Arithmetic", "MGPG": "Geometric"}[self.kerneltype]
+            table = mgp_kernel_table(eta, self.maxpoints, sym)
         self.tck = splrep(eta, table, k=self.order)
         deriv = splev(eta, self.tck, der=1) * (-1.0 * eta)
         self.tckD = splrep(eta, deriv, k=self.order)

@@ -15,9 +15,11 @@ _LIB = None
 OK, EINVAL, ECUDA, ECUFFT, ENOMEM, ESTATE = range(6)
 F64, F32 = 0, 1
 CALC_E, CALC_V = 1, 2
-E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, NE = range(10)
-S_TF, S_VW, S_NL, S_XC, S_H, NS = range(6)
-KE_TF, KE_VW, KE_WT, KE_LWT = 1, 2, 4, 8
+E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, E_GGA, NE = range(11)
+S_TF, S_VW, S_NL, S_XC, S_H, S_GGA, NS = range(7)
+KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA = 1, 2, 4, 8, 16
+(GGA_LKT, GGA_LKTVW, GGA_DK, GGA_LLP, GGA_OL, GGA_THAK, GGA_B86A, GGA_B86B, GGA_DK87, GGA_PW86, GGA_PW91O, GGA_PW91,
+ GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV, GGA_PBE2M, GGA_PG) = range(22)
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
 LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
 LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG = 0, 1, 2, 3
@@ -39,6 +41,8 @@ class Config(C.Structure):
         ("lwt_kfmin", C.c_double), ("lwt_kfmax", C.c_double), ("lwt_ldw", C.c_double), ("lwt_max_batch", C.c_int),
         ("xc_lda", C.c_int), ("hartree", C.c_int), ("pseudo", C.c_int), ("ewald_energy", C.c_double),
         ("lwt_pipeline", C.c_int), ("lwt_kernel", C.c_int), ("lwt_maxpoints", C.c_int),
+        ("gga_formula", C.c_int), ("gga_nparams", C.c_int), ("gga_params", C.c_double * 8),
+        ("gga_remove_vw", C.c_double),
     ]
 
 

@@ -15,6 +15,7 @@
 //              interpolation, hat-weighted R2C and the pot2 accumulation;
 //   post-pass  combine everything into V and the remaining energies.
 #include "common.cuh"
+#include "gga.cuh"
 #include "host_math.h"
 
 #include <algorithm>
@@ -22,6 +23,7 @@
 #include <cstring>
 
 using namespace ofdft;
+using namespace ofdft::gga;
 
 namespace {
 
@@ -735,7 +737,7 @@ struct ofdft_eval {
     bool fz_ran = false;           // the last evaluation ran the fused pipeline
     // terms of an evaluation whose energies have not been collected yet
     struct Pending {
-        bool tf, vw, wt, lwt, xc, h, pp, lp_active;
+        bool tf, vw, wt, lwt, xc, h, pp, lp_active, gga;
         int launches;
     } pend{};
     bool kf_set_min = false, kf_set_max = false;
@@ -867,6 +869,15 @@ void build_table(ofdft_eval* e) {
     e->tab_step = step;
     e->tab_limit = S.eval(etamax);
     e->tab_limitd = SD.eval(etamax);
+}
+
+GgaSpec gga_spec(const ofdft_config& c) {
+    GgaSpec s;
+    s.formula = c.gga_formula;
+    s.np = c.gga_nparams;
+    for (int i = 0; i < 8; ++i) s.p[i] = i < c.gga_nparams ? c.gga_params[i] : 0.0;
+    s.remove_vw = c.gga_remove_vw;
+    return s;
 }
 
 template <typename T>
@@ -1437,7 +1448,15 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     });
     OFDFT_LAUNCH_CHECK();
     launches += 2;
-    OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 24 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    // ---- GGA kinetic functional: its own gradient and divergence transforms, its
+    // potential added to V, its sums in results [40, 48)
+    const bool gga = (c.kedf_terms & OFDFT_KE_GGA) != 0;
+    if (gga) {
+        gga_enqueue<T>(g, e->sc, gga_spec(c), rho, Vw, true, false, g->d_results + 40, st);
+        launches += wantV ? 7 : 4;
+    }
+    OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, (gga ? 48 : 24) * sizeof(double), cudaMemcpyDeviceToHost,
+                             st));
     if (e->fz_ran) OFDFT_CK(cudaMemcpyAsync(e->h_fz_err, e->d_fz_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     e->pend.tf = tf;
     e->pend.vw = vw;
@@ -1447,6 +1466,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     e->pend.h = h;
     e->pend.pp = pp;
     e->pend.lp_active = lwt && lp.active;
+    e->pend.gga = gga;
     e->pend.launches = launches;
     if (!energies) return;
     OFDFT_CK(cudaStreamSynchronize(st));
@@ -1479,8 +1499,9 @@ void collect_energies(ofdft_eval* e, double* energies) {
     if (p.wt) E[OFDFT_E_NL] = R[18] * dV;
     if (p.lwt) E[OFDFT_E_NL] = p.lp_active ? R[18] * dV : 0.0;
     E[OFDFT_E_II] = c.ewald_energy;
+    E[OFDFT_E_GGA] = p.gga ? R[40] * dV : 0.0;
     E[OFDFT_E_TOTAL] = E[OFDFT_E_TF] + E[OFDFT_E_VW] + E[OFDFT_E_NL] + E[OFDFT_E_XC] + E[OFDFT_E_H] + E[OFDFT_E_PP] +
-                       E[OFDFT_E_II];
+                       E[OFDFT_E_II] + E[OFDFT_E_GGA];
     e->last_launches = p.launches;
 }
 
@@ -1588,40 +1609,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_stress_gspace(const typename Cp
     block_sum_store<12>(acc, partials);
 }
 
-// X_d = i g_d FFT(rho) / N for d = 0, 1, 2 (three planes, one after the
-// other).  The reference transforms these with numpy's irfftn, which keeps
-// only the Hermitian part of the k2 = 0 and k2 = n2/2 planes; on those planes
-// a Nyquist frequency index therefore counts as zero here, so that any C2R
-// gives numpy's result.
-template <typename T>
-__global__ void k_stress_grad(const typename Cplx<T>::type* __restrict__ rhoG, typename Cplx<T>::type* X, Geo geo,
-                              double invN) {
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < geo.Nc; idx += stride) {
-        const int k = (int)(idx % geo.n2h);
-        const long long t = idx / geo.n2h;
-        const int j = (int)(t % geo.n1);
-        const int i = (int)(t / geo.n1);
-        const bool edge = k == 0 || (geo.n2 % 2 == 0 && k == geo.n2 / 2);
-        double f0 = (double)freq_index(i, geo.n0), f1 = (double)freq_index(j, geo.n1), f2 = (double)k;
-        if (edge) {
-            if (geo.n0 % 2 == 0 && i == geo.n0 / 2) f0 = 0.0;
-            if (geo.n1 % 2 == 0 && j == geo.n1 / 2) f1 = 0.0;
-            if (geo.n2 % 2 == 0 && k == geo.n2 / 2) f2 = 0.0;
-        }
-        f0 *= geo.fv[0];
-        f1 *= geo.fv[1];
-        f2 *= geo.fv[2];
-        const double g[3] = {f0 * geo.b[0] + f1 * geo.b[3] + f2 * geo.b[6], f0 * geo.b[1] + f1 * geo.b[4] + f2 * geo.b[7],
-                             f0 * geo.b[2] + f1 * geo.b[5] + f2 * geo.b[8]};
-        const double rr = (double)rhoG[idx].x * invN, ri = (double)rhoG[idx].y * invN;
-        for (int d = 0; d < 3; ++d) {
-            X[d * geo.Nc + idx].x = (T)(-g[d] * ri);
-            X[d * geo.Nc + idx].y = (T)(g[d] * rr);
-        }
-    }
-}
-
 // sum_r d_i rho d_j rho / rho over the grid (six components)
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_stress_vw(const T* __restrict__ rho, const T* __restrict__ D,
@@ -1726,11 +1713,24 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
             for (int d = 0; d < 3; ++d) S[OFDFT_S_NL * 9 + 4 * d] -= 2.0 / 3.0 * E[OFDFT_E_NL] / V;
         }
     }
+    // GGA (gga.py:1306-1318): P = E - int pot1 rho - sum_i int w (d_i rho)^2, sigma_ii = P - int w (d_i rho)^2,
+    // sigma_ij = -int w d_i rho d_j rho, w = tf F' / rho^(8/3), over V
+    if (c.kedf_terms & OFDFT_KE_GGA) {
+        gga_enqueue<T>(g, e->sc, gga_spec(c), rho, nullptr, false, true, g->d_results + 40, st);
+        OFDFT_CK(cudaMemcpyAsync(g->h_results + 40, g->d_results + 40, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+        const double* R = g->h_results + 40;
+        const double P = R[0] * dV - R[1] * dV - (R[2] + R[5] + R[7]) * dV;
+        double w6[6];
+        for (int k = 0; k < 6; ++k) w6[k] = -R[2 + k] * dV / V;
+        put6(S + OFDFT_S_GGA * 9, w6, 1.0);
+        for (int d = 0; d < 3; ++d) S[OFDFT_S_GGA * 9 + 4 * d] += P / V;
+    }
     // vW: -(y/4) dV/V sum d_i rho d_j rho / rho
     if (vw) {
         C* X = (C*)e->sc.get("st_X", 3 * cb);
         T* D = (T*)e->sc.get("st_D", 3 * rb);
-        k_stress_grad<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N);
+        k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N);
         OFDFT_LAUNCH_CHECK();
         g->exec_c2r(X, D, 3, st);
         k_stress_vw<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, D, g->N, g->d_partials);
@@ -1767,6 +1767,11 @@ void ofdft_config_default(ofdft_config* c) {
     c->lwt_max_batch = 0;
     c->lwt_kernel = OFDFT_LWT_KERNEL_WT;
     c->lwt_maxpoints = 1000;
+    c->gga_formula = OFDFT_GGA_LKT;  // GGA_KEDF_list["LKT"] (gga.py:589)
+    c->gga_nparams = 2;
+    c->gga_params[0] = 1.3;
+    c->gga_params[1] = 1.0;
+    c->gga_remove_vw = 0.0;
     c->xc_lda = 1;
     c->hartree = 1;
     c->pseudo = 0;
@@ -1779,6 +1784,10 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
         const ofdft_config& c = *cfg;
         OFDFT_REQUIRE(!((c.kedf_terms & OFDFT_KE_WT) && (c.kedf_terms & OFDFT_KE_LWT)),
                       "only one nonlocal KEDF term at a time");
+        if (c.kedf_terms & OFDFT_KE_GGA) {
+            OFDFT_REQUIRE(c.gga_formula >= 0 && c.gga_formula < OFDFT_GGA_NFORMULAS, "gga_formula out of range");
+            OFDFT_REQUIRE(c.gga_nparams >= 1 && c.gga_nparams <= 8, "gga_nparams must be 1..8");
+        }
         if (c.kedf_terms & OFDFT_KE_LWT) {
             OFDFT_REQUIRE(c.lwt_kdd >= 1 && c.lwt_kdd <= 3, "lwt_kdd must be 1, 2 or 3");
             OFDFT_REQUIRE(c.lwt_neta >= 4 && c.lwt_etamax > 0, "bad kernel table size");

@@ -155,8 +155,13 @@ def empty_config():
 
 
 def config_key(cfg):
-    return tuple(getattr(cfg, f) if not isinstance(getattr(cfg, f), float) or not np.isnan(getattr(cfg, f))
-                 else "nan" for f, _ in cfg._fields_)
+    def key(v):
+        if isinstance(v, float):
+            return "nan" if np.isnan(v) else v
+        if hasattr(v, "_length_"):  # ctypes array field
+            return tuple(v)
+        return v
+    return tuple(key(getattr(cfg, f)) for f, _ in cfg._fields_)
 
 
 class NativeFunctional(AbstractFunctional):

@@ -2,7 +2,9 @@
 (src/dftpy/functional/kedf/__init__.py:27-191): TF, vW, their combinations,
 Wang-Teter (WT) and the density-dependent k_F-node kernel: LWT with the WT
 kernel table (the WGC-style workload) and LMGP / LMGPA / LMGPG with the MGP
-tables (kedf/lwt.py:571-578, kedf/kernel.py:267-322)."""
+tables (kedf/lwt.py:571-578, kedf/kernel.py:267-322); and the GGA functionals
+(kedf/gga.py), selected as the reference selects them (name 'GGA' with k_str,
+or 'GGA_<functional>')."""
 import copy
 
 import numpy as np
@@ -13,7 +15,7 @@ from .functional_output import FunctionalOutput, ZeroFunctional
 
 __all__ = ["KEDF", "KEDFEngines"]
 
-_BITS = {"TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+_BITS = {"GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -38,13 +40,45 @@ KEDFEngines = {
     "LMGP-NL": ("LMGP-NL",),
     "LMGPA-NL": ("LMGPA-NL",),
     "LMGPG-NL": ("LMGPG-NL",),
+    "GGA": ("GGA",),
+}
+
+# GGA_KEDF_list (gga.py:587-643): functional -> (formula, default parameters).  The
+# reference looks names up upper-cased, so its mixed-case 'PW91k' key is unreachable.
+_L = _lib
+GGA_FUNCTIONALS = {
+    "LKT-VW": (_L.GGA_LKTVW, [1.3]), "LKT": (_L.GGA_LKT, [1.3, 1.0]),
+    "DK": (_L.GGA_DK, [0.95, 14.28111, -19.5762, -0.05, 9.99802, 2.96085]),
+    "LLP": (_L.GGA_LLP, [0.0044188, 0.0253]), "LLP91": (_L.GGA_LLP, [0.0044188, 0.0253]),
+    "OL1": (_L.GGA_OL, [0.00677, 0.0]), "OL": (_L.GGA_OL, [0.00677, 0.0]), "OL2": (_L.GGA_OL, [0.0887, 1.0]),
+    "T92": (_L.GGA_THAK, [0.0055, 0.0253, 0.072]), "THAK": (_L.GGA_THAK, [0.0055, 0.0253, 0.072]),
+    "B86A": (_L.GGA_B86A, [0.0039, 0.004]), "B86": (_L.GGA_B86A, [0.0039, 0.004]),
+    "B86B": (_L.GGA_B86B, [0.00403, 0.007]),
+    "DK87": (_L.GGA_DK87, [7.0 / 324.0 / (18.0 * np.pi ** 4) ** (1.0 / 3.0), 0.861504, 0.044286]),
+    "PW86": (_L.GGA_PW86, [1.296, 14.0, 0.2]),
+    "PW91O": (_L.GGA_PW91O, [0.093907, 0.26608, 0.0809615, 100.0, 76.320, 0.57767e-4]),
+    "PW91": (_L.GGA_PW91, [0.19645, 0.2747, 0.1508, 100.0, 7.7956, 0.004]),
+    "LG94": (_L.GGA_LG94, [(1e-8 + 0.1234) / 0.024974, 29.790, 22.417, 12.119, 1570.1, 55.944, 0.024974]),
+    "E00": (_L.GGA_P92, [135.0, 28.0, 5.0, 3.0]), "P92": (_L.GGA_P92, [1.0, 88.3960, 16.3683, 88.2108]),
+    "PBE2": (_L.GGA_PBE, [2.0309 / 0.2942, 2.0309]), "PBE3": (_L.GGA_PBE, [-3.7425 / 4.1355, -3.7425, 50.258]),
+    "PBE4": (_L.GGA_PBE, [-7.2333 / 1.7107, -7.2333, 61.645, -93.683]), "P82": (_L.GGA_P82, [5.0 / 27.0]),
+    "TW02": (_L.GGA_PBE, [0.8438, 0.2319]), "APBE": (_L.GGA_PBE, [0.804, 0.23889]),
+    "APBEK": (_L.GGA_PBE, [0.804, 0.23889]), "REVAPBEK": (_L.GGA_PBE, [1.245, 0.23889]),
+    "REVAPBE": (_L.GGA_PBE, [1.245, 0.23889]), "RPBE": (_L.GGA_PBE, [1.9632, 0.01979]),
+    "VJKS00": (_L.GGA_VJKS00, [0.8944, 0.6511, 0.0431]),
+    "LC94": (_L.GGA_PW91, [0.093907, 0.26608, 0.0809615, 100.0, 76.32, 0.000057767]),
+    "VT84F": (_L.GGA_VT84F, [2.777028126, 2.777028126 - 40.0 / 27.0]),
+    "TF": (_L.GGA_TFVW, [1.0, 0.0]), "VW": (_L.GGA_TFVW, [0.0, 1.0]), "X_TF_Y_VW": (_L.GGA_TFVW, [1.0, 1.0]),
+    "TFVW": (_L.GGA_TFVW, [1.0, 1.0]), "STV": (_L.GGA_STV, [1.0, 1.0, 0.01, 1.0]),
+    "PBE2M": (_L.GGA_PBE2M, [1.0, 0.2942, 2.0309]), "PG": (_L.GGA_PG, [0.75, 1.0]),
 }
 
 
 # engines with a stress (KEDFEngines_Stress, kedf/__init__.py:76-92): slot in the
 # stress and energy arrays of the native evaluator
-_STRESS = {"TF": (_lib.S_TF, _lib.E_TF), "VW": (_lib.S_VW, _lib.E_VW), "WT-NL": (_lib.S_NL, _lib.E_NL)}
-_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL")
+_STRESS = {"TF": (_lib.S_TF, _lib.E_TF), "VW": (_lib.S_VW, _lib.E_VW), "WT-NL": (_lib.S_NL, _lib.E_NL),
+           "GGA": (_lib.S_GGA, _lib.E_GGA)}
+_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL", "GGA")
 
 
 class KEDF(NativeFunctional):
@@ -57,6 +91,12 @@ class KEDF(NativeFunctional):
     def __init__(self, name="WT", kedf=None, **kwargs):
         self.type = "KEDF"
         self.name = (kedf or name).upper()
+        kwargs = dict(kwargs)
+        if self.name.startswith("GGA_"):  # kedf/__init__.py:134-137
+            kwargs["k_str"] = self.name[4:]
+            self.name = "GGA"
+        if self.name.startswith("MGGA_") or self.name == "MGGA":
+            raise NotImplementedError("meta-GGA kinetic functionals are not supported")
         if self.name not in KEDFEngines:
             raise NotImplementedError("KEDF %r is not on the accelerated path (have %s)" % (self.name,
                                                                                           sorted(KEDFEngines)))
@@ -81,6 +121,12 @@ class KEDF(NativeFunctional):
             raise NotImplementedError("kernel tables use cubic splines (order=3) only")
         if o.get("temperature") or o.get("temperature0"):
             raise NotImplementedError("finite-temperature TF is not supported")
+        if "GGA" in self.engines():
+            if o.get("mgga"):
+                raise NotImplementedError("meta-GGA kinetic functionals are not supported")
+            k = o.get("k_str")
+            if k is not None and str(k).upper() not in GGA_FUNCTIONALS:
+                raise AttributeError("%s GGA KEDF to be implemented" % str(k).upper())
 
     def engines(self, name=None):
         return KEDFEngines[(name or self.name).upper()]
@@ -130,6 +176,20 @@ class KEDF(NativeFunctional):
             table = "MGPA" if o.get("symmetrization") == "Arithmetic" else "MGPG"
         cfg.lwt_kernel = _KERNELS[table]
         cfg.lwt_maxpoints = int(o.get("maxpoints", 1000))
+        if "GGA" in engines:  # gga.py:1212-1270: the functional named by k_str, default LKT
+            name = str(o.get("k_str") or "LKT").upper()
+            formula, p0 = GGA_FUNCTIONALS[name]
+            params = o.get("params")
+            p = list(p0)
+            if params is not None:  # prefix replaced, extra values dropped (gga.py:1255-1265)
+                params = [params] if isinstance(params, (int, float)) else list(params)
+                p[:min(len(params), len(p))] = params[:len(p)]
+            cfg.gga_formula = formula
+            cfg.gga_nparams = len(p)
+            for i, v in enumerate(p):
+                cfg.gga_params[i] = float(v)
+            rv = o.get("gga_remove_vw")
+            cfg.gga_remove_vw = 0.0 if rv is None else (float(rv) if isinstance(rv, (int, float)) else 1.0)
 
     def prepare(self, ev, grid, dtype):
         s = self.ke_kernel_saved

@@ -41,9 +41,9 @@ enum { OFDFT_CALC_E = 1, OFDFT_CALC_V = 2 };
 
 /* energy slots written by ofdft_eval_compute (Hartree) */
 enum { OFDFT_E_TF = 0, OFDFT_E_VW, OFDFT_E_NL, OFDFT_E_XC, OFDFT_E_H, OFDFT_E_PP, OFDFT_E_II,
-       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_NE };
+       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_E_GGA, OFDFT_NE };
 /* stress tensors written by ofdft_eval_stress, 9 doubles (3 x 3, row-major) each */
-enum { OFDFT_S_TF = 0, OFDFT_S_VW, OFDFT_S_NL, OFDFT_S_XC, OFDFT_S_H, OFDFT_NS };
+enum { OFDFT_S_TF = 0, OFDFT_S_VW, OFDFT_S_NL, OFDFT_S_XC, OFDFT_S_H, OFDFT_S_GGA, OFDFT_NS };
 
 /* ---------------------------------------------------------------- errors */
 const char* ofdft_last_error(void);
@@ -85,7 +85,14 @@ int ofdft_dot_noalloc(const void* a, const void* b, long long n, int precision, 
  * Configuration of the terms of TotalFunctional (src/dftpy/functional/
  * total_functional.py:49-146) and the KEDF dispatcher (kedf/__init__.py:27-69,
  * :124-191).  kedf_terms is a bit set of OFDFT_KE_*. */
-enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8 };
+enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8, OFDFT_KE_GGA = 16 };
+/* enhancement-factor formulas of the GGA kinetic functionals (kedf/gga.py:18-586);
+ * a named functional of the reference's GGA_KEDF_list (:587-643) is a formula plus
+ * its parameters, e.g. LC94 = PW91 with its own six, REVAPBEK = PBE with (1.245, 0.23889) */
+enum { OFDFT_GGA_LKT = 0, OFDFT_GGA_LKTVW, OFDFT_GGA_DK, OFDFT_GGA_LLP, OFDFT_GGA_OL, OFDFT_GGA_THAK,
+       OFDFT_GGA_B86A, OFDFT_GGA_B86B, OFDFT_GGA_DK87, OFDFT_GGA_PW86, OFDFT_GGA_PW91O, OFDFT_GGA_PW91,
+       OFDFT_GGA_LG94, OFDFT_GGA_P92, OFDFT_GGA_PBE, OFDFT_GGA_P82, OFDFT_GGA_VJKS00, OFDFT_GGA_VT84F,
+       OFDFT_GGA_TFVW, OFDFT_GGA_STV, OFDFT_GGA_PBE2M, OFDFT_GGA_PG, OFDFT_GGA_NFORMULAS };
 enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
 /* k_F-node kernel pipeline: AUTO takes FUSED where it applies (float32 grid,
  * linear interpolation, every axis a power of two in 32..256, the last axis
@@ -125,6 +132,11 @@ typedef struct {
     int    lwt_pipeline;      /* OFDFT_LWT_PIPE_*: how the k_F-node kernel runs   */
     int    lwt_kernel;        /* OFDFT_LWT_KERNEL_*: the kernel table              */
     int    lwt_maxpoints;     /* MGP tables: points of the t integral (default 1000) */
+    /* GGA kinetic functional (kedf/gga.py:1212-1325), with OFDFT_KE_GGA              */
+    int    gga_formula;       /* OFDFT_GGA_*                                       */
+    int    gga_nparams;       /* parameters in gga_params (1..8)                   */
+    double gga_params[8];
+    double gga_remove_vw;     /* gga_remove_vw: vW share subtracted from F (0: none) */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

@@ -929,6 +929,334 @@ class Ewald:
 
 
 # --------------------------------------------------------------------------
+# GGA KEDFs (kedf/gga.py:18-586 enhancement factors, :1212-1325 GGA)
+# --------------------------------------------------------------------------
+TKF0 = 6.18733545256027186194       # src/dftpy/constants.py:83
+CBRT_TWO = 1.25992104989487316477   # src/dftpy/constants.py:84
+
+
+def _power_int(x, num, den=1):
+    """PowerInt (math_utils.py:158-173)."""
+    y = x.copy()
+    for _ in range(num - 1):
+        y = y * x
+    if den == 1:
+        return y
+    if den == 2:
+        return np.sqrt(y)
+    if den == 3:
+        return np.cbrt(y)
+    if den == 4:
+        return np.sqrt(np.sqrt(y))
+    return np.power(y, 1.0 / den)
+
+
+def _tkf0(f):
+    """s_with_tkf0 (gga.py:18-40): the formula in ss = s/TKF0, dF/ds2 rescaled."""
+    def w(s, p):
+        F, d = f(s / TKF0, p)
+        return F, d / (TKF0 * TKF0)
+    return w
+
+
+@_tkf0
+def _lkt_mvw(ss, p):
+    e1, e2 = np.exp(-p[0] * ss), np.exp(-2.0 * p[0] * ss)
+    F = 2.0 * e1 / (1.0 + e2)
+    return F, -p[0] * (1.0 - e2) / (1.0 + e2) * F / ss
+
+
+def _dk(s, p):
+    x = s * s / (72 * C_TF)
+    Fa = 9.0 * p[5] * x ** 4 + p[2] * x ** 3 + p[1] * x ** 2 + p[0] * x + 1.0
+    Fb = p[5] * x ** 3 + p[4] * x ** 2 + p[3] * x + 1.0
+    d = (36.0 * p[5] * x ** 3 + 3 * p[2] * x ** 2 + 2 * p[1] * x + p[0]) / Fb - Fa / (Fb * Fb) * (
+        3.0 * p[5] * x ** 2 + 2.0 * p[4] * x + p[3])
+    return Fa / Fb, d / (36.0 * C_TF)
+
+
+def _llp(s, p):
+    bs = CBRT_TWO * s
+    bs2 = bs * bs
+    Fa = p[0] * bs2
+    Fb = 1.0 + p[1] * bs * np.arcsinh(bs)
+    d = 2.0 * p[0] / Fb - (p[0] * p[1] * bs * np.arcsinh(bs) + Fa * p[1] / np.sqrt(1.0 + bs2)) / (Fb * Fb)
+    return 1.0 + Fa / Fb, d * (CBRT_TWO * CBRT_TWO)
+
+
+def _ol(s, p):
+    F = 1.0 + s * s / 72.0 / C_TF + p[0] / C_TF * s / (1 + p[1] * 4 * s)
+    d = 1.0 / 36.0 / C_TF * np.ones_like(s)
+    m = s > 1.0e-8
+    d[m] += p[0] / C_TF / _power_int(1 + p[1] * 4 * s[m], 2) / s[m]
+    return F, d
+
+
+def _thak(s, p):
+    bs = CBRT_TWO * s
+    bs2 = bs * bs
+    F = 1.0 + p[0] * bs2 / (1.0 + p[1] * bs * np.arcsinh(bs)) - p[2] * bs / (1.0 + 2 ** (5.0 / 3.0) * bs)
+    Fb = (1.0 + p[1] * bs * np.arcsinh(bs)) ** 2
+    d = (-(p[0] * p[1] * bs2) / np.sqrt(1 + bs2) + (p[0] * p[1] * bs * np.arcsinh(bs)) + 2.0 * p[0]) / Fb
+    m = s > 1.0e-8
+    d[m] -= p[2] / (1.0 + 2 ** (5.0 / 3.0) * bs[m]) ** 2 / bs[m]
+    return F, d * (CBRT_TWO * CBRT_TWO)
+
+
+def _b86a(s, p):
+    bs = CBRT_TWO * s
+    bs2 = bs * bs
+    Fb = 1.0 + p[1] * bs2
+    return 1.0 + p[0] * bs2 / Fb, 2 * p[0] / (Fb * Fb) * (CBRT_TWO * CBRT_TWO)
+
+
+def _b86b(s, p):
+    bs = CBRT_TWO * s
+    bs2 = bs * bs
+    Fb = _power_int(1.0 + p[1] * bs2, 4, 5)
+    d = (2 * p[0] * (p[1] * bs2 + 5.0)) / (5 * (1.0 + p[1] * bs2) * Fb) * (CBRT_TWO * CBRT_TWO)
+    return 1.0 + p[0] * bs2 / Fb, d
+
+
+def _dk87(s, p):
+    bs = CBRT_TWO * s
+    bs2 = bs * bs
+    Fa = p[0] * bs2 * (1 + p[1] * bs)
+    Fb = 1.0 + p[2] * bs2
+    d = p[0] * (2.0 + 3.0 * p[1] * bs + p[1] * p[2] * bs2 * bs) / (Fb * Fb) * (CBRT_TWO * CBRT_TWO)
+    return 1.0 + Fa / Fb, d
+
+
+@_tkf0
+def _pw86(ss, p):
+    s2 = ss * ss
+    s4 = s2 * s2
+    Fa = 1.0 + p[0] * s2 + p[1] * s4 + p[2] * s2 * s4
+    return np.power(Fa, 1.0 / 15.0), 2.0 / 15.0 * (p[0] + 2 * p[1] * s2 + 3 * p[2] * s4) / np.power(Fa, 14.0 / 15.0)
+
+
+@_tkf0
+def _pw91o(ss, p):
+    s2 = ss * ss
+    s4 = s2 * s2
+    ex = np.exp(-p[3] * s2)
+    Fa = (p[1] - p[2] * ex) * s2 - p[5] * s4
+    Fb = 1.0 + p[0] * ss * np.arcsinh(p[4] * ss) + p[5] * s4
+    Fa_s2 = (p[1] - p[2] * ex) - p[5] * s2
+    d = 2.0 * (p[1] + (p[3] * s2 - 1) * p[2] * ex - 4.0 * p[5] * s2) / Fb - Fa_s2 * ss / (Fb * Fb) * (
+        (p[0] * p[4] * ss) / (p[4] ** 2 * s2 + 1) + p[0] * np.arcsinh(p[4] * ss) + 4.0 * p[5] * s2)
+    return 1.0 + Fa / Fb, d
+
+
+@_tkf0
+def _pw91(ss, p):
+    s2 = ss * ss
+    s4 = s2 * s2
+    ex = np.exp(-p[3] * s2)
+    ash = np.arcsinh(p[4] * ss)
+    Fa = 1.0 + p[0] * ss * ash + (p[1] - p[2] * ex) * s2
+    Fb = 1.0 + p[0] * ss * ash + p[5] * s4
+    sq = np.sqrt(p[4] ** 2 * s2 + 1)
+    Fa_s = p[0] * p[4] * ss / sq + p[0] * ash + 2.0 * ss * (p[1] + 2.0 * p[2] * p[3] * s2 * ex - 2.0 * p[2] * ex)
+    d = Fa_s / Fb - Fa / (Fb * Fb) * (p[0] * p[4] * ss / sq + (p[0] * ash + 4.0 * p[5] * s2 * ss))
+    m = ss > 1.0e-8
+    d[m] /= ss[m]
+    return Fa / Fb, d
+
+
+@_tkf0
+def _lg94(ss, p):
+    s2 = ss * ss
+    s4 = s2 * s2
+    s6 = s4 * s2
+    s8 = s4 * s4
+    s10 = s4 * s6
+    s12 = s6 * s6
+    Fa = 1.0 + p[0] * s2 + p[1] * s4 + p[2] * s6 + p[3] * s8 + p[4] * s10 + p[5] * s12
+    Fb = 1.0 + 1e-8 * s2
+    F = np.power(Fa / Fb, p[6])
+    d = -2 * p[6] * F * (1e-8 * Fa - Fb * (p[0] + 2 * p[1] * s2 + 3 * p[2] * s4 + 4 * p[3] * s6 + 5 * p[4] * s8
+                                          + 6 * p[5] * s10)) / (Fa * Fb)
+    return F, d
+
+
+@_tkf0
+def _p92(ss, p):
+    s2 = ss * ss
+    Fa = p[0] + p[1] * s2 + p[2] * s2 * s2
+    Fb = p[0] + p[3] * s2
+    return Fa / Fb, (2.0 * p[1] + 4.0 * p[2] * s2) / Fb - (2.0 * p[3] * Fa) / (Fb * Fb)
+
+
+@_tkf0
+def _pbe(ss, p):
+    s2 = ss * ss
+    Fb = 1.0 + p[1] / p[0] * s2
+    Fb2 = Fb * Fb
+    F = 1.0 + p[1] * s2 / Fb
+    d = 2.0 * p[1] / Fb2
+    if len(p) > 2:
+        s4 = s2 * s2
+        Fb3 = Fb2 * Fb
+        F = F + p[2] * s4 / Fb2
+        d = d + 4 * p[2] * s2 / Fb3
+        if len(p) > 3:
+            F = F + p[3] * s4 * s2 / Fb3
+            d = d + 6 * p[3] * s4 / (Fb3 * Fb)
+    return F, d
+
+
+@_tkf0
+def _p82(ss, p):
+    s2 = ss * ss
+    s6 = s2 * s2 * s2
+    Fb = 1 + s6
+    return 1.0 + p[0] * s2 / Fb, p[0] * (2.0 / Fb - 6.0 * s6 / (Fb * Fb))
+
+
+@_tkf0
+def _vjks00(ss, p):
+    s2 = ss * ss
+    s4 = s2 * s2
+    Fa = 1.0 + p[0] * s2 - p[2] * s4 * s2
+    Fb = 1.0 + p[1] * s2 + p[2] * s4
+    return Fa / Fb, (2.0 * p[0] - 6.0 * p[2] * s4) / Fb - (2.0 * p[1] + 4.0 * p[2] * s2) * Fa / (Fb * Fb)
+
+
+@_tkf0
+def _vt84f(ss, p):
+    s2 = ss * ss
+    s2 = np.where(s2 < 1.0e-8, 1.0e-8, s2)
+    s4 = s2 * s2
+    e1, e2 = np.exp(-p[1] * s2), np.exp(-p[1] * s4)
+    F = 1.0 + 5.0 / 3.0 * s2 + p[0] * s2 * e1 / (1 + p[0] * s2) + (1 - e2) * (1.0 / s2 - 1.0)
+    d = (10.0 / 3.0 + 2.0 * p[0] * e1 * (1.0 - p[1] * s2) / (1 + p[0] * s2)
+         - 2.0 * p[0] * s2 * e1 / _power_int(1 + p[0] * s2, 2) + 4.0 * p[1] * s2 * (1.0 / s2 - 1.0) * e2
+         - 2.0 * (1 - e2) / s4)
+    return F, d
+
+
+@_tkf0
+def _tfvw(ss, p):
+    return p[0] + 5.0 / 3.0 * p[1] * ss * ss, 10.0 / 3.0 * p[1] * np.ones_like(ss)
+
+
+@_tkf0
+def _stv(ss, p):
+    s2 = ss * ss
+    Fb = p[3] + p[2] * s2
+    return p[0] + 5.0 / 3.0 * p[1] * s2 / Fb, 5.0 / 3.0 * p[1] * (2.0 / Fb - 2.0 * s2 * p[2] / (Fb * Fb))
+
+
+@_tkf0
+def _pbe2m(ss, p):
+    s2 = ss * ss
+    Fb = p[0] + p[1] * s2
+    return 1.0 + p[2] * s2 / Fb, 2.0 * p[2] / (Fb * Fb)
+
+
+@_tkf0
+def _pg(ss, p):
+    s2 = ss * ss
+    Fa = np.exp(-p[0] * s2)
+    return Fa + 5.0 / 3.0 * p[1] * s2, -2.0 * p[0] * Fa + 10.0 / 3.0 * p[1]
+
+
+@_tkf0
+def _lkt(ss, p):
+    s2 = ss * ss
+    F = np.empty_like(ss)
+    d = np.empty_like(ss)
+    m1 = ss > 100.0
+    m2 = ss < 1e-5
+    m = ~(m1 | m2)
+    F[m] = 1.0 / np.cosh(p[0] * ss[m]) + 5.0 / 3.0 * s2[m] * p[1]
+    F[m1] = 5.0 / 3.0 * s2[m1] * p[1]
+    F[m2] = 1.0 + (5.0 / 3.0 * p[1] - 0.5 * p[0] ** 2) * s2[m2] + 5.0 / 24.0 * p[0] ** 4 * s2[m2] ** 2
+    d[m] = 10.0 / 3.0 * p[1] - p[0] * np.sinh(p[0] * ss[m]) / np.cosh(p[0] * ss[m]) ** 2 / ss[m]
+    d[m1] = 10.0 / 3.0 * p[1]
+    d[m2] = 10.0 / 3.0 * p[1] - p[0] ** 2 + 5.0 / 6.0 * p[0] ** 4 * s2[m2] - 61.0 / 120.0 * p[0] ** 6 * s2[m2] ** 2
+    return F, d
+
+
+# GGA_KEDF_list (gga.py:587-643): name -> (formula, default params)
+GGA_FUNCTIONALS = {
+    "LKT-VW": (_lkt_mvw, [1.3]), "LKT": (_lkt, [1.3, 1.0]),
+    "DK": (_dk, [0.95, 14.28111, -19.5762, -0.05, 9.99802, 2.96085]),
+    "LLP": (_llp, [0.0044188, 0.0253]), "LLP91": (_llp, [0.0044188, 0.0253]),
+    "OL1": (_ol, [0.00677, 0.0]), "OL": (_ol, [0.00677, 0.0]), "OL2": (_ol, [0.0887, 1.0]),
+    "T92": (_thak, [0.0055, 0.0253, 0.072]), "THAK": (_thak, [0.0055, 0.0253, 0.072]),
+    "B86A": (_b86a, [0.0039, 0.004]), "B86": (_b86a, [0.0039, 0.004]), "B86B": (_b86b, [0.00403, 0.007]),
+    "DK87": (_dk87, [7.0 / 324.0 / (18.0 * np.pi ** 4) ** (1.0 / 3.0), 0.861504, 0.044286]),
+    "PW86": (_pw86, [1.296, 14.0, 0.2]),
+    "PW91O": (_pw91o, [0.093907, 0.26608, 0.0809615, 100.0, 76.320, 0.57767e-4]),
+    "PW91": (_pw91, [0.19645, 0.2747, 0.1508, 100.0, 7.7956, 0.004]),
+    "LG94": (_lg94, [(1e-8 + 0.1234) / 0.024974, 29.790, 22.417, 12.119, 1570.1, 55.944, 0.024974]),
+    "E00": (_p92, [135.0, 28.0, 5.0, 3.0]), "P92": (_p92, [1.0, 88.3960, 16.3683, 88.2108]),
+    "PBE2": (_pbe, [2.0309 / 0.2942, 2.0309]), "PBE3": (_pbe, [-3.7425 / 4.1355, -3.7425, 50.258]),
+    "PBE4": (_pbe, [-7.2333 / 1.7107, -7.2333, 61.645, -93.683]), "P82": (_p82, [5.0 / 27.0]),
+    "TW02": (_pbe, [0.8438, 0.2319]), "APBE": (_pbe, [0.804, 0.23889]), "APBEK": (_pbe, [0.804, 0.23889]),
+    "REVAPBEK": (_pbe, [1.245, 0.23889]), "REVAPBE": (_pbe, [1.245, 0.23889]), "RPBE": (_pbe, [1.9632, 0.01979]),
+    "VJKS00": (_vjks00, [0.8944, 0.6511, 0.0431]),
+    "LC94": (_pw91, [0.093907, 0.26608, 0.0809615, 100.0, 76.32, 0.000057767]),
+    "VT84F": (_vt84f, [2.777028126, 2.777028126 - 40.0 / 27.0]),
+    "TF": (_tfvw, [1.0, 0.0]), "VW": (_tfvw, [0.0, 1.0]), "X_TF_Y_VW": (_tfvw, [1.0, 1.0]),
+    "TFVW": (_tfvw, [1.0, 1.0]), "STV": (_stv, [1.0, 1.0, 0.01, 1.0]), "PBE2M": (_pbe2m, [1.0, 0.2942, 2.0309]),
+    "PG": (_pg, [0.75, 1.0]),
+}
+
+
+def _gradient(rho, grid):
+    """DirectField.standard_gradient (field.py:267-281): irfftn(i g rho(G))."""
+    rhoG = fft(rho, grid)
+    return [ifft(1j * grid.g[i] * rhoG, grid) for i in range(3)]
+
+
+def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw=None):
+    """GGA (kedf/gga.py:1212-1325) without gradient smoothing (sigma None)."""
+    name = functional.upper()
+    fn, p0 = GGA_FUNCTIONALS[name]
+    p = list(p0)
+    if params is not None:
+        params = [params] if isinstance(params, (int, float)) else list(params)
+        p[:min(len(params), len(p))] = params[:len(p)]
+    rhom = rho.copy()
+    rhom[rhom < 1e-16] = 1e-16
+    rho23 = _power_int(rhom, 2, 3)
+    rho53 = rho23 * rhom
+    tf = C_TF * rho53
+    rho43 = rho23 * rho23
+    rho83 = rho43 * rho43
+    grad = _gradient(rho, grid)
+    s = np.sqrt(_power_int(grad[0], 2) + _power_int(grad[1], 2) + _power_int(grad[2], 2)) / rho43
+    s[s < 1e-16] = 1e-16
+    F, dFds2 = fn(s, p)
+    if gga_remove_vw is not None:
+        pa = float(gga_remove_vw) if isinstance(gga_remove_vw, (int, float)) else 1.0
+        Fv, dv = _tfvw(s, [0.0, pa])
+        F, dFds2 = F - Fv, dFds2 - dv
+    out = {"E": (tf * F).sum() * grid.dV}
+    if "V" in calc or "S" in calc:
+        pot1 = 5.0 / 3.0 * C_TF * rho23 * F - 4.0 / 3.0 * tf * dFds2 * s * s / rhom
+        p3 = [fft(tf * dFds2 * grad[i] / rho83, grid) for i in range(3)]
+        pot3G = grid.g[0] * p3[0] + grid.g[1] * p3[1] + grid.g[2] * p3[2]
+        out["V"] = pot1 - ifft(1j * pot3G, grid)
+    if "S" in calc:
+        vkin2 = tf * dFds2 / rho83
+        P = out["E"] - (pot1 * rho).sum() * grid.dV
+        for i in range(3):
+            P -= (grad[i] * grad[i] * vkin2).sum() * grid.dV
+        S = np.zeros((3, 3))
+        for i in range(3):
+            S[i, i] = P
+            for j in range(i, 3):
+                S[i, j] -= (vkin2 * grad[i] * grad[j]).sum() * grid.dV
+                S[j, i] = S[i, j]
+        out["S"] = S / grid.volume
+    return out
+
+
+# --------------------------------------------------------------------------
 # stress (calcType 'S'): 3x3 tensors in Ha/Bohr^3
 # --------------------------------------------------------------------------
 _SYM6 = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]

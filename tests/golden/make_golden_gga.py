@@ -1,0 +1,55 @@
+"""Generate tests/golden/reference_gga.npz: GGA kinetic functionals
+(src/dftpy/functional/kedf/gga.py) computed by the REFERENCE implementation.
+
+Run in a container that has the reference sources:
+
+    python tests/golden/make_golden_gga.py /root/reference
+
+Cases: every functional of GGA_KEDF_list on the smooth anisotropic density of
+system A (24x20x18; energy, potential and stress), LKT with user parameters
+and with gga_remove_vw, and the reference's own test of GGA 'lc94' on its
+Al_fde_rho.pp density (test_functional.py:10-21, energy 1.6821337114254904).
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from make_golden import ref_objects, setup  # noqa: E402
+
+
+def main(ref_root):
+    setup(ref_root)
+    DirectGrid, DirectField, Ions = ref_objects()
+    from dftpy.functional import Functional
+    from dftpy.functional.kedf.gga import GGA, GGA_KEDF_list
+
+    g0 = dict(np.load(os.path.join(HERE, "reference_golden.npz")))
+    out = {}
+    grid = DirectGrid(lattice=g0["E_lattice"], nr=g0["E_nr"], full=False)
+    rho = DirectField(grid=grid, data=g0["E_rho"].copy())
+    e = Functional(type="KEDF", name="GGA", k_str="lc94")(rho).energy
+    out["fixture_E_LC94"] = float(e)
+    print("fixture GGA lc94", e, "(the reference test expects 1.6821337114254904)")
+
+    gridA = DirectGrid(lattice=g0["A_lattice"], nr=g0["A_nr"], full=False)
+    # GGA() looks names up upper-cased, so a mixed-case key ('PW91k') is unreachable
+    names = sorted(n for n in GGA_KEDF_list if n.upper() in GGA_KEDF_list)
+    out["names"] = np.array(names)
+    cases = [(n, n, {}) for n in names] + [("LKT_P", "LKT", {"params": [1.1, 0.9]}),
+                                          ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0})]
+    for tag, name, kw in cases:
+        rA = DirectField(grid=gridA, data=g0["A_rho"].copy())
+        r = GGA(rA, functional=name, calcType={"E", "V", "S"}, **kw)
+        out["A_E_" + tag] = float(r.energy)
+        out["A_V_" + tag] = np.asarray(r.potential)
+        out["A_S_" + tag] = np.asarray(r.stress)
+    np.savez_compressed(os.path.join(HERE, "reference_gga.npz"), **out)
+    print(len(cases), "cases")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

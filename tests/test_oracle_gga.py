@@ -1,0 +1,33 @@
+"""Pin the oracle's GGA kinetic functionals against the reference's outputs
+(tests/golden/make_golden_gga.py): every functional of the reference's list,
+energy, potential and stress, plus the reference's own 'lc94' test."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ofdft_np as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GG = dict(np.load(os.path.join(HERE, "golden", "reference_gga.npz")))
+CASES = [(n, n, {}) for n in GG["names"]] + [("LKT_P", "LKT", {"params": [1.1, 0.9]}),
+                                             ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0})]
+
+
+@pytest.mark.parametrize("tag,name,kw", CASES, ids=[c[0] for c in CASES])
+def test_gga_system_a(golden, tag, name, kw):
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    r = O.gga(golden["A_rho"], grid, name, calc=("E", "V", "S"), **kw)
+    e = GG["A_E_" + tag]
+    assert abs(r["E"] - e) <= 1e-11 * max(1.0, abs(e)), (r["E"], e)
+    v = GG["A_V_" + tag]
+    np.testing.assert_allclose(r["V"], v, rtol=0, atol=1e-10 * max(1.0, np.abs(v).max()))
+    s = GG["A_S_" + tag]
+    np.testing.assert_allclose(r["S"], s, rtol=0, atol=1e-10 * max(1e-12, np.abs(s).max()))
+
+
+def test_gga_reference_fixture(golden):
+    grid = O.Grid(golden["E_lattice"], golden["E_nr"])
+    e = O.gga(golden["E_rho"], grid, "LC94", calc=("E",))["E"]
+    assert abs(e - GG["fixture_E_LC94"]) <= 1e-12 * abs(e)
+    assert np.isclose(e, 1.6821337114254904)  # the reference's own test value

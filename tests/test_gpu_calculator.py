@@ -88,3 +88,24 @@ def test_relaxation_keeps_density_resident():
     assert all(b <= a + 1e-6 for a, b in zip(energies, energies[1:]))
     # later steps start from the previous ground state, not from the uniform density
     assert max(iters[2:]) < iters[0]
+
+
+def test_restart_from_density_file(tmp_path):
+    """A converged density written to snpy and read back restarts the optimiser
+    at its ground state (formats/io.py, restart)."""
+    from dftpy_gb300 import formats as F
+    lat, pos = syn.fcc_cell(7.6)
+    pos = pos + np.random.default_rng(5).normal(0, 0.1, pos.shape)
+    _, grid, pp, tot, rho0 = _system(pos)
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS", optimization_options=_opts())
+    rho = opt.optimize_rho(guess_rho=rho0)
+    fn = str(tmp_path / "rho.snpy")
+    F.write_density(fn, data=rho, ions=pp.ions)
+    back = F.read_density(fn)
+    assert back.is_cuda and torch.equal(back.as_subclass(torch.Tensor), rho.as_subclass(torch.Tensor))
+    _, grid2, pp2, tot2, _ = _system(pos)
+    back2 = D.DirectField(grid2, data=back.as_subclass(torch.Tensor))
+    opt2 = D.Optimization(EnergyEvaluator=tot2, optimization_method="LBFGS", optimization_options=_opts())
+    opt2.optimize_rho(guess_rho=back2)
+    assert opt2.result.niter <= 2
+    assert abs(opt2.functional.energy - opt.functional.energy) <= 1e-8 * 4

@@ -22,7 +22,8 @@ KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA = 1, 2, 4, 8, 16
  GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV, GGA_PBE2M, GGA_PG) = range(22)
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
 LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
-LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG = 0, 1, 2, 3
+LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG, LWT_KERNEL_USER = 0, 1, 2, 3, 4
+LWT_FAMILY_LWT, LWT_FAMILY_HC = 0, 1
 OPT_TN, OPT_LBFGS, OPT_CGHS = 0, 1, 2
 
 
@@ -42,7 +43,7 @@ class Config(C.Structure):
         ("xc_lda", C.c_int), ("hartree", C.c_int), ("pseudo", C.c_int), ("ewald_energy", C.c_double),
         ("lwt_pipeline", C.c_int), ("lwt_kernel", C.c_int), ("lwt_maxpoints", C.c_int),
         ("gga_formula", C.c_int), ("gga_nparams", C.c_int), ("gga_params", C.c_double * 8),
-        ("gga_remove_vw", C.c_double),
+        ("gga_remove_vw", C.c_double), ("lwt_family", C.c_int),
     ]
 
 
@@ -85,6 +86,7 @@ _SIGS = {
     "ofdft_eval_set_ewald": (_I, [_P, _D]),
     "ofdft_eval_compute": (_I, [_P, _P, _P, C.c_uint, _PD, _P]),
     "ofdft_eval_stress": (_I, [_P, _P, _PD, _PD, _P]),
+    "ofdft_eval_set_lwt_table": (_I, [_P, _PD, _I]),
     "ofdft_eval_get_kfbounds": (_I, [_P, _PD, _PD]),
     "ofdft_eval_set_kfbounds": (_I, [_P, _D, _D]),
     "ofdft_eval_last_stats": (_I, [_P, _PI, _PI]),

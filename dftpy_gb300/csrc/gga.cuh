@@ -355,6 +355,65 @@ __global__ void __launch_bounds__(RED_THREADS) k_gga_point(const T* __restrict__
     block_sum_store<8>(acc, partials);
 }
 
+// HC k_F field (hc.py:88-138): rho clamped at 1e-30, s = |D| / rho^(4/3) from
+// the gradient D of the clamped density (not floored), F and F' of the
+// enhancement factor, k_F = F (3 pi^2 rho)^(1/3); for the potential
+// c1 = k_F,std (F - 4 F' s^2) / (3 rho) and c2 = k_F,std F' / rho^(8/3)
+// (hc.py:312-313).  Partials: [0] min k_F, [1] max k_F.
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_hc_point(const T* __restrict__ rho, const T* __restrict__ D, T* kf,
+                                                          T* c1, T* c2, long long N, GgaSpec sp, double* partials) {
+    using M = T;
+    M kmin = (M)INFINITY, kmax = -(M)INFINITY;
+    const M threepi2 = (M)(3.0 * M_PI * M_PI);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += stride) {
+        const M r = rho[i];
+        const M rc = r < (M)1e-30 ? (M)1e-30 : r;
+        const M rho43 = pow(rc, (M)(4.0 / 3.0));
+        const M rho83 = rho43 * rho43;
+        const M dx = D[i], dy = D[N + i], dz = D[2 * N + i];
+        const M s = sqrt(dx * dx + dy * dy + dz * dz) / rho43;
+        M F, dF;
+        gga_formula(sp, s, F, dF);
+        const M kstd = cbrt(threepi2 * rc);
+        const M k = F * kstd;
+        kf[i] = k;
+        if (c1) {
+            c1[i] = kstd / ((M)3 * rc) * (F - (M)4 * dF * s * s);
+            c2[i] = kstd * dF / rho83;
+        }
+        kmin = k < kmin ? k : kmin;
+        kmax = k > kmax ? k : kmax;
+    }
+    double acc[2] = {(double)kmin, (double)kmax};
+    const int kinds[2] = {1, 2};
+    block_reduce_store<2>(acc, kinds, partials);
+}
+
+// rho clamped at 1e-30 (hc.py:88-90)
+template <typename T>
+__global__ void k_hc_clamp(const T* __restrict__ rho, T* out, long long N) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += stride) {
+        const T r = rho[i];
+        out[i] = r < (T)1e-30 ? (T)1e-30 : r;
+    }
+}
+
+// p_d = d_d rho c2 rho^alpha pot3, in place of the gradient planes (hc.py:313-318)
+template <typename T>
+__global__ void k_hc_p(T* D, const T* __restrict__ c2, const T* __restrict__ pa, const T* __restrict__ pot3,
+                       long long N) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += stride) {
+        const T w = c2[i] * (pa[i] * pot3[i]);
+        D[i] *= w;
+        D[N + i] *= w;
+        D[2 * N + i] *= w;
+    }
+}
+
 // V (+)= pot1 - q
 template <typename T>
 __global__ void k_gga_combine(T* V, const T* __restrict__ pot1, const T* __restrict__ q, long long N, int accumulate) {

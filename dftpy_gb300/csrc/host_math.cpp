@@ -276,6 +276,55 @@ void guess_kf_bound(double kf_l, double kf_r, bool fixed_min, double kfmin_in, b
     out_max = kfmax;
 }
 
+std::vector<double> hc_kf_nodes(double kf_l, double kf_r, bool fixed_min, double kfmin_in, bool fixed_max,
+                                double kfmax_in, bool& set_min, double& st_min, bool& set_max, double& st_max,
+                                double ratio, int nsp, double delta) {
+    const double kf0 = 1.0;
+    double kfmin = kfmin_in, kfmax = kfmax_in;
+    if (!fixed_min) {
+        kfmin = std::max(kf_l, 1e-3);
+        const int n = (int)std::floor(std::log(kfmin / kf0) / std::log(ratio)) - 1;
+        kfmin = kf0 * std::pow(ratio, (double)n);
+    }
+    if (!fixed_max) {
+        kfmax = std::min(kf_r, 100.0);
+        const int n = (int)std::ceil(std::log(kfmax / kf0) / std::log(ratio)) + 1;
+        kfmax = kf0 * std::pow(ratio, (double)n);
+    }
+    if (set_min && kfmin > st_min && (kfmin - st_min) < 0.2) kfmin = st_min;
+    if (set_max && kfmax < st_max && (st_max - kfmax) < 1) kfmax = st_max;
+    std::vector<double> k;
+    if (nsp > 0) {
+        if (kfmax - kfmin < 1e-3) {
+            k = {kfmin, kfmax};
+        } else {
+            const double step = (kfmax - kfmin) / (double)(nsp - 1);
+            k.resize(nsp);
+            for (int i = 0; i < nsp; ++i) k[i] = kfmin + step * (double)i;
+        }
+    } else if (delta > 0) {
+        const int n = (int)std::ceil((kfmax - kfmin) / delta) + 1;
+        k.resize(n);
+        if (n == 1) {
+            k[0] = kfmin;
+        } else {
+            const double step = (kfmax - kfmin) / (double)(n - 1);
+            for (int i = 0; i < n; ++i) k[i] = (double)i * step + kfmin;
+            k[n - 1] = kfmax;
+        }
+    } else {
+        const int n = (int)(std::log(kfmax / kfmin) / std::log(ratio)) + 1;
+        k.resize(n);
+        for (int i = 0; i < n; ++i) k[i] = kfmin * std::pow(ratio, (double)i);
+    }
+    k.front() -= 1e-16;  // savetol
+    k.back() += 1e-16;
+    set_min = set_max = true;
+    st_min = kfmin;
+    st_max = kfmax;
+    return k;
+}
+
 std::vector<double> kf_nodes(double kfMin, double kfMax, int nsp, double delta, double ratio) {
     std::vector<double> k;
     if (nsp > 0) {

@@ -37,6 +37,13 @@ void guess_kf_bound(double kf_l, double kf_r, bool fixed_min, double kfmin_in, b
 // k_F nodes (lwt.py:174-190): nsp uniform nodes, spacing delta, or ratio.
 std::vector<double> kf_nodes(double kfMin, double kfMax, int nsp, double delta, double ratio);
 
+// k_F nodes of the HC kernels (get_kflist, hc.py:16-66): bounds snapped to powers
+// of ratio (kf0 = 1), kept from the saved state when they moved little; the
+// state is updated.
+std::vector<double> hc_kf_nodes(double kf_l, double kf_r, bool fixed_min, double kfmin_in, bool fixed_max,
+                                double kfmax_in, bool& set_min, double& st_min, bool& set_max, double& st_max,
+                                double ratio, int nsp, double delta);
+
 // Cardinal B-spline values of CBspline.calc_Mn (src/dftpy/ewald.py:63-82):
 // out[n] = M_order(x + n - 1), n = 1..order (out has order_full+1 entries).
 void bspline_mn(double x, int order, int order_full, double* out);

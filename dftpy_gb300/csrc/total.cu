@@ -314,7 +314,21 @@ struct Table {
     double limit, limitd;  // values at etamax
     double factor, lbda;   // table = factor * F(eta; lbda, 1); closed form used above eta_series
     double eta_series;     // FP32 path: closed-form large-eta series at and above this eta
+    int hc;                // HC scaling (HCKernelXi, kernel.py:496-506): node inverses are 1/(2k)
 };
+
+// Node kernel and derivative kernel of one node from the table values K, KD at
+// eta = q c: LWT K and KD c (c = 1/k); HC (c = 1/(2k)) K c^3 and (KD - 3K) c^3 2c.
+template <typename T>
+__device__ inline void scale_node(const Table<T>& tab, T c, T& K, T& kd, T KD) {
+    if (tab.hc) {
+        const T c3 = c * c * c;
+        kd = (KD - (T)3 * K) * c3 * ((T)2 * c);
+        K = K * c3;
+    } else {
+        kd = KD * c;
+    }
+}
 
 // Large-eta branch of the inverse Lindhard function (kernel.py:79-133) with
 // mu = 1: F = -lbda - 0.6 + sum_k c_k eta^{-2k}, and -eta dF/deta = sum_k 2k c_k
@@ -401,14 +415,14 @@ __global__ void k_lwt_nodes(const typename Cplx<T>::type* __restrict__ rbG, type
         const auto z = rbG[i];
         const T zr = z.x * invNt, zi = z.y * invNt;
         for (int jj = 0; jj < nb; ++jj) {
-            T K, KD;
+            T K, KD, kd;
             node_kernel(tab, q, sinvk[jj], mcalc != 0, i, K, KD);
+            scale_node(tab, sinvk[jj], K, kd, KD);
             typename Cplx<T>::type o;
             o.x = K * zr;
             o.y = K * zi;
             XY[(long long)jj * geo.Nc + i] = o;
             if (mcalc) {
-                const T kd = KD * sinvk[jj];
                 o.x = kd * zr;
                 o.y = kd * zi;
                 XY[(long long)(nb + jj) * geo.Nc + i] = o;
@@ -435,13 +449,14 @@ __global__ void k_lwt_pot2(const typename Cplx<T>::type* __restrict__ U, typenam
             si = pot2G[i].y;
         }
         for (int jj = 0; jj < nb; ++jj) {
-            T K, KD;
+            T K, KD, kd0;
             node_kernel(tab, q, sinvk[jj], hermite != 0, i, K, KD);
+            scale_node(tab, sinvk[jj], K, kd0, KD);
             const auto u = U[(long long)jj * geo.Nc + i];
             sr += K * invNt * u.x;
             si += K * invNt * u.y;
             if (hermite) {
-                const T kd = KD * sinvk[jj] * invNt;
+                const T kd = kd0 * invNt;
                 const auto w = U[(long long)(nb + jj) * geo.Nc + i];
                 sr += kd * w.x;
                 si += kd * w.y;
@@ -628,6 +643,10 @@ struct PostArgs {
     const T* pot1;
     const T* pot2;
     const T* pot3;
+    // HC: c1 = k_F,std (F - 4 F' s^2)/(3 rho) and the divergence term
+    int hc;
+    const T* hc_c1;
+    const T* hc_q;
     long long N;
     int vw, h, wt, lwt, same_ab, wantV, kdd;
     double vw_y;
@@ -679,7 +698,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
                 if (a.wantV) v += alpha * (pa / rc) * c1 + beta * (pb / rc) * a.nl2[i];
             }
         }
-        if (a.lwt) {
+        if (a.lwt && a.hc) {
+            // HC (hc.py:294-330): the energy without the low-density factor, the potential
+            // factor * (alpha rho^(alpha-1) pot1 + beta rho^(beta-1) pot2 + c1 rho^alpha pot3 - div)
+            const M rc = r < zero_clamp ? zero_clamp : r;
+            const M pa = a.same_ab ? a.rb[i] : a.ra[i];
+            sum[2].add(pa * a.pot1[i]);
+            if (a.wantV) {
+                M f = (M)1;
+                if (rc < (M)1e-6) f = mpow(fabs(rc), ld) / mpow(rhomax, ld);
+                const M pb = a.rb[i];
+                v += f * (alpha * (pa / rc) * a.pot1[i] + beta * (pb / rc) * a.pot2[i] + a.hc_c1[i] * pa * a.pot3[i] -
+                          a.hc_q[i]);
+            }
+        } else if (a.lwt) {
             // low-density factor (lwt.py:315-322) and the final combination (:324-339)
             M f = (M)1;
             if (r < (M)1e-6) f = mpow(fabs(r), ld) / mpow(rhomax, ld);
@@ -721,6 +753,7 @@ struct ofdft_eval {
     Scratch sc;
     void* vloc = nullptr;  // grid precision
     bool have_vloc = false;
+    bool tab_set = false;  // the k_F-node kernel table is on the device
     double* wtstate = nullptr;  // device [rho0, flag, tkf, factor, init]
     // density-dependent kernel
     void* tab_c = nullptr;
@@ -831,24 +864,10 @@ void timed(ofdft_eval* e, int cls, double bytes, cudaStream_t st, F&& f) {
     prof_end(e, idx, st);
 }
 
+// splines of the table values y(eta) and of -eta y'(eta) (lwt.py:554-556), uploaded
 template <typename T>
-void build_table(ofdft_eval* e) {
-    const ofdft_config& c = e->cfg;
-    const int neta = c.lwt_neta;
-    const double etamax = c.lwt_etamax;
-    std::vector<double> eta(neta), y(neta);
-    // numpy linspace(0, etamax, neta)
-    const double step = etamax / (double)(neta - 1);
-    for (int i = 0; i < neta; ++i) eta[i] = (double)i * step;
-    eta[neta - 1] = etamax;
-    if (c.lwt_kernel == OFDFT_LWT_KERNEL_WT) {
-        // WTKernelTable (kernel.py:344-352): F(eta; x, 1) * (4/5) * 0.3 (3 pi^2)^(2/3)
-        const double factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
-        for (int i = 0; i < neta; ++i) y[i] = lindhard(eta[i], c.lwt_x, 1.0) * factor;
-    } else {
-        const int sym = c.lwt_kernel == OFDFT_LWT_KERNEL_MGPA ? 1 : (c.lwt_kernel == OFDFT_LWT_KERNEL_MGPG ? 2 : 0);
-        y = mgp_kernel_table(eta, c.lwt_maxpoints, sym);
-    }
+void upload_table(ofdft_eval* e, const std::vector<double>& eta, const std::vector<double>& y) {
+    const int neta = (int)eta.size();
     CubicSpline S;
     S.fit(eta, y);
     std::vector<double> yd(neta);
@@ -861,14 +880,43 @@ void build_table(ofdft_eval* e) {
         hc[i] = (T)S.c[i];
         hcd[i] = (T)SD.c[i];
     }
-    OFDFT_CK(cudaMalloc(&e->tab_c, hc.size() * sizeof(T)));
-    OFDFT_CK(cudaMalloc(&e->tab_cd, hcd.size() * sizeof(T)));
+    if (!e->tab_c) OFDFT_CK(cudaMalloc(&e->tab_c, hc.size() * sizeof(T)));
+    if (!e->tab_cd) OFDFT_CK(cudaMalloc(&e->tab_cd, hcd.size() * sizeof(T)));
     upload_now(e->tab_c, hc.data(), hc.size() * sizeof(T));
     upload_now(e->tab_cd, hcd.data(), hcd.size() * sizeof(T));
     e->tab_nint = nint;
-    e->tab_step = step;
-    e->tab_limit = S.eval(etamax);
-    e->tab_limitd = SD.eval(etamax);
+    e->tab_step = eta[1] - eta[0];
+    e->tab_limit = S.eval(eta[neta - 1]);
+    e->tab_limitd = SD.eval(eta[neta - 1]);
+    e->tab_set = true;
+}
+
+// numpy linspace(0, etamax, neta)
+std::vector<double> table_eta(const ofdft_config& c) {
+    const int neta = c.lwt_neta;
+    std::vector<double> eta(neta);
+    const double step = c.lwt_etamax / (double)(neta - 1);
+    for (int i = 0; i < neta; ++i) eta[i] = (double)i * step;
+    eta[neta - 1] = c.lwt_etamax;
+    return eta;
+}
+
+template <typename T>
+void build_table(ofdft_eval* e) {
+    const ofdft_config& c = e->cfg;
+    if (c.lwt_kernel == OFDFT_LWT_KERNEL_USER) return;  // ofdft_eval_set_lwt_table supplies it
+    const int neta = c.lwt_neta;
+    const std::vector<double> eta = table_eta(c);
+    std::vector<double> y(neta);
+    if (c.lwt_kernel == OFDFT_LWT_KERNEL_WT) {
+        // WTKernelTable (kernel.py:344-352): F(eta; x, 1) * (4/5) * 0.3 (3 pi^2)^(2/3)
+        const double factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
+        for (int i = 0; i < neta; ++i) y[i] = lindhard(eta[i], c.lwt_x, 1.0) * factor;
+    } else {
+        const int sym = c.lwt_kernel == OFDFT_LWT_KERNEL_MGPA ? 1 : (c.lwt_kernel == OFDFT_LWT_KERNEL_MGPG ? 2 : 0);
+        y = mgp_kernel_table(eta, c.lwt_maxpoints, sym);
+    }
+    upload_table<T>(e, eta, y);
 }
 
 GgaSpec gga_spec(const ofdft_config& c) {
@@ -895,6 +943,7 @@ Table<T> table_of(const ofdft_eval* e) {
     t.lbda = e->cfg.lwt_x;
     // the large-eta series is the inverse Lindhard function's: WT tables only
     t.eta_series = e->cfg.lwt_kernel == OFDFT_LWT_KERNEL_WT ? 4.0 : INFINITY;
+    t.hc = e->cfg.lwt_family == OFDFT_LWT_FAMILY_HC ? 1 : 0;
     return t;
 }
 
@@ -1154,6 +1203,8 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     const bool wantV = (calc & OFDFT_CALC_V) != 0;
     const bool tf = c.kedf_terms & OFDFT_KE_TF, vw = c.kedf_terms & OFDFT_KE_VW;
     const bool wt = c.kedf_terms & OFDFT_KE_WT, lwt = c.kedf_terms & OFDFT_KE_LWT;
+    const bool hc = lwt && c.lwt_family == OFDFT_LWT_FAMILY_HC;
+    OFDFT_REQUIRE(!lwt || e->tab_set, "k_F-node kernel: no table set (ofdft_eval_set_lwt_table)");
     const bool nl = wt || lwt;
     const double alpha = wt ? c.wt_alpha : c.lwt_alpha, beta = wt ? c.wt_beta : c.lwt_beta;
     const bool same_ab = wt ? std::fabs(beta - alpha) < 1e-9 : std::fabs(alpha - beta) < 1e-8;
@@ -1185,10 +1236,10 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     pa.xc = xc;
     pa.pp = pp;
     pa.nl = nl;
-    pa.lwt = lwt;
+    pa.lwt = lwt && !hc;  // HC builds its k_F from the gradient below
     pa.same_ab = same_ab;
     pa.wantV = wantV;
-    pa.nl_is_lwt = lwt;
+    pa.nl_is_lwt = lwt && !hc;  // HC clamps rho at 1e-30 as WT does (hc.py:88-90)
     pa.tf_x = c.tf_x;
     pa.alpha = alpha;
     pa.beta = beta;
@@ -1223,10 +1274,61 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         launches++;
     }
 
+    // ---- HC: k_F = F(s) (3 pi^2 rho)^(1/3) from the gradient of the clamped density
+    T *hcD = nullptr, *hc_c1 = nullptr, *hc_c2 = nullptr;
+    C* hcX = nullptr;
+    C* hcG = nullptr;
+    if (hc) {
+        const int gblk = blocks_for(Nc, 256, g->sms * 16), rblk = blocks_for(N, 256, g->sms * 16);
+        T* rc = (T*)e->sc.get("hc_rc", rb);
+        hcG = (C*)e->sc.get("hc_G", cb);
+        hcX = (C*)e->sc.get("hc_X", 3 * cb);
+        hcD = (T*)e->sc.get("hc_D", 3 * rb);
+        if (wantV) {
+            hc_c1 = (T*)e->sc.get("hc_c1", rb);
+            hc_c2 = (T*)e->sc.get("hc_c2", rb);
+        }
+        k_hc_clamp<T><<<rblk, 256, 0, st>>>(rho, rc, N);
+        OFDFT_LAUNCH_CHECK();
+        r2c(rc, hcG, 1);
+        k_grad_spectra<T><<<gblk, 256, 0, st>>>(hcG, hcX, g->geo, 1.0 / (double)N);
+        OFDFT_LAUNCH_CHECK();
+        c2r(hcX, hcD, 3);
+        k_hc_point<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, hcD, kfv, hc_c1, hc_c2, N, gga_spec(c),
+                                                             g->d_partials);
+        OFDFT_LAUNCH_CHECK();
+        reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, 2, (1ull << 0) | (2ull << 2),
+                                                   g->d_results + 48);
+        OFDFT_LAUNCH_CHECK();
+        launches += 5;
+    }
+
     // ---- k_F node plan on the host (needs min/max k_F and max rho)
     LwtPlan lp;
     double rhomax = 0.0;
-    if (lwt) {
+    if (hc) {  // get_kflist (hc.py:144-158): nodes first (the state moves), then the HEG test
+        OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, 50 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OFDFT_CK(cudaStreamSynchronize(st));
+        const double kf_l = g->h_results[48], kf_r = g->h_results[49];
+        rhomax = g->h_results[6];
+        const bool fmin_ = !std::isnan(c.lwt_kfmin), fmax_ = !std::isnan(c.lwt_kfmax);
+        lp.nodes = hc_kf_nodes(kf_l, kf_r, fmin_, c.lwt_kfmin, fmax_, c.lwt_kfmax, e->kf_set_min, e->kf_st_min,
+                               e->kf_set_max, e->kf_st_max, c.lwt_ratio, c.lwt_nsp, c.lwt_delta);
+        const int m = (int)lp.nodes.size();
+        lp.active = !(std::fabs(kf_r - kf_l) < 1e-8 || m < 3);
+        if (lp.active) {
+            OFDFT_REQUIRE(m <= kMaxNodes, "density-dependent kernel: %d nodes (max %d)", m, kMaxNodes);
+            lp.kfclip = lp.nodes.back();
+            for (int i = 0; i < m; ++i) {
+                e->h_nodes[i] = lp.nodes[i];
+                e->h_nodes[kMaxNodes + i] = 1.0 / (2.0 * lp.nodes[i]);  // HCKernelXi: xi = 2k
+                e->h_nodes[2 * kMaxNodes + i] = lp.nodes[i] + 1e-18;
+            }
+            OFDFT_CK(cudaMemcpyAsync(e->d_nodes, e->h_nodes, 3 * kMaxNodes * sizeof(double), cudaMemcpyHostToDevice,
+                                     st));
+        }
+        e->last_nsp = lp.active ? m : 0;
+    } else if (lwt) {
         OFDFT_CK(cudaMemcpyAsync(g->h_results, g->d_results, PRE_NS * sizeof(double), cudaMemcpyDeviceToHost, st));
         OFDFT_CK(cudaStreamSynchronize(st));
         const double kf_l = g->h_results[4], kf_r = g->h_results[5];
@@ -1295,7 +1397,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
 
     // ---- density-dependent kernel
     T *pot1 = nullptr, *pot2 = nullptr, *pot3 = nullptr;
-    int kdd = wantV ? c.lwt_kdd : 1;
+    int kdd = wantV ? (hc ? 3 : c.lwt_kdd) : 1;  // HC keeps every derivative term
     if (lwt && lp.active) {
         const int m = (int)lp.nodes.size();
         const bool hermite = c.lwt_interp == OFDFT_INTERP_HERMITE;
@@ -1308,7 +1410,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         nd.invk = e->d_nodes + kMaxNodes;
         bool fused = false;
         if (c.lwt_pipeline != OFDFT_LWT_PIPE_CUFFT) {
-            fused = fz_applies(g, hermite, m);
+            fused = c.lwt_family == OFDFT_LWT_FAMILY_LWT && fz_applies(g, hermite, m);
             OFDFT_REQUIRE(fused || c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED,
                           "fused k_F-node pipeline: needs a float32 grid, linear interpolation, at most %d nodes and "
                           "power-of-two axes (32..256, the last 32..512)",
@@ -1404,6 +1506,19 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
             c2r(pot2G, pot2, 1);
         }
     }
+    // ---- HC: the divergence term of dk_F/d(grad rho) (hc.py:313-318)
+    T* hc_q = nullptr;
+    if (hc && wantV && lp.active) {
+        const int gblk = blocks_for(Nc, 256, g->sms * 16), rblk = blocks_for(N, 256, g->sms * 16);
+        k_hc_p<T><<<rblk, 256, 0, st>>>(hcD, hc_c2, same_ab ? rbp : rap, pot3, N);
+        OFDFT_LAUNCH_CHECK();
+        r2c(hcD, hcX, 3);
+        k_gga_div<T><<<gblk, 256, 0, st>>>(hcX, hcG, g->geo, 1.0 / (double)N);
+        OFDFT_LAUNCH_CHECK();
+        hc_q = hcD;  // the first gradient plane is free again
+        c2r(hcG, hc_q, 1);
+        launches += 4;
+    }
 
     // ---- post-pass
     PostArgs<T> qa;
@@ -1434,6 +1549,9 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     qa.rhomax = rhomax;
     qa.ld = std::max(0.1, c.lwt_ldw);
     qa.kfclip = lp.kfclip;
+    qa.hc = hc;
+    qa.hc_c1 = hc_c1;
+    qa.hc_q = hc_q;
     {
         const bool lw = lwt && lp.active;
         int reads = 1 + wantV + 2 * vw + h + (wt ? 2 + !same_ab * 2 : 0) +
@@ -1772,6 +1890,7 @@ void ofdft_config_default(ofdft_config* c) {
     c->gga_params[0] = 1.3;
     c->gga_params[1] = 1.0;
     c->gga_remove_vw = 0.0;
+    c->lwt_family = OFDFT_LWT_FAMILY_LWT;
     c->xc_lda = 1;
     c->hartree = 1;
     c->pseudo = 0;
@@ -1795,8 +1914,14 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
                           "lwt_interp must be linear or hermite");
             OFDFT_REQUIRE(c.lwt_nsp > 0 || c.lwt_delta > 0 || c.lwt_ratio > 1.0, "need nsp, delta or ratio > 1");
             OFDFT_REQUIRE(c.lwt_nsp != 1, "nsp must be >= 2");
-            OFDFT_REQUIRE(c.lwt_kernel >= OFDFT_LWT_KERNEL_WT && c.lwt_kernel <= OFDFT_LWT_KERNEL_MGPG,
+            OFDFT_REQUIRE(c.lwt_kernel >= OFDFT_LWT_KERNEL_WT && c.lwt_kernel <= OFDFT_LWT_KERNEL_USER,
                           "lwt_kernel must be one of OFDFT_LWT_KERNEL_*");
+            OFDFT_REQUIRE(c.lwt_family == OFDFT_LWT_FAMILY_LWT || c.lwt_family == OFDFT_LWT_FAMILY_HC,
+                          "lwt_family must be one of OFDFT_LWT_FAMILY_*");
+            OFDFT_REQUIRE(c.lwt_family != OFDFT_LWT_FAMILY_HC ||
+                              (c.lwt_interp == OFDFT_INTERP_HERMITE && c.gga_formula >= 0 &&
+                               c.gga_formula < OFDFT_GGA_NFORMULAS && c.gga_nparams >= 1 && c.gga_nparams <= 8),
+                          "HC: Hermite interpolation and a GGA enhancement factor are required");
             OFDFT_REQUIRE(c.lwt_kernel == OFDFT_LWT_KERNEL_WT || c.lwt_maxpoints >= 1, "lwt_maxpoints must be >= 1");
         }
         auto* e = new ofdft_eval();
@@ -1871,6 +1996,19 @@ int ofdft_eval_stress(ofdft_eval* e, const void* rho, const double* energies, do
         OFDFT_REQUIRE(e && rho && stress, "ofdft_eval_stress: null argument");
         if (e->g->prec == OFDFT_F64) stress_t<double>(e, (const double*)rho, energies, stress, (cudaStream_t)s);
         else stress_t<float>(e, (const float*)rho, energies, stress, (cudaStream_t)s);
+    });
+}
+
+int ofdft_eval_set_lwt_table(ofdft_eval* e, const double* table, int neta) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && table, "ofdft_eval_set_lwt_table: null argument");
+        OFDFT_REQUIRE(e->cfg.kedf_terms & OFDFT_KE_LWT, "ofdft_eval_set_lwt_table: no k_F-node term configured");
+        OFDFT_REQUIRE(neta == e->cfg.lwt_neta, "ofdft_eval_set_lwt_table: %d values, the evaluator has lwt_neta %d",
+                      neta, e->cfg.lwt_neta);
+        const std::vector<double> eta = table_eta(e->cfg);
+        const std::vector<double> y(table, table + neta);
+        if (e->g->prec == OFDFT_F64) upload_table<double>(e, eta, y);
+        else upload_table<float>(e, eta, y);
     });
 }
 

@@ -62,6 +62,12 @@ class NativeEval:
         _lib.check(self.lib.ofdft_eval_set_vloc(self.h, _lib.C.c_void_p(t.data_ptr()), stream_ptr()))
         self.vloc_token = token
 
+    def set_lwt_table(self, table):
+        """Kernel table of the k_F-node term (values at linspace(0, etamax, neta))."""
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        _lib.check(self.lib.ofdft_eval_set_lwt_table(self.h, t.ctypes.data_as(_lib._PD), len(t)))
+        self.lwt_table_set = True
+
     def set_ewald(self, energy):
         _lib.check(self.lib.ofdft_eval_set_ewald(self.h, float(energy)))
 

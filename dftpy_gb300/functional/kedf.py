@@ -15,7 +15,7 @@ from .functional_output import FunctionalOutput, ZeroFunctional
 
 __all__ = ["KEDF", "KEDFEngines"]
 
-_BITS = {"GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+_BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -41,7 +41,68 @@ KEDFEngines = {
     "LMGPA-NL": ("LMGPA-NL",),
     "LMGPG-NL": ("LMGPG-NL",),
     "GGA": ("GGA",),
+    "HC": ("TF", "VW", "HC-NL"),
+    "REVHC": ("TF", "VW", "REVHC-NL"),
+    "HC-NL": ("HC-NL",),
+    "REVHC-NL": ("REVHC-NL",),
 }
+
+# HC and revHC (hc.py:333-439): their defaults, and the enhancement factor of k_F
+_HC = {"HC-NL": {"functional": "HC", "params": None}, "REVHC-NL": {"functional": "PBE2", "params": [0.1, 0.45]}}
+
+
+def _hc_factor(functional, params):
+    """The GGA formula and parameters of F(s) in HC's k_F (hc.py:115-131):
+    'HC' F = 1 + lambda s^2 (the TFVW formula, p = [1, 3/5 lambda TKF0^2]);
+    'PBE2/3/4' of GGAFs (gga.py:936-968), F = 1 + b ss^2 / (1 + a ss^2) (+ ...),
+    which is the PBE formula with p = [b / a, b, ...]."""
+    f = str(functional).upper()
+    tk = 6.18733545256027186194
+    if f == "HC":
+        lam = 0.0 if params is None else float(params[0])
+        return _lib.GGA_TFVW, [1.0, 3.0 / 5.0 * lam * tk * tk]
+    if f in ("PBE2", "PBE3", "PBE4"):
+        p = list(GGA_FUNCTIONALS[f][1]) if params is None else list(params)
+        n = {"PBE2": 2, "PBE3": 3, "PBE4": 4}[f]
+        p = (p + list(GGA_FUNCTIONALS[f][1])[len(p):])[:n]
+        return _lib.GGA_PBE, [p[1] / p[0]] + p[1:]
+    raise NotImplementedError("HC with the %s enhancement factor is not supported (HC, PBE2-4 are)" % f)
+
+
+_HC_TABLES = {}
+
+
+def hc_kernel_table(eta, beta=2.0 / 3.0, x=1.0):
+    """HCKernelTable (kernel.py:460-478): beta eta K' = -5/3 F(eta; x, 1) + (5 - 3 beta)
+    beta K integrated with scipy's odeint from eta[-1], K(eta[-1]) = -8/3 / ((5 - 3 beta)
+    beta), down to 0; K[0] = 0; times C_TF 8 (3 pi^2).  F is evaluated as the
+    reference evaluates it on the float odeint passes: the closed form wherever it
+    applies (no large-eta series)."""
+    key = (float(beta), float(x), float(eta[-1]), len(eta))
+    if key in _HC_TABLES:
+        return _HC_TABLES[key]
+    from scipy.integrate import odeint
+
+    def lind(e, lbda, mu, tol=1e-10):
+        tol2 = tol / 10
+        if e > tol2 and abs(e - 1.0) > tol2:
+            return 1.0 / (0.5 + 0.25 * (1.0 - e ** 2) * np.log((1.0 + e) / np.abs(1.0 - e)) / e) - 3.0 * mu * e ** 2 - lbda
+        if e < tol:
+            return 1.0 - lbda + e ** 2 * (1.0 / 3.0 - 3.0 * mu)
+        return 2.0 - lbda - 3.0 * mu + 20.0 * (e - 1.0)
+
+    def deriv(k, e):
+        d = -5.0 / 3.0 * lind(e, x, 1) + (5.0 - 3.0 * beta) * beta * k
+        if e > 1e-20:
+            d /= beta * e
+        return d
+
+    sol = odeint(deriv, -8.0 / 3.0 / ((5.0 - 3.0 * beta) * beta), eta[::-1])
+    k = sol.ravel()[::-1].copy()
+    k[0] = 0.0
+    k *= 0.3 * (3.0 * np.pi ** 2) ** (2.0 / 3.0) * 8.0 * 3.0 * np.pi ** 2
+    _HC_TABLES[key] = k
+    return k
 
 # GGA_KEDF_list (gga.py:587-643): functional -> (formula, default parameters).  The
 # reference looks names up upper-cased, so its mixed-case 'PW91k' key is unreachable.
@@ -138,8 +199,10 @@ class KEDF(NativeFunctional):
         x = float(o.get("x", 1.0))
         cfg.tf_x = x
         cfg.vw_y = float(o.get("y", 1.0))
-        a = float(o.get("alpha", 5.0 / 6.0))
-        b = float(o.get("beta", 5.0 / 6.0))
+        engines = engines if engines is not None else self.engines()
+        hc = next((e for e in engines if e in _HC), None)
+        a = float(o.get("alpha", 2.0 if hc else 5.0 / 6.0))
+        b = float(o.get("beta", 2.0 / 3.0 if hc else 5.0 / 6.0))
         cfg.wt_alpha, cfg.wt_beta, cfg.wt_x = a, b, x
         rho0 = o.get("rho0")
         cfg.wt_rho0 = float(rho0) if rho0 else 0.0
@@ -149,7 +212,7 @@ class KEDF(NativeFunctional):
         cfg.lwt_delta = float(delta) if (nsp is None and delta is not None) else 0.0
         cfg.lwt_ratio = float(o.get("ratio", 1.15))
         cfg.lwt_kdd = int(o.get("kdd", 3))
-        interp = str(o.get("interp", "linear")).lower()
+        interp = str(o.get("interp", "hermite" if hc else "linear")).lower()
         if interp == "newton":
             interp = "linear"
         if interp not in ("linear", "hermite"):
@@ -176,6 +239,17 @@ class KEDF(NativeFunctional):
             table = "MGPA" if o.get("symmetrization") == "Arithmetic" else "MGPG"
         cfg.lwt_kernel = _KERNELS[table]
         cfg.lwt_maxpoints = int(o.get("maxpoints", 1000))
+        if hc:  # HC / revHC: k_F from F(s), HC nodes and kernel, the table integrated on the host
+            if interp != "hermite":
+                raise NotImplementedError("HC is built with Hermite interpolation (its default) only")
+            d = _HC[hc]
+            formula, p = _hc_factor(o.get("functional", d["functional"]), o.get("params", d["params"]))
+            cfg.lwt_family = _lib.LWT_FAMILY_HC
+            cfg.lwt_kernel = _lib.LWT_KERNEL_USER
+            cfg.gga_formula = formula
+            cfg.gga_nparams = len(p)
+            for i, v in enumerate(p):
+                cfg.gga_params[i] = float(v)
         if "GGA" in engines:  # gga.py:1212-1270: the functional named by k_str, default LKT
             name = str(o.get("k_str") or "LKT").upper()
             formula, p0 = GGA_FUNCTIONALS[name]
@@ -194,6 +268,10 @@ class KEDF(NativeFunctional):
     def prepare(self, ev, grid, dtype):
         s = self.ke_kernel_saved
         ev.set_kfbounds(s.get("kfmin"), s.get("kfmax"))
+        if ev.cfg.lwt_family == _lib.LWT_FAMILY_HC and not getattr(ev, "lwt_table_set", False):
+            c = ev.cfg
+            eta = np.linspace(0, c.lwt_etamax, c.lwt_neta)
+            ev.set_lwt_table(hc_kernel_table(eta, beta=c.lwt_beta, x=c.lwt_x))
 
     def finish(self, ev):
         kmin, kmax = ev.kfbounds()

@@ -104,7 +104,12 @@ enum { OFDFT_LWT_PIPE_AUTO = 0, OFDFT_LWT_PIPE_CUFFT = 1, OFDFT_LWT_PIPE_FUSED =
 /* kernel table of the k_F-node kernel (lwt.py:535-548): the WT table
  * (kernel.py:344-352, LWT) or the MGP table (kernel.py:267-322; LMGP, and with
  * the arithmetic / geometric symmetrisation LMGPA / LMGPG, lwt.py:571-578) */
-enum { OFDFT_LWT_KERNEL_WT = 0, OFDFT_LWT_KERNEL_MGP = 1, OFDFT_LWT_KERNEL_MGPA = 2, OFDFT_LWT_KERNEL_MGPG = 3 };
+enum { OFDFT_LWT_KERNEL_WT = 0, OFDFT_LWT_KERNEL_MGP = 1, OFDFT_LWT_KERNEL_MGPA = 2, OFDFT_LWT_KERNEL_MGPG = 3,
+       OFDFT_LWT_KERNEL_USER = 4 /* values from ofdft_eval_set_lwt_table */ };
+/* the k_F-node family: LWT (lwt.py:82-341) or HC (hc.py:68-331: k_F = F(s) (3 pi^2 rho)^(1/3)
+ * with F from gga_formula/gga_params, nodes by get_kflist, kernel T(q/2k)/(2k)^3, Hermite
+ * interpolation, and the gradient terms of dk_F/drho in the potential) */
+enum { OFDFT_LWT_FAMILY_LWT = 0, OFDFT_LWT_FAMILY_HC = 1 };
 
 typedef struct {
     int    kedf_terms;
@@ -137,6 +142,7 @@ typedef struct {
     int    gga_nparams;       /* parameters in gga_params (1..8)                   */
     double gga_params[8];
     double gga_remove_vw;     /* gga_remove_vw: vW share subtracted from F (0: none) */
+    int    lwt_family;        /* OFDFT_LWT_FAMILY_*                                */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);
@@ -169,6 +175,12 @@ int ofdft_eval_compute(ofdft_eval* e, const void* rho, void* v_out, unsigned cal
  * density-dependent (LWT) kernel it fails with OFDFT_EINVAL, as the reference's
  * KEDF.stress raises for 'LWT' (no stress engine, kedf/__init__.py:76-92). */
 int ofdft_eval_stress(ofdft_eval* e, const void* rho, const double* energies, double* stress, ofdft_stream s);
+
+/* Kernel table of the k_F-node term (lwt.py:535-566): its values at eta =
+ * linspace(0, lwt_etamax, lwt_neta) (neta = lwt_neta), splined as the built-in
+ * tables are.  Required with OFDFT_LWT_KERNEL_USER, e.g. the HC table, which the
+ * reference integrates with scipy's odeint (kernel.py:460-478). */
+int ofdft_eval_set_lwt_table(ofdft_eval* e, const double* table, int neta);
 
 /* Stateful parts of the evaluator that persist across calls like the
  * reference's ke_kernel_saved (kedf/__init__.py:101-111): the k_F bound state

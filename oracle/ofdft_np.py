@@ -578,6 +578,198 @@ class LWT:
 
 
 # --------------------------------------------------------------------------
+# HC / revHC (kedf/hc.py:16-439, kernel.py:460-506)
+# --------------------------------------------------------------------------
+def hc_kernel_table(eta, beta=2.0 / 3.0, x=1.0):
+    """HCKernelTable (kernel.py:460-478): the ODE beta eta K' = -5/3 F(eta; x, 1) +
+    (5 - 3 beta) beta K integrated by scipy's odeint from eta[-1] (K = -8/3 /
+    ((5 - 3 beta) beta)) down to 0, K[0] = 0, times C_TF 8 (3 pi^2)."""
+    from scipy.integrate import odeint
+
+    def lind_scalar(e, lbda, mu, tol=1e-10):
+        # LindhardFunction on a Python float (kernel.py:36-44): the first true
+        # branch wins, so above eta = 3.65 the closed form is used, not the series
+        tol2 = tol / 10
+        if e > tol2 and abs(e - 1.0) > tol2:
+            return 1.0 / (0.5 + 0.25 * (1.0 - e ** 2) * np.log((1.0 + e) / np.abs(1.0 - e)) / e) - 3.0 * mu * e ** 2 - lbda
+        if e < tol:
+            return 1.0 - lbda + e ** 2 * (1.0 / 3.0 - 3.0 * mu)
+        if abs(e - 1.0) < tol:
+            return 2.0 - lbda - 3.0 * mu + 20.0 * (e - 1.0)
+        return float(lindhard(np.array([e]), lbda, mu)[0])
+
+    def deriv(k, e):  # hc_ode_deriv (kernel.py:481-492), e a float as odeint passes it
+        d = -5.0 / 3.0 * lind_scalar(e, x, 1) + (5.0 - 3.0 * beta) * beta * k
+        if e > 1e-20:
+            d /= beta * e
+        return d
+
+    k_inf = -8.0 / 3.0 / ((5.0 - 3.0 * beta) * beta)
+    sol = odeint(deriv, k_inf, eta[::-1])
+    kernel = sol.ravel()[::-1].copy()
+    kernel[0] = 0.0
+    return kernel * (3.0 / 10.0) * (3.0 * np.pi ** 2) ** (2.0 / 3.0) * 8.0 * 3.0 * np.pi ** 2
+
+
+def hc_kflist(kf_min, kf_max, saved, kf0=1.0, ratio=1.15, nsp=None, delta=None, kfmin=None, kfmax=None,
+              savetol=1e-16):
+    """get_kflist (hc.py:16-66): bounds snapped to powers of ratio, kept from the
+    saved state when they moved little, nodes by nsp, delta or ratio."""
+    kfmin_prev, kfmax_prev = saved.get("kfmin"), saved.get("kfmax")
+    if kfmin is None:
+        kfmin = max(kf_min, 1e-3)
+        n = int(np.floor(np.log(kfmin / kf0) / np.log(ratio))) - 1
+        kfmin = kf0 * ratio ** n
+    if kfmax is None:
+        kfmax = min(kf_max, 100)
+        n = int(np.ceil(np.log(kfmax / kf0) / np.log(ratio))) + 1
+        kfmax = kf0 * ratio ** n
+    if kfmin_prev is not None and kfmin > kfmin_prev and (kfmin - kfmin_prev) < 0.2:
+        kfmin = kfmin_prev
+    if kfmax_prev is not None and kfmax < kfmax_prev and (kfmax_prev - kfmax) < 1:
+        kfmax = kfmax_prev
+    if nsp is not None:
+        if kfmax - kfmin < 1e-3:
+            kfl = np.array([kfmin, kfmax], dtype=np.float64)
+        else:
+            kfl = kfmin + (kfmax - kfmin) / (nsp - 1) * np.arange(nsp)
+    elif delta is not None:
+        kfl = np.linspace(kfmin, kfmax, int(np.ceil((kfmax - kfmin) / delta)) + 1)
+    else:
+        kfl = kfmin * ratio ** np.arange(int(np.log(kfmax / kfmin) / np.log(ratio)) + 1)
+    kfl = np.asarray(kfl, dtype=np.float64)
+    kfl[0] -= savetol
+    kfl[-1] += savetol
+    saved["kfmin"], saved["kfmax"] = kfmin, kfmax
+    return kfl
+
+
+def _ggafs_hc(s, functional, params):
+    """The enhancement factors HC and revHC use (hc.py:115-131, GGAFs gga.py:653-1210):
+    'HC' F = 1 + lambda s^2; 'PBE2' F = 1 + p1 ss^2 / (1 + p0 ss^2), ss = s / TKF0."""
+    f = functional.upper()
+    if f == "HC":
+        lam = 0.0 if params is None else params[0]
+        return 1 + lam * s * s, 2 * lam * np.ones_like(s)
+    if f == "PBE2":
+        p = [2.0309 / 0.2942, 2.0309] if params is None else list(params)
+        ss = s / TKF0
+        s2 = ss * ss
+        Fb = 1.0 + p[0] * s2
+        return 1.0 + p[1] * s2 / Fb, 2.0 * p[1] / (Fb * Fb) / (TKF0 * TKF0)
+    raise NotImplementedError(functional)
+
+
+class HC:
+    """HC / revHC (hc.py:68-439) with Hermite interpolation between nodes."""
+
+    def __init__(self, alpha=2.0, beta=2.0 / 3.0, x=1.0, etamax=50.0, neta=50000, ratio=1.15, nsp=None,
+                 delta=None, kfmin=None, kfmax=None, ldw=None, functional="HC", params=None):
+        self.alpha, self.beta, self.etamax = alpha, beta, etamax
+        self.ratio, self.nsp, self.delta, self.kfmin, self.kfmax, self.ldw = ratio, nsp, delta, kfmin, kfmax, ldw
+        self.functional, self.params = functional, params
+        eta = np.linspace(0, etamax, neta)
+        table = hc_kernel_table(eta, beta=beta, x=x)
+        self.tck = splrep(eta, table, k=3)
+        self.tckD = splrep(eta, splev(eta, self.tck, der=1) * (-1.0 * eta), k=3)
+        self.saved = {"kfmin": None, "kfmax": None}
+
+    def _xi(self, q, k):
+        """HCKernelXi (kernel.py:496-506): xi = 2k, K = T(q/xi)/xi^3, K' = (TD - 3T)/xi^3."""
+        xi = 2.0 * k
+        T = kernel_kf(q, xi, self.tck, self.etamax)
+        TD = kernel_kf(q, xi, self.tckD, self.etamax)
+        return T / xi ** 3, (TD - 3 * T) / xi ** 3
+
+    def __call__(self, rho_in, grid, calc=("E", "V")):
+        alpha, beta = self.alpha, self.beta
+        rho = rho_in.copy()
+        rho[rho < ZERO] = ZERO                                        # hc.py:88-90
+        rA = rho ** alpha
+        rA1 = rA / rho
+        if abs(alpha - beta) < 1e-8:
+            rB, rB1 = rA, rA1
+        else:
+            rB = rho ** beta
+            rB1 = rB / rho
+        rBG = fft(rB, grid)
+        rho43 = rho ** (4.0 / 3.0)
+        rho83 = rho43 * rho43
+        q = grid.q
+        rG = fft(rho, grid)
+        grad = [ifft(grid.g[i] * rG * 1j, grid) for i in range(3)]
+        s = np.sqrt(grad[0] ** 2 + grad[1] ** 2 + grad[2] ** 2) / rho43
+        F, dFds2 = _ggafs_hc(s, self.functional, self.params)
+        kf_std = np.cbrt(3.0 * np.pi ** 2 * rho)
+        kf = F * kf_std
+        kfl = hc_kflist(kf.min(), kf.max(), self.saved, 1.0, self.ratio, self.nsp, self.delta, self.kfmin,
+                        self.kfmax)
+        nsp = len(kfl)
+        out = {}
+        if abs(kf.max() - kf.min()) < 1e-8 or nsp < 3:              # hc.py:150-158 (HEG)
+            out["E"] = 0.0
+            out["V"] = np.zeros_like(rho)
+            return out
+        kf = np.where(kf > kfl[-1], kfl[-1], kf)
+        pot1 = np.zeros_like(rho)
+        pot3 = np.zeros_like(rho)
+
+        def node(j):
+            K, KD = self._xi(q, kfl[j])
+            KD = KD / kfl[j]
+            return K, ifft(K * rBG, grid), KD, ifft(KD * rBG, grid)
+
+        K0, p0, KD0, m0 = node(0)
+        small = kf < kfl[0] + 1e-18                                   # hc.py:203-215
+        t = (kf - kfl[0]) / kfl[0]
+        pot1[small] = p0[small] * t[small]
+        pot2G = K0 * fft(rA * np.where(small, t, 0.0), grid)
+        for i in range(nsp - 1):
+            K1, p1, KD1, m1 = node(i + 1)
+            m = np.logical_and(kf > kfl[i], kf < kfl[i + 1] + 1e-18)
+            u = np.where(m, rA, 0.0)
+            Dkf = kfl[i + 1] - kfl[i]
+            t = (kf - kfl[i]) / Dkf
+            t2 = t * t
+            t3 = t2 * t
+            h00 = 2.0 * t3 - 3.0 * t2 + 1.0
+            h10 = t3 - 2.0 * t2 + t
+            h01 = 1.0 - h00
+            h11 = t3 - t2
+            pot1[m] = h00[m] * p0[m] + h01[m] * p1[m] + Dkf * (h10[m] * m0[m] + h11[m] * m1[m])
+            pot2G = pot2G + (K0 * fft(u * h00, grid) + K1 * fft(u * h01, grid)
+                             + Dkf * (KD0 * fft(u * h10, grid) + KD1 * fft(u * h11, grid)))
+            tm, t2m = t[m], t2[m]
+            h00D = 6.0 * t2m - 6 * tm
+            h10D = 3.0 * t2m - 4 * tm + 1.0
+            h01D = -h00D
+            h11D = 3.0 * t2m - 2 * tm
+            pot3[m] = (h00D * p0[m] + h01D * p1[m]) / Dkf + h10D * m0[m] + h11D * m1[m]
+            K0, p0, KD0, m0 = K1, p1, KD1, m1
+        pot2 = ifft(pot2G, grid)
+        out["E"] = (rA * pot1).sum() * grid.dV                         # hc.py:294-297
+        if "V" in calc:                                               # hc.py:301-331
+            pot1 = pot1 * alpha * rA1
+            pot2 = pot2 * beta * rB1
+            pot3 = pot3 * rA
+            pot3_1 = kf_std / (3 * rho) * (F - 4 * dFds2 * s * s) * pot3
+            pot_dn = kf_std * dFds2 / rho83 * pot3
+            p3 = [fft(grad[i] * pot_dn, grid) for i in range(3)]
+            pot3G = grid.g[0] * p3[0] + grid.g[1] * p3[1] + grid.g[2] * p3[2]
+            pot3_2 = ifft(1j * pot3G, grid)
+            pot = pot1 + pot2 + pot3_1 - pot3_2
+            ldw = 1.0 / 6.0 if self.ldw is None else self.ldw
+            factor = np.ones_like(rho)
+            rhov = rho.max()
+            lm = rho < 1e-6
+            ld = max(0.1, ldw)
+            factor[lm] = np.abs(rho[lm]) ** ld / (rhov ** ld)
+            factor[rho < 0] = 0.0
+            out["V"] = pot * factor
+        return out
+
+
+# --------------------------------------------------------------------------
 # pseudopotential: recpot I/O, radial lines, PME structure factor
 # --------------------------------------------------------------------------
 def write_recpot(fname, gmax_bohr_inv, v_ha_bohr3, header="synthetic"):

@@ -15,7 +15,7 @@ _LIB = None
 OK, EINVAL, ECUDA, ECUFFT, ENOMEM, ESTATE = range(6)
 F64, F32 = 0, 1
 CALC_E, CALC_V = 1, 2
-E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, E_GGA, NE = range(11)
+E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, E_GGA, E_EXT, NE = range(12)
 S_TF, S_VW, S_NL, S_XC, S_H, S_GGA, NS = range(7)
 KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA = 1, 2, 4, 8, 16
 (GGA_LKT, GGA_LKTVW, GGA_DK, GGA_LLP, GGA_OL, GGA_THAK, GGA_B86A, GGA_B86B, GGA_DK87, GGA_PW86, GGA_PW91O, GGA_PW91,
@@ -25,6 +25,8 @@ LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
 LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG, LWT_KERNEL_USER = 0, 1, 2, 3, 4
 LWT_FAMILY_LWT, LWT_FAMILY_HC = 0, 1
 OPT_TN, OPT_LBFGS, OPT_CGHS = 0, 1, 2
+PRED_NONE, PRED_KERKER, PRED_INVERSE_KERKER, PRED_RESTA = 0, 1, 2, 3
+MIX_MAXM = 8
 
 
 class OfdftError(RuntimeError):
@@ -43,7 +45,7 @@ class Config(C.Structure):
         ("xc_lda", C.c_int), ("hartree", C.c_int), ("pseudo", C.c_int), ("ewald_energy", C.c_double),
         ("lwt_pipeline", C.c_int), ("lwt_kernel", C.c_int), ("lwt_maxpoints", C.c_int),
         ("gga_formula", C.c_int), ("gga_nparams", C.c_int), ("gga_params", C.c_double * 8),
-        ("gga_remove_vw", C.c_double), ("lwt_family", C.c_int),
+        ("gga_remove_vw", C.c_double), ("lwt_family", C.c_int), ("external", C.c_int),
     ]
 
 
@@ -58,6 +60,14 @@ class OptOptions(C.Structure):
 class OptResult(C.Structure):
     _fields_ = [("converged", C.c_int), ("niter", C.c_int), ("nfev", C.c_int), ("energy", C.c_double),
                 ("mu", C.c_double), ("dP", C.c_double)]
+
+
+class MixArgs(C.Structure):
+    _fields_ = [
+        ("predtype", C.c_int), ("predcoef", C.c_double * 3), ("cutoff", C.c_int), ("predecut", C.c_double),
+        ("coef", C.c_double), ("mask_coef", C.c_double), ("resw", C.c_double), ("ns", C.c_int),
+        ("dn", C.c_void_p * MIX_MAXM), ("dr", C.c_void_p * MIX_MAXM), ("x", C.c_double * MIX_MAXM),
+    ]
 
 
 PHI_FN = C.CFUNCTYPE(C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
@@ -84,6 +94,7 @@ _SIGS = {
     "ofdft_eval_destroy": (None, [_P]),
     "ofdft_eval_set_vloc": (_I, [_P, _P, _P]),
     "ofdft_eval_set_ewald": (_I, [_P, _D]),
+    "ofdft_eval_set_external": (_I, [_P, _P, _P]),
     "ofdft_eval_compute": (_I, [_P, _P, _P, C.c_uint, _PD, _P]),
     "ofdft_eval_stress": (_I, [_P, _P, _PD, _PD, _P]),
     "ofdft_eval_set_lwt_table": (_I, [_P, _PD, _I]),
@@ -107,6 +118,9 @@ _SIGS = {
     "ofdft_optimize_v": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P, _P]),
     "ofdft_optimize_batch": (_I, [_I, C.POINTER(_P), C.POINTER(_P), C.POINTER(OptOptions), C.POINTER(C.c_double),
                                   C.POINTER(OptResult), C.POINTER(_P), _P]),
+    "ofdft_mix_history": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P]),
+    "ofdft_mix_gram": (_I, [_P, C.POINTER(_P), _I, _PD, _P]),
+    "ofdft_mix_density": (_I, [_P, _P, _P, C.POINTER(MixArgs), _P, _P]),
     "ofdft_linesearch": (_I, [PHI_FN, _P, _D, _D, _D, _D, _D, _D, _D, _D, _I, _PD, _PD, _PD, _PI]),
 }
 

@@ -105,21 +105,22 @@ template <typename T>
 struct PreArgs {
     const T* rho;
     const T* vloc;
+    const T* vext;  // frozen external potential (ExternalPotential)
     T* V;
     T* sq;
     T* rb;
     T* ra;
     T* kf;
     long long N;
-    int tf, vw, xc, pp, nl, lwt, same_ab, wantV;
+    int tf, vw, xc, pp, ext, nl, lwt, same_ab, wantV;
     int nl_is_lwt;  // clamp rule: LWT clamps rho<=0, WT clamps rho<1e-30
     double tf_x;
     double alpha, beta;
     Consts k;
 };
 
-// slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho
-constexpr int PRE_NS = 7;
+// slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho, 7 external
+constexpr int PRE_NS = 8;
 
 // Per-thread running sum of a field reduction: float64 in the FP64 path; in the
 // FP32 path a float32 Kahan-compensated sum over the thread's points (GB300
@@ -150,9 +151,9 @@ struct RunSum<float> {
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* partials) {
     using M = T;
-    RunSum<M> sum[4];
+    RunSum<M> sum[5];
     M kfmin = (M)INFINITY, kfmax = -(M)INFINITY, rmax = -(M)INFINITY;
-    const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2};
+    const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2, 0};
     const M cTF_E = (M)a.k.cTF_E, cTF_V = (M)a.k.cTF_V, tf_x = (M)a.tf_x;
     const LdaC<M> lc(a.k);
     const M threepi2 = (M)a.k.threepi2, alpha = (M)a.alpha, beta = (M)a.beta;
@@ -184,6 +185,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
             sum[2].add(vl * r);
             v += vl;
         }
+        if (a.ext) {  // external_potential.py:30-35
+            const M ve = a.vext[i];
+            sum[4].add(ve * r);
+            v += ve;
+        }
         if (a.vw) a.sq[i] = msqrt(r > (M)0 ? r : tiny);  // kedf/vw.py:34-44
         if (a.nl) {
             const M rc = a.nl_is_lwt ? (r > (M)0 ? r : tiny) : (r < zero_clamp ? zero_clamp : r);
@@ -199,7 +205,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
         if (a.wantV) a.V[i] = v;
     }
     double acc[PRE_NS] = {sum[0].get(), sum[1].get(), sum[2].get(), sum[3].get(), (double)kfmin, (double)kfmax,
-                          (double)rmax};
+                          (double)rmax, sum[4].get()};
     block_reduce_store<PRE_NS>(acc, kinds, partials);
 }
 
@@ -753,6 +759,8 @@ struct ofdft_eval {
     Scratch sc;
     void* vloc = nullptr;  // grid precision
     bool have_vloc = false;
+    void* vext = nullptr;  // grid precision
+    bool have_vext = false;
     bool tab_set = false;  // the k_F-node kernel table is on the device
     double* wtstate = nullptr;  // device [rho0, flag, tkf, factor, init]
     // density-dependent kernel
@@ -770,7 +778,7 @@ struct ofdft_eval {
     bool fz_ran = false;           // the last evaluation ran the fused pipeline
     // terms of an evaluation whose energies have not been collected yet
     struct Pending {
-        bool tf, vw, wt, lwt, xc, h, pp, lp_active, gga;
+        bool tf, vw, wt, lwt, xc, h, pp, ext, lp_active, gga;
         int launches;
     } pend{};
     bool kf_set_min = false, kf_set_max = false;
@@ -1210,6 +1218,8 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     const bool same_ab = wt ? std::fabs(beta - alpha) < 1e-9 : std::fabs(alpha - beta) < 1e-8;
     const bool h = c.hartree != 0, xc = c.xc_lda != 0, pp = c.pseudo != 0 && e->have_vloc;
     OFDFT_REQUIRE(!(c.pseudo && !e->have_vloc), "ofdft_eval_compute: pseudo enabled but no v_loc set");
+    const bool ext = c.external != 0;
+    OFDFT_REQUIRE(!(ext && !e->have_vext), "ofdft_eval_compute: external potential enabled but not set");
     OFDFT_REQUIRE(!(wantV && !V), "ofdft_eval_compute: V requested but v_out is NULL");
     int launches = 0;
     const size_t rb = g->real_bytes(), cb = g->cplx_bytes();
@@ -1225,6 +1235,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     PreArgs<T> pa;
     pa.rho = rho;
     pa.vloc = pp ? (const T*)e->vloc : nullptr;
+    pa.vext = ext ? (const T*)e->vext : nullptr;
     pa.V = Vw;
     pa.sq = sq;
     pa.rb = rbp;
@@ -1235,6 +1246,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     pa.vw = vw;
     pa.xc = xc;
     pa.pp = pp;
+    pa.ext = ext;
     pa.nl = nl;
     pa.lwt = lwt && !hc;  // HC builds its k_F from the gradient below
     pa.same_ab = same_ab;
@@ -1247,7 +1259,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     const double s = (double)sizeof(T), Nd = (double)N, Ncd = (double)Nc;
     {
         // algorithmic bytes: read rho (+ v_loc); write V, sqrt(rho), rho^beta (+ rho^alpha), k_F as active
-        double b = Nd * s * (1 + pp + wantV + vw + nl + (nl && !same_ab) + lwt);
+        double b = Nd * s * (1 + pp + ext + wantV + vw + nl + (nl && !same_ab) + lwt);
         timed(e, P_PREPASS, b, st, [&] { k_prepass<T><<<g->red_blocks, RED_THREADS, 0, st>>>(pa, g->d_partials); });
     }
     OFDFT_LAUNCH_CHECK();
@@ -1583,6 +1595,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     e->pend.xc = xc;
     e->pend.h = h;
     e->pend.pp = pp;
+    e->pend.ext = ext;
     e->pend.lp_active = lwt && lp.active;
     e->pend.gga = gga;
     e->pend.launches = launches;
@@ -1618,8 +1631,9 @@ void collect_energies(ofdft_eval* e, double* energies) {
     if (p.lwt) E[OFDFT_E_NL] = p.lp_active ? R[18] * dV : 0.0;
     E[OFDFT_E_II] = c.ewald_energy;
     E[OFDFT_E_GGA] = p.gga ? R[40] * dV : 0.0;
+    E[OFDFT_E_EXT] = p.ext ? R[7] * dV : 0.0;
     E[OFDFT_E_TOTAL] = E[OFDFT_E_TF] + E[OFDFT_E_VW] + E[OFDFT_E_NL] + E[OFDFT_E_XC] + E[OFDFT_E_H] + E[OFDFT_E_PP] +
-                       E[OFDFT_E_II] + E[OFDFT_E_GGA];
+                       E[OFDFT_E_II] + E[OFDFT_E_GGA] + E[OFDFT_E_EXT];
     e->last_launches = p.launches;
 }
 
@@ -1949,6 +1963,7 @@ void ofdft_eval_destroy(ofdft_eval* e) {
     if (!e) return;
     e->sc.release_all();
     if (e->vloc) cudaFree(e->vloc);
+    if (e->vext) cudaFree(e->vext);
     if (e->wtstate) cudaFree(e->wtstate);
     if (e->tab_c) cudaFree(e->tab_c);
     if (e->tab_cd) cudaFree(e->tab_cd);
@@ -1970,6 +1985,15 @@ int ofdft_eval_set_vloc(ofdft_eval* e, const void* vloc_dev, ofdft_stream s) {
         if (!e->vloc) OFDFT_CK(cudaMalloc(&e->vloc, e->g->real_bytes()));
         OFDFT_CK(cudaMemcpyAsync(e->vloc, vloc_dev, e->g->real_bytes(), cudaMemcpyDeviceToDevice, (cudaStream_t)s));
         e->have_vloc = true;
+    });
+}
+
+int ofdft_eval_set_external(ofdft_eval* e, const void* v_dev, ofdft_stream s) {
+    return guard([&] {
+        OFDFT_REQUIRE(e && v_dev, "ofdft_eval_set_external: null argument");
+        if (!e->vext) OFDFT_CK(cudaMalloc(&e->vext, e->g->real_bytes()));
+        OFDFT_CK(cudaMemcpyAsync(e->vext, v_dev, e->g->real_bytes(), cudaMemcpyDeviceToDevice, (cudaStream_t)s));
+        e->have_vext = true;
     });
 }
 

@@ -1,5 +1,6 @@
 """Functional plugin API (src/dftpy/functional/__init__.py:11-51)."""
 from .abstract_functional import AbstractFunctional
+from .external_potential import ExternalPotential
 from .functional_output import FunctionalOutput, ZeroFunctional
 from .kedf import KEDF
 from .pseudo import LocalPseudo, ReadPseudo, RECPOT, read_recpot, write_recpot
@@ -7,13 +8,14 @@ from .semilocal import XC, Hartree
 from .total_functional import TotalFunctional
 
 __all__ = ["Functional", "FunctionalOutput", "ZeroFunctional", "AbstractFunctional", "TotalFunctional", "KEDF", "XC",
-           "Hartree", "LocalPseudo", "ReadPseudo", "RECPOT", "read_recpot", "write_recpot", "FunctionalTypeDict"]
+           "Hartree", "ExternalPotential", "LocalPseudo", "ReadPseudo", "RECPOT", "read_recpot", "write_recpot", "FunctionalTypeDict"]
 
 FunctionalTypeDict = {
     "KEDF": KEDF,
     "PSEUDO": LocalPseudo,
     "HARTREE": Hartree,
     "XC": XC,
+    "EXT": ExternalPotential,
 }
 
 

@@ -62,6 +62,10 @@ class NativeEval:
         _lib.check(self.lib.ofdft_eval_set_vloc(self.h, _lib.C.c_void_p(t.data_ptr()), stream_ptr()))
         self.vloc_token = token
 
+    def set_external(self, v):
+        """Copy a frozen external potential (device tensor of the evaluator dtype) in."""
+        _lib.check(self.lib.ofdft_eval_set_external(self.h, _lib.C.c_void_p(v.data_ptr()), stream_ptr()))
+
     def set_lwt_table(self, table):
         """Kernel table of the k_F-node term (values at linspace(0, etamax, neta))."""
         t = np.ascontiguousarray(table, dtype=np.float64)

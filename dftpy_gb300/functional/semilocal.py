@@ -60,10 +60,29 @@ class XC(NativeFunctional):
         return self._native_stress(density, E)[_lib.S_XC].copy()
 
 
+class _ClassOrInstance:
+    """A method that also works on the class, through one shared instance
+    (Hartree.compute is a classmethod in hartree.py:22-45)."""
+
+    def __init__(self, f):
+        self.f = f
+
+    def __get__(self, obj, cls):
+        if obj is None:
+            obj = cls.__dict__.get("_shared") or cls._make_shared()
+        return self.f.__get__(obj, cls)
+
+
 class Hartree(NativeFunctional):
     energy_slot = _lib.E_TOTAL
     out_name = "Hartree"
     _energy = None
+    _shared = None
+
+    @classmethod
+    def _make_shared(cls):
+        cls._shared = cls()
+        return cls._shared
 
     def __init__(self, **kwargs):
         self.type = "HARTREE"
@@ -76,6 +95,7 @@ class Hartree(NativeFunctional):
     def configure(self, cfg):
         cfg.hartree = 1
 
+    @_ClassOrInstance
     def compute(self, density, calcType={"E", "V"}, **kwargs):
         out = NativeFunctional.compute(self, density, calcType)
         if "E" in calcType:

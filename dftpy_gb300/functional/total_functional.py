@@ -70,7 +70,7 @@ class TotalFunctional(AbstractFunctional):
         for f in self.funcDict.values():
             cfg = empty_config()
             f.configure(cfg)
-            bits = cfg.kedf_terms | (cfg.xc_lda << 8) | (cfg.hartree << 9) | (cfg.pseudo << 10)
+            bits = cfg.kedf_terms | (cfg.xc_lda << 8) | (cfg.hartree << 9) | (cfg.pseudo << 10) | (cfg.external << 11)
             if bits & seen:
                 return False  # a term configured twice: evaluate separately and sum
             seen |= bits
@@ -127,7 +127,7 @@ class TotalFunctional(AbstractFunctional):
             v._N = None
             out.potential = v
         out.energies = {"TF": E[_lib.E_TF], "VW": E[_lib.E_VW], "NL": E[_lib.E_NL], "XC": E[_lib.E_XC],
-                        "HARTREE": E[_lib.E_H], "PSEUDO": E[_lib.E_PP], "II": E[_lib.E_II]}
+                        "HARTREE": E[_lib.E_H], "PSEUDO": E[_lib.E_PP], "II": E[_lib.E_II], "EXT": E[_lib.E_EXT]}
         return out
 
     def _separate(self, rho, calcType, split):

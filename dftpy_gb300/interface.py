@@ -1,0 +1,95 @@
+"""Config-driven density optimisation (src/dftpy/interface.py:150-229,
+OptimizeDensityConf) on the device backend.
+
+``config`` is the reference's nested configuration dictionary; the sections
+this path reads are OPT, MIX, JOB, MATH, DENSITY and OUTPUT, with the
+reference's defaults (src/dftpy/config/configentries.json) for any key left
+out.  With ``config['OPT']['algorithm'] == 'OESCF'`` the optimisation runs as
+OE-SCF with the embedding evaluator ``evaluator_emb`` and the configured mixer.
+"""
+import copy
+
+from .api import evaluator2results
+from .constants import HARTREE
+from .mixer import Mixer
+from .optimization import OESCF, Optimization
+
+__all__ = ["OptimizeDensityConf", "default_config"]
+
+# the reference's defaults of the sections OptimizeDensityConf reads
+_DEFAULTS = {
+    "OPT": {"method": "CG-HS", "algorithm": "EMM", "vector": "Orthogonalization", "c1": 1e-4, "c2": 0.2,
+            "maxls": 10, "econv": 1e-6, "maxfun": 50, "maxiter": 100, "xtol": 1e-12, "h0": 1},
+    "MIX": {"scheme": "pulay", "predtype": "kerker", "predcoef": [1.0, 1.0, 1.0], "predecut": None, "maxm": 7,
+            "coef": 0.7, "delay": 2, "restarted": False, "kf": "auto"},
+    "JOB": {"task": "Optdensity", "calctype": "Energy"},
+    "MATH": {"linearii": True, "linearie": True, "twostep": False, "multistep": 1, "reuse": True},
+    "DENSITY": {"densityoutput": None},
+    "OUTPUT": {"electrostatic_potential": None, "stress": True},
+    "GRID": {"gfull": False},
+}
+
+
+def default_config():
+    """A fresh copy of the defaults of the sections OptimizeDensityConf reads."""
+    return copy.deepcopy(_DEFAULTS)
+
+
+def _merged(config):
+    cfg = default_config()
+    for sec, vals in (config or {}).items():
+        if isinstance(vals, dict):
+            cfg.setdefault(sec, {}).update(vals)
+        else:
+            cfg[sec] = vals
+    return cfg
+
+
+def OptimizeDensityConf(config, ions=None, rho=None, E_v_Evaluator=None, nr2=None, evaluator_emb=None, **kwargs):
+    """interface.py:150-229: optimise the density as ``config`` says (OE-SCF or
+    a direct optimisation), then evaluate what JOB.calctype asks for and return
+    the results dictionary of evaluator2results."""
+    config = _merged(config)
+    rho_ini = rho
+    lscf = config["OPT"]["algorithm"] == "OESCF"
+    if config["MATH"]["multistep"] > 1:
+        raise NotImplementedError("multi-step grid refinement (MATH.multistep > 1) is not supported")
+    mix_kwargs = dict(config["MIX"])
+    if mix_kwargs.get("predecut"):
+        mix_kwargs["predecut"] *= 1.0 / HARTREE  # eV -> Hartree
+    mixer = Mixer(nspin=1, **mix_kwargs)
+    if "Optdensity" in config["JOB"]["task"]:
+        optimization_options = dict(config["OPT"])
+        optimization_options["econv"] *= ions.nat
+        if lscf:
+            optimization_options["algorithm"] = "EMM"
+            if evaluator_emb is None:
+                raise AttributeError("OE-SCF needs the embedding evaluator (evaluator_emb)")
+        opt = Optimization(EnergyEvaluator=E_v_Evaluator, optimization_options=optimization_options,
+                           optimization_method=config["OPT"]["method"])
+        if lscf:
+            opt = OESCF(optimization=opt, evaluator_emb=evaluator_emb, mixer=mixer)
+        rho = opt.optimize_rho(guess_rho=rho_ini)
+    if lscf:
+        E_v_Evaluator.UpdateFunctional(newFuncDict=evaluator_emb.funcDict)
+    calcType = set()
+    ct = config["JOB"]["calctype"]
+    if "Both" in ct:
+        calcType.update({"E", "V"})
+    if "Potential" in ct:
+        calcType.add("V")
+    if "Energy" in ct:
+        calcType.add("E")
+    if "Force" in ct:
+        calcType.add("F")
+    if "Stress" in ct:
+        calcType.add("S")
+    if config["DENSITY"]["densityoutput"]:
+        from .formats import write_density
+        write_density(config["DENSITY"]["densityoutput"], data=rho, ions=ions)
+    if config["OUTPUT"]["electrostatic_potential"]:
+        raise NotImplementedError("electrostatic potential output is not supported")
+    results = evaluator2results(E_v_Evaluator, rho=rho, calcType=calcType, ions=ions, **kwargs)
+    if lscf:
+        E_v_Evaluator.UpdateFunctional(keysToRemove=evaluator_emb.funcDict)
+    return results

@@ -17,7 +17,7 @@ from .functional.abstract_functional import NativeFunctional, stream_ptr
 from .functional.functional_output import FunctionalOutput
 from .functional.total_functional import TotalFunctional
 
-__all__ = ["Optimization", "optimize_rho_batch"]
+__all__ = ["Optimization", "optimize_rho_batch", "OESCF"]
 
 _METHODS = {"TN": _lib.OPT_TN, "LBFGS": _lib.OPT_LBFGS, "CG-HS": _lib.OPT_CGHS, "CG": _lib.OPT_CGHS}
 
@@ -263,3 +263,101 @@ def optimize_rho_batch(optimizations, guess_rhos, dtype=None, refine=None):
             o.phi = torch.sqrt(rho)
             out.append(rho)
     return out
+
+
+class OESCF:
+    """OE-SCF (src/dftpy/optimization/scf.py:6-119): the nonlocal part of the
+    kinetic functional (``evaluator_emb``) is frozen as an external potential,
+    the density is optimised with the rest (``optimization``, vW and the other
+    terms) on the device, and the outer loop mixes the densities (``mixer``,
+    dftpy_gb300.mixer) until the energy changes by less than econv.  The inner
+    convergence threshold tightens with the Hartree energy of the density
+    change (scf.py:62-81)."""
+
+    def __init__(self, optimization=None, evaluator_emb=None, guess_rho=None, mixer=None, maxiter=0):
+        from .functional.external_potential import ExternalPotential
+        self.optimization = optimization
+        self.evaluator_emb = evaluator_emb
+        self.rho = guess_rho
+        self.mixer = mixer
+        self.maxiter = maxiter
+        self.iter = 0
+        self.residual_norm_prev = 1.0
+        if self.maxiter < 1:
+            self.maxiter = self.options["maxiter"]
+        self.extfunctional = ExternalPotential()
+        self.error = 1.0
+        self.converged = False
+
+    @property
+    def options(self):
+        return self.optimization.optimization_options
+
+    def optimize_rho(self, **kwargs):
+        return self.run(**kwargs)
+
+    def run(self, guess_rho=None, **kwargs):
+        if guess_rho is None and self.rho is None:
+            raise AttributeError("Must provide a guess density")
+        elif guess_rho is not None:
+            self.rho = guess_rho
+        self.ncharges = float(self.rho.integral())
+        self.econv = self.options["econv"] * 1.0
+        self.energyhistory = []
+        self.converged = False
+        for i in range(self.maxiter):
+            self.get_density()
+            self.mix()
+            if self.error < self.econv:
+                self.converged = True
+                break
+        return self.rho
+
+    def get_density(self, norm=None, **kwargs):
+        self.iter += 1
+        scale = 1e-2
+        if norm is None:
+            if self.iter == 1:
+                norm = self.ncharges * 1e-1
+                self.options["econv"] = 1e10
+            elif self.iter == 2:
+                norm = self.ncharges * 1e-3
+            else:
+                norm = self.dp_norm
+        econv = max(norm * scale, 1e-7 * self.ncharges)
+        if econv < self.options["econv"]:
+            self.options["econv"] = econv
+        self.iterative(**kwargs)
+
+    def iterative(self, **kwargs):
+        self.rho_prev = self.rho.clone()
+        func = self.evaluator_emb(self.rho, calcType={"E", "V"})
+        self.extfunctional.v = func.potential
+        self.extenergy = func.energy - self.extfunctional(self.rho, calcType={"E"}).energy
+        funcs = self.optimization.EnergyEvaluator.funcDict
+        funcs["EMB"] = self.extfunctional
+        try:
+            self.optimization.optimize_rho(guess_rho=self.rho)
+        finally:
+            del funcs["EMB"]
+        self.rho = self.optimization.rho
+        self.functional = self.optimization.functional
+        self.functional.energy += self.extenergy
+        energy = self.functional.energy
+        if len(self.energyhistory) > 0:
+            self.error = abs(energy - self.energyhistory[-1])
+        else:
+            self.error = abs(energy)
+        self.energyhistory.append(energy)
+
+    def mix(self, **kwargs):
+        from .functional.semilocal import Hartree
+        r = self.rho - self.rho_prev
+        self.dp_norm = Hartree.compute(r, calcType={"E"}).energy
+        if self.iter == 1:
+            self.dp_norm_prev = self.dp_norm
+        else:
+            self.dp_norm, self.dp_norm_prev = self.dp_norm_prev, self.dp_norm
+            self.dp_norm = (self.dp_norm + self.dp_norm_prev) / 2
+        if self.mixer:
+            self.rho = self.mixer(self.rho_prev, self.rho, **kwargs)

@@ -41,7 +41,7 @@ enum { OFDFT_CALC_E = 1, OFDFT_CALC_V = 2 };
 
 /* energy slots written by ofdft_eval_compute (Hartree) */
 enum { OFDFT_E_TF = 0, OFDFT_E_VW, OFDFT_E_NL, OFDFT_E_XC, OFDFT_E_H, OFDFT_E_PP, OFDFT_E_II,
-       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_E_GGA, OFDFT_NE };
+       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_E_GGA, OFDFT_E_EXT, OFDFT_NE };
 /* stress tensors written by ofdft_eval_stress, 9 doubles (3 x 3, row-major) each */
 enum { OFDFT_S_TF = 0, OFDFT_S_VW, OFDFT_S_NL, OFDFT_S_XC, OFDFT_S_H, OFDFT_S_GGA, OFDFT_NS };
 
@@ -143,6 +143,7 @@ typedef struct {
     double gga_params[8];
     double gga_remove_vw;     /* gga_remove_vw: vW share subtracted from F (0: none) */
     int    lwt_family;        /* OFDFT_LWT_FAMILY_*                                */
+    int    external;          /* add the external potential set by ofdft_eval_set_external */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);
@@ -153,6 +154,11 @@ void ofdft_eval_destroy(ofdft_eval* e);
  * the evaluator (LocalPseudo._vreal, src/dftpy/functional/pseudo/__init__.py:219-234). */
 int ofdft_eval_set_vloc(ofdft_eval* e, const void* vloc_dev, ofdft_stream s);
 int ofdft_eval_set_ewald(ofdft_eval* e, double energy);
+/* Copy a frozen external potential (device pointer, grid precision) into the
+ * evaluator: ExternalPotential (functional/external_potential.py:7-40), energy
+ * dV sum(v rho) in OFDFT_E_EXT, v added to the potential.  OE-SCF freezes the
+ * embedding potential this way (optimization/scf.py:83-96). */
+int ofdft_eval_set_external(ofdft_eval* e, const void* v_dev, ofdft_stream s);
 
 /* TotalFunctional.compute(rho, calcType) (total_functional.py:107-146).
  * rho: device field (not modified).  v_out: device field for the total
@@ -160,6 +166,44 @@ int ofdft_eval_set_ewald(ofdft_eval* e, double energy);
  * host array of OFDFT_NE doubles (per-term energies, total, electron count). */
 int ofdft_eval_compute(ofdft_eval* e, const void* rho, void* v_out, unsigned calc,
                        double* energies, ofdft_stream s);
+
+/* ---- density mixing of OE-SCF (src/dftpy/mixer/mixer.py:8-169, pulay.py:8-120,
+ * linear.py:4-35).  Fields are device arrays in the grid's precision. */
+enum { OFDFT_PRED_NONE = 0, OFDFT_PRED_KERKER = 1, OFDFT_PRED_INVERSE_KERKER = 2, OFDFT_PRED_RESTA = 3 };
+#define OFDFT_MIX_MAXM 8
+
+/* PulayMixer history step (pulay.py:53-68, :101-102): r = nout - nin; unless
+ * first != 0, dn = nin - prev_n and dr = r - prev_r; then prev_n = nin and
+ * prev_r = r.  dn and dr may be NULL when first != 0. */
+int ofdft_mix_history(ofdft_grid* g, const void* nin, const void* nout, void* prev_n, void* prev_r, void* dn,
+                      void* dr, int first, ofdft_stream s);
+
+/* gram[i*nf+j] = sum over points of f_i f_j for nf fields (1..OFDFT_MIX_MAXM+1) in
+ * one pass: the Pulay matrix and right-hand side (pulay.py:70-77).  gram: host. */
+int ofdft_mix_gram(ofdft_grid* g, const void* const* fields, int nf, double* gram, ofdft_stream s);
+
+typedef struct {
+    int    predtype;          /* OFDFT_PRED_*: the G-space matrix (mixer.py:28-40, 72-117) */
+    double predcoef[3];       /* [a0 or epsilon, q0, amin or rs]                   */
+    int    cutoff;            /* nonzero: above gmax mix linearly (mixer.py:56-70, 136-139) */
+    double predecut;          /* Hartree: gmax = 2 predecut, or, below 2, the largest
+                                 |G|^2 along the three axes + 2                     */
+    double coef;              /* multiplies the residual term (pulay.py:90, linear.py:26) */
+    double mask_coef;         /* weight of nout above gmax                          */
+    double resw;              /* weight of nout - nin in the residual: 1 for the
+                                 mixers, 0 for a residual given as dr[0] with x[0] = 1 */
+    int    ns;                /* history terms used, 0..OFDFT_MIX_MAXM              */
+    const void* dn[OFDFT_MIX_MAXM];  /* NULL entries add nothing                   */
+    const void* dr[OFDFT_MIX_MAXM];
+    double x[OFDFT_MIX_MAXM]; /* Pulay coefficients                                 */
+} ofdft_mix_args;
+
+/* Mixed density (SpecialPrecondition.compute, mixer.py:126-140, with the Pulay
+ * combination of pulay.py:78-92): out = IFFT(FFT(nin + sum x_i dn_i) +
+ * M(G) FFT(coef (resw (nout - nin) + sum x_i dr_i))), and FFT((1 - mask_coef) nin +
+ * mask_coef nout) where |G|^2 > gmax.  out must not alias nin or nout. */
+int ofdft_mix_density(ofdft_grid* g, const void* nin, const void* nout, const ofdft_mix_args* a, void* out,
+                      ofdft_stream s);
 
 /* Stress tensors (Ha/Bohr^3) of the evaluator's terms on density rho, the
  * parts of TotalFunctional.get_stress (total_functional.py:176-208) that the

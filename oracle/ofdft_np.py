@@ -1888,3 +1888,174 @@ def _cg_direction(resA, dirA, method="CG-HS"):
     if not dirA:
         return -resA[-1]
     return -resA[-1] + beta * dirA[-1]
+
+
+# --------------------------------------------------------------------------
+# density mixing and OE-SCF
+# --------------------------------------------------------------------------
+def pred_matrix(grid, predtype, predcoef):
+    """SpecialPrecondition.matrix (mixer/mixer.py:28-40): None -> 1, kerker
+    (:72-80), inverse_kerker (:82-95, 0 at G = 0), resta (:97-113, 1 at G = 0)."""
+    pc = list(predcoef) + [1.0] * (3 - len(predcoef)) if predcoef else [0.8, 1.0, 1.0]
+    gg = grid.gg
+    if predtype is None:
+        return np.ones(gg.shape)
+    if predtype == "kerker":
+        return pc[0] * np.minimum(gg / (gg + pc[1] ** 2), pc[2])
+    if predtype == "inverse_kerker":
+        g = gg.copy()
+        g[0, 0, 0] = 1.0
+        m = pc[0] ** 2 / g + 1.0
+        m[0, 0, 0] = 0.0
+        return m
+    if predtype == "resta":
+        q = np.sqrt(gg)
+        q[0, 0, 0] = 1.0
+        m = (pc[1] ** 2 * np.sin(q * pc[2]) / (pc[0] * q * pc[2]) + gg) / (pc[1] ** 2 + gg)
+        m[0, 0, 0] = 1.0
+        return m
+    raise ValueError(predtype)
+
+
+def pred_mask(grid, predecut):
+    """SpecialPrecondition.mask (mixer.py:56-70): |G|^2 above gmax."""
+    gg = grid.gg
+    if predecut is None:
+        return np.zeros(gg.shape, dtype=bool)
+    if predecut < 2:
+        gmax = max(gg[:, 0, 0].max(), gg[0, :, 0].max(), gg[0, 0, :].max()) + 2
+    else:
+        gmax = 2.0 * predecut
+    return gg > gmax
+
+
+def precondition(nin, nout, grid, predtype, predcoef, predecut, drho=None, residual=None, coef=0.7):
+    """SpecialPrecondition.compute (mixer.py:126-140)."""
+    nin_g = fft(nin, grid)
+    results = nin_g.copy()
+    if drho is not None:
+        results += fft(drho, grid)
+    if residual is not None:
+        results += fft(residual, grid) * pred_matrix(grid, predtype, predcoef)
+    mask = pred_mask(grid, predecut)
+    if mask.any():
+        results[mask] = nin_g[mask] * (1 - coef) + coef * fft(nout, grid)[mask]
+    return ifft(results, grid)
+
+
+class PulayMixer:
+    """PulayMixer (mixer/pulay.py:8-120), Kresse and Furthmueller (1996)."""
+
+    def __init__(self, grid, predtype=None, predcoef=(0.8, 1.0, 1.0), maxm=5, coef=0.7, delay=0, predecut=None,
+                 restarted=False):
+        self.grid, self.predtype, self.predcoef, self.predecut = grid, predtype, list(predcoef), predecut
+        self.maxm, self.coef, self.delay, self.restarted = maxm, coef, delay, restarted
+        self.it = 0
+        self.dr_mat = self.dn_mat = None
+        self.prev_density = self.prev_residual = None
+
+    def _pred(self, nin, nout, drho=None, residual=None, coef=0.7):
+        return precondition(nin, nout, self.grid, self.predtype, self.predcoef, self.predecut, drho, residual, coef)
+
+    def __call__(self, nin, nout, coef=None):
+        from scipy import linalg
+        coef = self.coef if coef is None else coef
+        self.it += 1
+        r = nout - nin
+        if self.it == 1 and self.delay < 1:
+            results = self._pred(nin, nout, residual=r * coef)
+        elif self.it > self.delay:
+            if self.restarted and (self.it - self.delay) % (self.maxm + 1) == 0:
+                self.dr_mat = self.dn_mat = None
+            dn = nin - self.prev_density
+            dr = r - self.prev_residual
+            if self.dr_mat is None:
+                self.dr_mat, self.dn_mat = dr[None].copy(), dn[None].copy()
+            elif len(self.dr_mat) < self.maxm:
+                self.dr_mat = np.concatenate((self.dr_mat, dr[None]))
+                self.dn_mat = np.concatenate((self.dn_mat, dn[None]))
+            else:
+                self.dr_mat = np.roll(self.dr_mat, -1, axis=0)
+                self.dr_mat[-1] = dr
+                self.dn_mat = np.roll(self.dn_mat, -1, axis=0)
+                self.dn_mat[-1] = dn
+            ns = len(self.dr_mat)
+            amat = np.empty((ns, ns))
+            b = np.empty(ns)
+            for i in range(ns):
+                for j in range(i + 1):
+                    amat[i, j] = amat[j, i] = (self.dr_mat[i] * self.dr_mat[j]).sum()
+                b[i] = -(self.dr_mat[i] * r).sum()
+            try:
+                x = linalg.solve(amat, b, assume_a="sym")
+                drho = x[0] * self.dn_mat[0]
+                res = r + x[0] * self.dr_mat[0]
+                for i in range(1, ns):
+                    drho += x[i] * self.dn_mat[i]
+                    res += x[i] * self.dr_mat[i]
+                res *= coef
+                results = self._pred(nin, nout, drho, res, coef)
+            except Exception:
+                results = self._pred(nin, nout, residual=r * coef, coef=coef)
+        else:
+            results = nout.copy()
+        self.prev_density = nin + 0.0
+        self.prev_residual = r + 0.0
+        return results
+
+
+class LinearMixer:
+    """LinearMixer (mixer/linear.py:4-35)."""
+
+    def __init__(self, grid, predtype="inverse_kerker", predcoef=(0.8, 1.0, 1.0), coef=0.7, delay=0, predecut=None):
+        self.grid, self.predtype, self.predcoef, self.predecut = grid, predtype, list(predcoef), predecut
+        self.coef, self.delay, self.it = coef, delay, 0
+
+    def __call__(self, nin, nout, coef=None):
+        self.it += 1
+        coef = self.coef if coef is None else coef
+        if self.it > self.delay and coef < 1.0 - 1e-10:
+            return precondition(nin, nout, self.grid, self.predtype, self.predcoef, self.predecut,
+                                residual=(nout - nin) * coef, coef=coef)
+        return nout.copy()
+
+
+def oescf(terms, emb_terms, rho0, grid, mixer, econv, maxiter=100, method="CG-HS", opt_kw=None, ewald_energy=None):
+    """OESCF.run (optimization/scf.py:37-119): ``terms`` the inner functional (vW
+    and the rest, plus the Ewald energy), ``emb_terms`` the frozen embedding
+    part, both as make_terms lists; the inner optimisation is ``optimize``.
+    Returns (rho, {'history', 'iter'})."""
+    opts = dict(opt_kw or {})
+    ncharges = rho0.sum() * grid.dV
+    rho = rho0.copy()
+    state = {"econv": econv}
+    history, it, dp_norm, dp_prev = [], 0, None, None
+    for _ in range(maxiter):
+        it += 1
+        norm = ncharges * 1e-1 if it == 1 else (ncharges * 1e-3 if it == 2 else dp_norm)
+        if it == 1:
+            state["econv"] = 1e10
+        e = max(norm * 1e-2, 1e-7 * ncharges)
+        if e < state["econv"]:
+            state["econv"] = e
+        rho_prev = rho.copy()
+        emb = Total(grid, emb_terms)(rho, ("E", "V"))
+        v = emb["V"]
+        extenergy = emb["E"] - (v * rho).sum() * grid.dV
+        ev = Total(grid, list(terms) + [("EXT", lambda r, c, v=v: {"E": (v * r).sum() * grid.dV, "V": v})],
+                   ewald_energy=ewald_energy)
+        rho, info = optimize(ev, rho, grid, method=method, econv=state["econv"], **opts)
+        energy = info["energy"] + extenergy
+        error = abs(energy - history[-1]) if history else abs(energy)
+        history.append(energy)
+        dp = hartree(rho - rho_prev, grid, ("E",))["E"]
+        if it == 1:
+            dp_norm = dp_prev = dp
+        else:
+            dp_norm, dp_prev = dp_prev, dp
+            dp_norm = (dp_norm + dp_prev) / 2
+        if mixer is not None:
+            rho = mixer(rho_prev, rho)
+        if error < econv:
+            break
+    return rho, {"history": history, "iter": it}

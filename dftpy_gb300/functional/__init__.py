@@ -8,7 +8,8 @@ from .semilocal import XC, Hartree
 from .total_functional import TotalFunctional
 
 __all__ = ["Functional", "FunctionalOutput", "ZeroFunctional", "AbstractFunctional", "TotalFunctional", "KEDF", "XC",
-           "Hartree", "ExternalPotential", "LocalPseudo", "ReadPseudo", "RECPOT", "read_recpot", "write_recpot", "FunctionalTypeDict"]
+           "Hartree", "ExternalPotential", "LocalPseudo", "ReadPseudo", "RECPOT", "read_recpot", "write_recpot",
+           "FunctionalTypeDict"]
 
 FunctionalTypeDict = {
     "KEDF": KEDF,
@@ -20,7 +21,7 @@ FunctionalTypeDict = {
 
 
 def Functional(type=None, optional_kwargs=None, **kwargs):
-    """Functional(type='KEDF'|'XC'|'HARTREE'|'PSEUDO', **kwargs)."""
+    """Functional(type='KEDF'|'XC'|'HARTREE'|'PSEUDO'|'EXT', **kwargs)."""
     type = type.upper()
     if optional_kwargs is not None:
         kwargs.update(optional_kwargs)

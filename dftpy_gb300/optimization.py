@@ -304,6 +304,7 @@ class OESCF:
         self.ncharges = float(self.rho.integral())
         self.econv = self.options["econv"] * 1.0
         self.energyhistory = []
+        self.inner_stats = []  # per outer iteration: inner iterations, evaluations, econv
         self.converged = False
         for i in range(self.maxiter):
             self.get_density()
@@ -341,6 +342,9 @@ class OESCF:
         finally:
             del funcs["EMB"]
         self.rho = self.optimization.rho
+        res = self.optimization.result
+        if res is not None:
+            self.inner_stats.append({"niter": res.niter, "nfev": res.nfev, "econv": self.options["econv"]})
         self.functional = self.optimization.functional
         self.functional.energy += self.extenergy
         energy = self.functional.energy

@@ -86,6 +86,7 @@ _SIGS = {
     "ofdft_grid_info": (_I, [_P, _PI, _PD, _PD, _PI]),
     "ofdft_fft": (_I, [_P, _P, _P, _P]),
     "ofdft_ifft": (_I, [_P, _P, _P, _P]),
+    "ofdft_grid_map": (_I, [_P, _P, _P, _P, _D, _P]),
     "ofdft_dot": (_I, [_P, _P, _P, _PD, _P]),
     "ofdft_dot3": (_I, [_P, _P, _P, _P, _PD, _P]),
     "ofdft_dot_noalloc": (_I, [_P, _P, C.c_longlong, _I, _P, _P]),

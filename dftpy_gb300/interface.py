@@ -9,7 +9,12 @@ OE-SCF with the embedding evaluator ``evaluator_emb`` and the configured mixer.
 """
 import copy
 
+import numpy as np
+
 from .api import evaluator2results
+from .field import DirectField
+from .grid import DirectGrid
+from .utils import field2distrib
 from .constants import HARTREE
 from .mixer import Mixer
 from .optimization import OESCF, Optimization
@@ -52,8 +57,6 @@ def OptimizeDensityConf(config, ions=None, rho=None, E_v_Evaluator=None, nr2=Non
     config = _merged(config)
     rho_ini = rho
     lscf = config["OPT"]["algorithm"] == "OESCF"
-    if config["MATH"]["multistep"] > 1:
-        raise NotImplementedError("multi-step grid refinement (MATH.multistep > 1) is not supported")
     mix_kwargs = dict(config["MIX"])
     if mix_kwargs.get("predecut"):
         mix_kwargs["predecut"] *= 1.0 / HARTREE  # eV -> Hartree
@@ -70,6 +73,25 @@ def OptimizeDensityConf(config, ions=None, rho=None, E_v_Evaluator=None, nr2=Non
         if lscf:
             opt = OESCF(optimization=opt, evaluator_emb=evaluator_emb, mixer=mixer)
         rho = opt.optimize_rho(guess_rho=rho_ini)
+        # further steps on denser grids (interface.py:183-205)
+        grid = rho_ini.grid
+        nr = np.array(grid.nrR, dtype=int)
+        charge_total = ions.get_ncharges()
+        for istep in range(2, config["MATH"]["multistep"] + 1):
+            if istep == config["MATH"]["multistep"]:
+                if nr2 is None:
+                    nr2 = nr * 2
+                nr = np.array(nr2, dtype=int)
+            else:
+                nr = nr * 2
+            grid2 = DirectGrid(lattice=grid.lattice, nr=nr, full=config["GRID"]["gfull"])
+            rho_ini = DirectField(grid2, dtype=rho.dtype)
+            field2distrib(rho, rho_ini, root=0)
+            rho_ini = rho_ini * (charge_total / float(rho_ini.integral()))
+            pseudo = getattr(E_v_Evaluator, "PSEUDO", None)
+            if pseudo is not None:
+                pseudo.restart(full=False, ions=pseudo.ions, grid=grid2)
+            rho = opt.optimize_rho(guess_rho=rho_ini)
     if lscf:
         E_v_Evaluator.UpdateFunctional(newFuncDict=evaluator_emb.funcDict)
     calcType = set()

@@ -62,6 +62,14 @@ int ofdft_grid_info(const ofdft_grid* g, int nr[3], double* volume, double* dV, 
  * ofdft_ifft is not modified (it is copied to scratch first). */
 int ofdft_fft(ofdft_grid* g, const void* in_real, void* out_cplx, ofdft_stream s);
 int ofdft_ifft(ofdft_grid* g, const void* in_cplx, void* out_real, ofdft_stream s);
+/* Fourier interpolation of a real field from grid src to grid dst of the same
+ * cell (grid_map_data / grid_map_index, src/dftpy/utils/utils.py:50-128): the
+ * source coefficients keep their frequencies, those the destination lacks are
+ * dropped, the rest are zero.  dst must be finer or coarser on every axis.
+ * floor_value: values below it are raised to it (field2distrib's tol,
+ * utils.py:265), or -INFINITY for none.  in: src precision; out: dst field. */
+int ofdft_grid_map(ofdft_grid* src, ofdft_grid* dst, const void* in, void* out, double floor_value,
+                   ofdft_stream s);
 
 /* Reductions over a real field in float64 with a fixed summation order
  * (mp.einsum/vsum, src/dftpy/mpi/mpi.py:199-246).  out[0] = sum(a*b) (b may be

@@ -2059,3 +2059,39 @@ def oescf(terms, emb_terms, rho0, grid, mixer, econv, maxiter=100, method="CG-HS
         if error < econv:
             break
     return rho, {"history": history, "iter": it}
+
+
+# --------------------------------------------------------------------------
+# Fourier interpolation between grids of one cell
+# --------------------------------------------------------------------------
+def grid_map_index(nr, nr2):
+    """grid_map_index (utils/utils.py:50-78) for half grids: the coarse half
+    spectrum's indices in the fine one, and whether nr2 is the fine grid."""
+    coarse, fine = np.array(nr, dtype=int), np.array(nr2, dtype=int)
+    lfine = True
+    if np.all(fine < coarse) or (not np.all(fine > coarse) and not np.prod(fine) > np.prod(coarse)):
+        coarse, fine, lfine = fine, coarse, False
+    coarse = np.minimum(fine, coarse)
+    dnr = coarse.copy()
+    dnr[:2] = coarse[:2] // 2
+    index = np.mgrid[:coarse[0], :coarse[1], :coarse[2]].reshape((3, -1))
+    for i in range(3):
+        m = index[i] > dnr[i]
+        index[i][m] += fine[i] - coarse[i]
+    return index, lfine
+
+
+def grid_map(f, grid, nr_dst):
+    """grid_map_data(data, nr) (utils/utils.py:80-128): the field on the grid of
+    the same cell with nr_dst points."""
+    F = fft(f, grid)
+    g2 = Grid(grid.lattice, nr_dst)
+    nr1, nr2 = F.shape, tuple(g2.nrG)
+    G = np.zeros(nr2, dtype=np.complex128)
+    index, lfine = grid_map_index(nr1, nr2)
+    bd = np.minimum(nr1, nr2)
+    if lfine:
+        G[index[0], index[1], index[2]] = F[:bd[0], :bd[1], :bd[2]].ravel()
+    else:
+        G[:bd[0], :bd[1], :bd[2]] = F[index[0], index[1], index[2]].reshape(bd)
+    return ifft(G, g2)

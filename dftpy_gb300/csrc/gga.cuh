@@ -25,6 +25,7 @@ struct GgaSpec {
     int formula, np;
     double p[8];
     double remove_vw;  // gga_remove_vw: subtract F = 5/3 pa ss^2 (0: nothing)
+    double sigma;      // > 0: gradient smoothed by exp(-G^2 sigma^2/2)
 };
 
 constexpr double kTKF0 = 6.18733545256027186194;      // src/dftpy/constants.py:83
@@ -246,7 +247,8 @@ __device__ inline void gga_formula(const GgaSpec& sp, M s, M& F, M& d) {
 // numpy's gradient (DirectField.standard_gradient, field.py:267-281).
 template <typename T>
 __global__ void k_grad_spectra(const typename Cplx<T>::type* __restrict__ rhoG, typename Cplx<T>::type* X, Geo geo,
-                               double invN) {
+                               double invN, double sigma) {
+    const double s2 = sigma > 0.0 ? sigma * sigma / 2.0 : 0.0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < geo.Nc; idx += stride) {
         const int k = (int)(idx % geo.n2h);
@@ -265,7 +267,9 @@ __global__ void k_grad_spectra(const typename Cplx<T>::type* __restrict__ rhoG, 
         f2 *= geo.fv[2];
         const double g[3] = {f0 * geo.b[0] + f1 * geo.b[3] + f2 * geo.b[6], f0 * geo.b[1] + f1 * geo.b[4] + f2 * geo.b[7],
                              f0 * geo.b[2] + f1 * geo.b[5] + f2 * geo.b[8]};
-        const double rr = (double)rhoG[idx].x * invN, ri = (double)rhoG[idx].y * invN;
+        double sc = invN;
+        if (s2 > 0.0) sc *= exp(-gsq(geo, idx) * s2);  // field.py:243-248
+        const double rr = (double)rhoG[idx].x * sc, ri = (double)rhoG[idx].y * sc;
         for (int d = 0; d < 3; ++d) {
             X[d * geo.Nc + idx].x = (T)(-g[d] * ri);
             X[d * geo.Nc + idx].y = (T)(g[d] * rr);
@@ -439,7 +443,7 @@ void gga_enqueue(ofdft_grid* g, Scratch& sc, const GgaSpec& sp, const T* rho, T*
     T* D = (T*)sc.get("gga_D", 3 * rb);
     T* pot1 = V ? (T*)sc.get("gga_pot1", rb) : nullptr;
     g->exec_r2c(rho, rhoG, 1, st);
-    k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / (double)g->N);
+    k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / (double)g->N, sp.sigma);
     OFDFT_LAUNCH_CHECK();
     g->exec_c2r(X, D, 3, st);
     k_gga_point<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, D, pot1, g->N, sp, V ? 1 : 0, want_stress ? 1 : 0,

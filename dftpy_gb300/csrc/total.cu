@@ -64,6 +64,8 @@ __device__ inline double msqrt(double x) { return sqrt(x); }
 __device__ inline float msqrt(float x) { return sqrtf(x); }
 __device__ inline double mpow(double x, double y) { return pow(x, y); }
 __device__ inline float mpow(float x, float y) { return powf(x, y); }
+__device__ inline double mexp(double x) { return exp(x); }
+__device__ inline float mexp(float x) { return expf(x); }
 template <typename M>
 __device__ inline M pz(int k) {
     return sizeof(M) == 8 ? (M)cPZ[k] : (M)cPZf[k];
@@ -219,6 +221,7 @@ struct GArgs {
     T* wtK;                        // cached WT kernel (Nc)
     const double* wtstate;         // [saved rho0, recompute flag, tkf, factor]
     double wt_x;
+    double vw_s;                   // sigma^2/4 of the vW smoothing (0: none)
     Geo geo;
     double invN;
 };
@@ -261,8 +264,9 @@ __global__ void k_gspace(GArgs<T> a) {
             z.y = z.y * f;
             a.rhoG[i] = z;
         }
-        if (a.sqG) {  // vW: G^2 (vw.py:45-51) with the 1/2 folded in
-            const M f = half * gg * invN;
+        if (a.sqG) {  // vW: G^2 (vw.py:45-51) with the 1/2 folded in, smoothed with sigma (:47-48)
+            M f = half * gg * invN;
+            if (a.vw_s > 0.0) f *= mexp(-gg * (M)a.vw_s);
             auto z = a.sqG[i];
             z.x = z.x * f;
             z.y = z.y * f;
@@ -933,6 +937,7 @@ GgaSpec gga_spec(const ofdft_config& c) {
     s.np = c.gga_nparams;
     for (int i = 0; i < 8; ++i) s.p[i] = i < c.gga_nparams ? c.gga_params[i] : 0.0;
     s.remove_vw = c.gga_remove_vw;
+    s.sigma = c.gga_sigma;
     return s;
 }
 
@@ -1303,7 +1308,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         k_hc_clamp<T><<<rblk, 256, 0, st>>>(rho, rc, N);
         OFDFT_LAUNCH_CHECK();
         r2c(rc, hcG, 1);
-        k_grad_spectra<T><<<gblk, 256, 0, st>>>(hcG, hcX, g->geo, 1.0 / (double)N);
+        k_grad_spectra<T><<<gblk, 256, 0, st>>>(hcG, hcX, g->geo, 1.0 / (double)N, 0.0);
         OFDFT_LAUNCH_CHECK();
         c2r(hcX, hcD, 3);
         k_hc_point<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, hcD, kfv, hc_c1, hc_c2, N, gga_spec(c),
@@ -1390,6 +1395,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         ga.wtK = wtK;
         ga.wtstate = e->wtstate;
         ga.wt_x = c.wt_x;
+        ga.vw_s = c.vw_sigma > 0.0 ? c.vw_sigma * c.vw_sigma / 4.0 : 0.0;
         ga.geo = g->geo;
         ga.invN = 1.0 / (double)N;
         // read + write of each active complex plane (+ the cached WT kernel)
@@ -1862,7 +1868,7 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
     if (vw) {
         C* X = (C*)e->sc.get("st_X", 3 * cb);
         T* D = (T*)e->sc.get("st_D", 3 * rb);
-        k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N);
+        k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N, 0.0);
         OFDFT_LAUNCH_CHECK();
         g->exec_c2r(X, D, 3, st);
         k_stress_vw<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, D, g->N, g->d_partials);

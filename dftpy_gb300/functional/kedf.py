@@ -169,8 +169,6 @@ class KEDF(NativeFunctional):
 
     def _check_options(self):
         o = self.options
-        if o.get("sigma") is not None:
-            raise NotImplementedError("Gaussian smoothing of the vW term (sigma) is not supported")
         if str(o.get("kerneltype", "WT")).upper() not in _KERNELS:
             raise NotImplementedError("kernel tables WT, MGP, MGPA and MGPG are supported (got %r)"
                                       % o.get("kerneltype"))
@@ -200,6 +198,11 @@ class KEDF(NativeFunctional):
         cfg.tf_x = x
         cfg.vw_y = float(o.get("y", 1.0))
         engines = engines if engines is not None else self.engines()
+        # Gaussian smoothing: of the vW Laplacian (vw.py:45-48) and of the GGA gradient (gga.py:1246-1250)
+        sigma = o.get("sigma")
+        sigma = 0.0 if sigma is None else float(sigma)
+        cfg.vw_sigma = sigma if "VW" in engines else 0.0
+        cfg.gga_sigma = sigma if "GGA" in engines else 0.0
         hc = next((e for e in engines if e in _HC), None)
         a = float(o.get("alpha", 2.0 if hc else 5.0 / 6.0))
         b = float(o.get("beta", 2.0 / 3.0 if hc else 5.0 / 6.0))

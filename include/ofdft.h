@@ -152,6 +152,9 @@ typedef struct {
     double gga_remove_vw;     /* gga_remove_vw: vW share subtracted from F (0: none) */
     int    lwt_family;        /* OFDFT_LWT_FAMILY_*                                */
     int    external;          /* add the external potential set by ofdft_eval_set_external */
+    double vw_sigma;          /* > 0: vW Laplacian times exp(-G^2 sigma^2/4) (kedf/vw.py:45-48) */
+    double gga_sigma;         /* > 0: GGA gradient times exp(-G^2 sigma^2/2), the
+                                 'supersmooth' gradient (gga.py:1246-1250, field.py:229-262) */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

@@ -161,13 +161,17 @@ def tf(rho, grid, x=1.0, calc=("E", "V")):
     return out
 
 
-def vw(rho, grid, y=1.0, calc=("E", "V")):
-    """von Weizsaecker (kedf/vw.py:29-53 potential, :84-94 energy, :115-131)."""
+def vw(rho, grid, y=1.0, calc=("E", "V"), sigma=None):
+    """von Weizsaecker (kedf/vw.py:29-53 potential, :84-94 energy, :115-131);
+    sigma: the Laplacian times exp(-G^2 sigma^2/4) (:45-48)."""
     tol = 1e-30
     rhom = rho.copy()
     rhom[~(rho > 0)] = tol
     sq = np.sqrt(rhom)
-    a = ifft(fft(sq, grid) * grid.gg, grid) * 0.5
+    if sigma is None:
+        a = ifft(fft(sq, grid) * grid.gg, grid) * 0.5
+    else:
+        a = ifft(fft(sq, grid) * np.exp(-grid.gg * sigma ** 2 / 4.0) * grid.gg, grid) * 0.5
     sq[np.abs(sq) < tol] = tol
     pot = a / sq
     out = {}
@@ -1398,14 +1402,17 @@ GGA_FUNCTIONALS = {
 }
 
 
-def _gradient(rho, grid):
-    """DirectField.standard_gradient (field.py:267-281): irfftn(i g rho(G))."""
+def _gradient(rho, grid, sigma=None):
+    """DirectField.standard_gradient (field.py:267-281): irfftn(i g rho(G)); with
+    sigma the 'supersmooth' gradient (field.py:229-262), times exp(-G^2 sigma^2/2)."""
     rhoG = fft(rho, grid)
-    return [ifft(1j * grid.g[i] * rhoG, grid) for i in range(3)]
+    if sigma is None:
+        return [ifft(1j * grid.g[i] * rhoG, grid) for i in range(3)]
+    return [ifft(grid.g[i] * (rhoG * 1j) * np.exp(-grid.gg * sigma ** 2 / 2.0), grid) for i in range(3)]
 
 
-def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw=None):
-    """GGA (kedf/gga.py:1212-1325) without gradient smoothing (sigma None)."""
+def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw=None, sigma=None):
+    """GGA (kedf/gga.py:1212-1325); sigma smooths the density gradient (:1246-1250)."""
     name = functional.upper()
     fn, p0 = GGA_FUNCTIONALS[name]
     p = list(p0)
@@ -1419,7 +1426,7 @@ def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw
     tf = C_TF * rho53
     rho43 = rho23 * rho23
     rho83 = rho43 * rho43
-    grad = _gradient(rho, grid)
+    grad = _gradient(rho, grid, sigma)
     s = np.sqrt(_power_int(grad[0], 2) + _power_int(grad[1], 2) + _power_int(grad[2], 2)) / rho43
     s[s < 1e-16] = 1e-16
     F, dFds2 = fn(s, p)

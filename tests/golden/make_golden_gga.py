@@ -40,15 +40,23 @@ def main(ref_root):
     names = sorted(n for n in GGA_KEDF_list if n.upper() in GGA_KEDF_list)
     out["names"] = np.array(names)
     cases = [(n, n, {}) for n in names] + [("LKT_P", "LKT", {"params": [1.1, 0.9]}),
-                                          ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0})]
+                                          ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0}),
+                                          ("LKT_SIG", "LKT", {"sigma": 0.2}),
+                                          ("LC94_SIG", "LC94", {"sigma": 0.35})]
     for tag, name, kw in cases:
         rA = DirectField(grid=gridA, data=g0["A_rho"].copy())
         r = GGA(rA, functional=name, calcType={"E", "V", "S"}, **kw)
         out["A_E_" + tag] = float(r.energy)
         out["A_V_" + tag] = np.asarray(r.potential)
         out["A_S_" + tag] = np.asarray(r.stress)
+    # the vW term with Gaussian smoothing of its Laplacian (vw.py:29-53)
+    for tag, kw in (("VW_SIG", {"sigma": 0.2}), ("TFVW_SIG", {"sigma": 0.35})):
+        rA = DirectField(grid=gridA, data=g0["A_rho"].copy())
+        r = Functional(type="KEDF", name=tag.split("_")[0], **kw)(rA)
+        out["A_E_" + tag] = float(r.energy)
+        out["A_V_" + tag] = np.asarray(r.potential)
     np.savez_compressed(os.path.join(HERE, "reference_gga.npz"), **out)
-    print(len(cases), "cases")
+    print(len(cases) + 2, "cases")
 
 
 if __name__ == "__main__":

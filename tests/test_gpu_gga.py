@@ -22,7 +22,8 @@ from dftpy_gb300 import synthetic as syn
 HERE = os.path.dirname(os.path.abspath(__file__))
 GG = dict(np.load(os.path.join(HERE, "golden", "reference_gga.npz")))
 CASES = [(str(n), str(n), {}) for n in GG["names"]] + [("LKT_P", "LKT", {"params": [1.1, 0.9]}),
-                                                       ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0})]
+                                                       ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0}),
+                                                       ("LKT_SIG", "LKT", {"sigma": 0.2}), ("LC94_SIG", "LC94", {"sigma": 0.35})]
 
 
 def _np(f):
@@ -95,3 +96,28 @@ def test_gga_ground_state():
     mix.optimize_rho_mixed(guess_rho=rho0, refine="optimize")
     # both stop at the econv rule (1e-6 Ha/atom per iteration), from different paths
     assert abs(mix.functional.energy - opt.functional.energy) / 4 <= 1e-5
+
+
+@pytest.mark.parametrize("tag,name,sigma", [("VW_SIG", "vW", 0.2), ("TFVW_SIG", "TFVW", 0.35)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32], ids=["f64", "f32"])
+def test_vw_sigma_against_reference(golden, tag, name, sigma, dtype):
+    """vW with the Laplacian smoothed by exp(-G^2 sigma^2/4) (vw.py:29-53)."""
+    grid = D.DirectGrid(golden["A_lattice"], golden["A_nr"])
+    rho = D.DirectField(grid, data=golden["A_rho"], dtype=dtype)
+    o = D.Functional(type="KEDF", name=name, sigma=sigma)(rho)
+    e, v = GG["A_E_" + tag], GG["A_V_" + tag]
+    tol = (1e-10, 1e-9) if dtype == torch.float64 else (2e-6, 1e-4)
+    assert abs(o.energy - e) <= tol[0] * abs(e), (o.energy, e)
+    assert float(np.abs(_np(o.potential) - v).max()) <= tol[1] * float(np.abs(v).max())
+
+
+def test_gga_sigma_fp32():
+    grid = D.DirectGrid(np.diag([15.2, 15.2, 15.2]), (64, 64, 64))
+    rho_np = syn.smooth_density(grid.lattice, (64, 64, 64), 32.0, seed=12, amp=0.5)
+    out = {}
+    for dt in (torch.float64, torch.float32):
+        o = D.Functional(type="KEDF", name="GGA", k_str="LKT", sigma=0.3)(D.DirectField(grid, data=rho_np, dtype=dt))
+        out[dt] = (o.energy, _np(o.potential))
+    (e64, v64), (e32, v32) = out[torch.float64], out[torch.float32]
+    assert abs(e32 - e64) <= 2e-6 * abs(e64)
+    assert float(np.abs(v32 - v64).max()) <= 1e-4 * float(np.abs(v64).max())

@@ -11,7 +11,8 @@ from oracle import ofdft_np as O
 HERE = os.path.dirname(os.path.abspath(__file__))
 GG = dict(np.load(os.path.join(HERE, "golden", "reference_gga.npz")))
 CASES = [(n, n, {}) for n in GG["names"]] + [("LKT_P", "LKT", {"params": [1.1, 0.9]}),
-                                             ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0})]
+                                             ("LKT_RVW", "LKT", {"gga_remove_vw": 1.0}),
+                                             ("LKT_SIG", "LKT", {"sigma": 0.2}), ("LC94_SIG", "LC94", {"sigma": 0.35})]
 
 
 @pytest.mark.parametrize("tag,name,kw", CASES, ids=[c[0] for c in CASES])
@@ -31,3 +32,17 @@ def test_gga_reference_fixture(golden):
     e = O.gga(golden["E_rho"], grid, "LC94", calc=("E",))["E"]
     assert abs(e - GG["fixture_E_LC94"]) <= 1e-12 * abs(e)
     assert np.isclose(e, 1.6821337114254904)  # the reference's own test value
+
+
+@pytest.mark.parametrize("tag,name,sigma", [("VW_SIG", "VW", 0.2), ("TFVW_SIG", "TFVW", 0.35)])
+def test_vw_sigma(golden, tag, name, sigma):
+    """The vW term with the Gaussian-smoothed Laplacian (vw.py:29-53)."""
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    rho = golden["A_rho"]
+    r = O.vw(rho, grid, sigma=sigma)
+    e, v = r["E"], r["V"]
+    if name == "TFVW":
+        t = O.tf(rho, grid)
+        e, v = e + t["E"], v + t["V"]
+    assert abs(e - GG["A_E_" + tag]) <= 1e-11 * abs(e)
+    np.testing.assert_allclose(v, GG["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(v).max())

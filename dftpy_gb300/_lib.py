@@ -19,7 +19,7 @@ E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, E_GGA, E_EXT, NE = ra
 S_TF, S_VW, S_NL, S_XC, S_H, S_GGA, NS = range(7)
 KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA = 1, 2, 4, 8, 16
 (GGA_LKT, GGA_LKTVW, GGA_DK, GGA_LLP, GGA_OL, GGA_THAK, GGA_B86A, GGA_B86B, GGA_DK87, GGA_PW86, GGA_PW91O, GGA_PW91,
- GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV, GGA_PBE2M, GGA_PG) = range(22)
+ GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV, GGA_PBE2M, GGA_PG, GGA_GE2, GGA_GE4, GGA_PGSL, GGA_PGSLR) = range(26)
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
 LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
 LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG, LWT_KERNEL_USER = 0, 1, 2, 3, 4

@@ -18,7 +18,9 @@ namespace gga {
 enum GgaFormula {
     GGA_LKT = 0, GGA_LKTVW, GGA_DK, GGA_LLP, GGA_OL, GGA_THAK, GGA_B86A, GGA_B86B, GGA_DK87, GGA_PW86,
     GGA_PW91O, GGA_PW91, GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV,
-    GGA_PBE2M, GGA_PG, GGA_NFORMULAS
+    GGA_PBE2M, GGA_PG,
+    // MGGA_KEDF_list (gga.py:645-650), F(s, q)
+    GGA_GE2, GGA_GE4, GGA_PGSL, GGA_PGSLR, GGA_NFORMULAS
 };
 
 struct GgaSpec {
@@ -26,6 +28,7 @@ struct GgaSpec {
     double p[8];
     double remove_vw;  // gga_remove_vw: subtract F = 5/3 pa ss^2 (0: nothing)
     double sigma;      // > 0: gradient smoothed by exp(-G^2 sigma^2/2)
+    int meta;          // a Laplacian-level formula (formula >= GGA_GE2)
 };
 
 constexpr double kTKF0 = 6.18733545256027186194;      // src/dftpy/constants.py:83
@@ -241,13 +244,58 @@ __device__ inline void gga_formula(const GgaSpec& sp, M s, M& F, M& d) {
     }
 }
 
-// X_d = i g_d FFT(rho) / N, d = 0, 1, 2, as three consecutive planes.  numpy's
+// Meta-GGA F(s, q), F' = (1/s) dF/ds and dF/dq (GE2, GE4, PGSL, PGSLr,
+// gga.py:492-545), all in ss = s / TKF0 with F' rescaled by 1/TKF0^2, and
+// gga_remove_vw as in gga_formula.
+template <typename M>
+__device__ inline void mgga_formula(const GgaSpec& sp, M s, M q, M& F, M& d, M& dq) {
+    const M p0 = (M)sp.p[0], p1 = (M)sp.p[1], p2 = (M)sp.p[2], p3 = (M)sp.p[3], p4 = (M)sp.p[4], p5 = (M)sp.p[5];
+    const M tk = (M)kTKF0;
+    const M ss = s / tk;
+    const M s2 = ss * ss;
+    switch (sp.formula) {
+        case GGA_GE2:
+            F = p0 + p1 * s2 + p2 * q;
+            d = (M)2 * p1;
+            dq = p2;
+            break;
+        case GGA_GE4:
+            F = (p0 + p1 * s2 + p2 * q) + (p3 * q * q + p4 * q * s2 + p5 * s2 * s2);
+            d = (M)2 * p1 + ((M)2 * p4 * q + (M)4 * p5 * s2);
+            dq = p2 + ((M)2 * p3 * q + p4 * s2);
+            break;
+        case GGA_PGSL: {
+            const M Fa = exp(-p1 * s2);
+            F = Fa + q * q * p0 + (M)(5.0 / 3.0) * p2 * s2;
+            d = (M)-2 * p1 * Fa + (M)(10.0 / 3.0) * p2;
+            dq = (M)2 * p0 * q;
+            break;
+        }
+        default: {  // GGA_PGSLR: PGSL with the parameters from the third on
+            const M Fa = exp(-p3 * s2);
+            F = (Fa + q * q * p2 + (M)(5.0 / 3.0) * p4 * s2) + (-p0 * q * s2 + p1 * s2 * s2);
+            d = ((M)-2 * p3 * Fa + (M)(10.0 / 3.0) * p4) + ((M)-2 * p0 * q + (M)4 * p1 * s2);
+            dq = (M)2 * p2 * q + (-p0 * s2);
+            break;
+        }
+    }
+    d /= tk * tk;
+    if (sp.remove_vw != 0.0) {
+        const M pa = (M)sp.remove_vw;
+        F -= (M)(5.0 / 3.0) * pa * s2;
+        d -= (M)(10.0 / 3.0) * pa / (tk * tk);
+    }
+}
+
+// X_d = i g_d FFT(rho) / N, d = 0, 1, 2, as three consecutive planes, and with
+// lap != 0 a fourth, -G^2 FFT(rho) / N (DirectField.laplacian, field.py:379-386).
+// Under sigma both are smoothed by exp(-G^2 sigma^2/2).  numpy's
 // irfftn keeps only the Hermitian part of the k2 = 0 and k2 = n2/2 planes, so
 // there a Nyquist frequency index counts as zero; any C2R of X then returns
 // numpy's gradient (DirectField.standard_gradient, field.py:267-281).
 template <typename T>
 __global__ void k_grad_spectra(const typename Cplx<T>::type* __restrict__ rhoG, typename Cplx<T>::type* X, Geo geo,
-                               double invN, double sigma) {
+                               double invN, double sigma, int lap) {
     const double s2 = sigma > 0.0 ? sigma * sigma / 2.0 : 0.0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < geo.Nc; idx += stride) {
@@ -274,15 +322,23 @@ __global__ void k_grad_spectra(const typename Cplx<T>::type* __restrict__ rhoG, 
             X[d * geo.Nc + idx].x = (T)(-g[d] * ri);
             X[d * geo.Nc + idx].y = (T)(g[d] * rr);
         }
+        if (lap) {
+            const double gg = gsq(geo, idx);
+            X[3 * geo.Nc + idx].x = (T)(-gg * rr);
+            X[3 * geo.Nc + idx].y = (T)(-gg * ri);
+        }
     }
 }
 
 // Y = i (g . P(G)) / N from the three planes P_d = FFT(p_d), with the same
 // Hermitian-part rule on the k2 = 0 and k2 = n2/2 planes (the reference's
 // (1j * pot3G).ifft(force_real=True), gga.py:1297-1301)
+// With lap != 0, the fourth plane P_q enters as + G^2 exp(-G^2 sigma^2/2) P_q / N:
+// minus the Laplacian of p_q (gga.py:1305-1308), as Y is subtracted from pot1.
 template <typename T>
 __global__ void k_gga_div(const typename Cplx<T>::type* __restrict__ P, typename Cplx<T>::type* Y, Geo geo,
-                          double invN) {
+                          double invN, int lap, double sigma) {
+    const double s2 = sigma > 0.0 ? sigma * sigma / 2.0 : 0.0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < geo.Nc; idx += stride) {
         const int k = (int)(idx % geo.n2h);
@@ -306,8 +362,16 @@ __global__ void k_gga_div(const typename Cplx<T>::type* __restrict__ P, typename
             sr += g[d] * (double)P[d * geo.Nc + idx].x;
             si += g[d] * (double)P[d * geo.Nc + idx].y;
         }
-        Y[idx].x = (T)(-si * invN);
-        Y[idx].y = (T)(sr * invN);
+        double yr = -si * invN, yi = sr * invN;
+        if (lap) {
+            const double gg = gsq(geo, idx);
+            double f = gg * invN;
+            if (s2 > 0.0) f *= exp(-gg * s2);
+            yr += f * (double)P[3 * geo.Nc + idx].x;
+            yi += f * (double)P[3 * geo.Nc + idx].y;
+        }
+        Y[idx].x = (T)yr;
+        Y[idx].y = (T)yi;
     }
 }
 
@@ -333,11 +397,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_gga_point(const T* __restrict__
         const M dx = D[i], dy = D[N + i], dz = D[2 * N + i];
         M s = sqrt(dx * dx + dy * dy + dz * dz) / rho43;
         if (s < (M)1e-16) s = (M)1e-16;
-        M F, dF;
-        gga_formula(sp, s, F, dF);
+        M F, dF, dq = (M)0, q = (M)0;
+        if (sp.meta) {
+            q = D[3 * N + i] / (M)(kTKF0 * kTKF0) / rho53;  // gga.py:1254-1257
+            mgga_formula(sp, s, q, F, dF, dq);
+        } else {
+            gga_formula(sp, s, F, dF);
+        }
         acc[0] += (double)(tf * F);
         if (pot1 || want_stress) {
-            const M p1 = (M)(5.0 / 3.0) * ctf * rho23 * F + (M)(-4.0 / 3.0) * tf * dF * s * s / rm;
+            M p1 = (M)(5.0 / 3.0) * ctf * rho23 * F + (M)(-4.0 / 3.0) * tf * dF * s * s / rm;
+            if (sp.meta) {  // tf dF/dq dq0, and p_q = tf dF/dq dq2 for the Laplacian (gga.py:1305-1308)
+                p1 += tf * dq * ((M)(-5.0 / 3.0) * q / rm);
+                if (want_p) D[3 * N + i] = tf * dq * ((M)(1.0 / (kTKF0 * kTKF0)) / rho53);
+            }
             if (pot1) pot1[i] = p1;
             const M w = tf * dF / rho83;
             if (want_stress) {
@@ -439,21 +512,22 @@ void gga_enqueue(ofdft_grid* g, Scratch& sc, const GgaSpec& sp, const T* rho, T*
     const int gblk = blocks_for(g->Nc, 256, g->sms * 16);
     const int rblk = blocks_for(g->N, 256, g->sms * 16);
     C* rhoG = (C*)sc.get("gga_rhoG", cb);
-    C* X = (C*)sc.get("gga_X", 3 * cb);
-    T* D = (T*)sc.get("gga_D", 3 * rb);
+    const int np = sp.meta ? 4 : 3;  // gradient planes, and the Laplacian for a meta-GGA
+    C* X = (C*)sc.get("gga_X", np * cb);
+    T* D = (T*)sc.get("gga_D", np * rb);
     T* pot1 = V ? (T*)sc.get("gga_pot1", rb) : nullptr;
     g->exec_r2c(rho, rhoG, 1, st);
-    k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / (double)g->N, sp.sigma);
+    k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / (double)g->N, sp.sigma, sp.meta);
     OFDFT_LAUNCH_CHECK();
-    g->exec_c2r(X, D, 3, st);
+    g->exec_c2r(X, D, np, st);
     k_gga_point<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, D, pot1, g->N, sp, V ? 1 : 0, want_stress ? 1 : 0,
                                                           g->d_partials);
     OFDFT_LAUNCH_CHECK();
     reduce_finalize<<<1, RED_THREADS, 0, st>>>(g->d_partials, g->red_blocks, 8, 0ull, out_dev);
     OFDFT_LAUNCH_CHECK();
     if (!V) return;
-    g->exec_r2c(D, X, 3, st);
-    k_gga_div<T><<<gblk, 256, 0, st>>>(X, rhoG, g->geo, 1.0 / (double)g->N);
+    g->exec_r2c(D, X, np, st);
+    k_gga_div<T><<<gblk, 256, 0, st>>>(X, rhoG, g->geo, 1.0 / (double)g->N, sp.meta, sp.sigma);
     OFDFT_LAUNCH_CHECK();
     T* q = D;  // the first gradient plane is free again
     g->exec_c2r(rhoG, q, 1, st);

@@ -938,6 +938,7 @@ GgaSpec gga_spec(const ofdft_config& c) {
     for (int i = 0; i < 8; ++i) s.p[i] = i < c.gga_nparams ? c.gga_params[i] : 0.0;
     s.remove_vw = c.gga_remove_vw;
     s.sigma = c.gga_sigma;
+    s.meta = c.gga_formula >= OFDFT_GGA_GE2 ? 1 : 0;
     return s;
 }
 
@@ -1308,7 +1309,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         k_hc_clamp<T><<<rblk, 256, 0, st>>>(rho, rc, N);
         OFDFT_LAUNCH_CHECK();
         r2c(rc, hcG, 1);
-        k_grad_spectra<T><<<gblk, 256, 0, st>>>(hcG, hcX, g->geo, 1.0 / (double)N, 0.0);
+        k_grad_spectra<T><<<gblk, 256, 0, st>>>(hcG, hcX, g->geo, 1.0 / (double)N, 0.0, 0);
         OFDFT_LAUNCH_CHECK();
         c2r(hcX, hcD, 3);
         k_hc_point<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, hcD, kfv, hc_c1, hc_c2, N, gga_spec(c),
@@ -1531,7 +1532,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         k_hc_p<T><<<rblk, 256, 0, st>>>(hcD, hc_c2, same_ab ? rbp : rap, pot3, N);
         OFDFT_LAUNCH_CHECK();
         r2c(hcD, hcX, 3);
-        k_gga_div<T><<<gblk, 256, 0, st>>>(hcX, hcG, g->geo, 1.0 / (double)N);
+        k_gga_div<T><<<gblk, 256, 0, st>>>(hcX, hcG, g->geo, 1.0 / (double)N, 0, 0.0);
         OFDFT_LAUNCH_CHECK();
         hc_q = hcD;  // the first gradient plane is free again
         c2r(hcG, hc_q, 1);
@@ -1854,6 +1855,7 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
     // GGA (gga.py:1306-1318): P = E - int pot1 rho - sum_i int w (d_i rho)^2, sigma_ii = P - int w (d_i rho)^2,
     // sigma_ij = -int w d_i rho d_j rho, w = tf F' / rho^(8/3), over V
     if (c.kedf_terms & OFDFT_KE_GGA) {
+        OFDFT_REQUIRE(c.gga_formula < OFDFT_GGA_GE2, "ofdft_eval_stress: no stress for a meta-GGA (gga.py:1313-1314)");
         gga_enqueue<T>(g, e->sc, gga_spec(c), rho, nullptr, false, true, g->d_results + 40, st);
         OFDFT_CK(cudaMemcpyAsync(g->h_results + 40, g->d_results + 40, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
         OFDFT_CK(cudaStreamSynchronize(st));
@@ -1868,7 +1870,7 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
     if (vw) {
         C* X = (C*)e->sc.get("st_X", 3 * cb);
         T* D = (T*)e->sc.get("st_D", 3 * rb);
-        k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N, 0.0);
+        k_grad_spectra<T><<<gblk, 256, 0, st>>>(rhoG, X, g->geo, 1.0 / N, 0.0, 0);
         OFDFT_LAUNCH_CHECK();
         g->exec_c2r(X, D, 3, st);
         k_stress_vw<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rho, D, g->N, g->d_partials);
@@ -1940,7 +1942,7 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
                           "lwt_family must be one of OFDFT_LWT_FAMILY_*");
             OFDFT_REQUIRE(c.lwt_family != OFDFT_LWT_FAMILY_HC ||
                               (c.lwt_interp == OFDFT_INTERP_HERMITE && c.gga_formula >= 0 &&
-                               c.gga_formula < OFDFT_GGA_NFORMULAS && c.gga_nparams >= 1 && c.gga_nparams <= 8),
+                               c.gga_formula < OFDFT_GGA_GE2 && c.gga_nparams >= 1 && c.gga_nparams <= 8),
                           "HC: Hermite interpolation and a GGA enhancement factor are required");
             OFDFT_REQUIRE(c.lwt_kernel == OFDFT_LWT_KERNEL_WT || c.lwt_maxpoints >= 1, "lwt_maxpoints must be >= 1");
         }

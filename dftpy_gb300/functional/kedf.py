@@ -41,6 +41,7 @@ KEDFEngines = {
     "LMGPA-NL": ("LMGPA-NL",),
     "LMGPG-NL": ("LMGPG-NL",),
     "GGA": ("GGA",),
+    "MGGA": ("GGA",),
     "HC": ("TF", "VW", "HC-NL"),
     "REVHC": ("TF", "VW", "REVHC-NL"),
     "HC-NL": ("HC-NL",),
@@ -134,6 +135,14 @@ GGA_FUNCTIONALS = {
     "PBE2M": (_L.GGA_PBE2M, [1.0, 0.2942, 2.0309]), "PG": (_L.GGA_PG, [0.75, 1.0]),
 }
 
+# MGGA_KEDF_list (gga.py:645-650): Laplacian-level functionals F(s, q)
+MGGA_FUNCTIONALS = {
+    "GE2": (_L.GGA_GE2, [1.0, 5.0 / 27.0, 20.0 / 9.0]),
+    "GE4": (_L.GGA_GE4, [1.0, 5.0 / 27.0, 20.0 / 9.0, 8.0 / 81.0, -1.0 / 9.0, 8.0 / 243.0]),
+    "PGSL": (_L.GGA_PGSL, [0.25, 40.0 / 27.0, 1.0]),
+    "PGSLR": (_L.GGA_PGSLR, [0.40, 0.20, 0.25, 40.0 / 27.0, 1.0]),
+}
+
 
 # engines with a stress (KEDFEngines_Stress, kedf/__init__.py:76-92): slot in the
 # stress and energy arrays of the native evaluator
@@ -156,8 +165,11 @@ class KEDF(NativeFunctional):
         if self.name.startswith("GGA_"):  # kedf/__init__.py:134-137
             kwargs["k_str"] = self.name[4:]
             self.name = "GGA"
-        if self.name.startswith("MGGA_") or self.name == "MGGA":
-            raise NotImplementedError("meta-GGA kinetic functionals are not supported")
+        if self.name.startswith("MGGA_"):  # kedf/__init__.py:138-142
+            kwargs["k_str"] = self.name[5:]
+            self.name = "MGGA"
+        if self.name == "MGGA":
+            kwargs["mgga"] = True
         if self.name not in KEDFEngines:
             raise NotImplementedError("KEDF %r is not on the accelerated path (have %s)" % (self.name,
                                                                                           sorted(KEDFEngines)))
@@ -181,10 +193,11 @@ class KEDF(NativeFunctional):
         if o.get("temperature") or o.get("temperature0"):
             raise NotImplementedError("finite-temperature TF is not supported")
         if "GGA" in self.engines():
-            if o.get("mgga"):
-                raise NotImplementedError("meta-GGA kinetic functionals are not supported")
             k = o.get("k_str")
-            if k is not None and str(k).upper() not in GGA_FUNCTIONALS:
+            if o.get("mgga"):  # gga.py:1226-1230
+                if str(k or "LKT").upper() not in MGGA_FUNCTIONALS:
+                    raise AttributeError("%s MGGA KEDF to be implemented" % str(k or "LKT").upper())
+            elif k is not None and str(k).upper() not in GGA_FUNCTIONALS:
                 raise AttributeError("%s GGA KEDF to be implemented" % str(k).upper())
 
     def engines(self, name=None):
@@ -255,7 +268,7 @@ class KEDF(NativeFunctional):
                 cfg.gga_params[i] = float(v)
         if "GGA" in engines:  # gga.py:1212-1270: the functional named by k_str, default LKT
             name = str(o.get("k_str") or "LKT").upper()
-            formula, p0 = GGA_FUNCTIONALS[name]
+            formula, p0 = (MGGA_FUNCTIONALS if o.get("mgga") else GGA_FUNCTIONALS)[name]
             params = o.get("params")
             p = list(p0)
             if params is not None:  # prefix replaced, extra values dropped (gga.py:1255-1265)
@@ -318,6 +331,8 @@ class KEDF(NativeFunctional):
         name = name.upper()
         if name not in _STRESS_NAMES:
             raise AttributeError("'{}' has not implemented.".format(name))
+        if "GGA" in self.engines(name) and self.options.get("mgga"):
+            raise AttributeError("Stress not support MGGA yet")
         engines = self.engines(name)
         if len(self.energies) < len(engines):
             self.compute(density, calcType={"E"}, name=name, split=True)

@@ -100,7 +100,10 @@ enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8, OFDF
 enum { OFDFT_GGA_LKT = 0, OFDFT_GGA_LKTVW, OFDFT_GGA_DK, OFDFT_GGA_LLP, OFDFT_GGA_OL, OFDFT_GGA_THAK,
        OFDFT_GGA_B86A, OFDFT_GGA_B86B, OFDFT_GGA_DK87, OFDFT_GGA_PW86, OFDFT_GGA_PW91O, OFDFT_GGA_PW91,
        OFDFT_GGA_LG94, OFDFT_GGA_P92, OFDFT_GGA_PBE, OFDFT_GGA_P82, OFDFT_GGA_VJKS00, OFDFT_GGA_VT84F,
-       OFDFT_GGA_TFVW, OFDFT_GGA_STV, OFDFT_GGA_PBE2M, OFDFT_GGA_PG, OFDFT_GGA_NFORMULAS };
+       OFDFT_GGA_TFVW, OFDFT_GGA_STV, OFDFT_GGA_PBE2M, OFDFT_GGA_PG,
+       /* Laplacian-level (meta-GGA) formulas of MGGA_KEDF_list (gga.py:645-650): F(s, q)
+        * with q = lap(rho) / (TKF0^2 rho^(5/3)); no stress (gga.py:1313-1314) */
+       OFDFT_GGA_GE2, OFDFT_GGA_GE4, OFDFT_GGA_PGSL, OFDFT_GGA_PGSLR, OFDFT_GGA_NFORMULAS };
 enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
 /* k_F-node kernel pipeline: AUTO takes FUSED where it applies (float32 grid,
  * linear interpolation, every axis a power of two in 32..256, the last axis

@@ -1411,10 +1411,57 @@ def _gradient(rho, grid, sigma=None):
     return [ifft(grid.g[i] * (rhoG * 1j) * np.exp(-grid.gg * sigma ** 2 / 2.0), grid) for i in range(3)]
 
 
-def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw=None, sigma=None):
-    """GGA (kedf/gga.py:1212-1325); sigma smooths the density gradient (:1246-1250)."""
+def _mgga_ge2(ss, q, p):
+    """GE2 (gga.py:492-503), in ss = s / TKF0."""
+    s2 = ss * ss
+    return p[0] + p[1] * s2 + p[2] * q, 2.0 * p[1], p[2] + 0.0 * q
+
+
+def _mgga_ge4(ss, q, p):
+    """GE4 (gga.py:505-517)."""
+    F, d, dq = _mgga_ge2(ss, q, p[:3])
+    s2 = ss * ss
+    return (F + (p[3] * q * q + p[4] * q * s2 + p[5] * s2 * s2), d + (2.0 * p[4] * q + 4.0 * p[5] * s2),
+            dq + (2.0 * p[3] * q + p[4] * s2))
+
+
+def _mgga_pgsl(ss, q, p):
+    """PGSL (gga.py:519-531)."""
+    s2 = ss * ss
+    Fa = np.exp(-p[1] * s2)
+    return Fa + q ** 2 * p[0] + 5.0 / 3.0 * p[2] * s2, -2.0 * p[1] * Fa + 10.0 / 3.0 * p[2], 2.0 * p[0] * q
+
+
+def _mgga_pgslr(ss, q, p):
+    """PGSLr (gga.py:533-545)."""
+    F, d, dq = _mgga_pgsl(ss, q, p[2:])
+    s2 = ss * ss
+    return (F + (-p[0] * q * s2 + p[1] * s2 * s2), d + (-2.0 * p[0] * q + 4.0 * p[1] * s2), dq + (-p[0] * s2))
+
+
+# MGGA_KEDF_list (gga.py:645-650)
+MGGA_FUNCTIONALS = {
+    "GE2": (_mgga_ge2, [1.0, 5.0 / 27.0, 20.0 / 9.0]),
+    "GE4": (_mgga_ge4, [1.0, 5.0 / 27.0, 20.0 / 9.0, 8.0 / 81.0, -1.0 / 9.0, 8.0 / 243.0]),
+    "PGSL": (_mgga_pgsl, [0.25, 40.0 / 27.0, 1.0]),
+    "PGSLR": (_mgga_pgslr, [0.40, 0.20, 0.25, 40.0 / 27.0, 1.0]),
+}
+
+
+def _laplacian(f, grid, sigma=None):
+    """DirectField.laplacian(force_real=True) (field.py:379-386)."""
+    F = fft(f, grid)
+    if sigma is None or sigma == 0:
+        return ifft(-grid.gg * F, grid)
+    return ifft(-grid.gg * F * np.exp(-grid.gg * sigma ** 2 / 2.0), grid)
+
+
+def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw=None, sigma=None, mgga=False):
+    """GGA (kedf/gga.py:1212-1325); sigma smooths the density gradient (:1246-1250);
+    mgga: the Laplacian-level functionals of MGGA_KEDF_list (:1226-1230, 1254-1257,
+    1305-1308), without stress."""
     name = functional.upper()
-    fn, p0 = GGA_FUNCTIONALS[name]
+    fn, p0 = (MGGA_FUNCTIONALS if mgga else GGA_FUNCTIONALS)[name]
     p = list(p0)
     if params is not None:
         params = [params] if isinstance(params, (int, float)) else list(params)
@@ -1429,7 +1476,12 @@ def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw
     grad = _gradient(rho, grid, sigma)
     s = np.sqrt(_power_int(grad[0], 2) + _power_int(grad[1], 2) + _power_int(grad[2], 2)) / rho43
     s[s < 1e-16] = 1e-16
-    F, dFds2 = fn(s, p)
+    if mgga:
+        q = _laplacian(rho, grid, sigma) / (TKF0 ** 2) / rho53
+        F, dFds2, dFdq = fn(s / TKF0, q, p)
+        dFds2 = dFds2 / (TKF0 * TKF0)
+    else:
+        F, dFds2 = fn(s, p)
     if gga_remove_vw is not None:
         pa = float(gga_remove_vw) if isinstance(gga_remove_vw, (int, float)) else 1.0
         Fv, dv = _tfvw(s, [0.0, pa])
@@ -1440,7 +1492,12 @@ def gga(rho, grid, functional="LKT", params=None, calc=("E", "V"), gga_remove_vw
         p3 = [fft(tf * dFds2 * grad[i] / rho83, grid) for i in range(3)]
         pot3G = grid.g[0] * p3[0] + grid.g[1] * p3[1] + grid.g[2] * p3[2]
         out["V"] = pot1 - ifft(1j * pot3G, grid)
+        if mgga:
+            out["V"] = out["V"] + tf * dFdq * (-5.0 / 3.0 * q / rhom)
+            out["V"] = out["V"] + _laplacian(tf * dFdq * (1.0 / (TKF0 ** 2) / rho53), grid, sigma)
     if "S" in calc:
+        if mgga:
+            raise AttributeError("Stress not support MGGA yet")
         vkin2 = tf * dFds2 / rho83
         P = out["E"] - (pot1 * rho).sum() * grid.dV
         for i in range(3):

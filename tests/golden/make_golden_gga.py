@@ -49,6 +49,17 @@ def main(ref_root):
         out["A_E_" + tag] = float(r.energy)
         out["A_V_" + tag] = np.asarray(r.potential)
         out["A_S_" + tag] = np.asarray(r.stress)
+    # meta-GGA (Laplacian-level) functionals, energy and potential (no stress)
+    from dftpy.functional.kedf.gga import MGGA_KEDF_list
+    mcases = [(n, n, {}) for n in sorted(MGGA_KEDF_list)] + [("PGSL_SIG", "PGSL", {"sigma": 0.3}),
+                                                             ("GE4_P", "GE4", {"params": [1.0, 0.2, 2.0]}),
+                                                             ("PGSL_RVW", "PGSL", {"gga_remove_vw": 0.5})]
+    out["mgga_names"] = np.array(sorted(MGGA_KEDF_list))
+    for tag, name, kw in mcases:
+        rA = DirectField(grid=gridA, data=g0["A_rho"].copy())
+        r = Functional(type="KEDF", name="MGGA_" + name, **kw)(rA)
+        out["A_E_M" + tag] = float(r.energy)
+        out["A_V_M" + tag] = np.asarray(r.potential)
     # the vW term with Gaussian smoothing of its Laplacian (vw.py:29-53)
     for tag, kw in (("VW_SIG", {"sigma": 0.2}), ("TFVW_SIG", {"sigma": 0.35})):
         rA = DirectField(grid=gridA, data=g0["A_rho"].copy())

@@ -121,3 +121,26 @@ def test_gga_sigma_fp32():
     (e64, v64), (e32, v32) = out[torch.float64], out[torch.float32]
     assert abs(e32 - e64) <= 2e-6 * abs(e64)
     assert float(np.abs(v32 - v64).max()) <= 1e-4 * float(np.abs(v64).max())
+
+
+MCASES = [(str(n), str(n), {}) for n in GG["mgga_names"]] + [("PGSL_SIG", "PGSL", {"sigma": 0.3}),
+                                                            ("GE4_P", "GE4", {"params": [1.0, 0.2, 2.0]}),
+                                                            ("PGSL_RVW", "PGSL", {"gga_remove_vw": 0.5})]
+
+
+@pytest.mark.parametrize("tag,name,kw", MCASES, ids=[c[0] for c in MCASES])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32], ids=["f64", "f32"])
+def test_mgga_against_reference(golden, tag, name, kw, dtype):
+    """Meta-GGA (MGGA_<name>, gga.py:1226-1308): energy and potential; FP32 within
+    2e-6 relative and 1e-4 of max|V|."""
+    grid = D.DirectGrid(golden["A_lattice"], golden["A_nr"])
+    rho = D.DirectField(grid, data=golden["A_rho"], dtype=dtype)
+    f = D.Functional(type="KEDF", name="MGGA_" + name, **kw)
+    o = f(rho)
+    e, v = GG["A_E_M" + tag], GG["A_V_M" + tag]
+    tol = (1e-10, 1e-9) if dtype == torch.float64 else (2e-6, 1e-4)
+    assert abs(o.energy - e) <= tol[0] * abs(e), (o.energy, e)
+    assert float(np.abs(_np(o.potential) - v).max()) <= tol[1] * float(np.abs(v).max())
+    if dtype == torch.float64:
+        with pytest.raises(AttributeError):
+            f.stress(rho)

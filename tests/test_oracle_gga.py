@@ -46,3 +46,19 @@ def test_vw_sigma(golden, tag, name, sigma):
         e, v = e + t["E"], v + t["V"]
     assert abs(e - GG["A_E_" + tag]) <= 1e-11 * abs(e)
     np.testing.assert_allclose(v, GG["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(v).max())
+
+
+MCASES = [(str(n), str(n), {}) for n in GG["mgga_names"]] + [("PGSL_SIG", "PGSL", {"sigma": 0.3}),
+                                                            ("GE4_P", "GE4", {"params": [1.0, 0.2, 2.0]}),
+                                                            ("PGSL_RVW", "PGSL", {"gga_remove_vw": 0.5})]
+
+
+@pytest.mark.parametrize("tag,name,kw", MCASES, ids=[c[0] for c in MCASES])
+def test_mgga_system_a(golden, tag, name, kw):
+    """The Laplacian-level functionals (gga.py:492-545, 645-650), E and V."""
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    r = O.gga(golden["A_rho"], grid, name, mgga=True, **kw)
+    e = GG["A_E_M" + tag]
+    assert abs(r["E"] - e) <= 1e-11 * abs(e)
+    v = GG["A_V_M" + tag]
+    np.testing.assert_allclose(r["V"], v, rtol=0, atol=1e-10 * np.abs(v).max())

@@ -110,7 +110,10 @@ def OptimizeDensityConf(config, ions=None, rho=None, E_v_Evaluator=None, nr2=Non
         from .formats import write_density
         write_density(config["DENSITY"]["densityoutput"], data=rho, ions=ions)
     if config["OUTPUT"]["electrostatic_potential"]:
-        raise NotImplementedError("electrostatic potential output is not supported")
+        from .formats import write_density
+        from .properties import get_electrostatic_potential
+        write_density(config["OUTPUT"]["electrostatic_potential"], data=get_electrostatic_potential(rho, E_v_Evaluator),
+                      ions=ions)
     results = evaluator2results(E_v_Evaluator, rho=rho, calcType=calcType, ions=ions, **kwargs)
     if lscf:
         E_v_Evaluator.UpdateFunctional(keysToRemove=evaluator_emb.funcDict)

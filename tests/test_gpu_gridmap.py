@@ -77,3 +77,33 @@ def test_multistep_optimize_density_conf():
                          optimization_options={"econv": 1e-9 * 4, "maxiter": 300})
     opt.optimize_rho(guess_rho=rho02)
     assert abs(res["energypotential"]["TOTAL"].energy - opt.functional.energy) <= 1e-7 * 4
+
+
+def test_electrostatic_potential_and_outputs(tmp_path):
+    """get_electrostatic_potential (properties/potential.py:3-7) is v_loc + v_H, and
+    OptimizeDensityConf writes it and the density when DENSITY.densityoutput and
+    OUTPUT.electrostatic_potential name files."""
+    from dftpy_gb300 import formats as F
+    from dftpy_gb300.interface import OptimizeDensityConf
+    from dftpy_gb300.properties import get_electrostatic_potential
+    lat, pos = syn.fcc_cell(7.6)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    grid = D.DirectGrid(lat, (24, 24, 24))
+    ions = D.Ions(symbols=["Al"] * 4, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+    ha = D.Functional(type="HARTREE")
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="TFVW"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=ha, PSEUDO=pp)
+    rho0 = D.DirectField(grid) + 12.0 / grid.volume
+    fd, fv = str(tmp_path / "rho.xsf"), str(tmp_path / "ves.xsf")
+    cfg = {"OPT": {"method": "LBFGS", "econv": 1e-8}, "DENSITY": {"densityoutput": fd},
+           "OUTPUT": {"electrostatic_potential": fv}}
+    res = OptimizeDensityConf(cfg, ions=ions, rho=rho0, E_v_Evaluator=tot)
+    rho = res["density"]
+    v = get_electrostatic_potential(rho, tot)
+    ref = pp(rho, calcType={"V"}).potential.as_subclass(torch.Tensor) + ha(rho, calcType={"V"}).potential.as_subclass(
+        torch.Tensor)
+    assert torch.allclose(v.as_subclass(torch.Tensor), ref, rtol=0, atol=1e-14)
+    back_v, back_rho = F.read_density(fv), F.read_density(fd)
+    assert float(np.abs(_np(back_v) - _np(v)).max()) <= 1e-12 * float(np.abs(_np(v)).max())
+    assert float(np.abs(_np(back_rho) - _np(rho)).max()) <= 1e-12 * float(np.abs(_np(rho)).max())

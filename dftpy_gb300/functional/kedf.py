@@ -15,7 +15,7 @@ from .functional_output import FunctionalOutput, ZeroFunctional
 
 __all__ = ["KEDF", "KEDFEngines"]
 
-_BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+_BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "SM-NL": _lib.KE_WT, "FP-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -32,6 +32,10 @@ KEDFEngines = {
     "TFVW": ("TF", "VW"),
     "WT": ("TF", "VW", "WT-NL"),
     "WT-NL": ("WT-NL",),
+    "SM": ("TF", "VW", "SM-NL"),  # Smargiassi-Madden (sm.py): the WT engine with alpha = beta = 1/2
+    "SM-NL": ("SM-NL",),
+    "FP": ("TF", "VW", "FP-NL"),  # Perrot (fp.py): the WT engine with alpha = beta = 1
+    "FP-NL": ("FP-NL",),
     "LWT": ("TF", "VW", "LWT-NL"),
     "LWT-NL": ("LWT-NL",),
     "LMGP": ("TF", "VW", "LMGP-NL"),
@@ -147,8 +151,10 @@ MGGA_FUNCTIONALS = {
 # engines with a stress (KEDFEngines_Stress, kedf/__init__.py:76-92): slot in the
 # stress and energy arrays of the native evaluator
 _STRESS = {"TF": (_lib.S_TF, _lib.E_TF), "VW": (_lib.S_VW, _lib.E_VW), "WT-NL": (_lib.S_NL, _lib.E_NL),
-           "GGA": (_lib.S_GGA, _lib.E_GGA)}
-_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL", "GGA")
+           "SM-NL": (_lib.S_NL, _lib.E_NL), "FP-NL": (_lib.S_NL, _lib.E_NL), "GGA": (_lib.S_GGA, _lib.E_GGA)}
+_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL", "SM", "SM-NL", "FP", "FP-NL", "GGA")
+# default exponents of the WT-engine variants (sm.py:14, fp.py:14); SMStress defaults to 1 (sm.py:18)
+_WT_AB = {"SM-NL": 0.5, "FP-NL": 1.0}
 
 
 class KEDF(NativeFunctional):
@@ -217,8 +223,9 @@ class KEDF(NativeFunctional):
         cfg.vw_sigma = sigma if "VW" in engines else 0.0
         cfg.gga_sigma = sigma if "GGA" in engines else 0.0
         hc = next((e for e in engines if e in _HC), None)
-        a = float(o.get("alpha", 2.0 if hc else 5.0 / 6.0))
-        b = float(o.get("beta", 2.0 / 3.0 if hc else 5.0 / 6.0))
+        wtv = next((_WT_AB[e] for e in engines if e in _WT_AB), None)
+        a = float(o.get("alpha", 2.0 if hc else (wtv if wtv is not None else 5.0 / 6.0)))
+        b = float(o.get("beta", 2.0 / 3.0 if hc else (wtv if wtv is not None else 5.0 / 6.0)))
         cfg.wt_alpha, cfg.wt_beta, cfg.wt_x = a, b, x
         rho0 = o.get("rho0")
         cfg.wt_rho0 = float(rho0) if rho0 else 0.0
@@ -339,7 +346,11 @@ class KEDF(NativeFunctional):
         E = np.zeros(_lib.NE)
         for e in engines:
             E[_STRESS[e][1]] = self.energies[e]
-        sub = KEDF(name=name, **self.options)
+        opts = dict(self.options)
+        if "SM-NL" in engines:  # SMStress takes alpha = beta = 1 unless given (sm.py:18-19)
+            opts.setdefault("alpha", 1.0)
+            opts.setdefault("beta", 1.0)
+        sub = KEDF(name=name, **opts)
         sub.ke_kernel_saved = self.ke_kernel_saved
         S = sub._native_stress(density, E)
         out = {e: S[_STRESS[e][0]].copy() for e in engines}

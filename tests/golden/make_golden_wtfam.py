@@ -1,0 +1,43 @@
+"""Generate tests/golden/reference_wtfam.npz: the Smargiassi-Madden and Perrot
+kinetic functionals (src/dftpy/functional/kedf/sm.py, fp.py: the WT engine with
+their own exponents) computed by the REFERENCE implementation, energy,
+potential and stress, on the smooth anisotropic density of system A.
+
+Run in a container that has the reference sources:
+
+    python tests/golden/make_golden_wtfam.py /root/reference
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from make_golden import ref_objects, setup  # noqa: E402
+
+CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6})]
+
+
+def main(ref_root):
+    setup(ref_root)
+    DirectGrid, DirectField, Ions = ref_objects()
+    from dftpy.functional.kedf import KEDF
+
+    g0 = dict(np.load(os.path.join(HERE, "reference_golden.npz")))
+    out = {}
+    grid = DirectGrid(lattice=g0["A_lattice"], nr=g0["A_nr"], full=False)
+    for tag, name, kw in CASES:
+        f = KEDF(name=name, **kw)
+        rho = DirectField(grid=grid, data=g0["A_rho"].copy())
+        r = f(rho)
+        out["A_E_" + tag] = float(r.energy)
+        out["A_V_" + tag] = np.asarray(r.potential)
+        out["A_S_" + tag] = np.asarray(f.stress(DirectField(grid=grid, data=g0["A_rho"].copy())))
+        print(tag, r.energy)
+    np.savez_compressed(os.path.join(HERE, "reference_wtfam.npz"), **out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

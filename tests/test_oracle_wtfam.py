@@ -1,0 +1,32 @@
+"""The Smargiassi-Madden and Perrot kinetic functionals (kedf/sm.py, fp.py: the
+WT engine with alpha = beta = 1/2 and 1) restated with the oracle's WT term,
+against the reference's outputs (tests/golden/make_golden_wtfam.py); the SM
+stress takes alpha = beta = 1 unless given (sm.py:18-19)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ofdft_np as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WF = dict(np.load(os.path.join(HERE, "golden", "reference_wtfam.npz")))
+# tag -> (local terms, energy exponent, stress exponent)
+CASES = {"SM": (True, 0.5, 1.0), "FP": (True, 1.0, 1.0), "SMNL": (False, 0.5, 1.0), "SMA": (True, 0.6, 0.6)}
+
+
+@pytest.mark.parametrize("tag", sorted(CASES))
+def test_wt_family(golden, tag):
+    local, a, a_s = CASES[tag]
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    rho = golden["A_rho"]
+    nl = O.WT(alpha=a, beta=a)(rho, grid)
+    E, V = nl["E"], nl["V"]
+    S = O.wt_stress(rho, grid, nl["E"], alpha=a_s, beta=a_s)
+    if local:
+        t, w = O.tf(rho, grid), O.vw(rho, grid)
+        E, V = E + t["E"] + w["E"], V + t["V"] + w["V"]
+        S = S + O.tf_stress(grid, t["E"]) + O.vw_stress(rho, grid)
+    assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
+    np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())
+    np.testing.assert_allclose(S, WF["A_S_" + tag], rtol=0, atol=1e-10 * np.abs(S).max())

@@ -46,7 +46,7 @@ class Config(C.Structure):
         ("lwt_pipeline", C.c_int), ("lwt_kernel", C.c_int), ("lwt_maxpoints", C.c_int),
         ("gga_formula", C.c_int), ("gga_nparams", C.c_int), ("gga_params", C.c_double * 8),
         ("gga_remove_vw", C.c_double), ("lwt_family", C.c_int), ("external", C.c_int),
-        ("vw_sigma", C.c_double), ("gga_sigma", C.c_double),
+        ("vw_sigma", C.c_double), ("gga_sigma", C.c_double), ("wte", C.c_int),
     ]
 
 

@@ -115,6 +115,7 @@ struct PreArgs {
     T* kf;
     long long N;
     int tf, vw, xc, pp, ext, nl, lwt, same_ab, wantV;
+    int tf_v;       // add the TF potential (off under WTE, which scales it afterwards)
     int nl_is_lwt;  // clamp rule: LWT clamps rho<=0, WT clamps rho<1e-30
     double tf_x;
     double alpha, beta;
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
             r5 *= r;
             r5 *= r;
             sum[0].add(mcbrt(r5) * cTF_E);
-            if (a.wantV) v += cTF_V * mcbrt(r * r) * tf_x;
+            if (a.wantV && a.tf_v) v += cTF_V * mcbrt(r * r) * tf_x;
         }
         if (a.xc) {
             M ex, vx;
@@ -641,6 +642,7 @@ template <typename T>
 struct PostArgs {
     const T* rho;
     T* V;
+    T* Vnl;  // WTE: the WT potential goes here instead of into V
     const T* sq;
     const T* lap;   // (1/2) IFFT(G^2 FFT(sqrt rho)) (already normalised)
     const T* vH;
@@ -694,18 +696,25 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
             const M rc = r < zero_clamp ? zero_clamp : r;
             const M pb = a.rb[i];
             const M c1 = a.nl1[i];
+            M vnl = (M)0;
             if (a.same_ab) {
                 const M pot = (M)2 * alpha * (pb / rc) * c1;  // wt.py:19-23
                 if (a.wantV) {
                     sum[2].add(pot * r / ((M)2 * alpha));  // wt.py:124-125
-                    v += pot;
+                    vnl = pot;
                 } else {
                     sum[2].add(c1 * pb);  // wt.py:44-56
                 }
             } else {
                 const M pa = a.ra[i];
                 sum[2].add(c1 * pa);
-                if (a.wantV) v += alpha * (pa / rc) * c1 + beta * (pb / rc) * a.nl2[i];
+                if (a.wantV) vnl = alpha * (pa / rc) * c1 + beta * (pb / rc) * a.nl2[i];
+            }
+            if (a.wantV) {
+                if (a.Vnl)
+                    a.Vnl[i] = vnl;
+                else
+                    v += vnl;
             }
         }
         if (a.lwt && a.hc) {
@@ -743,6 +752,21 @@ __global__ void __launch_bounds__(RED_THREADS) k_postpass(PostArgs<T> a, double*
     }
     double acc[POST_NS] = {sum[0].get(), sum[1].get(), sum[2].get()};
     block_sum_store<POST_NS>(acc, partials);
+}
+
+// WTE potential (wte.py:15-18) from the prepass TF sum (R0[0]) and the
+// postpass WT sum (R16[2]): V += exp(r) ((1 - r) V_TF + V_WT), r = E_WT / E_TF.
+template <typename T>
+__global__ void k_wte_combine(const T* __restrict__ rho, T* V, const T* __restrict__ Vnl, long long N,
+                              const double* R0, const double* R16, double dV, double tf_x, double cTF_V) {
+    const double etf = R0[0] * dV * tf_x, ewt = R16[2] * dV;
+    const double r = ewt / etf, ex = exp(r);
+    const T c1 = (T)(ex * (1.0 - r)), c2 = (T)ex, ctf = (T)cTF_V, tx = (T)tf_x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += stride) {
+        const T x = rho[i];
+        V[i] += c1 * (ctf * mcbrt(x * x) * tx) + c2 * Vnl[i];
+    }
 }
 
 template <typename T>
@@ -1223,6 +1247,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     const double alpha = wt ? c.wt_alpha : c.lwt_alpha, beta = wt ? c.wt_beta : c.lwt_beta;
     const bool same_ab = wt ? std::fabs(beta - alpha) < 1e-9 : std::fabs(alpha - beta) < 1e-8;
     const bool h = c.hartree != 0, xc = c.xc_lda != 0, pp = c.pseudo != 0 && e->have_vloc;
+    const bool wte = c.wte != 0 && tf && wt;  // WTE scales the TF and WT potentials after the sums
     OFDFT_REQUIRE(!(c.pseudo && !e->have_vloc), "ofdft_eval_compute: pseudo enabled but no v_loc set");
     const bool ext = c.external != 0;
     OFDFT_REQUIRE(!(ext && !e->have_vext), "ofdft_eval_compute: external potential enabled but not set");
@@ -1249,6 +1274,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     pa.kf = kfv;
     pa.N = N;
     pa.tf = tf;
+    pa.tf_v = !wte;
     pa.vw = vw;
     pa.xc = xc;
     pa.pp = pp;
@@ -1543,6 +1569,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     PostArgs<T> qa;
     qa.rho = rho;
     qa.V = Vw;
+    qa.Vnl = (wte && wantV) ? (T*)e->sc.get("wte_vnl", rb) : nullptr;
     qa.sq = sq;
     qa.lap = lap;
     qa.vH = vH;
@@ -1585,6 +1612,13 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     });
     OFDFT_LAUNCH_CHECK();
     launches += 2;
+    if (wte && wantV) {  // wte.py:15-18: V += exp(r) ((1 - r) V_TF + V_WT), r = E_WT / E_TF, from the device sums
+        const int nb = blocks_for(N, 256, g->sms * 8);
+        k_wte_combine<T><<<nb, 256, 0, st>>>(rho, V, qa.Vnl, N, g->d_results, g->d_results + 16, g->dV, c.tf_x,
+                                             e->k.cTF_V);
+        OFDFT_LAUNCH_CHECK();
+        ++launches;
+    }
     // ---- GGA kinetic functional: its own gradient and divergence transforms, its
     // potential added to V, its sums in results [40, 48)
     const bool gga = (c.kedf_terms & OFDFT_KE_GGA) != 0;
@@ -1629,6 +1663,7 @@ void collect_energies(ofdft_eval* e, double* energies) {
     double* E = energies;
     for (int i = 0; i < OFDFT_NE; ++i) E[i] = 0.0;
     E[OFDFT_E_TF] = p.tf ? R[0] * dV * c.tf_x : 0.0;
+    const double e_wt_raw = p.wt ? R[18] * dV : 0.0;
     E[OFDFT_E_XC] = p.xc ? R[1] * dV : 0.0;
     E[OFDFT_E_PP] = p.pp ? R[2] * dV : 0.0;
     E[OFDFT_E_NELEC] = R[3] * dV;
@@ -1639,6 +1674,10 @@ void collect_energies(ofdft_eval* e, double* energies) {
     E[OFDFT_E_II] = c.ewald_energy;
     E[OFDFT_E_GGA] = p.gga ? R[40] * dV : 0.0;
     E[OFDFT_E_EXT] = p.ext ? R[7] * dV : 0.0;
+    if (c.wte && p.tf && p.wt) {  // wte.py:20-22
+        E[OFDFT_E_NL] = E[OFDFT_E_TF] * std::exp(e_wt_raw / E[OFDFT_E_TF]);
+        E[OFDFT_E_TF] = 0.0;
+    }
     E[OFDFT_E_TOTAL] = E[OFDFT_E_TF] + E[OFDFT_E_VW] + E[OFDFT_E_NL] + E[OFDFT_E_XC] + E[OFDFT_E_H] + E[OFDFT_E_PP] +
                        E[OFDFT_E_II] + E[OFDFT_E_GGA] + E[OFDFT_E_EXT];
     e->last_launches = p.launches;
@@ -1778,6 +1817,21 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
     double E[OFDFT_NE];
     if (energies) std::copy(energies, energies + OFDFT_NE, E);
     else compute_t<T>(e, rho, nullptr, OFDFT_CALC_E, E, st);
+    // WTEStress (wte.py:25-37) evaluates the TF and WT energies itself
+    const bool wte = c.wte && (c.kedf_terms & OFDFT_KE_TF) && (c.kedf_terms & OFDFT_KE_WT);
+    if (wte) {
+        double Er[OFDFT_NE];
+        e->cfg.wte = 0;
+        try {
+            compute_t<T>(e, rho, nullptr, OFDFT_CALC_E, Er, st);
+        } catch (...) {
+            e->cfg.wte = 1;
+            throw;
+        }
+        e->cfg.wte = 1;
+        E[OFDFT_E_TF] = Er[OFDFT_E_TF];
+        E[OFDFT_E_NL] = Er[OFDFT_E_NL];
+    }
     for (int i = 0; i < OFDFT_NS * 9; ++i) S[i] = 0.0;
     const double V = g->volume, dV = g->dV, N = (double)g->N;
     const bool vw = c.kedf_terms & OFDFT_KE_VW, wt = c.kedf_terms & OFDFT_KE_WT;
@@ -1877,6 +1931,15 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
         OFDFT_LAUNCH_CHECK();
         fetch(g->red_blocks, 6);
         put6(S + OFDFT_S_VW * 9, g->h_results, -0.25 / V * dV * c.vw_y);
+    }
+    // WTE (wte.py:33-37): exp(E_WT/E_TF) (sigma_WT + 2/3 E_WT/V on the diagonal + sigma_TF), in the NL slot
+    if (wte) {
+        const double ex = std::exp(E[OFDFT_E_NL] / E[OFDFT_E_TF]);
+        for (int d = 0; d < 3; ++d) S[OFDFT_S_NL * 9 + 4 * d] += 2.0 / 3.0 * E[OFDFT_E_NL] / V;
+        for (int k = 0; k < 9; ++k) {
+            S[OFDFT_S_NL * 9 + k] = (S[OFDFT_S_NL * 9 + k] + S[OFDFT_S_TF * 9 + k]) * ex;
+            S[OFDFT_S_TF * 9 + k] = 0.0;
+        }
     }
 }
 

@@ -15,7 +15,8 @@ from .functional_output import FunctionalOutput, ZeroFunctional
 
 __all__ = ["KEDF", "KEDFEngines"]
 
-_BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "SM-NL": _lib.KE_WT, "FP-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+_BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "SM-NL": _lib.KE_WT, "FP-NL": _lib.KE_WT,
+         "WTE-NL": _lib.KE_TF | _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -36,6 +37,8 @@ KEDFEngines = {
     "SM-NL": ("SM-NL",),
     "FP": ("TF", "VW", "FP-NL"),  # Perrot (fp.py): the WT engine with alpha = beta = 1
     "FP-NL": ("FP-NL",),
+    "WTE": ("VW", "WTE-NL"),  # WTE (wte.py): E_TF exp(E_WT / E_TF)
+    "WTE-NL": ("WTE-NL",),
     "LWT": ("TF", "VW", "LWT-NL"),
     "LWT-NL": ("LWT-NL",),
     "LMGP": ("TF", "VW", "LMGP-NL"),
@@ -151,8 +154,10 @@ MGGA_FUNCTIONALS = {
 # engines with a stress (KEDFEngines_Stress, kedf/__init__.py:76-92): slot in the
 # stress and energy arrays of the native evaluator
 _STRESS = {"TF": (_lib.S_TF, _lib.E_TF), "VW": (_lib.S_VW, _lib.E_VW), "WT-NL": (_lib.S_NL, _lib.E_NL),
-           "SM-NL": (_lib.S_NL, _lib.E_NL), "FP-NL": (_lib.S_NL, _lib.E_NL), "GGA": (_lib.S_GGA, _lib.E_GGA)}
-_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL", "SM", "SM-NL", "FP", "FP-NL", "GGA")
+           "SM-NL": (_lib.S_NL, _lib.E_NL), "FP-NL": (_lib.S_NL, _lib.E_NL), "WTE-NL": (_lib.S_NL, _lib.E_NL),
+           "GGA": (_lib.S_GGA, _lib.E_GGA)}
+_STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL", "SM", "SM-NL", "FP", "FP-NL", "WTE",
+                 "WTE-NL", "GGA")
 # default exponents of the WT-engine variants (sm.py:14, fp.py:14); SMStress defaults to 1 (sm.py:18)
 _WT_AB = {"SM-NL": 0.5, "FP-NL": 1.0}
 
@@ -221,6 +226,7 @@ class KEDF(NativeFunctional):
         sigma = o.get("sigma")
         sigma = 0.0 if sigma is None else float(sigma)
         cfg.vw_sigma = sigma if "VW" in engines else 0.0
+        cfg.wte = 1 if "WTE-NL" in engines else 0
         cfg.gga_sigma = sigma if "GGA" in engines else 0.0
         hc = next((e for e in engines if e in _HC), None)
         wtv = next((_WT_AB[e] for e in engines if e in _WT_AB), None)

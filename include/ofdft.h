@@ -158,6 +158,9 @@ typedef struct {
     double vw_sigma;          /* > 0: vW Laplacian times exp(-G^2 sigma^2/4) (kedf/vw.py:45-48) */
     double gga_sigma;         /* > 0: GGA gradient times exp(-G^2 sigma^2/2), the
                                  'supersmooth' gradient (gga.py:1246-1250, field.py:229-262) */
+    int    wte;               /* with TF and WT: WTE (kedf/wte.py:15-57), E = E_TF exp(E_WT/E_TF)
+                                 and V = exp(E_WT/E_TF)((1 - E_WT/E_TF) V_TF + V_WT), reported
+                                 in OFDFT_E_NL (OFDFT_E_TF = 0) */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

@@ -1,7 +1,7 @@
 """Generate tests/golden/reference_wtfam.npz: the Smargiassi-Madden and Perrot
 kinetic functionals (src/dftpy/functional/kedf/sm.py, fp.py: the WT engine with
-their own exponents) computed by the REFERENCE implementation, energy,
-potential and stress, on the smooth anisotropic density of system A.
+their own exponents) and WTE (wte.py) computed by the REFERENCE implementation,
+energy, potential and stress, on the smooth anisotropic density of system A.
 
 Run in a container that has the reference sources:
 
@@ -17,7 +17,8 @@ sys.path.insert(0, HERE)
 
 from make_golden import ref_objects, setup  # noqa: E402
 
-CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6})]
+CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6}),
+         ("WTE", "WTE", {}), ("WTENL", "WTE-NL", {}), ("WTEX", "WTE", {"x": 0.8, "alpha": 0.9, "beta": 0.7})]
 
 
 def main(ref_root):

@@ -1,5 +1,5 @@
 """GPU parity of the Smargiassi-Madden and Perrot kinetic functionals (kedf/sm.py,
-fp.py) against the reference's outputs (tests/golden/make_golden_wtfam.py):
+fp.py) and of WTE (wte.py) against the reference's outputs (tests/golden/make_golden_wtfam.py):
 energy within 1e-10 relative, potential within 1e-9 and stress within 1e-9 of
 their largest values in FP64; FP32 energy within 2e-6 relative."""
 import os
@@ -14,7 +14,8 @@ import dftpy_gb300 as D
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WF = dict(np.load(os.path.join(HERE, "golden", "reference_wtfam.npz")))
-CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6})]
+CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6}),
+         ("WTE", "WTE", {}), ("WTENL", "WTE-NL", {}), ("WTEX", "WTE", {"x": 0.8, "alpha": 0.9, "beta": 0.7})]
 
 
 def _np(f):
@@ -34,3 +35,24 @@ def test_wt_family_against_reference(golden, tag, name, kw):
     assert float(np.abs(st - s).max()) <= 1e-9 * float(np.abs(s).max())
     o32 = f(D.DirectField(grid, data=golden["A_rho"], dtype=torch.float32))
     assert abs(o32.energy - e) <= 2e-6 * abs(e)
+
+
+def test_wte_ground_state():
+    """WTE in a fused total functional drives the native optimiser; at its ground
+    state the potential is flat up to the chemical potential."""
+    from dftpy_gb300 import synthetic as syn
+    lat, pos = syn.fcc_cell(7.6)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    grid = D.DirectGrid(lat, (24, 24, 24))
+    ions = D.Ions(symbols=["Al"] * 4, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WTE"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
+                         optimization_options={"econv": 1e-9 * 4, "maxiter": 300})
+    rho = opt.optimize_rho(guess_rho=D.DirectField(grid) + 12.0 / grid.volume)
+    assert opt.converged == 0
+    v = _np(opt.functional.potential)
+    r = _np(rho)
+    assert np.abs((v - opt.mu) * np.sqrt(r)).max() < 1e-3

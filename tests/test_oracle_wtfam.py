@@ -30,3 +30,25 @@ def test_wt_family(golden, tag):
     assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
     np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())
     np.testing.assert_allclose(S, WF["A_S_" + tag], rtol=0, atol=1e-10 * np.abs(S).max())
+
+
+@pytest.mark.parametrize("tag,local,kw", [("WTE", True, {}), ("WTENL", False, {}),
+                                          ("WTEX", True, {"x": 0.8, "alpha": 0.9, "beta": 0.7})])
+def test_wte(golden, tag, local, kw):
+    """WTE (wte.py:15-57): E_TF exp(E_WT/E_TF), its potential and stress, plus vW for 'WTE'."""
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    rho = golden["A_rho"]
+    x, a, b = kw.get("x", 1.0), kw.get("alpha", 5.0 / 6.0), kw.get("beta", 5.0 / 6.0)
+    t = O.tf(rho, grid, x=x)
+    w = O.WT(x=x, alpha=a, beta=b)(rho, grid)
+    r = w["E"] / t["E"]
+    E = t["E"] * np.exp(r)
+    V = np.exp(r) * ((1 - r) * t["V"] + w["V"])
+    S = O.wt_stress(rho, grid, w["E"], alpha=a, beta=b) + np.eye(3) * (2.0 / 3.0 * w["E"] / grid.volume)
+    S = (S + O.tf_stress(grid, t["E"])) * np.exp(r)
+    if local:
+        vw = O.vw(rho, grid)
+        E, V, S = E + vw["E"], V + vw["V"], S + O.vw_stress(rho, grid)
+    assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
+    np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())
+    np.testing.assert_allclose(S, WF["A_S_" + tag], rtol=0, atol=1e-10 * np.abs(S).max())

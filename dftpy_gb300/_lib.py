@@ -47,6 +47,8 @@ class Config(C.Structure):
         ("gga_formula", C.c_int), ("gga_nparams", C.c_int), ("gga_params", C.c_double * 8),
         ("gga_remove_vw", C.c_double), ("lwt_family", C.c_int), ("external", C.c_int),
         ("vw_sigma", C.c_double), ("gga_sigma", C.c_double), ("wte", C.c_int),
+        ("wt_kernel", C.c_int), ("wt_maxpoints", C.c_int), ("wt_lump", C.c_int), ("wt_lump_abc", C.c_double * 3),
+        ("wt_revke", C.c_int),
     ]
 
 

@@ -223,6 +223,7 @@ struct GArgs {
     const double* wtstate;         // [saved rho0, recompute flag, tkf, factor]
     double wt_x;
     double vw_s;                   // sigma^2/4 of the vW smoothing (0: none)
+    int mgp;                       // the kernel comes from k_mgp_kernel
     Geo geo;
     double invN;
 };
@@ -254,7 +255,7 @@ template <typename T>
 __global__ void k_gspace(GArgs<T> a) {
     using M = T;  // working precision of the multipliers
     const long long stride = (long long)gridDim.x * blockDim.x;
-    const bool recompute = a.wtK && a.wtstate[1] != 0.0;
+    const bool recompute = a.wtK && a.wtstate[1] != 0.0 && !a.mgp;
     const M invN = (M)a.invN, fourpi = (M)(4.0 * M_PI), half = (M)0.5;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.geo.Nc; i += stride) {
         const M gg = gsq_t<M>(a.geo, i);
@@ -310,6 +311,82 @@ __global__ void k_wt_plan(const double* results, double* state, double rho0_fixe
         state[4] = 1.0;
     } else {
         state[1] = 0.0;
+    }
+}
+
+// ------------------------------------------------------------ MGP kernels
+struct MgpArgs {
+    const double* x;  // spline data points (log-spaced eta)
+    const double* c;  // 4 per interval
+    int n;
+    int maxpoints, sym, lump, revke;
+    double abc[3];
+    double volume;
+};
+
+// splev(eta, table, ext=3) of the Lindhard spline: the boundary value outside the table
+__device__ inline double mgp_splev(const MgpArgs& m, double v) {
+    if (v <= m.x[0]) return m.c[0];
+    if (v >= m.x[m.n - 1]) {
+        const double* p = m.c + 4 * (m.n - 2);
+        const double u = m.x[m.n - 1] - m.x[m.n - 2];
+        return p[0] + u * (p[1] + u * (p[2] + u * p[3]));
+    }
+    int lo = 0, hi = m.n - 1;  // x[lo] <= v < x[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (m.x[mid] <= v)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const double* p = m.c + 4 * lo;
+    const double u = v - m.x[lo];
+    return p[0] + u * (p[1] + u * (p[2] + u * p[3]));
+}
+
+// MGPKernel + MGPOmegaE at the saved rho0 (mgp.py:39-46, kernel.py:251-322, 408-440),
+// written when k_wt_plan flagged a rebuild (state[1]); K(G=0) = 0.
+template <typename T>
+__global__ void k_mgp_kernel(T* K, Geo geo, const double* state, MgpArgs m) {
+    if (state[1] == 0.0) return;
+    const double rho0 = state[0], tkf = state[2];
+    const double cTF = 0.3 * pow(3.0 * M_PI * M_PI, 2.0 / 3.0), dt = 1.0 / m.maxpoints;
+    const double coe = 4.0 / 5.0 * cTF * 5.0 / 6.0 * dt;
+    double a = m.abc[0], b = m.abc[1];
+    if (m.lump == 1) {
+        a = a / pow(rho0 * m.volume, 2.0 / 3.0);
+        b = a;
+    }
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < geo.Nc; idx += stride) {
+        if (idx == 0) {
+            K[0] = (T)0;
+            continue;
+        }
+        const double q = sqrt(gsq(geo, idx));
+        const double eta = q / tkf;
+        double s = 0.0;
+        for (int i = 1; i <= m.maxpoints; ++i) {
+            const double t = i * dt;
+            const double t16 = m.sym == 2 ? pow(t, -2.0 / 3.0) : pow(t, 1.0 / 6.0);
+            s += mgp_splev(m, eta / cbrt(t)) / t16;
+        }
+        double k;
+        if (m.sym == 1)
+            k = 0.5 * (s * coe + lindhard_dev(eta, 1.0, 1.0) * (4.0 / 5.0 * cTF));
+        else if (m.sym == 2)
+            k = s * (2.0 * coe);
+        else
+            k = s * coe;
+        if (m.lump) {
+            const double gg = q * q;
+            const double er = m.revke ? erf(m.abc[2] * gg) : erf(m.abc[2] * q);
+            double corr = 4.0 * M_PI * er * er * a * exp(-gg * b) / gg;
+            if (!m.revke) corr *= 3.0 / 5.0;
+            k += corr;
+        }
+        K[idx] = (T)k;
     }
 }
 
@@ -789,6 +866,10 @@ struct ofdft_eval {
     bool have_vloc = false;
     void* vext = nullptr;  // grid precision
     bool have_vext = false;
+    // MGP kernels of the WT term: the Lindhard spline on the log-spaced eta table
+    double* mgp_x = nullptr;  // knots (data points)
+    double* mgp_c = nullptr;  // 4 per interval
+    int mgp_n = 0;
     bool tab_set = false;  // the k_F-node kernel table is on the device
     double* wtstate = nullptr;  // device [rho0, flag, tkf, factor, init]
     // density-dependent kernel
@@ -1316,6 +1397,22 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
                                    e->k.cTF_wt);
         OFDFT_LAUNCH_CHECK();
         launches++;
+        if (c.wt_kernel != OFDFT_LWT_KERNEL_WT) {  // MGP kernel at rho0, rebuilt when k_wt_plan says so
+            MgpArgs m;
+            m.x = e->mgp_x;
+            m.c = e->mgp_c;
+            m.n = e->mgp_n;
+            m.maxpoints = c.wt_maxpoints;
+            m.sym = c.wt_kernel == OFDFT_LWT_KERNEL_MGPA ? 1 : (c.wt_kernel == OFDFT_LWT_KERNEL_MGPG ? 2 : 0);
+            m.lump = c.wt_lump;
+            for (int k = 0; k < 3; ++k) m.abc[k] = c.wt_lump_abc[k];
+            m.revke = c.wt_revke;
+            m.volume = g->volume;
+            const int nb = blocks_for(Nc, 128, g->sms * 8);
+            k_mgp_kernel<T><<<nb, 128, 0, st>>>(wtK, g->geo, e->wtstate, m);
+            OFDFT_LAUNCH_CHECK();
+            launches++;
+        }
     }
 
     // ---- HC: k_F = F(s) (3 pi^2 rho)^(1/3) from the gradient of the clamped density
@@ -1420,6 +1517,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         ga.rbG = wt ? rbG : nullptr;
         ga.raG = raG;
         ga.wtK = wtK;
+        ga.mgp = c.wt_kernel != OFDFT_LWT_KERNEL_WT;
         ga.wtstate = e->wtstate;
         ga.wt_x = c.wt_x;
         ga.vw_s = c.vw_sigma > 0.0 ? c.vw_sigma * c.vw_sigma / 4.0 : 0.0;
@@ -1976,6 +2074,13 @@ void ofdft_config_default(ofdft_config* c) {
     c->gga_params[1] = 1.0;
     c->gga_remove_vw = 0.0;
     c->lwt_family = OFDFT_LWT_FAMILY_LWT;
+    c->wt_kernel = OFDFT_LWT_KERNEL_WT;
+    c->wt_maxpoints = 1000;
+    c->wt_lump = 0;
+    c->wt_lump_abc[0] = 0.2;
+    c->wt_lump_abc[1] = 0.2;
+    c->wt_lump_abc[2] = 1.0;
+    c->wt_revke = 1;
     c->xc_lda = 1;
     c->hartree = 1;
     c->pseudo = 0;
@@ -2009,6 +2114,13 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
                           "HC: Hermite interpolation and a GGA enhancement factor are required");
             OFDFT_REQUIRE(c.lwt_kernel == OFDFT_LWT_KERNEL_WT || c.lwt_maxpoints >= 1, "lwt_maxpoints must be >= 1");
         }
+        if (c.kedf_terms & OFDFT_KE_WT) {
+            OFDFT_REQUIRE(c.wt_kernel >= OFDFT_LWT_KERNEL_WT && c.wt_kernel <= OFDFT_LWT_KERNEL_MGPG,
+                          "wt_kernel must be OFDFT_LWT_KERNEL_WT, _MGP, _MGPA or _MGPG");
+            OFDFT_REQUIRE(c.wt_kernel == OFDFT_LWT_KERNEL_WT || (c.wt_maxpoints >= 1 && !c.wte),
+                          "MGP kernels: wt_maxpoints >= 1, and not with WTE");
+            OFDFT_REQUIRE(c.wt_lump >= 0 && c.wt_lump <= 2, "wt_lump must be 0, 1 or 2");
+        }
         auto* e = new ofdft_eval();
         e->g = g;
         e->cfg = c;
@@ -2016,6 +2128,24 @@ int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) 
         try {
             OFDFT_CK(cudaMalloc(&e->wtstate, 8 * sizeof(double)));
             zero_now(e->wtstate, 8 * sizeof(double));
+            if ((c.kedf_terms & OFDFT_KE_WT) && c.wt_kernel != OFDFT_LWT_KERNEL_WT) {
+                // MGPKernelTable (kernel.py:281-292): splrep of LindhardFunction(eta, 1, 1) on
+                // logspace(log10(1e-4), log10(52), 10000)
+                const int n = 10000;
+                const double l0 = std::log10(1e-4), l1 = std::log10(52.0), step = (l1 - l0) / (n - 1);
+                std::vector<double> x(n), y(n);
+                for (int i = 0; i < n; ++i) {
+                    x[i] = std::pow(10.0, i == n - 1 ? l1 : l0 + i * step);
+                    y[i] = lindhard(x[i], 1.0, 1.0);
+                }
+                CubicSpline sp;
+                sp.fit(x, y);
+                e->mgp_n = n;
+                OFDFT_CK(cudaMalloc(&e->mgp_x, n * sizeof(double)));
+                OFDFT_CK(cudaMalloc(&e->mgp_c, sp.c.size() * sizeof(double)));
+                upload_now(e->mgp_x, sp.x.data(), n * sizeof(double));
+                upload_now(e->mgp_c, sp.c.data(), sp.c.size() * sizeof(double));
+            }
             if (c.kedf_terms & OFDFT_KE_LWT) {
                 if (g->prec == OFDFT_F64) build_table<double>(e);
                 else build_table<float>(e);
@@ -2035,6 +2165,8 @@ void ofdft_eval_destroy(ofdft_eval* e) {
     e->sc.release_all();
     if (e->vloc) cudaFree(e->vloc);
     if (e->vext) cudaFree(e->vext);
+    if (e->mgp_x) cudaFree(e->mgp_x);
+    if (e->mgp_c) cudaFree(e->mgp_c);
     if (e->wtstate) cudaFree(e->wtstate);
     if (e->tab_c) cudaFree(e->tab_c);
     if (e->tab_cd) cudaFree(e->tab_cd);

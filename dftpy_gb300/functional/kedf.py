@@ -16,7 +16,8 @@ from .functional_output import FunctionalOutput, ZeroFunctional
 __all__ = ["KEDF", "KEDFEngines"]
 
 _BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "SM-NL": _lib.KE_WT, "FP-NL": _lib.KE_WT,
-         "WTE-NL": _lib.KE_TF | _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+         "WTE-NL": _lib.KE_TF | _lib.KE_WT, "MGP-NL": _lib.KE_WT, "MGPA-NL": _lib.KE_WT, "MGPG-NL": _lib.KE_WT,
+         "MGP0-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -39,6 +40,14 @@ KEDFEngines = {
     "FP-NL": ("FP-NL",),
     "WTE": ("VW", "WTE-NL"),  # WTE (wte.py): E_TF exp(E_WT / E_TF)
     "WTE-NL": ("WTE-NL",),
+    "MGP": ("TF", "VW", "MGP-NL"),  # density-independent MGP kernels (mgp.py)
+    "MGPA": ("TF", "VW", "MGPA-NL"),
+    "MGPG": ("TF", "VW", "MGPG-NL"),
+    "MGP0": ("TF", "VW", "MGP0-NL"),
+    "MGP-NL": ("MGP-NL",),
+    "MGPA-NL": ("MGPA-NL",),
+    "MGPG-NL": ("MGPG-NL",),
+    "MGP0-NL": ("MGP0-NL",),
     "LWT": ("TF", "VW", "LWT-NL"),
     "LWT-NL": ("LWT-NL",),
     "LMGP": ("TF", "VW", "LMGP-NL"),
@@ -158,6 +167,8 @@ _STRESS = {"TF": (_lib.S_TF, _lib.E_TF), "VW": (_lib.S_VW, _lib.E_VW), "WT-NL": 
            "GGA": (_lib.S_GGA, _lib.E_GGA)}
 _STRESS_NAMES = ("TF", "VW", "X_TF_Y_VW", "XTFYVW", "TFVW", "WT", "WT-NL", "SM", "SM-NL", "FP", "FP-NL", "WTE",
                  "WTE-NL", "GGA")
+# MGP engines -> their fixed symmetrization (None: the symmetrization option)
+_MGP = {"MGP-NL": None, "MGPA-NL": "Arithmetic", "MGPG-NL": "Geometric", "MGP0-NL": None}
 # default exponents of the WT-engine variants (sm.py:14, fp.py:14); SMStress defaults to 1 (sm.py:18)
 _WT_AB = {"SM-NL": 0.5, "FP-NL": 1.0}
 
@@ -197,8 +208,8 @@ class KEDF(NativeFunctional):
                                       % o.get("kerneltype"))
         if o.get("symmetrization") not in (None, "None", "Arithmetic", "Geometric"):
             raise NotImplementedError("MGP symmetrization must be None, 'Arithmetic' or 'Geometric'")
-        if o.get("lumpfactor") is not None:
-            raise NotImplementedError("MGP lump factors are not supported")
+        if o.get("lumpfactor") is not None and any(e in _TABLE_OF for e in self.engines()):
+            raise NotImplementedError("lump factors of the LMGP family are not supported")
         if o.get("order", 3) != 3:
             raise NotImplementedError("kernel tables use cubic splines (order=3) only")
         if o.get("temperature") or o.get("temperature0"):
@@ -227,6 +238,29 @@ class KEDF(NativeFunctional):
         sigma = 0.0 if sigma is None else float(sigma)
         cfg.vw_sigma = sigma if "VW" in engines else 0.0
         cfg.wte = 1 if "WTE-NL" in engines else 0
+        mgp = next((e for e in engines if e in _MGP), None)
+        if mgp:  # mgp.py:15-119: the kernel at rho0, its t integral and the lump correction
+            sym = _MGP[mgp] or o.get("symmetrization")
+            cfg.wt_kernel = {None: _lib.LWT_KERNEL_MGP, "None": _lib.LWT_KERNEL_MGP,
+                             "Arithmetic": _lib.LWT_KERNEL_MGPA, "Geometric": _lib.LWT_KERNEL_MGPG}[sym]
+            cfg.wt_maxpoints = int(o.get("maxpoint", 1000))
+            cfg.wt_revke = 0 if mgp == "MGP0-NL" else 1
+            lf = o.get("lumpfactor")
+            if lf is None:  # KEDF drops options set to None (kedf/__init__.py:144): the default stays
+                lf = 0.2
+            cfg.wt_lump_abc[2] = 1.0
+            if lf is None:
+                cfg.wt_lump = 0
+            elif isinstance(lf, (list, tuple)):
+                cfg.wt_lump_abc[0] = float(lf[0])
+                if len(lf) > 1:
+                    cfg.wt_lump, cfg.wt_lump_abc[1] = 2, float(lf[1])
+                else:
+                    cfg.wt_lump = 1
+                if len(lf) > 2:
+                    cfg.wt_lump_abc[2] = float(lf[2])
+            else:
+                cfg.wt_lump, cfg.wt_lump_abc[0] = 1, float(lf)
         cfg.gga_sigma = sigma if "GGA" in engines else 0.0
         hc = next((e for e in engines if e in _HC), None)
         wtv = next((_WT_AB[e] for e in engines if e in _WT_AB), None)

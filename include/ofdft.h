@@ -161,6 +161,15 @@ typedef struct {
     int    wte;               /* with TF and WT: WTE (kedf/wte.py:15-57), E = E_TF exp(E_WT/E_TF)
                                  and V = exp(E_WT/E_TF)((1 - E_WT/E_TF) V_TF + V_WT), reported
                                  in OFDFT_E_NL (OFDFT_E_TF = 0) */
+    /* kernel of the density-independent nonlocal term (OFDFT_KE_WT): OFDFT_LWT_KERNEL_WT
+     * (Lindhard, kernel.py:325-334) or the MGP kernels at rho0 (kedf/mgp.py:15-119,
+     * kernel.py:251-322): OFDFT_LWT_KERNEL_MGP/MGPA/MGPG, with wt_maxpoints t points and
+     * the lump correction MGPOmegaE (kernel.py:408-440) */
+    int    wt_kernel;
+    int    wt_maxpoints;      /* default 1000                                        */
+    int    wt_lump;           /* 0 none; 1 a = lump[0] / Ne^(2/3) = b; 2 a, b = lump[0..1] */
+    double wt_lump_abc[3];    /* a, b, c (c = 1 by default)                          */
+    int    wt_revke;          /* 1: erf(c G^2)^2 (MGP, MGPA, MGPG); 0: 3/5 erf(c |G|)^2 (MGP0) */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

@@ -2159,3 +2159,73 @@ def grid_map(f, grid, nr_dst):
     else:
         G[:bd[0], :bd[1], :bd[2]] = F[index[0], index[1], index[2]].reshape(bd)
     return ifft(G, g2)
+
+
+# --------------------------------------------------------------------------
+# density-independent MGP kernels
+# --------------------------------------------------------------------------
+def mgp_kernel(grid, rho0, maxpoints=1000, symmetrization=None, lumpfactor=0.2, revke=True):
+    """MGPKernel (kedf/kernel.py:251-263) with MGPKernelTable (:267-322) on the 3-D
+    grid (splrep of LindhardFunction(eta, 1, 1) on 10000 log-spaced points from
+    1e-4 to 52, splev with ext=3) plus MGPOmegaE (:408-440) at Ne = rho0 V."""
+    from scipy.interpolate import splev, splrep
+    q = np.sqrt(grid.gg)
+    tkf = 2.0 * (3.0 * rho0 * np.pi ** 2) ** (1.0 / 3.0)
+    eta = q / tkf
+    gp = np.logspace(np.log10(1e-4), np.log10(52), num=10000)
+    tab = splrep(gp, lindhard(gp, 1.0, 1.0))
+    dt = 1.0 / maxpoints
+    cTF = 0.3 * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+    coe = 4.0 / 5.0 * cTF * 5.0 / 6.0 * dt
+    k = np.zeros_like(eta)
+    for i in range(1, maxpoints + 1):
+        t = i * dt
+        t16 = t ** (-2.0 / 3.0) if symmetrization == "Geometric" else t ** (1.0 / 6.0)
+        k += splev(eta / np.cbrt(t), tab, ext=3) / t16
+    if symmetrization == "Arithmetic":
+        k = 0.5 * (k * coe + wt_kernel_table(eta))
+    elif symmetrization == "Geometric":
+        k *= 2.0 * coe
+    else:
+        k *= coe
+    k[0, 0, 0] = 0.0
+    if lumpfactor is not None:
+        c, b = 1.0, None
+        if isinstance(lumpfactor, (list, tuple)):
+            a = lumpfactor[0]
+            if len(lumpfactor) > 1:
+                b = lumpfactor[1]
+            if len(lumpfactor) > 2:
+                c = lumpfactor[2]
+        else:
+            a = lumpfactor
+        if b is None:
+            a = float(a / (rho0 * grid.volume) ** (2.0 / 3.0))
+            b = a
+        qq = q.copy()
+        qq[0, 0, 0] = 1.0
+        gg = qq ** 2
+        if revke:
+            corr = 4 * np.pi * sp.erf(c * gg) ** 2 * a * np.exp(-gg * b) / gg
+        else:
+            corr = 4 * np.pi * sp.erf(c * qq) ** 2 * a * np.exp(-gg * b) / gg * (3.0 / 5.0)
+        corr[0, 0, 0] = 0.0
+        k = k + corr
+    return k
+
+
+class MGP(WT):
+    """MGP / MGPA / MGPG / MGP0 (kedf/mgp.py:15-119): the WT machinery with the MGP
+    kernel at rho0 = the mean density."""
+
+    def __init__(self, alpha=5.0 / 6.0, beta=5.0 / 6.0, maxpoint=1000, symmetrization=None, lumpfactor=0.2,
+                 revke=True):
+        super().__init__(alpha=alpha, beta=beta)
+        self.opts = dict(maxpoints=maxpoint, symmetrization=symmetrization, lumpfactor=lumpfactor, revke=revke)
+
+    def kernel(self, rho, grid):
+        rho0 = rho.mean()
+        if abs(self._saved_rho0 - rho0) > 1e-6 or rho.shape != self._shape:
+            self._kernel = mgp_kernel(grid, rho0, **self.opts)
+            self._saved_rho0, self._shape = rho0, rho.shape
+        return self._kernel

@@ -1,7 +1,8 @@
 """Generate tests/golden/reference_wtfam.npz: the Smargiassi-Madden and Perrot
 kinetic functionals (src/dftpy/functional/kedf/sm.py, fp.py: the WT engine with
-their own exponents) and WTE (wte.py) computed by the REFERENCE implementation,
-energy, potential and stress, on the smooth anisotropic density of system A.
+their own exponents), WTE (wte.py) and the MGP kernels (mgp.py) computed by the
+REFERENCE implementation, energy, potential and (but for MGP) stress, on the
+smooth anisotropic density of system A.
 
 Run in a container that has the reference sources:
 
@@ -19,6 +20,10 @@ from make_golden import ref_objects, setup  # noqa: E402
 
 CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6}),
          ("WTE", "WTE", {}), ("WTENL", "WTE-NL", {}), ("WTEX", "WTE", {"x": 0.8, "alpha": 0.9, "beta": 0.7})]
+# the density-independent MGP kernels (mgp.py): energy and potential only (no stress engine)
+MGP_CASES = [("MGP", "MGP", {}), ("MGPA", "MGPA", {}), ("MGPG", "MGPG", {}), ("MGP0", "MGP0", {}),
+             ("MGPNL", "MGP-NL", {"maxpoint": 200, "lumpfactor": None}),
+             ("MGP0L", "MGP0", {"lumpfactor": [0.1, 0.3, 2.0]}), ("MGPS", "MGP", {"symmetrization": "Geometric"})]
 
 
 def main(ref_root):
@@ -36,6 +41,12 @@ def main(ref_root):
         out["A_E_" + tag] = float(r.energy)
         out["A_V_" + tag] = np.asarray(r.potential)
         out["A_S_" + tag] = np.asarray(f.stress(DirectField(grid=grid, data=g0["A_rho"].copy())))
+        print(tag, r.energy)
+    for tag, name, kw in MGP_CASES:
+        rho = DirectField(grid=grid, data=g0["A_rho"].copy())
+        r = KEDF(name=name, **kw)(rho)
+        out["A_E_" + tag] = float(r.energy)
+        out["A_V_" + tag] = np.asarray(r.potential)
         print(tag, r.energy)
     np.savez_compressed(os.path.join(HERE, "reference_wtfam.npz"), **out)
 

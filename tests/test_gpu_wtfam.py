@@ -56,3 +56,24 @@ def test_wte_ground_state():
     v = _np(opt.functional.potential)
     r = _np(rho)
     assert np.abs((v - opt.mu) * np.sqrt(r)).max() < 1e-3
+
+
+MGP_CASES = [("MGP", "MGP", {}), ("MGPA", "MGPA", {}), ("MGPG", "MGPG", {}), ("MGP0", "MGP0", {}),
+             ("MGPNL", "MGP-NL", {"maxpoint": 200, "lumpfactor": None}),
+             ("MGP0L", "MGP0", {"lumpfactor": [0.1, 0.3, 2.0]}), ("MGPS", "MGP", {"symmetrization": "Geometric"})]
+
+
+@pytest.mark.parametrize("tag,name,kw", MGP_CASES, ids=[c[0] for c in MGP_CASES])
+def test_mgp_against_reference(golden, tag, name, kw):
+    """The MGP kernels at rho0 (mgp.py:15-119), the t integral evaluated on the device."""
+    grid = D.DirectGrid(golden["A_lattice"], golden["A_nr"])
+    rho = D.DirectField(grid, data=golden["A_rho"])
+    f = D.Functional(type="KEDF", name=name, **kw)
+    o = f(rho)
+    e, v = WF["A_E_" + tag], WF["A_V_" + tag]
+    assert abs(o.energy - e) <= 1e-10 * abs(e), (o.energy, e)
+    assert float(np.abs(_np(o.potential) - v).max()) <= 1e-9 * float(np.abs(v).max())
+    o32 = f(D.DirectField(grid, data=golden["A_rho"], dtype=torch.float32))
+    assert abs(o32.energy - e) <= 2e-6 * abs(e)
+    with pytest.raises(AttributeError):
+        f.stress(rho)

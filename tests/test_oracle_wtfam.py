@@ -52,3 +52,26 @@ def test_wte(golden, tag, local, kw):
     assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
     np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())
     np.testing.assert_allclose(S, WF["A_S_" + tag], rtol=0, atol=1e-10 * np.abs(S).max())
+
+
+MGP_ORACLE = {"MGP": (True, {}), "MGPA": (True, {"symmetrization": "Arithmetic"}),
+              "MGPG": (True, {"symmetrization": "Geometric"}), "MGP0": (True, {"revke": False}),
+              # KEDF drops options set to None (kedf/__init__.py:144), so the lump default 0.2 stays
+              "MGPNL": (False, {"maxpoint": 200}),
+              "MGP0L": (True, {"revke": False, "lumpfactor": [0.1, 0.3, 2.0]}),
+              "MGPS": (True, {"symmetrization": "Geometric"})}
+
+
+@pytest.mark.parametrize("tag", sorted(MGP_ORACLE))
+def test_mgp(golden, tag):
+    """The density-independent MGP kernels (mgp.py:15-119), E and V."""
+    local, kw = MGP_ORACLE[tag]
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    rho = golden["A_rho"]
+    nl = O.MGP(**kw)(rho, grid)
+    E, V = nl["E"], nl["V"]
+    if local:
+        t, w = O.tf(rho, grid), O.vw(rho, grid)
+        E, V = E + t["E"] + w["E"], V + t["V"] + w["V"]
+    assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
+    np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())

@@ -17,7 +17,7 @@ __all__ = ["KEDF", "KEDFEngines"]
 
 _BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "SM-NL": _lib.KE_WT, "FP-NL": _lib.KE_WT,
          "WTE-NL": _lib.KE_TF | _lib.KE_WT, "MGP-NL": _lib.KE_WT, "MGPA-NL": _lib.KE_WT, "MGPG-NL": _lib.KE_WT,
-         "MGP0-NL": _lib.KE_WT, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+         "MGP0-NL": _lib.KE_WT, "LKT": _lib.KE_GGA | _lib.KE_VW, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -58,6 +58,7 @@ KEDFEngines = {
     "LMGPG-NL": ("LMGPG-NL",),
     "GGA": ("GGA",),
     "MGGA": ("GGA",),
+    "LKT": ("LKT",),  # lkt.py: GGA 'LKT-VW' plus vW
     "HC": ("TF", "VW", "HC-NL"),
     "REVHC": ("TF", "VW", "REVHC-NL"),
     "HC-NL": ("HC-NL",),
@@ -236,7 +237,7 @@ class KEDF(NativeFunctional):
         # Gaussian smoothing: of the vW Laplacian (vw.py:45-48) and of the GGA gradient (gga.py:1246-1250)
         sigma = o.get("sigma")
         sigma = 0.0 if sigma is None else float(sigma)
-        cfg.vw_sigma = sigma if "VW" in engines else 0.0
+        cfg.vw_sigma = sigma if ("VW" in engines or "LKT" in engines) else 0.0
         cfg.wte = 1 if "WTE-NL" in engines else 0
         mgp = next((e for e in engines if e in _MGP), None)
         if mgp:  # mgp.py:15-119: the kernel at rho0, its t integral and the lump correction
@@ -261,7 +262,7 @@ class KEDF(NativeFunctional):
                     cfg.wt_lump_abc[2] = float(lf[2])
             else:
                 cfg.wt_lump, cfg.wt_lump_abc[0] = 1, float(lf)
-        cfg.gga_sigma = sigma if "GGA" in engines else 0.0
+        cfg.gga_sigma = sigma if ("GGA" in engines or "LKT" in engines) else 0.0
         hc = next((e for e in engines if e in _HC), None)
         wtv = next((_WT_AB[e] for e in engines if e in _WT_AB), None)
         a = float(o.get("alpha", 2.0 if hc else (wtv if wtv is not None else 5.0 / 6.0)))
@@ -313,8 +314,8 @@ class KEDF(NativeFunctional):
             cfg.gga_nparams = len(p)
             for i, v in enumerate(p):
                 cfg.gga_params[i] = float(v)
-        if "GGA" in engines:  # gga.py:1212-1270: the functional named by k_str, default LKT
-            name = str(o.get("k_str") or "LKT").upper()
+        if "GGA" in engines or "LKT" in engines:  # gga.py:1212-1270: k_str's functional, default LKT
+            name = "LKT-VW" if "LKT" in engines else str(o.get("k_str") or "LKT").upper()
             formula, p0 = (MGGA_FUNCTIONALS if o.get("mgga") else GGA_FUNCTIONALS)[name]
             params = o.get("params")
             p = list(p0)

@@ -60,6 +60,12 @@ def main(ref_root):
         r = Functional(type="KEDF", name="MGGA_" + name, **kw)(rA)
         out["A_E_M" + tag] = float(r.energy)
         out["A_V_M" + tag] = np.asarray(r.potential)
+    # the LKT engine (lkt.py): GGA 'LKT-VW' plus vW
+    for tag, kw in (("LKTE", {}), ("LKTE_P", {"params": [1.1]}), ("LKTE_S", {"sigma": 0.2, "y": 0.9})):
+        rA = DirectField(grid=gridA, data=g0["A_rho"].copy())
+        r = Functional(type="KEDF", name="LKT", **kw)(rA)
+        out["A_E_" + tag] = float(r.energy)
+        out["A_V_" + tag] = np.asarray(r.potential)
     # the vW term with Gaussian smoothing of its Laplacian (vw.py:29-53)
     for tag, kw in (("VW_SIG", {"sigma": 0.2}), ("TFVW_SIG", {"sigma": 0.35})):
         rA = DirectField(grid=gridA, data=g0["A_rho"].copy())

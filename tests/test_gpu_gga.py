@@ -144,3 +144,14 @@ def test_mgga_against_reference(golden, tag, name, kw, dtype):
     if dtype == torch.float64:
         with pytest.raises(AttributeError):
             f.stress(rho)
+
+
+@pytest.mark.parametrize("tag,kw", [("LKTE", {}), ("LKTE_P", {"params": [1.1]}), ("LKTE_S", {"sigma": 0.2, "y": 0.9})])
+def test_lkt_engine_against_reference(golden, tag, kw):
+    """KEDF 'LKT' (lkt.py): GGA 'LKT-VW' plus vW in one fused evaluation."""
+    grid = D.DirectGrid(golden["A_lattice"], golden["A_nr"])
+    rho = D.DirectField(grid, data=golden["A_rho"])
+    o = D.Functional(type="KEDF", name="LKT", **kw)(rho)
+    e, v = GG["A_E_" + tag], GG["A_V_" + tag]
+    assert abs(o.energy - e) <= 1e-10 * abs(e), (o.energy, e)
+    assert float(np.abs(_np(o.potential) - v).max()) <= 1e-9 * float(np.abs(v).max())

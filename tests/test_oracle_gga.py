@@ -62,3 +62,15 @@ def test_mgga_system_a(golden, tag, name, kw):
     assert abs(r["E"] - e) <= 1e-11 * abs(e)
     v = GG["A_V_M" + tag]
     np.testing.assert_allclose(r["V"], v, rtol=0, atol=1e-10 * np.abs(v).max())
+
+
+@pytest.mark.parametrize("tag,kw", [("LKTE", {}), ("LKTE_P", {"params": [1.1]}), ("LKTE_S", {"sigma": 0.2, "y": 0.9})])
+def test_lkt_engine(golden, tag, kw):
+    """The LKT engine (lkt.py): GGA 'LKT-VW' plus vW, sigma passed to both."""
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    rho = golden["A_rho"]
+    g = O.gga(rho, grid, "LKT-VW", params=kw.get("params"), sigma=kw.get("sigma"))
+    w = O.vw(rho, grid, y=kw.get("y", 1.0), sigma=kw.get("sigma"))
+    E, V = g["E"] + w["E"], g["V"] + w["V"]
+    assert abs(E - GG["A_E_" + tag]) <= 1e-11 * abs(E)
+    np.testing.assert_allclose(V, GG["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())

@@ -15,9 +15,9 @@ _LIB = None
 OK, EINVAL, ECUDA, ECUFFT, ENOMEM, ESTATE = range(6)
 F64, F32 = 0, 1
 CALC_E, CALC_V = 1, 2
-E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, E_GGA, E_EXT, NE = range(12)
+E_TF, E_VW, E_NL, E_XC, E_H, E_PP, E_II, E_TOTAL, E_NELEC, E_GGA, E_EXT, E_DTTF, NE = range(13)
 S_TF, S_VW, S_NL, S_XC, S_H, S_GGA, NS = range(7)
-KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA = 1, 2, 4, 8, 16
+KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA, KE_DTTF = 1, 2, 4, 8, 16, 32
 (GGA_LKT, GGA_LKTVW, GGA_DK, GGA_LLP, GGA_OL, GGA_THAK, GGA_B86A, GGA_B86B, GGA_DK87, GGA_PW86, GGA_PW91O, GGA_PW91,
  GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV, GGA_PBE2M, GGA_PG, GGA_GE2, GGA_GE4, GGA_PGSL, GGA_PGSLR) = range(26)
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
@@ -48,7 +48,7 @@ class Config(C.Structure):
         ("gga_remove_vw", C.c_double), ("lwt_family", C.c_int), ("external", C.c_int),
         ("vw_sigma", C.c_double), ("gga_sigma", C.c_double), ("wte", C.c_int),
         ("wt_kernel", C.c_int), ("wt_maxpoints", C.c_int), ("wt_lump", C.c_int), ("wt_lump_abc", C.c_double * 3),
-        ("wt_revke", C.c_int),
+        ("wt_revke", C.c_int), ("tf_temperature", C.c_double), ("tf_temp_old", C.c_int),
     ]
 
 

@@ -116,14 +116,16 @@ struct PreArgs {
     long long N;
     int tf, vw, xc, pp, ext, nl, lwt, same_ab, wantV;
     int tf_v;       // add the TF potential (off under WTE, which scales it afterwards)
+    int dttf, dttf_old;
+    double temp;    // DTTF temperature (Hartree) and the TF-energy x
     int nl_is_lwt;  // clamp rule: LWT clamps rho<=0, WT clamps rho<1e-30
     double tf_x;
     double alpha, beta;
     Consts k;
 };
 
-// slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho, 7 external
-constexpr int PRE_NS = 8;
+// slots: 0 TF, 1 XC, 2 PP, 3 sum rho, 4 min kF, 5 max kF, 6 max rho, 7 external, 8 DTTF
+constexpr int PRE_NS = 9;
 
 // Per-thread running sum of a field reduction: float64 in the FP64 path; in the
 // FP32 path a float32 Kahan-compensated sum over the thread's points (GB300
@@ -154,9 +156,9 @@ struct RunSum<float> {
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* partials) {
     using M = T;
-    RunSum<M> sum[5];
+    RunSum<M> sum[6];
     M kfmin = (M)INFINITY, kfmax = -(M)INFINITY, rmax = -(M)INFINITY;
-    const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2, 0};
+    const int kinds[PRE_NS] = {0, 0, 0, 0, 1, 2, 2, 0, 0};
     const M cTF_E = (M)a.k.cTF_E, cTF_V = (M)a.k.cTF_V, tf_x = (M)a.tf_x;
     const LdaC<M> lc(a.k);
     const M threepi2 = (M)a.k.threepi2, alpha = (M)a.alpha, beta = (M)a.beta;
@@ -188,6 +190,36 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
             sum[2].add(vl * r);
             v += vl;
         }
+        if (a.dttf) {  // TTF - TF (tf.py:101-204): theta = T / v_TF, fitted forms below/above 1.36
+            const M T = (M)a.temp, vtf = cTF_V * mcbrt(r * r), th = T / vtf, cc = (M)0.752252778063675;
+            const M r2 = sqrt((M)2), r23 = (M)2 * r2;  // 2^0.5, 2^1.5
+            const M tf_ed = mcbrt(r * r * r * r * r) * cTF_E;
+            const M t32 = (M)1 / sqrt(th * th * th);
+            const bool hi = th >= (M)1.36;
+            M vt;
+            if (hi)
+                vt = T * (mlog(cc * t32) + mlog((M)1 + cc * t32 / r23)) - vtf;
+            else
+                vt = vtf * (th * ((M)0.016 + th * ((M)-0.957 + th * ((M)-0.293 + th * (M)0.209))));
+            M ed;
+            if (a.dttf_old) {  // TemperatureTFEnergy_old (tf.py:180-204)
+                const M th52 = sqrt(th * th * th * th * th);
+                ed = (vt + vtf) * r - (M)(2.0 * 1.4142135623730951 / 3.0 / (M_PI * M_PI)) * (T * T * sqrt(T)) / th52 *
+                                         sqrt((M)0.16 + th * th) /
+                                         ((M)1 - (M)0.14 * (mexp(-th) - mexp((M)-3.68 * th))) -
+                     tf_ed;
+            } else if (hi) {  // TemperatureTFEnergy (tf.py:134-177)
+                const M k = T / cTF_V;
+                ed = ((M)-2 * r + r23 * k * sqrt(k) * atanh(cc * t32 / r23) / cc + r * mlog((M)1 + cc / r23 * t32) +
+                      r * mlog(cc * t32) + r2 * k * sqrt(th) * mcbrt(r) * mlog((M)8 * k * k * k - cc * cc * (r * r)) / cc) *
+                         T -
+                     tf_ed;
+            } else {
+                ed = T * (r * ((M)0.016 + th * ((M)(-0.957 * 3) + th * ((M)(-0.293 * -3) + th * (M)-0.209))));
+            }
+            sum[5].add(ed);
+            if (a.wantV) v += vt * tf_x;
+        }
         if (a.ext) {  // external_potential.py:30-35
             const M ve = a.vext[i];
             sum[4].add(ve * r);
@@ -208,7 +240,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_prepass(PreArgs<T> a, double* p
         if (a.wantV) a.V[i] = v;
     }
     double acc[PRE_NS] = {sum[0].get(), sum[1].get(), sum[2].get(), sum[3].get(), (double)kfmin, (double)kfmax,
-                          (double)rmax, sum[4].get()};
+                          (double)rmax, sum[4].get(), sum[5].get()};
     block_reduce_store<PRE_NS>(acc, kinds, partials);
 }
 
@@ -1356,6 +1388,9 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
     pa.N = N;
     pa.tf = tf;
     pa.tf_v = !wte;
+    pa.dttf = (c.kedf_terms & OFDFT_KE_DTTF) != 0;
+    pa.dttf_old = c.tf_temp_old;
+    pa.temp = c.tf_temperature;
     pa.vw = vw;
     pa.xc = xc;
     pa.pp = pp;
@@ -1772,12 +1807,13 @@ void collect_energies(ofdft_eval* e, double* energies) {
     E[OFDFT_E_II] = c.ewald_energy;
     E[OFDFT_E_GGA] = p.gga ? R[40] * dV : 0.0;
     E[OFDFT_E_EXT] = p.ext ? R[7] * dV : 0.0;
+    E[OFDFT_E_DTTF] = (c.kedf_terms & OFDFT_KE_DTTF) ? R[8] * dV * c.tf_x : 0.0;
     if (c.wte && p.tf && p.wt) {  // wte.py:20-22
         E[OFDFT_E_NL] = E[OFDFT_E_TF] * std::exp(e_wt_raw / E[OFDFT_E_TF]);
         E[OFDFT_E_TF] = 0.0;
     }
     E[OFDFT_E_TOTAL] = E[OFDFT_E_TF] + E[OFDFT_E_VW] + E[OFDFT_E_NL] + E[OFDFT_E_XC] + E[OFDFT_E_H] + E[OFDFT_E_PP] +
-                       E[OFDFT_E_II] + E[OFDFT_E_GGA] + E[OFDFT_E_EXT];
+                       E[OFDFT_E_II] + E[OFDFT_E_GGA] + E[OFDFT_E_EXT] + E[OFDFT_E_DTTF];
     e->last_launches = p.launches;
 }
 

@@ -17,7 +17,7 @@ __all__ = ["KEDF", "KEDFEngines"]
 
 _BITS = {"HC-NL": _lib.KE_LWT, "REVHC-NL": _lib.KE_LWT, "GGA": _lib.KE_GGA, "TF": _lib.KE_TF, "VW": _lib.KE_VW, "WT-NL": _lib.KE_WT, "SM-NL": _lib.KE_WT, "FP-NL": _lib.KE_WT,
          "WTE-NL": _lib.KE_TF | _lib.KE_WT, "MGP-NL": _lib.KE_WT, "MGPA-NL": _lib.KE_WT, "MGPG-NL": _lib.KE_WT,
-         "MGP0-NL": _lib.KE_WT, "LKT": _lib.KE_GGA | _lib.KE_VW, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
+         "MGP0-NL": _lib.KE_WT, "LKT": _lib.KE_GGA | _lib.KE_VW, "DTTF": _lib.KE_DTTF, "LWT-NL": _lib.KE_LWT, "LMGP-NL": _lib.KE_LWT,
          "LMGPA-NL": _lib.KE_LWT, "LMGPG-NL": _lib.KE_LWT}
 # kernel table of each k_F-node engine (lwt.py:571-578 fix kerneltype for the LMGP names)
 _TABLE_OF = {"LMGP-NL": "MGP", "LMGPA-NL": "MGPA", "LMGPG-NL": "MGPG"}
@@ -59,6 +59,7 @@ KEDFEngines = {
     "GGA": ("GGA",),
     "MGGA": ("GGA",),
     "LKT": ("LKT",),  # lkt.py: GGA 'LKT-VW' plus vW
+    "DTTF": ("DTTF",),  # TTF - TF (tf.py:83-204), added to any name given a temperature
     "HC": ("TF", "VW", "HC-NL"),
     "REVHC": ("TF", "VW", "REVHC-NL"),
     "HC-NL": ("HC-NL",),
@@ -213,8 +214,6 @@ class KEDF(NativeFunctional):
             raise NotImplementedError("lump factors of the LMGP family are not supported")
         if o.get("order", 3) != 3:
             raise NotImplementedError("kernel tables use cubic splines (order=3) only")
-        if o.get("temperature") or o.get("temperature0"):
-            raise NotImplementedError("finite-temperature TF is not supported")
         if "GGA" in self.engines():
             k = o.get("k_str")
             if o.get("mgga"):  # gga.py:1226-1230
@@ -239,6 +238,12 @@ class KEDF(NativeFunctional):
         sigma = 0.0 if sigma is None else float(sigma)
         cfg.vw_sigma = sigma if ("VW" in engines or "LKT" in engines) else 0.0
         cfg.wte = 1 if "WTE-NL" in engines else 0
+        # a temperature adds the finite-temperature TF correction (kedf/__init__.py:155-156)
+        t0, t = o.get("temperature0"), o.get("temperature")
+        if t0 or t:
+            cfg.kedf_terms |= _lib.KE_DTTF
+            cfg.tf_temperature = float(t0 if t0 is not None else (t if t is not None else 1e-3))
+            cfg.tf_temp_old = 1 if t0 is not None else 0
         mgp = next((e for e in engines if e in _MGP), None)
         if mgp:  # mgp.py:15-119: the kernel at rho0, its t integral and the lump correction
             sym = _MGP[mgp] or o.get("symmetrization")
@@ -355,8 +360,12 @@ class KEDF(NativeFunctional):
             sub.ke_kernel_saved = self.ke_kernel_saved
             return NativeFunctional.compute(sub, density, calcType)
         out = {}
+        o = self.options
+        if o.get("temperature0") or o.get("temperature"):  # DTTF as its own part (kedf/__init__.py:155-156)
+            engines = tuple(engines) + ("DTTF",)
+        plain = {k: v for k, v in o.items() if k not in ("temperature", "temperature0")}
         for e in engines:
-            sub = KEDF(name=e, **self.options)
+            sub = KEDF(name=e, **(o if e == "DTTF" else plain))
             sub.ke_kernel_saved = self.ke_kernel_saved
             r = NativeFunctional.compute(sub, density, calcType)
             r.name = e

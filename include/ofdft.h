@@ -41,7 +41,7 @@ enum { OFDFT_CALC_E = 1, OFDFT_CALC_V = 2 };
 
 /* energy slots written by ofdft_eval_compute (Hartree) */
 enum { OFDFT_E_TF = 0, OFDFT_E_VW, OFDFT_E_NL, OFDFT_E_XC, OFDFT_E_H, OFDFT_E_PP, OFDFT_E_II,
-       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_E_GGA, OFDFT_E_EXT, OFDFT_NE };
+       OFDFT_E_TOTAL, OFDFT_E_NELEC, OFDFT_E_GGA, OFDFT_E_EXT, OFDFT_E_DTTF, OFDFT_NE };
 /* stress tensors written by ofdft_eval_stress, 9 doubles (3 x 3, row-major) each */
 enum { OFDFT_S_TF = 0, OFDFT_S_VW, OFDFT_S_NL, OFDFT_S_XC, OFDFT_S_H, OFDFT_S_GGA, OFDFT_NS };
 
@@ -93,7 +93,8 @@ int ofdft_dot_noalloc(const void* a, const void* b, long long n, int precision, 
  * Configuration of the terms of TotalFunctional (src/dftpy/functional/
  * total_functional.py:49-146) and the KEDF dispatcher (kedf/__init__.py:27-69,
  * :124-191).  kedf_terms is a bit set of OFDFT_KE_*. */
-enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8, OFDFT_KE_GGA = 16 };
+enum { OFDFT_KE_TF = 1, OFDFT_KE_VW = 2, OFDFT_KE_WT = 4, OFDFT_KE_LWT = 8, OFDFT_KE_GGA = 16,
+       OFDFT_KE_DTTF = 32 /* finite-temperature TF correction TTF (kedf/tf.py:83-204), tf_temperature */ };
 /* enhancement-factor formulas of the GGA kinetic functionals (kedf/gga.py:18-586);
  * a named functional of the reference's GGA_KEDF_list (:587-643) is a formula plus
  * its parameters, e.g. LC94 = PW91 with its own six, REVAPBEK = PBE with (1.245, 0.23889) */
@@ -170,6 +171,8 @@ typedef struct {
     int    wt_lump;           /* 0 none; 1 a = lump[0] / Ne^(2/3) = b; 2 a, b = lump[0..1] */
     double wt_lump_abc[3];    /* a, b, c (c = 1 by default)                          */
     int    wt_revke;          /* 1: erf(c G^2)^2 (MGP, MGPA, MGPG); 0: 3/5 erf(c |G|)^2 (MGP0) */
+    double tf_temperature;    /* OFDFT_KE_DTTF: the temperature (Hartree)              */
+    int    tf_temp_old;       /* 1: the energy of TemperatureTFEnergy_old (temperature0) */
 } ofdft_config;
 
 void ofdft_config_default(ofdft_config* c);

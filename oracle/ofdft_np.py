@@ -2229,3 +2229,53 @@ class MGP(WT):
             self._kernel = mgp_kernel(grid, rho0, **self.opts)
             self._saved_rho0, self._shape = rho0, rho.shape
         return self._kernel
+
+
+# --------------------------------------------------------------------------
+# finite-temperature Thomas-Fermi correction
+# --------------------------------------------------------------------------
+def ttf(rho, grid, temperature, x=1.0, old=False, calc=("E", "V")):
+    """TTF (kedf/tf.py:83-204), the correction a temperature option adds to a KEDF
+    ('DTTF', kedf/__init__.py:155-156): TemperatureTFPotential, TemperatureTFEnergy
+    and, with temperature0 (old=True), TemperatureTFEnergy_old."""
+    T = temperature
+    factor = (3.0 / 10.0) * (5.0 / 3.0) * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+    vtf = factor * np.cbrt(rho * rho)
+    theta = T / vtf
+    c = 0.752252778063675
+    mask = theta >= 1.36
+    a = [0.016, -0.957, -0.293, 0.209]
+    pot = np.zeros_like(theta)
+    tmp = np.ones_like(theta)
+    for i in range(4):
+        tmp = tmp * theta
+        pot += a[i] * tmp
+    pot *= vtf
+    t32 = 1.0 / np.sqrt(theta * theta * theta)
+    pot[mask] = T * (np.log(c * t32[mask]) + np.log(1 + c * t32[mask] / 2.0 ** 1.5)) - vtf[mask]
+    out = {}
+    if "V" in calc:
+        out["V"] = pot * x
+    if "E" in calc:
+        tf_ed = np.cbrt(rho * rho * rho * rho * rho) * (3.0 / 10.0) * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+        if old:
+            ed = (pot + vtf) * rho
+            ed += -2 * np.sqrt(2) / 3 / np.pi ** 2 * T ** 2.5 / np.sqrt(theta ** 5) * np.sqrt(
+                0.16 + theta * theta) / (1.0 - 0.14 * (np.exp(-theta) - np.exp(-3.68 * theta)))
+            ed -= tf_ed
+        else:
+            b = [0.016, -0.957 * 3, -0.293 * -3, -0.209]
+            k = T / factor
+            ed = np.zeros_like(theta)
+            tmp = rho.copy()
+            for i in range(4):
+                ed += b[i] * tmp
+                tmp = tmp * theta
+            ed *= T
+            r = rho[mask]
+            ed[mask] = (-2.0 * r + 2 ** 1.5 * k ** 1.5 * np.arctanh(c * t32[mask] / 2 ** 1.5) / c
+                        + r * np.log(1.0 + c / 2 ** 1.5 * t32[mask]) + r * np.log(c * t32[mask])
+                        + 2 ** 0.5 * k * np.sqrt(theta[mask]) * np.cbrt(r) * np.log(8.0 * k ** 3.0 - c ** 2.0 * r * r)
+                        / c) * T - tf_ed[mask]
+        out["E"] = ed.sum() * grid.dV * x
+    return out

@@ -20,6 +20,8 @@ from make_golden import ref_objects, setup  # noqa: E402
 
 CASES = [("SM", "SM", {}), ("FP", "FP", {}), ("SMNL", "SM-NL", {}), ("SMA", "SM", {"alpha": 0.6, "beta": 0.6}),
          ("WTE", "WTE", {}), ("WTENL", "WTE-NL", {}), ("WTEX", "WTE", {"x": 0.8, "alpha": 0.9, "beta": 0.7})]
+TTF_CASES = [("TTF1", "TFVW", {"temperature": 0.5}), ("TTF2", "TF", {"temperature": 1.2, "x": 0.9}),
+             ("TTF0", "TFVW", {"temperature0": 0.5}), ("TTFW", "WT", {"temperature": 0.05})]
 # the density-independent MGP kernels (mgp.py): energy and potential only (no stress engine)
 MGP_CASES = [("MGP", "MGP", {}), ("MGPA", "MGPA", {}), ("MGPG", "MGPG", {}), ("MGP0", "MGP0", {}),
              ("MGPNL", "MGP-NL", {"maxpoint": 200, "lumpfactor": None}),
@@ -42,6 +44,16 @@ def main(ref_root):
         out["A_V_" + tag] = np.asarray(r.potential)
         out["A_S_" + tag] = np.asarray(f.stress(DirectField(grid=grid, data=g0["A_rho"].copy())))
         print(tag, r.energy)
+    # the finite-temperature TF correction (tf.py:83-204, added by a temperature option)
+    for tag, name, kw in TTF_CASES:
+        rho = DirectField(grid=grid, data=g0["A_rho"].copy())
+        f = KEDF(name=name, **kw)
+        r = f(rho)
+        out["A_E_" + tag] = float(r.energy)
+        out["A_V_" + tag] = np.asarray(r.potential)
+        parts = f(DirectField(grid=grid, data=g0["A_rho"].copy()), split=True)
+        out["A_EDTTF_" + tag] = float(parts["DTTF"].energy)
+        print(tag, r.energy, parts["DTTF"].energy)
     for tag, name, kw in MGP_CASES:
         rho = DirectField(grid=grid, data=g0["A_rho"].copy())
         r = KEDF(name=name, **kw)(rho)

@@ -77,3 +77,24 @@ def test_mgp_against_reference(golden, tag, name, kw):
     assert abs(o32.energy - e) <= 2e-6 * abs(e)
     with pytest.raises(AttributeError):
         f.stress(rho)
+
+
+TTF_CASES = [("TTF1", "TFVW", {"temperature": 0.5}), ("TTF2", "TF", {"temperature": 1.2, "x": 0.9}),
+             ("TTF0", "TFVW", {"temperature0": 0.5}), ("TTFW", "WT", {"temperature": 0.05})]
+
+
+@pytest.mark.parametrize("tag,name,kw", TTF_CASES, ids=[c[0] for c in TTF_CASES])
+def test_ttf_against_reference(golden, tag, name, kw):
+    """A temperature option adds the finite-temperature TF correction (tf.py:83-204);
+    split=True reports it as 'DTTF' (kedf/__init__.py:155-156)."""
+    grid = D.DirectGrid(golden["A_lattice"], golden["A_nr"])
+    rho = D.DirectField(grid, data=golden["A_rho"])
+    f = D.Functional(type="KEDF", name=name, **kw)
+    o = f(rho)
+    e, v = WF["A_E_" + tag], WF["A_V_" + tag]
+    assert abs(o.energy - e) <= 1e-10 * abs(e), (o.energy, e)
+    assert float(np.abs(_np(o.potential) - v).max()) <= 1e-9 * float(np.abs(v).max())
+    parts = f(rho, split=True)
+    assert abs(parts["DTTF"].energy - WF["A_EDTTF_" + tag]) <= 1e-10 * abs(WF["A_EDTTF_" + tag])
+    o32 = f(D.DirectField(grid, data=golden["A_rho"], dtype=torch.float32))
+    assert abs(o32.energy - e) <= 2e-6 * abs(e)

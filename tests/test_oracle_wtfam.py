@@ -75,3 +75,23 @@ def test_mgp(golden, tag):
         E, V = E + t["E"] + w["E"], V + t["V"] + w["V"]
     assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
     np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())
+
+
+TTF_ORACLE = {"TTF1": (("TF", "VW"), {}, 0.5, False, 1.0), "TTF2": (("TF",), {}, 1.2, False, 0.9),
+              "TTF0": (("TF", "VW"), {}, 0.5, True, 1.0), "TTFW": (("TF", "VW", "WT"), {}, 0.05, False, 1.0)}
+
+
+@pytest.mark.parametrize("tag", sorted(TTF_ORACLE))
+def test_ttf(golden, tag):
+    """A temperature option adds TTF (tf.py:83-204) to the KEDF."""
+    names, _, T, old, x = TTF_ORACLE[tag]
+    grid = O.Grid(golden["A_lattice"], golden["A_nr"])
+    rho = golden["A_rho"]
+    d = O.ttf(rho, grid, T, x=x, old=old)
+    assert abs(d["E"] - WF["A_EDTTF_" + tag]) <= 1e-11 * abs(d["E"])
+    E, V = d["E"], d["V"]
+    for n in names:
+        o = {"TF": lambda: O.tf(rho, grid, x=x), "VW": lambda: O.vw(rho, grid), "WT": lambda: O.WT()(rho, grid)}[n]()
+        E, V = E + o["E"], V + o["V"]
+    assert abs(E - WF["A_E_" + tag]) <= 1e-11 * abs(E)
+    np.testing.assert_allclose(V, WF["A_V_" + tag], rtol=0, atol=1e-10 * np.abs(V).max())

@@ -44,7 +44,7 @@ HBM_FALLBACK = 6800.0
 # the same kernels on the 256^3 grid with 16 nodes (dram__bytes_read.sum +
 # dram__bytes_write.sum over the bytes the launch must move); a launch at 64
 # nodes moves 4x the planes of that capture, so its traffic scales with them.
-TRAFFIC_SOURCE = "profiles/fused_kernels_256cube_nsp16.md (ncu, 256^3, 16 nodes, scaled by planes per launch)"
+TRAFFIC_SOURCE = "ncu dram__bytes of the same kernel at 256^3 with 16 nodes, scaled by planes per launch"
 TRAFFIC_RATIO = {
     "fz_axis1": (2.165 + 2.104) / (32 * 2 * 67633152 / 1e9),
     "lwt_nodes": (0.072 + 1.021) / ((16 + 1) * 67633152 / 1e9),

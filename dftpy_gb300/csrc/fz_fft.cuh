@@ -410,20 +410,36 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 }
 // orders this thread's earlier shared-memory accesses before later copies into it
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-// Waits for the phase of `parity` to complete, polling at most 2^22 times;
-// false when it did not (the caller records an error instead of hanging).
+// Elapsed-time limit of an mbarrier wait: a bulk copy of a few tens of KB
+// completes in microseconds, so 100 ms means the copy is not coming.
+constexpr unsigned long long kMbarWaitNs = 100000000ull;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ bool mbar_try(unsigned a, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Waits for the phase of `parity` to complete for at most kMbarWaitNs of
+// elapsed time (%globaltimer, read only once the first try has failed);
+// false when it did not complete (the caller records an error instead of
+// hanging).
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
     const unsigned a = smem_addr(bar);
-    for (int it = 0; it < (1 << 22); ++it) {
-        unsigned done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
+    if (mbar_try(a, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (;;) {
+        if (mbar_try(a, parity)) return true;
+        if (globaltimer_ns() - t0 > kMbarWaitNs) return false;
     }
-    return false;
 }
 
 template <int N, int E, int S, class Idx>

@@ -466,7 +466,19 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
     for (int jj = 0; jj < a.nb; ++jj) {
         const int j = a.j0 + jj;
         const int s = jj & 1;
-        if (!fz::mbar_wait(&bar[s], (jj >> 1) & 1)) atomicOr(a.err, 1u);
+        const bool ok = fz::mbar_wait(&bar[s], (jj >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            // a copy did not complete in time: record it once, let the copies in
+            // flight (planes jj and jj + 1) finish within the same limit, issue
+            // no more and leave pot untouched; the host raises the error
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, 1u);
+                fz::mbar_wait(&bar[s], (jj >> 1) & 1);
+                if (jj + 1 < a.nb) fz::mbar_wait(&bar[s ^ 1], ((jj + 1) >> 1) & 1);
+            }
+            __syncthreads();
+            return;
+        }
         float2 v[E];
         fz_c2r_pre<H>(stage + s * STAGE, l, t, a.tw.tr, v);
         fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, ix1, t, twr);

@@ -16,8 +16,12 @@
 //   * n must be in 1 .. kNoAllocMaxElems (4096 blocks x 16384 elements =
 //     67,108,864, e.g. a 406^3 grid); larger n is rejected with OFDFT_EINVAL.
 //   * The first call on each device looks the array's device address up with
-//     cudaGetSymbolAddress (with that device current) and caches it; make that
-//     first call before any stream capture.
+//     cudaGetSymbolAddress (with that device current), caches it, and queries
+//     the attributes of all three kernels.  Under CUDA's lazy module loading
+//     those steps make the driver load this module's code and the array onto
+//     the device, which takes device memory; after them no later call loads
+//     anything.  So make the first call on each device at start-up, before a
+//     pool reserves the device's memory and before any stream capture.
 //   * All calls share the one array and it keeps the last call's contents.
 //     Every partial a call reads is written earlier in the same call, so no
 //     clearing is needed, but two calls that overlap on the GPU (different
@@ -87,6 +91,12 @@ double* noalloc_scratch() {
     if (!g_noalloc_ptr[dev]) {
         void* p = nullptr;
         OFDFT_CK(cudaGetSymbolAddress(&p, g_noalloc_partials));
+        // load every kernel of this entry point now, so that no later call (a
+        // float32 call after float64 ones, say) makes the driver load code
+        cudaFuncAttributes fa;
+        OFDFT_CK(cudaFuncGetAttributes(&fa, k_noalloc_partial<double>));
+        OFDFT_CK(cudaFuncGetAttributes(&fa, k_noalloc_partial<float>));
+        OFDFT_CK(cudaFuncGetAttributes(&fa, k_noalloc_final));
         g_noalloc_ptr[dev] = (double*)p;
     }
     return g_noalloc_ptr[dev];

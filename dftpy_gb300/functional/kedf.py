@@ -251,13 +251,13 @@ class KEDF(NativeFunctional):
                              "Arithmetic": _lib.LWT_KERNEL_MGPA, "Geometric": _lib.LWT_KERNEL_MGPG}[sym]
             cfg.wt_maxpoints = int(o.get("maxpoint", 1000))
             cfg.wt_revke = 0 if mgp == "MGP0-NL" else 1
+            # lumpfactor=None does not turn the lump correction off: KEDF drops
+            # options set to None (kedf/__init__.py:144), so the default 0.2 applies
             lf = o.get("lumpfactor")
-            if lf is None:  # KEDF drops options set to None (kedf/__init__.py:144): the default stays
+            if lf is None:
                 lf = 0.2
             cfg.wt_lump_abc[2] = 1.0
-            if lf is None:
-                cfg.wt_lump = 0
-            elif isinstance(lf, (list, tuple)):
+            if isinstance(lf, (list, tuple)):
                 cfg.wt_lump_abc[0] = float(lf[0])
                 if len(lf) > 1:
                     cfg.wt_lump, cfg.wt_lump_abc[1] = 2, float(lf[1])

@@ -85,7 +85,9 @@ int ofdft_dot3(ofdft_grid* g, const void* a, const void* b, const void* c, doubl
  * may be NULL: sum(a)) over n elements of the given precision, written to
  * device memory in stream order.  Its scratch is a 32 KiB static device array
  * (4096 block partials), so n is limited to 67,108,864 (OFDFT_EINVAL beyond).
- * The first call on a device looks the array up and should come before any
+ * The first call on a device looks the array up and loads this entry point's
+ * kernels (under lazy module loading that load takes device memory), so make
+ * it at start-up, before a pool reserves the device's memory and before any
  * stream capture; calls that overlap on the GPU share the array and race. */
 int ofdft_dot_noalloc(const void* a, const void* b, long long n, int precision, double* out_dev, ofdft_stream s);
 

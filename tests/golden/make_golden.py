@@ -3,7 +3,7 @@ implementation (Quantum-MultiScale/DFTpy) on seeded inputs.
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference source tree>
 
 The reference needs ASE, which is not installed here; oracle/ase_shim provides
 the few members it uses.  Nothing else in the repository reads the reference
@@ -77,6 +77,26 @@ def terms_on(DirectGrid, DirectField, lattice, nr, rho_arr, ions, pp_list, prefi
     return grid, rho
 
 
+def edge_density(lattice, nr, positions, zvals, width):
+    """The B block's density, pinned here (not taken from dftpy_gb300.synthetic,
+    whose generator may change): periodic Gaussians summed over the whole grid
+    by minimum image, normalised to sum(zvals) electrons.  Reproduces the
+    stored B_rho bit for bit."""
+    s = [np.arange(n) / n for n in nr]
+    S = np.stack(np.meshgrid(*s, indexing="ij"), axis=-1)
+    inv = np.linalg.inv(lattice)
+    rho = np.zeros(tuple(nr), dtype=np.float64)
+    for p, z in zip(positions, zvals):
+        f = S - (p @ inv)
+        f -= np.round(f)
+        r = f @ lattice
+        rr = (r * r).sum(-1)
+        rho += z * np.exp(-rr / (2 * width ** 2)) / (2 * np.pi * width ** 2) ** 1.5
+    vol = abs(np.linalg.det(lattice))
+    rho *= float(np.sum(zvals)) / (rho.sum() * vol / rho.size)
+    return rho
+
+
 def main(ref_root):
     setup(ref_root)
     DirectGrid, DirectField, Ions = ref_objects()
@@ -130,7 +150,7 @@ def main(ref_root):
     latB = np.diag([9.0, 8.0, 10.0])
     posB = np.array([[1.0, 1.0, 1.0], [5.5, 4.0, 6.0]])
     nrB = (16, 18, 20)
-    rhoB = syn.atomic_density(latB, nrB, posB, [3.0, 3.0], width=0.9, floor=0.0)
+    rhoB = edge_density(latB, nrB, posB, [3.0, 3.0], width=0.9)
     rhoB[0, 0, 0] = -1e-5
     rhoB[1, 2, 3] = 0.0
     out["B_lattice"], out["B_nr"], out["B_rho"] = latB, np.array(nrB), rhoB
@@ -221,4 +241,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the reference source tree>" % sys.argv[0])
+    main(sys.argv[1])

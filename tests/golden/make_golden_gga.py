@@ -3,7 +3,7 @@
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden_gga.py /root/reference
+    python tests/golden/make_golden_gga.py <reference source tree>
 
 Cases: every functional of GGA_KEDF_list on the smooth anisotropic density of
 system A (24x20x18; energy, potential and stress), LKT with user parameters
@@ -77,4 +77,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the reference source tree>" % sys.argv[0])
+    main(sys.argv[1])

@@ -5,7 +5,7 @@ reference_io.npz).
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden_io.py /root/reference
+    python tests/golden/make_golden_io.py <reference source tree>
 """
 import os
 import sys
@@ -54,4 +54,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the reference source tree>" % sys.argv[0])
+    main(sys.argv[1])

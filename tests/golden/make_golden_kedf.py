@@ -4,7 +4,7 @@ kedf/kernel.py:267-322) computed by the REFERENCE implementation.
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden_kedf.py /root/reference
+    python tests/golden/make_golden_kedf.py <reference source tree>
 
 Cases:
   fixture  the reference's own Al_fde_rho.pp test density (read from
@@ -62,4 +62,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the reference source tree>" % sys.argv[0])
+    main(sys.argv[1])

@@ -10,7 +10,7 @@ the energy history and the final density.
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden_scf.py /root/reference
+    python tests/golden/make_golden_scf.py <reference source tree>
 """
 import os
 import sys
@@ -116,4 +116,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the reference source tree>" % sys.argv[0])
+    main(sys.argv[1])

@@ -3,7 +3,7 @@ REFERENCE implementation (Quantum-MultiScale/DFTpy) on seeded inputs.
 
 Run in a container that has the reference sources:
 
-    python tests/golden/make_golden_stress.py /root/reference
+    python tests/golden/make_golden_stress.py <reference source tree>
 
 The reference needs ASE, which is not installed here; oracle/ase_shim provides
 the few members it uses.  Tests read only the .npz this script writes.
@@ -120,4 +120,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s <path of the reference source tree>" % sys.argv[0])
+    main(sys.argv[1])

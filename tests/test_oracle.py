@@ -163,3 +163,18 @@ def test_optimizer_c1(golden, method):
         # the TN Hessian products use a 1e-9 finite difference, so iterates carry
         # ~1e-7 relative noise from summation order; the ground state agrees to ~1e-6
         np.testing.assert_allclose(rho, g["C_TN_rho"], rtol=2e-6, atol=0)
+
+
+def test_golden_recipe_reproduces_edge_density(golden):
+    """The committed generator pins the B block's input: its edge_density (plus
+    the two planted values) gives the stored B_rho bit for bit."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    rho = mg.edge_density(golden["B_lattice"], tuple(golden["B_nr"]), np.array([[1.0, 1.0, 1.0], [5.5, 4.0, 6.0]]),
+                          [3.0, 3.0], width=0.9)
+    rho[0, 0, 0] = -1e-5
+    rho[1, 2, 3] = 0.0
+    assert np.array_equal(rho, golden["B_rho"])

@@ -54,8 +54,9 @@ def test_noalloc_matches_handle_dot_twice(dtype):
     torch.cuda.set_device(0)
     gen = torch.Generator(device="cuda").manual_seed(7)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
-    # two calls in a row with different sizes: the second must not see the first's partials
-    for shape in ((37, 41, 43), (64, 64, 64)):
+    # two calls in a row, the larger first: the second uses fewer blocks, so a
+    # stale partial of the first call would change its sum if it were read
+    for shape in ((64, 64, 64), (37, 41, 43)):
         x = torch.randn(shape, dtype=dtype, device="cuda", generator=gen)
         y = torch.randn(shape, dtype=dtype, device="cuda", generator=gen)
         for b in (y, None):
@@ -63,6 +64,23 @@ def test_noalloc_matches_handle_dot_twice(dtype):
             got = _dot_noalloc(x, b, out)
             assert abs(got - ref) <= 1e-12 * max(1.0, float((x.double().abs() * (b.double().abs() if b is not None
                                                                                     else 1.0)).sum())), (got, ref)
+
+
+def test_noalloc_at_size_limit():
+    """n = 67,108,864 (every one of the 4096 static partials in use), float32,
+    against a float64 sum of the same values; then a small call after it."""
+    torch.cuda.set_device(0)
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    n = 67108864
+    x = torch.rand(n, dtype=torch.float32, device="cuda", generator=gen)
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    got = _dot_noalloc(x, None, out)
+    ref = float(x.double().sum().item())
+    assert abs(got - ref) <= 1e-12 * n, (got, ref)
+    y = x[:1000]
+    got2 = _dot_noalloc(y, None, out)
+    assert abs(got2 - float(y.double().sum().item())) <= 1e-12 * 1000
+    del x
 
 
 def test_noalloc_rejects_oversize():

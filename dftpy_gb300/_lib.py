@@ -35,6 +35,7 @@ class OfdftError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [
+        ("struct_size", C.c_uint),
         ("kedf_terms", C.c_int),
         ("tf_x", C.c_double), ("vw_y", C.c_double),
         ("wt_alpha", C.c_double), ("wt_beta", C.c_double), ("wt_x", C.c_double), ("wt_rho0", C.c_double),
@@ -93,6 +94,8 @@ _SIGS = {
     "ofdft_dot": (_I, [_P, _P, _P, _PD, _P]),
     "ofdft_dot3": (_I, [_P, _P, _P, _P, _PD, _P]),
     "ofdft_dot_noalloc": (_I, [_P, _P, C.c_longlong, _I, _P, _P]),
+    "ofdft_config_size": (C.c_size_t, []),
+    "ofdft_config_init": (_I, [C.POINTER(Config), C.c_size_t]),
     "ofdft_config_default": (None, [C.POINTER(Config)]),
     "ofdft_eval_create": (_I, [_P, C.POINTER(Config), C.POINTER(_P)]),
     "ofdft_eval_destroy": (None, [_P]),
@@ -153,6 +156,9 @@ def load(build_if_missing=True):
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.ofdft_config_size() != C.sizeof(Config):
+            raise OfdftError("the ctypes mirror of ofdft_config has %d bytes, the library's %d: update "
+                             "dftpy_gb300/_lib.py from include/ofdft.h" % (C.sizeof(Config), lib.ofdft_config_size()))
         _LIB = lib
         return lib
 

@@ -2081,8 +2081,11 @@ void stress_t(ofdft_eval* e, const T* rho, const double* energies, double* S, cu
 
 extern "C" {
 
+size_t ofdft_config_size(void) { return sizeof(ofdft_config); }
+
 void ofdft_config_default(ofdft_config* c) {
     memset(c, 0, sizeof(*c));
+    c->struct_size = (unsigned)sizeof(ofdft_config);
     c->kedf_terms = OFDFT_KE_TF | OFDFT_KE_VW;
     c->tf_x = 1.0;
     c->vw_y = 1.0;
@@ -2123,9 +2126,25 @@ void ofdft_config_default(ofdft_config* c) {
     c->ewald_energy = 0.0;
 }
 
+int ofdft_config_init(ofdft_config* c, size_t caller_size) {
+    return guard([&] {
+        OFDFT_REQUIRE(c, "ofdft_config_init: null argument");
+        OFDFT_REQUIRE(caller_size == sizeof(ofdft_config),
+                      "ofdft_config_init: the caller's struct has %zu bytes, this library's ofdft_config %zu: "
+                      "rebuild the binding from include/ofdft.h",
+                      caller_size, sizeof(ofdft_config));
+        ofdft_config_default(c);
+    });
+}
+
 int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out) {
     return guard([&] {
-        OFDFT_REQUIRE(g && cfg && out, "ofdft_eval_create: null argument");
+        OFDFT_REQUIRE(cfg && out, "ofdft_eval_create: null argument");
+        OFDFT_REQUIRE(cfg->struct_size == sizeof(ofdft_config),
+                      "ofdft_eval_create: ofdft_config.struct_size = %u, this library's ofdft_config has %zu bytes: "
+                      "fill the config with ofdft_config_init, from a binding that mirrors include/ofdft.h",
+                      cfg->struct_size, sizeof(ofdft_config));
+        OFDFT_REQUIRE(g, "ofdft_eval_create: null grid");
         const ofdft_config& c = *cfg;
         OFDFT_REQUIRE(!((c.kedf_terms & OFDFT_KE_WT) && (c.kedf_terms & OFDFT_KE_LWT)),
                       "only one nonlocal KEDF term at a time");

@@ -156,7 +156,7 @@ class AbstractFunctional(ABC):
 
 def empty_config():
     cfg = _lib.Config()
-    _lib.load().ofdft_config_default(_lib.C.byref(cfg))
+    _lib.check(_lib.load().ofdft_config_init(_lib.C.byref(cfg), _lib.C.sizeof(cfg)))
     cfg.kedf_terms = 0
     cfg.xc_lda = 0
     cfg.hartree = 0

@@ -125,7 +125,12 @@ enum { OFDFT_LWT_KERNEL_WT = 0, OFDFT_LWT_KERNEL_MGP = 1, OFDFT_LWT_KERNEL_MGPA 
  * interpolation, and the gradient terms of dk_F/drho in the potential) */
 enum { OFDFT_LWT_FAMILY_LWT = 0, OFDFT_LWT_FAMILY_HC = 1 };
 
+/* Configuration of one evaluator.  Bindings in other languages must mirror
+ * this struct member for member; struct_size guards against a stale mirror:
+ * ofdft_config_init (or ofdft_config_default) sets it to sizeof(ofdft_config),
+ * and ofdft_eval_create refuses a config whose struct_size differs. */
 typedef struct {
+    unsigned int struct_size; /* sizeof(ofdft_config) of the library: set by ofdft_config_init */
     int    kedf_terms;
     double tf_x;              /* TF prefactor x (kedf/tf.py:66)                    */
     double vw_y;              /* vW prefactor y (kedf/vw.py:115)                   */
@@ -177,6 +182,15 @@ typedef struct {
     int    tf_temp_old;       /* 1: the energy of TemperatureTFEnergy_old (temperature0) */
 } ofdft_config;
 
+/* sizeof(ofdft_config) in this library; a binding compares it with the size of
+ * its own mirror before it passes one in. */
+size_t ofdft_config_size(void);
+/* Defaults of every member (the reference's defaults) and struct_size.
+ * caller_size is the size of the caller's struct: when it differs from
+ * ofdft_config_size() nothing is written and OFDFT_EINVAL is returned, so a
+ * stale binding fails here instead of being written past. */
+int ofdft_config_init(ofdft_config* c, size_t caller_size);
+/* The same without the size check (the caller's struct must be this header's). */
 void ofdft_config_default(ofdft_config* c);
 
 int ofdft_eval_create(ofdft_grid* g, const ofdft_config* cfg, ofdft_eval** out);

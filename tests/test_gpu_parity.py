@@ -24,10 +24,18 @@ def e_close(a, b, scale=1.0):
     assert abs(a - b) <= E_RTOL * max(scale, abs(b)), (a, b, a - b)
 
 
-def v_close(v, ref, atol=V_ATOL):
+def v_close(v, ref, atol=V_ATOL, edge=False):
+    """Potential bar: atol a.u. max-abs.  edge=True (the B block's planted
+    rho = 0 and rho < 0 points, where the reference divides by sqrt(rho) =
+    1e-30 and |V| reaches 1e16, beyond float64's absolute resolution): each
+    point within atol * max(1, |V_ref|), i.e. absolute wherever |V_ref| <= 1."""
     v = v.numpy() if hasattr(v, "numpy") else np.asarray(v)
-    err = float(np.abs(v - ref).max())
-    assert err <= atol * max(1.0, float(np.abs(ref).max())), err
+    d = np.abs(v - ref)
+    if edge:
+        bad = d > atol * np.maximum(1.0, np.abs(ref))
+        assert not bad.any(), (float(d.max()), int(bad.sum()))
+    else:
+        assert float(d.max()) <= atol, float(d.max())
 
 
 def _pp(g):
@@ -53,7 +61,7 @@ def test_local_and_fft_terms(golden, pre):
     for k, f in funcs.items():
         out = f(rho)
         e_close(out.energy, float(golden[pre + "E_" + k]))
-        v_close(out.potential, golden[pre + "V_" + k])
+        v_close(out.potential, golden[pre + "V_" + k], edge=pre == "B_")
 
 
 @pytest.mark.parametrize("tag,kw", [
@@ -69,7 +77,7 @@ def test_density_dependent_kernel(golden, tag, kw):
     grid, rho = _setup(golden, pre)
     out = D.Functional(type="KEDF", name="LWT-NL", **kw)(rho)
     e_close(out.energy, float(golden[pre + "E_" + tag[2:]]))
-    v_close(out.potential, golden[pre + "V_" + tag[2:]])
+    v_close(out.potential, golden[pre + "V_" + tag[2:]], edge=pre == "B_")
 
 
 def test_density_dependent_kernel_batches(golden):

@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-gs", action="store_true", help="skip the ground-state timing")
-    p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused"],
+    p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused", "fused-split"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
     p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2", "relax", "oescf"],
                    help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems; "

@@ -21,10 +21,10 @@ KE_TF, KE_VW, KE_WT, KE_LWT, KE_GGA, KE_DTTF = 1, 2, 4, 8, 16, 32
 (GGA_LKT, GGA_LKTVW, GGA_DK, GGA_LLP, GGA_OL, GGA_THAK, GGA_B86A, GGA_B86B, GGA_DK87, GGA_PW86, GGA_PW91O, GGA_PW91,
  GGA_LG94, GGA_P92, GGA_PBE, GGA_P82, GGA_VJKS00, GGA_VT84F, GGA_TFVW, GGA_STV, GGA_PBE2M, GGA_PG, GGA_GE2, GGA_GE4, GGA_PGSL, GGA_PGSLR) = range(26)
 INTERP_LINEAR, INTERP_HERMITE = 0, 1
-LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED = 0, 1, 2
+LWT_PIPE_AUTO, LWT_PIPE_CUFFT, LWT_PIPE_FUSED, LWT_PIPE_FUSED_SPLIT = 0, 1, 2, 3
 LWT_KERNEL_WT, LWT_KERNEL_MGP, LWT_KERNEL_MGPA, LWT_KERNEL_MGPG, LWT_KERNEL_USER = 0, 1, 2, 3, 4
 LWT_FAMILY_LWT, LWT_FAMILY_HC = 0, 1
-OPT_TN, OPT_LBFGS, OPT_CGHS = 0, 1, 2
+OPT_TN, OPT_LBFGS, OPT_CGHS, OPT_CGPR, OPT_CGDY, OPT_CGCD, OPT_CGLS, OPT_CGFR, OPT_GD, OPT_DIIS = range(10)
 PRED_NONE, PRED_KERKER, PRED_INVERSE_KERKER, PRED_RESTA = 0, 1, 2, 3
 MIX_MAXM = 8
 

@@ -261,6 +261,18 @@ __global__ void k_lincomb(long long n, T* out, double a0, const T* x0, double a1
         out[i] = lin3(b0, x0, b1, x1, b2, x2, i);
 }
 
+// get_direction_CG with CG-CD (math_utils.py:341-342, 347): beta is the field
+// -(r*r)/s, so p = -r + (-(r*r)/s) d point by point
+template <typename T>
+__global__ void k_cg_cd(long long n, T* p, const T* r, const T* d, double s) {
+    const T ss = (T)s;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const T ri = r[i];
+        const T b = -mul_rn(ri, ri) / ss;
+        p[i] = fma_rn(b, d[i], -ri);
+    }
+}
+
 // sqrt(rho), 1e-300 where rho <= 0 (0 in float32, where 1e-300 underflows)
 template <typename T>
 __device__ inline T phi_floor();
@@ -466,6 +478,61 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
     const double eps = sizeof(T) == 8 ? 1.0e-9 : 1.0e-4;
     int converged = 2, it = 0, nfev = 1;
     for (it = 1; it < o.maxiter; ++it) {
+        if (o.method == OFDFT_OPT_DIIS) {
+            // The reference's DIIS (optimization.py:327-333, :429-441, :471-485):
+            // 'Scaling' leaves p = -r as it is; a step phi + 0.1 p renormalised to
+            // the current electron count, evaluated for V only; then a second step
+            // phi + 0.1 p from the new residual, whose renormalisation factor is
+            // rho.N / rho.integral() of the same fresh field, i.e. 1, so it is not
+            // renormalised; that density's E and V end the iteration.
+            op.lincomb(p, -1.0, rsd);
+            op.lincomb(nphi, 1.0, phi, 0.1, p);
+            k_square<T><<<op.eb, 256, 0, st>>>(N, nphi, nrho);
+            OFDFT_LAUNCH_CHECK();
+            double sn = 0.0;
+            ofdft_dot(g, nrho, nullptr, &sn, st);
+            const double norm = Nel / (sn * dV);
+            op.lincomb(nrho, norm, nrho);
+            op.lincomb(nphi, std::sqrt(norm), nphi);
+            op.eval(nrho, nV, OFDFT_CALC_V);
+            op.copy(old_phi, phi);
+            op.copy(phi, nphi);
+            k_square<T><<<op.eb, 256, 0, st>>>(N, phi, rho);
+            OFDFT_LAUNCH_CHECK();
+            ofdft_dot(g, rho, nullptr, &Nel, st);
+            Nel *= dV;
+            mu = op.dot(nV, rho) * dV / Nel;
+            k_resid<T><<<op.eb, 256, 0, st>>>(N, nV, mu, phi, rsd);
+            OFDFT_LAUNCH_CHECK();
+            op.lincomb(p, -1.0, rsd);
+            op.lincomb(phi, 1.0, phi, 0.1, p);
+            k_square<T><<<op.eb, 256, 0, st>>>(N, phi, rho);
+            OFDFT_LAUNCH_CHECK();
+            E = op.eval(rho, V, OFDFT_CALC_E | OFDFT_CALC_V);
+            nfev += 2;
+            ofdft_dot(g, rho, nullptr, &Nel, st);
+            Nel *= dV;
+            mu = op.dot(V, rho) * dV / Nel;
+            k_resid<T><<<op.eb, 256, 0, st>>>(N, V, mu, phi, rsd);
+            OFDFT_LAUNCH_CHECK();
+            Ehist.push_back(E);
+            const double resN = op.dot(rsd, rsd) * dV;
+            res.dP = resN;
+            if (o.verbose)
+                fprintf(stderr, "%-8d%-24.12E%-16.6E%-16.6E%-8d\n", it, E, Ehist[Ehist.size() - 1] - Ehist[Ehist.size() - 2],
+                        resN, 1);
+            bool conv = false;
+            if ((int)Ehist.size() - 1 >= o.ncheck) {
+                conv = true;
+                for (int i = 0; i < o.ncheck; ++i)
+                    if (std::fabs(Ehist[Ehist.size() - 2 - i] - E) > o.econv) conv = false;
+            }
+            if (conv) {
+                converged = 0;
+                break;
+            }
+            continue;
+        }
         // ---- direction
         if (o.method == OFDFT_OPT_TN) {
             // get_direction_TN (optimization.py:92-148)
@@ -539,13 +606,30 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
                 double b = lb[i].rho * op.dot(lb[i].y, p);
                 op.lincomb(p, 1.0, p, al[i] - b, lb[i].s);
             }
+        } else if (o.method == OFDFT_OPT_GD) {
+            // get_direction_GD (math_utils.py:352-354)
+            op.lincomb(p, -1.0, rsd);
         } else {
-            // get_direction_CG, CG-HS (math_utils.py:328-361)
+            // get_direction_CG (math_utils.py:326-349): beta from the last two
+            // residuals and the last direction; -r on the first iteration
             if (have_res_prev && have_dir_prev) {
                 T* dr = op.buf("cg_dr");
                 op.lincomb(dr, 1.0, rsd, -1.0, res_prev);
-                double beta = op.dot(rsd, dr) / op.dot(dir_prev, dr);
-                op.lincomb(p, -1.0, rsd, beta, dir_prev);
+                double beta = 0.0;
+                switch (o.method) {
+                    case OFDFT_OPT_CGHS: beta = op.dot(rsd, dr) / op.dot(dir_prev, dr); break;
+                    case OFDFT_OPT_CGPR: beta = std::max(op.dot(rsd, dr) / op.dot(res_prev, res_prev), 0.0); break;
+                    case OFDFT_OPT_CGDY: beta = op.dot(rsd, rsd) / op.dot(dir_prev, dr); break;
+                    case OFDFT_OPT_CGLS: beta = op.dot(rsd, dr) / op.dot(dir_prev, res_prev); break;
+                    case OFDFT_OPT_CGFR: beta = op.dot(rsd, rsd) / op.dot(res_prev, res_prev); break;
+                    default: break;
+                }
+                if (o.method == OFDFT_OPT_CGCD) {
+                    k_cg_cd<T><<<op.eb, 256, 0, st>>>(N, p, rsd, dir_prev, op.dot(dir_prev, res_prev));
+                    OFDFT_LAUNCH_CHECK();
+                } else {
+                    op.lincomb(p, -1.0, rsd, beta, dir_prev);
+                }
             } else {
                 op.lincomb(p, -1.0, rsd);
             }
@@ -1440,7 +1524,7 @@ int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft
                      ofdft_stream s) {
     return guard([&] {
         OFDFT_REQUIRE(e && rho && o && r, "ofdft_optimize: null argument");
-        OFDFT_REQUIRE(o->method >= 0 && o->method <= 2, "ofdft_optimize: unknown method");
+        OFDFT_REQUIRE(o->method >= OFDFT_OPT_TN && o->method <= OFDFT_OPT_DIIS, "ofdft_optimize: unknown method");
         OFDFT_REQUIRE(o->maxiter >= 1 && o->maxfun >= 1 && o->ncheck >= 1, "ofdft_optimize: bad limits");
         memset(r, 0, sizeof(*r));
         ofdft_grid* g = e_grid(e);

@@ -1145,7 +1145,7 @@ void fz_tables(ofdft_eval* e) {
     if (e->fz_tw) return;
     const ofdft_grid* g = e->g;
     const int n0 = g->nr[0], n1 = g->nr[1], n2 = g->nr[2], H = n2 / 2;
-    std::vector<float2> h((size_t)n0 + n1 + 2 * (size_t)H);
+    std::vector<float2> h((size_t)n0 + n1 + 2 * (size_t)H + kFzQ);
     auto fill = [&](size_t off, int count, int n) {
         for (int k = 0; k < count; ++k) {
             const double a = -2.0 * M_PI * (double)k / (double)n;
@@ -1156,6 +1156,7 @@ void fz_tables(ofdft_eval* e) {
     fill((size_t)n0, n1, n1);
     fill((size_t)n0 + n1, H, H);
     fill((size_t)n0 + n1 + H, H, n2);
+    fill((size_t)n0 + n1 + 2 * (size_t)H, kFzQ, kFzQ);  // the Q-point column transforms of the split path
     OFDFT_CK(cudaMalloc(&e->fz_tw, h.size() * sizeof(float2)));
     upload_now(e->fz_tw, h.data(), h.size() * sizeof(float2));
     OFDFT_CK(cudaMalloc(&e->d_fz_err, sizeof(unsigned)));
@@ -1204,7 +1205,10 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     tw.t1 = e->fz_tw + n0;
     tw.th = e->fz_tw + n0 + n1;
     tw.tr = e->fz_tw + n0 + n1 + H;
+    tw.tq = e->fz_tw + n0 + n1 + 2 * H;
     const FzTab tb = fz_tab(r.tab);
+    // the C2R chain with axis 1 split between its two passes (no axis-1 plane pass)
+    const bool split = e->cfg.lwt_pipeline == OFDFT_LWT_PIPE_FUSED_SPLIT;
     const size_t cb = g->cplx_bytes();
     const bool mc = r.kdd == 3;  // M planes feed pot3 only
     // planes per node: P (and M) for the C2R chain, one more for the R2C chain,
@@ -1244,29 +1248,6 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         // planes); nodes split over blocks when the tile count alone leaves a long
         // last wave
         const int nsplit = (nb >= 16 && tiles0 < 8 * g->sms) ? 2 : 1;
-        with_col(n0, [&](auto c0) {
-            constexpr int N0 = decltype(c0)::value;
-            const size_t smem = fz_col_smem(N0, nb, true);
-            auto launch = [&](auto kern, int plane0) {
-                fz_smem_optin(kern, smem);
-                timed(e, P_LWT_NODES, Ncd * 8.0 * (nsplit + nb), st, [&] {
-                    kern<<<tiles0 * nsplit, kFzLines * (N0 / kFzColE), smem, st>>>(
-                        r.rbG, XY, tb, knode, invk, j0, nb, plane0, tiles0, nsplit, g->geo, d, tw.t0, invN);
-                });
-                OFDFT_LAUNCH_CHECK();
-            };
-            launch(k_fz_nodes<N0, false>, 0);
-            if (mc) launch(k_fz_nodes<N0, true>, nb);
-        });
-        // ---- axis 1
-        with_col(n1, [&](auto c1) {
-            constexpr int N1 = decltype(c1)::value;
-            const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
-            timed(e, P_FZ_AXIS1, Ncd * 16.0 * nplanes, st,
-                  [&] { k_fz_axis1<N1, +1><<<tiles1 * nplanes, N1, smem, st>>>(XY, d, tw.t1); });
-        });
-        OFDFT_LAUNCH_CHECK();
-        // ---- axis 2 C2R with the interpolation into pot1 (pot3)
         FzRowArgs ra;
         ra.kf = r.kf;
         ra.rA = r.rA;
@@ -1283,7 +1264,59 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         ra.d = d;
         ra.tw = tw;
         ra.err = e->d_fz_err;
-        with_row(H, [&](auto ch) {
+        if (split) {
+            // axis 0 + the radix-4 stage of axis 1, then the cluster consumer
+            with_col(n0, [&](auto c0) {
+                constexpr int N0 = decltype(c0)::value;
+                const size_t smem = fz4_gen_smem(N0, nb);
+                auto launch = [&](auto kern, int plane0) {
+                    fz_smem_optin(kern, smem);
+                    timed(e, P_LWT_NODES, Ncd * 8.0 * (nsplit + nb), st, [&] {
+                        kern<<<tiles0 * nsplit, kFzLines * (N0 / kFzColE), smem, st>>>(
+                            r.rbG, XY, tb, knode, invk, j0, nb, plane0, tiles0, nsplit, g->geo, d, tw.t0, tw.t1,
+                            invN);
+                    });
+                    OFDFT_LAUNCH_CHECK();
+                };
+                launch(k_fz_nodes4<N0, false>, 0);
+                if (mc) launch(k_fz_nodes4<N0, true>, nb);
+            });
+            const size_t smem = fz_cl_smem(r.m);
+            const int grid = n0 * 4 * kFzCl;
+            auto launch = [&](auto kern, int plane0, float* pot) {
+                fz_smem_optin(kern, smem);
+                timed(e, P_LWT_INTERP, Ncd * 8.0 * nb + Nd * 4.0 * (1 + (first ? 1 : 2)), st,
+                      [&] { kern<<<grid, kFzRowThreads, smem, st>>>(ra, plane0, pot, tw.tq); });
+                OFDFT_LAUNCH_CHECK();
+            };
+            launch(k_fz_c2r_cl<true>, 0, r.pot1);
+            if (mc) launch(k_fz_c2r_cl<false>, nb, r.pot3);
+            launches += mc ? 4 : 2;
+        }
+        if (!split) with_col(n0, [&](auto c0) {
+            constexpr int N0 = decltype(c0)::value;
+            const size_t smem = fz_col_smem(N0, nb, true);
+            auto launch = [&](auto kern, int plane0) {
+                fz_smem_optin(kern, smem);
+                timed(e, P_LWT_NODES, Ncd * 8.0 * (nsplit + nb), st, [&] {
+                    kern<<<tiles0 * nsplit, kFzLines * (N0 / kFzColE), smem, st>>>(
+                        r.rbG, XY, tb, knode, invk, j0, nb, plane0, tiles0, nsplit, g->geo, d, tw.t0, invN);
+                });
+                OFDFT_LAUNCH_CHECK();
+            };
+            launch(k_fz_nodes<N0, false>, 0);
+            if (mc) launch(k_fz_nodes<N0, true>, nb);
+        });
+        // ---- axis 1
+        if (!split) with_col(n1, [&](auto c1) {
+            constexpr int N1 = decltype(c1)::value;
+            const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
+            timed(e, P_FZ_AXIS1, Ncd * 16.0 * nplanes, st,
+                  [&] { k_fz_axis1<N1, +1><<<tiles1 * nplanes, N1, smem, st>>>(XY, d, tw.t1); });
+        });
+        OFDFT_LAUNCH_CHECK();
+        // ---- axis 2 C2R with the interpolation into pot1 (pot3)
+        if (!split) with_row(H, [&](auto ch) {
             constexpr int HH = decltype(ch)::value;
             constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
             const size_t smem = fz_row_smem(HH, r.m, true);
@@ -1297,7 +1330,7 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
             launch(k_fz_c2r_rows<HH, true>, 0, r.pot1);
             if (mc) launch(k_fz_c2r_rows<HH, false>, nb, r.pot3);
         });
-        launches += mc ? 5 : 3;
+        if (!split) launches += mc ? 5 : 3;
         if (r.kdd > 1) {
             // ---- R2C on the second stream: hat-weighted rho^alpha along axis 2, then axis 1,
             // then axis 0 into pot2(G)
@@ -1589,7 +1622,10 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         bool fused = false;
         if (c.lwt_pipeline != OFDFT_LWT_PIPE_CUFFT) {
             fused = c.lwt_family == OFDFT_LWT_FAMILY_LWT && fz_applies(g, hermite, m);
-            OFDFT_REQUIRE(fused || c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED,
+            OFDFT_REQUIRE(c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT ||
+                              (g->nr[1] == kFzN1 && g->nr[2] == 256),
+                          "FUSED_SPLIT k_F-node pipeline: needs n1 = n2 = 256");
+            OFDFT_REQUIRE(fused || (c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED && c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT),
                           "fused k_F-node pipeline: needs a float32 grid, linear interpolation, at most %d nodes and "
                           "power-of-two axes (32..256, the last 32..512)",
                           kFzMaxNodes);

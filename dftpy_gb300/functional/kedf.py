@@ -295,7 +295,8 @@ class KEDF(NativeFunctional):
         cfg.lwt_ldw = 1.0 / 6.0 if ldw is None else float(ldw)
         cfg.lwt_max_batch = int(o.get("max_batch", 0))
         pipe = str(o.get("pipeline", "auto")).lower()
-        pipes = {"auto": _lib.LWT_PIPE_AUTO, "cufft": _lib.LWT_PIPE_CUFFT, "fused": _lib.LWT_PIPE_FUSED}
+        pipes = {"auto": _lib.LWT_PIPE_AUTO, "cufft": _lib.LWT_PIPE_CUFFT, "fused": _lib.LWT_PIPE_FUSED,
+                 "fused-split": _lib.LWT_PIPE_FUSED_SPLIT}
         if pipe not in pipes:
             raise ValueError("pipeline must be one of %s" % sorted(pipes))
         cfg.lwt_pipeline = pipes[pipe]

@@ -19,7 +19,11 @@ from .functional.total_functional import TotalFunctional
 
 __all__ = ["Optimization", "optimize_rho_batch", "OESCF"]
 
-_METHODS = {"TN": _lib.OPT_TN, "LBFGS": _lib.OPT_LBFGS, "CG-HS": _lib.OPT_CGHS, "CG": _lib.OPT_CGHS}
+# get_direction (optimization.py:179-203): "CG" is CG-HS; any other "CG-*" name falls
+# to get_direction_CG's last branch, Fletcher-Reeves (math_utils.py:345-346)
+_METHODS = {"TN": _lib.OPT_TN, "LBFGS": _lib.OPT_LBFGS, "CG-HS": _lib.OPT_CGHS, "CG": _lib.OPT_CGHS,
+            "CG-PR": _lib.OPT_CGPR, "CG-DY": _lib.OPT_CGDY, "CG-CD": _lib.OPT_CGCD, "CG-LS": _lib.OPT_CGLS,
+            "CG-FR": _lib.OPT_CGFR, "GD": _lib.OPT_GD, "DIIS": _lib.OPT_DIIS}
 
 
 class Optimization:
@@ -34,9 +38,9 @@ class Optimization:
         if EnergyEvaluator is None:
             raise AttributeError("Must provide an energy evaluator")
         self.EnergyEvaluator = EnergyEvaluator
-        if optimization_method not in _METHODS:
-            raise NotImplementedError("optimisation method %r is not on the accelerated path (have %s)"
-                                      % (optimization_method, sorted(_METHODS)))
+        # unknown names fail where the reference's get_direction does, in optimize_rho
+        self._method_code = _METHODS.get(optimization_method,
+                                         _lib.OPT_CGFR if str(optimization_method).startswith("CG") else None)
         o = self.optimization_options
         if o["algorithm"] != "EMM" or o["vector"] != "Orthogonalization":
             raise NotImplementedError("only algorithm='EMM' with vector='Orthogonalization' is supported")
@@ -62,7 +66,9 @@ class Optimization:
         o = self.optimization_options
         s = _lib.OptOptions()
         _lib.load().ofdft_opt_default(_lib.C.byref(s))
-        s.method = _METHODS[self.optimization_method]
+        if self._method_code is None:
+            raise AttributeError("The %s direction method not implemented." % self.optimization_method)
+        s.method = self._method_code
         s.maxiter, s.maxfun, s.maxls = int(o["maxiter"]), int(o["maxfun"]), int(o["maxls"])
         s.ncheck, s.maxcor = int(o["ncheck"]), int(o["maxcor"])
         s.econv = float(o["econv"]) if o["econv"] is not None else 0.0

@@ -113,8 +113,11 @@ enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
  * up to 512) and CUFFT otherwise; FUSED fails with OFDFT_EINVAL where it does
  * not apply.  FUSED folds the node kernel, the interpolation and the pot2 sum
  * into the library's own tile FFTs; CUFFT runs them as separate passes around
- * batched cuFFT transforms.  Both compute the same quantities. */
-enum { OFDFT_LWT_PIPE_AUTO = 0, OFDFT_LWT_PIPE_CUFFT = 1, OFDFT_LWT_PIPE_FUSED = 2 };
+ * batched cuFFT transforms.  Both compute the same quantities.  FUSED_SPLIT
+ * (grids with n1 = n2 = 256 only) is FUSED with the axis-1 transform of the C2R
+ * chain split between its axis-0 pass and a four-block cluster row pass, so that
+ * chain has no axis-1 plane pass. */
+enum { OFDFT_LWT_PIPE_AUTO = 0, OFDFT_LWT_PIPE_CUFFT = 1, OFDFT_LWT_PIPE_FUSED = 2, OFDFT_LWT_PIPE_FUSED_SPLIT = 3 };
 /* kernel table of the k_F-node kernel (lwt.py:535-548): the WT table
  * (kernel.py:344-352, LWT) or the MGP table (kernel.py:267-322; LMGP, and with
  * the arithmetic / geometric symmetrisation LMGPA / LMGPG, lwt.py:571-578) */
@@ -337,7 +340,14 @@ int ofdft_ewald_stress(ofdft_grid* g, int nat, const double* pos, const double* 
  * phi cos(theta) + p sin(theta), directions TN / LBFGS / CG-HS, and the
  * MINPACK-2 (More-Thuente) line search of scipy's line_search_wolfe1
  * (math_utils.py:37-52).  rho is overwritten with the optimised density. */
-enum { OFDFT_OPT_TN = 0, OFDFT_OPT_LBFGS = 1, OFDFT_OPT_CGHS = 2 };
+/* direction methods of Optimization.get_direction (optimization.py:179-203):
+ * TN, L-BFGS, the conjugate-gradient betas of get_direction_CG
+ * (math_utils.py:326-349: HS, PR with max(beta, 0), DY, CD, LS, FR; CD's beta is the
+ * reference's pointwise field -(r*r)/sum(d r_prev)), GD (steepest descent with the
+ * line search) and DIIS (the reference's damped fixed point: two steps of 0.1 per
+ * iteration, optimization.py:327-333, :429-441, :471-485) */
+enum { OFDFT_OPT_TN = 0, OFDFT_OPT_LBFGS = 1, OFDFT_OPT_CGHS = 2, OFDFT_OPT_CGPR = 3, OFDFT_OPT_CGDY = 4,
+       OFDFT_OPT_CGCD = 5, OFDFT_OPT_CGLS = 6, OFDFT_OPT_CGFR = 7, OFDFT_OPT_GD = 8, OFDFT_OPT_DIIS = 9 };
 typedef struct {
     int method, maxiter, maxfun, maxls, ncheck, maxcor;
     double econv, c1, c2, xtol, h0;

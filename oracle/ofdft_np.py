@@ -1760,7 +1760,8 @@ def optimize(evaluator, rho0, grid, method="TN", maxiter=100, maxfun=50, maxls=3
              c1=1e-4, c2=0.2, xtol=1e-12, ncheck=2, maxcor=6, h0=1.0, trace=None):
     """Optimization.optimize_rho (optimization/optimization.py:283-525) for one spin,
     algorithm EMM, vector 'Orthogonalization', line search = scipy line_search_wolfe1
-    started at theta=1 (math_utils.py:37-52: alpha0 is not forwarded).
+    started at theta=1 (math_utils.py:37-52: alpha0 is not forwarded); DIIS runs the
+    reference's damped fixed point instead (no line search, _diis_iteration).
     ``evaluator(rho, calc)`` returns {'E','V'}.  Returns (rho, info)."""
     from scipy.optimize._linesearch import line_search_wolfe1
     dV = grid.dV
@@ -1778,6 +1779,19 @@ def optimize(evaluator, rho0, grid, method="TN", maxiter=100, maxfun=50, maxls=3
     converged = 2
     nfev = 1
     for it in range(1, maxiter):
+        if method == "DIIS":
+            phi, rho, f, N, mu, res = _diis_iteration(evaluator, phi, resA[-1], N, dV)
+            nfev += 2
+            resA.append(res)
+            Ehist.append(f["E"])
+            if trace is not None:
+                trace.append((it, f["E"], (res * res).sum() * dV))
+            if _check_conv(Ehist, econv, ncheck):
+                converged = 0
+                break
+            if len(resA) > 2:
+                resA.pop(0)
+            continue
         if method == "TN":
             p, nd = _tn_direction(evaluator, resA[-1], phi, mu, maxfun)
             nfev += nd
@@ -1937,7 +1951,11 @@ def _lbfgs_direction(resA, lb, h0):
 
 
 def _cg_direction(resA, dirA, method="CG-HS"):
-    """get_direction_CG (math_utils.py:328-361)."""
+    """get_direction_CG (math_utils.py:326-349) and get_direction_GD (:352-354).
+    CG-CD's beta is a field, -(r*r)/sum(d r_prev), as in the reference; any other
+    CG name falls to the last branch (Fletcher-Reeves)."""
+    if method == "GD":
+        return -resA[-1]
     if len(resA) == 1:
         beta = 0.0
     elif method in ("CG-HS", "CG") and len(dirA) > 0:
@@ -1947,11 +1965,41 @@ def _cg_direction(resA, dirA, method="CG-HS"):
         beta = max((resA[-1] * (resA[-1] - resA[-2])).sum() / (resA[-2] ** 2).sum(), 0.0)
     elif method == "CG-DY" and len(dirA) > 0:
         beta = (resA[-1] ** 2).sum() / (dirA[-1] * (resA[-1] - resA[-2])).sum()
+    elif method == "CG-CD" and len(dirA) > 0:
+        beta = -(resA[-1] ** 2) / (dirA[-1] * resA[-2]).sum()
+    elif method == "CG-LS" and len(dirA) > 0:
+        beta = (resA[-1] * (resA[-1] - resA[-2])).sum() / (dirA[-1] * resA[-2]).sum()
     else:
         beta = (resA[-1] ** 2).sum() / (resA[-2] ** 2).sum()
     if not dirA:
         return -resA[-1]
     return -resA[-1] + beta * dirA[-1]
+
+
+def _diis_iteration(evaluator, phi, res, Ncur, dV):
+    """One iteration of the reference's DIIS (optimization.py:327-333, :429-441,
+    :471-485): p = -r left unscaled ('Scaling'); phi + 0.1 p renormalised to the
+    current electron count and evaluated for V only; then phi + 0.1 p from the new
+    residual, whose factor rho.N / rho.integral() is 1 (both the integral of the
+    same fresh field), evaluated for E and V.  Returns (phi, rho, f, N, mu, res)."""
+    nphi = phi + 0.1 * (-res)
+    nrho = nphi * nphi
+    norm = Ncur / (nrho.sum() * dV)
+    nrho = nrho * norm
+    nphi = nphi * np.sqrt(norm)
+    fv = evaluator(nrho, ("V",))
+    phi = nphi
+    rho = phi * phi
+    N = rho.sum() * dV
+    mu = (fv["V"] * rho).sum() * dV / N
+    res = (fv["V"] - mu) * phi
+    phi = phi + 0.1 * (-res)
+    rho = phi * phi
+    f = evaluator(rho, ("E", "V"))
+    N = rho.sum() * dV
+    mu = (f["V"] * rho).sum() * dV / N
+    res = (f["V"] - mu) * phi
+    return phi, rho, f, N, mu, res
 
 
 # --------------------------------------------------------------------------

@@ -8,7 +8,10 @@ relative; potential within 1e-5 of max|V| (float32 grids and transforms).
 The cases cover every tile-FFT length the fused path instantiates (columns
 32..256, rows 16..256), kdd 1, 2 and 3, node batches that accumulate into
 pot1/pot3/pot2 over several passes, and user k_F bounds that put points in the
-small-k_F branch of the first node and clip the largest k_F.
+small-k_F branch of the first node and clip the largest k_F; on n1 = n2 = 256
+grids the split variant (the axis-1 transform of the C2R chain split between
+the axis-0 pass and a cluster row pass), which must also agree with the
+three-pass pipeline.
 """
 import numpy as np
 import pytest
@@ -34,6 +37,11 @@ CASES = [
     ((128, 128, 128), 64, 3, {}),
     ((64, 64, 64), 32, 3, {"max_batch": 7}),
     ((64, 64, 64), 24, 3, {"kfmin": "lift", "kfmax": "cut"}),
+    # n1 = n2 = 256: the C2R chain with axis 1 split between its two passes
+    ((32, 256, 256), 16, 3, {}),
+    ((64, 256, 256), 24, 3, {"max_batch": 7}),
+    ((32, 256, 256), 12, 2, {"kfmin": "lift", "kfmax": "cut"}),
+    ((32, 256, 256), 8, 1, {}),
 ]
 
 
@@ -62,7 +70,7 @@ def test_fused_f32_against_f64(nr, nsp, kdd, extra):
         # a tenth of the points are clipped to the last node
         opts["kfmax"] = float(np.quantile(kf, 0.9))
     e64, v64 = _run(grid, rho, torch.float64, "cufft", nsp, kdd, opts)
-    e32, v32 = _run(grid, rho, torch.float32, "fused", nsp, kdd, opts)
+    e32, v32 = _run(grid, rho, torch.float32, "fused-split" if nr[1:] == (256, 256) else "fused", nsp, kdd, opts)
     ec, vc = _run(grid, rho, torch.float32, "cufft", nsp, kdd, opts)
     vmax = float(np.abs(v64).max())
     assert abs(e32 - e64) <= E_RTOL * abs(e64), (e32, e64)
@@ -80,3 +88,20 @@ def test_fused_repeatable_bitwise():
     b = _run(grid, rho, torch.float32, "fused", 32, 3, {})
     assert a[0] == b[0]
     assert np.array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("nr,nsp,kdd", [((32, 256, 256), 16, 3), ((64, 256, 256), 64, 3)])
+def test_split_axis1_matches_three_passes(nr, nsp, kdd):
+    """The split C2R chain (radix-4 stage in the axis-0 pass, Q-point transforms
+    in a 4-block cluster) and the three-pass chain compute the same float32
+    transforms in a different order: same energy and potential to float32
+    round-off, and the split path is bitwise repeatable."""
+    lat, rho = _density(nr, seed=7)
+    grid = D.DirectGrid(lat, nr)
+    e3, v3 = _run(grid, rho, torch.float32, "fused", nsp, kdd, {})
+    es, vs = _run(grid, rho, torch.float32, "fused-split", nsp, kdd, {})
+    es2, vs2 = _run(grid, rho, torch.float32, "fused-split", nsp, kdd, {})
+    vmax = float(np.abs(v3).max())
+    assert abs(es - e3) <= 2e-7 * abs(e3), (es, e3)
+    assert float(np.abs(vs - v3).max()) <= 2e-6 * vmax
+    assert es == es2 and np.array_equal(vs, vs2)

@@ -1,0 +1,78 @@
+"""The native optimiser's remaining direction methods against the reference's
+own runs (tests/golden/reference_opt.npz, from tests/golden/make_golden_opt.py):
+CG-PR, CG-DY, CG-CD (the reference's pointwise beta), CG-LS, CG-FR, GD and the
+reference's DIIS, FP64, on the 4-atom Al cell at 32^3 (TF + vW + LDA + Hartree +
+PME local PP) from the uniform density.
+
+Each method runs the reference's iteration budget: 10 iterations and 59 (DIIS:
+4, after which the reference diverges on this system).  Same convergence flag and
+iteration count; the electron count within 1e-12 relative; the energy within
+1e-10 relative (per-atom scale) at a converged ground state, 1e-9 along an
+unconverged path after 10 iterations and 1e-7 after 59 (the path amplifies
+each step's summation-order rounding); mu within 1e-8 and 1e-6 likewise.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+import dftpy_gb300 as D
+from dftpy_gb300 import synthetic as syn
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "reference_opt.npz")
+METHODS = ("CG-PR", "CG-DY", "CG-CD", "CG-LS", "CG-FR", "GD", "DIIS")
+
+
+@pytest.fixture(scope="module")
+def go():
+    return dict(np.load(GOLD))
+
+
+def _c1(golden):
+    lat, pos = syn.fcc_cell(7.60)
+    grid = D.DirectGrid(lat, (32, 32, 32))
+    ions = D.Ions(symbols=["Al"] * 4, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(
+        r=golden["recpot_gp"], v=golden["recpot_vp"], zval=int(golden["recpot_zval"]))}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="TFVW"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    return grid, tot, D.DirectField(grid) + 12.0 / grid.volume
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("run", ["short", "long"])
+def test_direction_method_matches_reference(golden, go, method, run):
+    key = "%s_%s_" % (method.replace("-", ""), run)
+    if key + "E" not in go:
+        pytest.skip("the reference diverges beyond 4 DIIS iterations on this system")
+    torch.cuda.set_device(0)
+    grid, tot, rho0 = _c1(golden)
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method,
+                         optimization_options={"econv": 1e-11 * 4, "maxiter": int(go[key + "maxiter"]),
+                                               "maxfun": 50})
+    rho = opt.optimize_rho(guess_rho=rho0)
+    conv = int(go[key + "converged"])
+    assert opt.converged == conv
+    assert opt.result.niter == int(go[key + "niter"])
+    E = tot.Energy(rho)
+    Eref = float(go[key + "E"])
+    if conv == 0:
+        e_bar, mu_bar = 1e-10 * max(4.0, abs(Eref)), 1e-8
+    elif run == "short":
+        e_bar, mu_bar = 1e-9 * abs(Eref), 1e-8
+    else:
+        e_bar, mu_bar = 1e-7 * abs(Eref), 1e-6
+    assert abs(E - Eref) <= e_bar, (E, Eref, E - Eref)
+    assert abs(opt.mu - float(go[key + "mu"])) <= mu_bar * abs(float(go[key + "mu"])), (opt.mu, go[key + "mu"])
+    assert abs(float(rho.integral()) - float(go[key + "N"])) <= 1e-12 * 12.0
+
+
+def test_unknown_method_fails_at_optimisation(golden):
+    grid, tot, rho0 = _c1(golden)
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method="NEWTON")
+    with pytest.raises(AttributeError):
+        opt.optimize_rho(guess_rho=rho0)

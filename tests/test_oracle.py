@@ -178,3 +178,36 @@ def test_golden_recipe_reproduces_edge_density(golden):
     rho[0, 0, 0] = -1e-5
     rho[1, 2, 3] = 0.0
     assert np.array_equal(rho, golden["B_rho"])
+
+
+OPT_METHODS = ("CG-PR", "CG-DY", "CG-CD", "CG-LS", "CG-FR", "GD", "DIIS")
+
+
+@pytest.fixture(scope="module")
+def golden_opt():
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_opt.npz")))
+
+
+@pytest.mark.parametrize("method", OPT_METHODS)
+def test_optimizer_methods_short(golden, golden_opt, method):
+    """The oracle's CG betas, GD and DIIS against the reference's own runs
+    (tests/golden/make_golden_opt.py): 10 iterations (DIIS: 4) from the uniform
+    density on the 4-atom Al cell at 32^3."""
+    g, go = golden, golden_opt
+    from dftpy_gb300.synthetic import fcc_cell
+    lat, pos = fcc_cell(7.60)
+    grid = O.Grid(lat, (32, 32, 32))
+    pp = O.LocalPseudo(grid, pos, np.zeros(4, dtype=int), [(g["recpot_gp"], g["recpot_vp"])], PME=True)
+    ew = O.Ewald(grid, pos, np.full(4, 3.0), PME=True)
+    tot = O.Total(grid, O.make_terms(grid, "TFVW", pseudo=pp), ewald_energy=ew.energy())
+    rho0 = np.full((32, 32, 32), 12.0 / grid.volume)
+    key = method.replace("-", "") + "_short_"
+    rho, info = O.optimize(tot, rho0, grid, method=method, maxiter=int(go[key + "maxiter"]), maxfun=50,
+                           econv=1e-11 * 4)
+    assert info["converged"] == int(go[key + "converged"])
+    assert info["niter"] == int(go[key + "niter"])
+    # an unconverged 10-step path amplifies the summation-order rounding of each
+    # step (numpy's sum here, einsum in the reference) to ~1e-10: 1e-9 relative
+    _close(tot(rho, ("E",))["E"], go[key + "E"], rtol=1e-9, atol=0)
+    _close(info["mu"], go[key + "mu"], rtol=1e-8, atol=0)
+    _close(rho.sum() * grid.dV, go[key + "N"], rtol=1e-12, atol=0)

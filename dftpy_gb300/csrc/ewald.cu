@@ -346,9 +346,8 @@ void ewald_t(ofdft_grid* g, int nat, const double* pos, const double* charges, d
         T* Q = (T*)sc.get("Q", rb);
         C* QG = (C*)sc.get("QG", cb);
         C* X = forces ? (C*)sc.get("X", cb) : nullptr;
-        OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
-        k_pme_spread<T><<<nat, 256, 0, st>>>(d_frac, d_q, nullptr, order, g->geo, Q);
-        OFDFT_LAUNCH_CHECK();
+        const PmeTiles tiles = pme_tiles_build(sc, "pme_", frac.data(), nullptr, nat, order, g->nr, st);
+        pme_spread<T>(tiles, d_frac, nullptr, d_q, g->geo, Q, rb, st);
         g->exec_r2c(Q, QG, 1, st);
         k_ewald_rec_pme<T><<<g->red_blocks, RED_THREADS, 0, st>>>(QG, X, bre, bim, g->geo, eta, g->d_partials);
         OFDFT_LAUNCH_CHECK();

@@ -716,7 +716,8 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
     if (v_out) OFDFT_CK(cudaMemcpyAsync(v_out, V, g->real_bytes(), cudaMemcpyDeviceToDevice, st));
     OFDFT_CK(cudaStreamSynchronize(st));
     res.converged = converged;
-    res.niter = it;
+    // iterations run, as the reference counts them: maxiter - 1 when the budget ran out
+    res.niter = std::min(it, o.maxiter - 1);
     res.nfev = nfev;
     res.energy = E;
     res.mu = mu;
@@ -1461,7 +1462,7 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         }
     }
     for (int s = 0; s < S; ++s)
-        if (run[s]) niter[s] = o.maxiter;  // the loop ran out of iterations (conv stays 2)
+        if (run[s]) niter[s] = o.maxiter - 1;  // the loop ran out of iterations (conv stays 2), counted as the reference does
     if (o.verbose)
         fprintf(stderr, "batch of %d: %.3f s, %lld evaluations (%.3f s enqueueing), %lld synchronisations (%.3f s "
                 "waiting)\n", S,

@@ -1,8 +1,15 @@
 // Smooth-PME building blocks shared by the local pseudopotential and Ewald:
-// cardinal B-spline charge spreading and the gradient gather for forces
-// (src/dftpy/ewald.py:63-82, :137-194, :810-864; pseudo/__init__.py:523-571).
+// cardinal B-spline charge spreading, Q[l0(i), l1(j), l2(k)] += w_a M(i) M(j) M(k)
+// with l_d(i) = (1 + floor(u_d) - i) mod n_d, u = frac * n (ewald.py:172-194),
+// and the gradient gather for forces (src/dftpy/ewald.py:63-82, :137-194,
+// :810-864; pseudo/__init__.py:523-571).
 #pragma once
 #include "common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
 
 namespace ofdft {
 
@@ -27,34 +34,135 @@ __device__ inline int pmod(long long a, int n) {
     return (int)(r < 0 ? r + n : r);
 }
 
-// One block per atom: Q[l0(i), l1(j), l2(k)] += w_a M(i) M(j) M(k) with
-// l_d(i) = (1 + floor(u_d) - i) mod n_d, u = frac * n (ewald.py:172-194).
-// frac: natoms x 3 fractional coordinates in [0, 1).
-template <typename T>
-__global__ void k_pme_spread(const double* __restrict__ frac, const double* __restrict__ w, const int* __restrict__ sel,
-                             int order, Geo geo, T* Q) {
-    __shared__ double M[3][kMaxOrder + 1];
-    __shared__ int base[3];
-    const int a = sel ? sel[blockIdx.x] : blockIdx.x;
-    if (threadIdx.x < 3) {
-        const int d = threadIdx.x;
+// ---------------------------------------------------------------------------
+// Deterministic spreading.  The grid is cut into 8^3 tiles; the host lists, for
+// every tile that some atom's order^3 stencil touches, the atoms (positions in
+// the spread list) that touch it, in list order.  One block per touched tile,
+// one thread per grid point: the thread sums the contributions of its tile's
+// atoms in that order in float64 and stores the point once.  The sum at every
+// point therefore has a fixed order and Q is the same bits on every run (a
+// per-atom scatter with global atomics sums in arrival order).
+constexpr int kPmeTile = 8;
+
+struct PmeTiles {
+    int ntiles = 0, nlist = 0, order = 0;
+    int* tile = nullptr;   // tile ids (t0 T1 + t1) T2 + t2
+    int* start = nullptr;  // ntiles + 1 offsets into atom
+    int* atom = nullptr;   // list positions
+    int* base = nullptr;   // 3 per list position: floor(u_d)
+    double* M = nullptr;   // 3 (order + 1) per list position: M_order(x + n - 1), n = 0..order
+};
+
+// Builds the tile lists on the host and uploads them into buffers of sc named
+// prefix + "...".  frac: 3 per atom of the whole set (host); list: the atoms to
+// spread (host, nullptr = 0..nlist-1).  The stencil base floor(frac n) is the
+// same IEEE product and floor the device computes.
+inline PmeTiles pme_tiles_build(Scratch& sc, const std::string& prefix, const double* frac, const int* list,
+                                int nlist, int order, const int nr[3], cudaStream_t st) {
+    PmeTiles t;
+    t.nlist = nlist;
+    t.order = order;
+    if (nlist <= 0) return t;
+    int nt[3];
+    for (int d = 0; d < 3; ++d) nt[d] = (nr[d] + kPmeTile - 1) / kPmeTile;
+    std::vector<long long> key;
+    key.reserve((size_t)nlist * 27);
+    for (int q = 0; q < nlist; ++q) {
+        const int a = list ? list[q] : q;
+        std::vector<int> tl[3];
+        for (int d = 0; d < 3; ++d) {
+            const long long b = (long long)std::floor(frac[3 * (size_t)a + d] * (double)nr[d]);
+            for (int i = 0; i < order; ++i) {
+                long long l = (1 + b - i) % nr[d];
+                if (l < 0) l += nr[d];
+                const int tt = (int)(l / kPmeTile);
+                if (std::find(tl[d].begin(), tl[d].end(), tt) == tl[d].end()) tl[d].push_back(tt);
+            }
+        }
+        for (int x : tl[0])
+            for (int y : tl[1])
+                for (int z : tl[2]) key.push_back((((long long)x * nt[1] + y) * nt[2] + z) * nlist + q);
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int> tile, start, atom(key.size());
+    for (size_t p = 0; p < key.size(); ++p) {
+        const int tid = (int)(key[p] / nlist);
+        atom[p] = (int)(key[p] % nlist);
+        if (tile.empty() || tile.back() != tid) {
+            tile.push_back(tid);
+            start.push_back((int)p);
+        }
+    }
+    start.push_back((int)key.size());
+    t.ntiles = (int)tile.size();
+    t.tile = (int*)sc.get(prefix + "tile", tile.size() * sizeof(int));
+    t.start = (int*)sc.get(prefix + "start", start.size() * sizeof(int));
+    t.atom = (int*)sc.get(prefix + "atom", atom.size() * sizeof(int));
+    t.base = (int*)sc.get(prefix + "base", 3 * (size_t)nlist * sizeof(int));
+    t.M = (double*)sc.get(prefix + "M", 3 * (size_t)(order + 1) * nlist * sizeof(double));
+    OFDFT_CK(cudaMemcpyAsync(t.tile, tile.data(), tile.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    OFDFT_CK(cudaMemcpyAsync(t.start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    OFDFT_CK(cudaMemcpyAsync(t.atom, atom.data(), atom.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    // the host vectors die with this call: let the copies finish first
+    OFDFT_CK(cudaStreamSynchronize(st));
+    return t;
+}
+
+// stencil base and B-spline weights of every list position (one thread each)
+static __global__ void k_pme_prep(const double* __restrict__ frac, const int* __restrict__ list, int nlist, int order,
+                                  Geo geo, int* base, double* M) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nlist) return;
+    const int a = list ? list[q] : q;
+    for (int d = 0; d < 3; ++d) {
         const int n = d == 0 ? geo.n0 : (d == 1 ? geo.n1 : geo.n2);
-        double up = frac[3 * a + d] * (double)n;
-        double fl = floor(up);
-        bspline_mn_dev(up - fl, order, M[d]);
-        base[d] = (int)fl;
+        const double up = frac[3 * a + d] * (double)n;
+        const double fl = floor(up);
+        bspline_mn_dev(up - fl, order, M + (3 * (size_t)q + d) * (order + 1));
+        base[3 * q + d] = (int)fl;
     }
-    __syncthreads();
-    const double wa = w ? w[a] : 1.0;
-    const int o3 = order * order * order;
-    for (int t = threadIdx.x; t < o3; t += blockDim.x) {
-        int i = t / (order * order), j = (t / order) % order, k = t % order;
-        int l0 = pmod(1LL + base[0] - i, geo.n0);
-        int l1 = pmod(1LL + base[1] - j, geo.n1);
-        int l2 = pmod(1LL + base[2] - k, geo.n2);
-        double v = wa * M[0][i + 1] * M[1][j + 1] * M[2][k + 1];
-        atomicAdd(&Q[((long long)l0 * geo.n1 + l1) * geo.n2 + l2], (T)v);
+}
+
+// Q at every point of a touched tile: sum over the tile's atoms, in list order,
+// of w_a M0(i) M1(j) M2(k) with i = (1 + base_0 - l0) mod n0 (< order), etc.
+template <typename T>
+__global__ void __launch_bounds__(kPmeTile* kPmeTile* kPmeTile)
+    k_pme_tiles(PmeTiles t, const double* __restrict__ w, const int* __restrict__ list, Geo geo, T* Q) {
+    const int tid = t.tile[blockIdx.x];
+    const int T1 = (geo.n1 + kPmeTile - 1) / kPmeTile, T2 = (geo.n2 + kPmeTile - 1) / kPmeTile;
+    const int l0 = (tid / (T1 * T2)) * kPmeTile + (threadIdx.x >> 6);
+    const int l1 = ((tid / T2) % T1) * kPmeTile + ((threadIdx.x >> 3) & 7);
+    const int l2 = (tid % T2) * kPmeTile + (threadIdx.x & 7);
+    if (l0 >= geo.n0 || l1 >= geo.n1 || l2 >= geo.n2) return;
+    const int order = t.order, o1 = order + 1;
+    double v = 0.0;
+    for (int p = t.start[blockIdx.x]; p < t.start[blockIdx.x + 1]; ++p) {
+        const int q = t.atom[p];
+        const int* b = t.base + 3 * q;
+        const double* M0 = t.M + (3 * (size_t)q) * o1;
+        const double* M1 = M0 + o1;
+        const double* M2 = M1 + o1;
+        const double wa = w ? w[list ? list[q] : q] : 1.0;
+        // n >= order in practice; the loops also cover a stencil that wraps onto itself
+        for (int i = pmod(1LL + b[0] - l0, geo.n0); i < order; i += geo.n0)
+            for (int j = pmod(1LL + b[1] - l1, geo.n1); j < order; j += geo.n1)
+                for (int k = pmod(1LL + b[2] - l2, geo.n2); k < order; k += geo.n2)
+                    v += wa * M0[i + 1] * M1[j + 1] * M2[k + 1];
     }
+    Q[((long long)l0 * geo.n1 + l1) * geo.n2 + l2] = (T)v;
+}
+
+// Q = the spread of the list (Q zeroed here); t from pme_tiles_build with the
+// same list and order.  d_frac, d_list, d_w on the device (d_list, d_w may be null).
+template <typename T>
+void pme_spread(const PmeTiles& t, const double* d_frac, const int* d_list, const double* d_w, const Geo& geo, T* Q,
+                size_t qbytes, cudaStream_t st) {
+    OFDFT_CK(cudaMemsetAsync(Q, 0, qbytes, st));
+    if (t.nlist <= 0 || t.ntiles <= 0) return;
+    k_pme_prep<<<(t.nlist + 127) / 128, 128, 0, st>>>(d_frac, d_list, t.nlist, t.order, geo, t.base, t.M);
+    OFDFT_LAUNCH_CHECK();
+    k_pme_tiles<T><<<t.ntiles, kPmeTile * kPmeTile * kPmeTile, 0, st>>>(t, d_w, d_list, geo, Q);
+    OFDFT_LAUNCH_CHECK();
 }
 
 // One block per atom: g_a = sum_{ijk} (dQ/du . cinv) * field[l(ijk)], the PME

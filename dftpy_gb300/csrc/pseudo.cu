@@ -328,6 +328,7 @@ struct ofdft_pseudo {
     double* d_bim = nullptr;
     double* d_cinv = nullptr;     // inv(lattice), row-major
     double* d_scale = nullptr;    // per-atom gather scale
+    std::vector<ofdft::PmeTiles> tiles;  // deterministic spreading work list per species (PME)
     Scratch sc;
 
     Line line(int s) const {
@@ -423,11 +424,8 @@ void vloc_t(ofdft_pseudo* p, T* out, cudaStream_t st) {
         bool first = true;
         for (int s = 0; s < p->ns; ++s) {
             const int n_s = p->sel_off[s + 1] - p->sel_off[s];
-            OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
-            if (n_s > 0) {
-                k_pme_spread<T><<<n_s, 256, 0, st>>>(p->d_frac, nullptr, p->d_sel + p->sel_off[s], p->order, g->geo, Q);
-                OFDFT_LAUNCH_CHECK();
-            }
+            if (n_s > 0) pme_spread<T>(p->tiles[s], p->d_frac, p->d_sel + p->sel_off[s], nullptr, g->geo, Q, rb, st);
+            else OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
             g->exec_r2c(Q, QG, 1, st);
             k_pp_accum_pme<T><<<gblk, 256, 0, st>>>(QG, vG, p->line(s), p->d_bre, p->d_bim, first, g->geo, scale);
             OFDFT_LAUNCH_CHECK();
@@ -516,9 +514,7 @@ void stress_t(ofdft_pseudo* p, const T* rho, double energy, double* S, cudaStrea
         for (int s = 0; s < p->ns; ++s) {
             const int n_s = p->sel_off[s + 1] - p->sel_off[s];
             if (n_s == 0) continue;
-            OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
-            k_pme_spread<T><<<n_s, 256, 0, st>>>(p->d_frac, nullptr, p->d_sel + p->sel_off[s], p->order, g->geo, Q);
-            OFDFT_LAUNCH_CHECK();
+            pme_spread<T>(p->tiles[s], p->d_frac, p->d_sel + p->sel_off[s], nullptr, g->geo, Q, rb, st);
             g->exec_r2c(Q, QG, 1, st);
             k_pp_stress_pme<T><<<g->red_blocks, RED_THREADS, 0, st>>>(rhoG, QG, p->line(s), p->d_bre, p->d_bim,
                                                                       g->geo, g->d_partials);
@@ -559,9 +555,7 @@ void vloc_grad_t(ofdft_pseudo* p, const T* rho, double* grad, cudaStream_t st) {
         if (n_s > 0) {
             if (p->pme) {
                 T* Q = (T*)p->sc.get("Q", rb);
-                OFDFT_CK(cudaMemsetAsync(Q, 0, rb, st));
-                k_pme_spread<T><<<n_s, 256, 0, st>>>(p->d_frac, nullptr, p->d_sel + p->sel_off[s], p->order, g->geo, Q);
-                OFDFT_LAUNCH_CHECK();
+                pme_spread<T>(p->tiles[s], p->d_frac, p->d_sel + p->sel_off[s], nullptr, g->geo, Q, rb, st);
                 g->exec_r2c(Q, SG, 1, st);
                 k_pp_grad_moments<T><<<gblk, 256, 0, st>>>(rhoG, SG, p->d_bre, p->d_bim, p->line(s), g->geo, scale,
                                                            mom, mom + 4 * (size_t)nint);
@@ -707,6 +701,14 @@ int ofdft_pseudo_set_ions(ofdft_pseudo* p, int nat, const double* pos, const int
         upload_now(p->d_spec, species, (size_t)nat * sizeof(int));
         upload_now(p->d_sel, sel.data(), (size_t)nat * sizeof(int));
         upload_now(p->d_scale, scale.data(), (size_t)nat * sizeof(double));
+        p->tiles.assign(p->ns, ofdft::PmeTiles());
+        if (p->pme) {
+            const int nr[3] = {p->g->nr[0], p->g->nr[1], p->g->nr[2]};
+            for (int s = 0; s < p->ns; ++s)
+                p->tiles[s] = ofdft::pme_tiles_build(p->sc, "pme" + std::to_string(s) + "_", p->frac.data(),
+                                                     sel.data() + p->sel_off[s], p->sel_off[s + 1] - p->sel_off[s],
+                                                     p->order, nr, cudaStreamPerThread);
+        }
     });
 }
 

@@ -109,3 +109,42 @@ def test_restart_from_density_file(tmp_path):
     opt2.optimize_rho(guess_rho=back2)
     assert opt2.result.niter <= 2
     assert abs(opt2.functional.energy - opt.functional.energy) <= 1e-8 * 4
+
+
+def test_calculator_matches_reference(tmp_path):
+    """The calculator against the reference's own DFTpyCalculator
+    (api4ase.py:11-119; tests/golden/reference_calc.npz from
+    tests/golden/make_golden_calc.py): three geometries in turn (displaced,
+    displaced again from the resident density, strained cell with a carried
+    density), energy in eV, forces in eV/A and Voigt stress in eV/A^3.  The
+    same recpot file, functional and L-BFGS options as the reference run; the
+    ground states agree to the optimiser's trajectory, so energies within
+    1e-10 relative, forces within 1e-7 eV/A and stress within 1e-8 eV/A^3."""
+    import os
+    from oracle.ofdft_np import write_recpot
+    gold = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_calc.npz")))
+    torch.cuda.set_device(0)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    fn = str(tmp_path / "Al.recpot")
+    write_recpot(fn, gp[-1], vp, header="analytic Z=3 rc=1")
+    lat, pos = gold["s1_lattice"], gold["s1_pos"]
+    grid = D.DirectGrid(lat, tuple(int(n) for n in gold["nr"]))
+    ions = D.Ions(symbols=["Al"] * 4, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": fn}, PME=True)
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"),
+                            HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+    opt = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
+                         optimization_options={"econv": float(gold["econv"]), "maxiter": 200, "maxfun": 50})
+    calc = DFTpyCalculator(evaluator=tot, rho=D.DirectField(grid) + 12.0 / grid.volume, optimizer=opt)
+    for k in (1, 2, 3):
+        atoms = Atoms(gold["s%d_pos" % k] * BOHR, gold["s%d_lattice" % k] * BOHR, ["Al"] * 4)
+        e = calc.get_potential_energy(atoms)
+        f = calc.get_forces(atoms)
+        s = calc.get_stress(atoms)
+        e_ref = float(gold["s%d_energy" % k])
+        assert abs(e - e_ref) <= 1e-10 * abs(e_ref), (k, e, e_ref)
+        np.testing.assert_allclose(f, gold["s%d_forces" % k], rtol=0, atol=1e-7, err_msg="forces %d" % k)
+        np.testing.assert_allclose(s, gold["s%d_stress" % k], rtol=0, atol=1e-8, err_msg="stress %d" % k)
+        assert abs(float(calc.dftpy_results["density"].integral()) - float(gold["s%d_N" % k])) <= 1e-10
+    assert calc.nsteps == 3

@@ -114,6 +114,31 @@ def test_ewald(golden):
     np.testing.assert_allclose(ex.forces, g["A_ewaldex_F"], rtol=0, atol=F_ATOL)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_pme_spreading_deterministic(golden, dtype):
+    """PME spreading sums every grid point's atom contributions in a fixed
+    order (no atomics), so two independent constructions of the local
+    pseudopotential and of the PME Ewald give the same bits: v_loc, the PP
+    energy and forces, the Ewald energy and forces.  256 displaced atoms on a
+    48^3 grid, so that many order-10 stencils overlap at every point."""
+    torch.cuda.set_device(0)
+    lat, pos = syn.fcc_supercell(7.6, 4)
+    pos = pos + np.random.default_rng(11).normal(0, 0.1, pos.shape)
+    grid = D.DirectGrid(lat, (48, 48, 48))
+    rho = D.DirectField(grid, data=syn.smooth_density(lat, (48, 48, 48), 3.0 * len(pos), seed=5, amp=0.3))
+    ions = D.Ions(symbols=["Al"] * len(pos), positions=pos, cell=lat, charges=3.0)
+    outs = []
+    for _ in range(2):
+        pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": _pp(golden)}, PME=True)
+        v = pp.vreal_for(dtype).as_subclass(torch.Tensor).clone()
+        ew = D.ewald(ions=ions, grid=grid, PME=True)
+        outs.append((v, pp(rho).energy, pp.forces(rho), ew.energy, ew.forces))
+    a, b = outs
+    assert torch.equal(a[0], b[0])
+    assert a[1] == b[1] and a[3] == b[3]
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[4], b[4])
+
+
 def test_two_species_wt_system(golden):
     g = golden
     grid, rho = _setup(g, "D_")

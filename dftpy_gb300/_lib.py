@@ -125,6 +125,12 @@ _SIGS = {
     "ofdft_optimize_v": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P, _P]),
     "ofdft_optimize_batch": (_I, [_I, C.POINTER(_P), C.POINTER(_P), C.POINTER(OptOptions), C.POINTER(C.c_double),
                                   C.POINTER(OptResult), C.POINTER(_P), _P]),
+    "ofdft_batch_eval_eligible": (_I, [_P]),
+    "ofdft_batch_eval_create": (_I, [_I, C.POINTER(_P), _I, C.POINTER(_P), C.POINTER(_P), _P, C.POINTER(_P)]),
+    "ofdft_batch_eval_run": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_ubyte), _PD, _P]),
+    "ofdft_batch_eval_shape": (_I, [_P, _PI, _PI, _PI, _PI, _PD]),
+    "ofdft_batch_eval_set_shape": (_I, [_P, _I, _I, _I]),
+    "ofdft_batch_eval_destroy": (None, [_P]),
     "ofdft_mix_history": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P]),
     "ofdft_mix_gram": (_I, [_P, C.POINTER(_P), _I, _PD, _P]),
     "ofdft_mix_density": (_I, [_P, _P, _P, C.POINTER(MixArgs), _P, _P]),

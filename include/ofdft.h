@@ -382,6 +382,43 @@ int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft
 int ofdft_optimize_batch(int n, ofdft_eval** evs, void** rho, const ofdft_opt_options* o, const double* econv,
                          ofdft_opt_result* r, void** v_out, ofdft_stream s);
 
+/* ---- Persistent batched evaluation.  No counterpart in the reference, which
+ * evaluates one system per call; it serves many small independent systems.
+ * One cooperative launch evaluates E and V of every system of a batch (uneven
+ * grids, one precision): the pre-pass, the forward and inverse transforms
+ * (the library's own mixed-radix FFTs, axis lengths products of 2, 3 and 5 up
+ * to 128), the Hartree and vW G-space factors and the post-pass of all
+ * systems, stage by stage, with grid-wide barriers between stages.
+ * Eligible evaluators use only TF, vW (no smoothing), LDA, Hartree and the
+ * local pseudopotential; ofdft_batch_eval_eligible tells (1) or not (0).
+ * Energies equal the evaluator's own to rounding (its transforms are cuFFT's);
+ * repeated runs give the same bits. */
+typedef struct ofdft_batch_eval ofdft_batch_eval;
+int ofdft_batch_eval_eligible(ofdft_eval* e);
+/* n (1..128) evaluators.  tune != 0 with rho and v_work (device fields of each
+ * system, grid precision): a project autotuner times every candidate launch
+ * shape (block 128/256 threads, 2/4/8 rows per row tile, 8/16/32 lines per
+ * column tile) on this batch, overwriting v_work, and keeps the fastest for
+ * every later batch of the same grids and precision in this process; otherwise
+ * the kept shape, or block 256, 4 rows, 16 lines. */
+int ofdft_batch_eval_create(int n, ofdft_eval** evs, int tune, void* const* rho, void* const* v_work,
+                            ofdft_stream s, ofdft_batch_eval** out);
+/* E and V of the systems with active[i] != 0 (active NULL: all): rho[i] in,
+ * v_out[i] out (device, grid precision).  energies (host, n x OFDFT_NE, may be
+ * NULL): filled for the active systems after the stream has been waited for;
+ * with NULL the call returns once the work is enqueued. */
+int ofdft_batch_eval_run(ofdft_batch_eval* b, void* const* rho, void* const* v_out, const unsigned char* active,
+                         double* energies, ofdft_stream s);
+/* the launch shape in use: threads per block, rows per row tile, lines per
+ * column tile, blocks of the cooperative grid, and the tuned time per run (ms,
+ * 0 when not tuned here) */
+int ofdft_batch_eval_shape(const ofdft_batch_eval* b, int* block, int* rows, int* lines, int* grid,
+                           double* tuned_ms);
+/* a launch shape from a stored tuning table (block 128 or 256, rows 1..16,
+ * lines 1..64); kept for later batches of the same grids */
+int ofdft_batch_eval_set_shape(ofdft_batch_eval* b, int block, int rows, int lines);
+void ofdft_batch_eval_destroy(ofdft_batch_eval* b);
+
 /* The scalar MINPACK-2 line search on a host callback, exposed for testing
  * against scipy.optimize line_search_wolfe1 (scalar_search_wolfe1). */
 typedef int (*ofdft_phi_fn)(double alpha, double* f, double* g, void* ctx);

@@ -11,8 +11,10 @@ the members it uses (ase.Atoms, ase.units, ase.cell, ase.calculators.calculator)
 Tests read only the .npz this script writes.
 
 System: fcc Al, 4 atoms, a = 7.6 Bohr, 32^3 grid, WT + LDA + Hartree + local
-PP (PME, the analytic Z=3 rc=1.0 potential written as a recpot), L-BFGS with
-econv 1e-10 Ha, starting from the uniform density.  The calculator is given
+PP (PME, the analytic Z=3 rc=1.0 potential written as a recpot), truncated
+Newton with econv 1e-12 Ha (tight, so that the ground-state densities and
+hence the forces are pinned, not only the energies), starting from the
+uniform density.  The calculator is given
 the evaluator, the initial density and the optimiser (run_normal) and is
 asked, for each of three geometries in turn, for the energy (eV), forces
 (eV/A) and Voigt stress (eV/A^3):
@@ -34,7 +36,7 @@ sys.path.insert(0, HERE)
 
 from make_golden import make_ions, ref_objects, setup, write_pp  # noqa: E402
 
-ECONV = 1e-10
+ECONV = 1e-12
 NR = (32, 32, 32)
 STRAIN = (1.01, 0.995, 1.0)
 
@@ -73,7 +75,7 @@ def main(ref_root):
                          XCFunctional=Functional(type="XC", name="LDA", libxc=False),
                          HARTREE=Functional(type="HARTREE"), PSEUDO=pp)
     rho0 = DirectField(grid=grid) + 12.0 / grid.volume
-    opt = Optimization(EnergyEvaluator=ev, optimization_method="LBFGS",
+    opt = Optimization(EnergyEvaluator=ev, optimization_method="TN",
                        optimization_options={"econv": ECONV, "maxiter": 200, "maxfun": 50})
     calc = DFTpyCalculator(evaluator=ev, rho=rho0, optimizer=opt)
     out = {"nr": np.array(NR), "econv": ECONV, "strain": np.array(STRAIN)}

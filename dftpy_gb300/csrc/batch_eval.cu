@@ -541,7 +541,27 @@ struct ofdft_batch_eval {
     double tuned_ms = 0.0;
     std::string sig;
     Scratch sc;
+    // field sets of the batched optimiser: a descriptor array per (rho, V)
+    // pointer set and the evaluation captured once as a CUDA graph (the active
+    // mask upload, the cooperative launch, the energies' copy back), replayed
+    // on a stream of its own forked from and joined back to the caller's
+    struct FieldSet {
+        std::vector<void*> key;
+        void* d_sys = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        bool graph_failed = false;
+    };
+    std::vector<FieldSet> sets;
+    cudaStream_t gst = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     ~ofdft_batch_eval() {
+        for (FieldSet& f : sets) {
+            if (f.exec) cudaGraphExecDestroy(f.exec);
+            cudaFree(f.d_sys);
+        }
+        if (gst) cudaStreamDestroy(gst);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
         cudaFree(d_sys);
         cudaFree(d_fft);
         cudaFree(d_tw);
@@ -688,9 +708,9 @@ void build_t(ofdft_batch_eval* b) {
 }
 
 template <typename T>
-void launch_t(ofdft_batch_eval* b, cudaStream_t st) {
+void launch_t(ofdft_batch_eval* b, cudaStream_t st, void* d_sys) {
     PbArgs<T> a;
-    a.sys = (PbSys<T>*)b->d_sys;
+    a.sys = (PbSys<T>*)(d_sys ? d_sys : b->d_sys);
     a.S = b->S;
     a.act = b->d_act;
     a.fft = b->d_fft;
@@ -718,9 +738,9 @@ void build(ofdft_batch_eval* b) {
     else build_t<float>(b);
 }
 
-void launch(ofdft_batch_eval* b, cudaStream_t st) {
-    if (b->prec == OFDFT_F64) launch_t<double>(b, st);
-    else launch_t<float>(b, st);
+void launch(ofdft_batch_eval* b, cudaStream_t st, void* d_sys = nullptr) {
+    if (b->prec == OFDFT_F64) launch_t<double>(b, st, d_sys);
+    else launch_t<float>(b, st, d_sys);
 }
 
 // rho/V pointers of a call into the device descriptors (one small upload)
@@ -740,6 +760,105 @@ void set_fields(ofdft_batch_eval* b, void* const* rho, void* const* v, cudaStrea
 }
 
 }  // namespace
+
+// ------------------------------------------------ the batched optimiser's use
+namespace {
+
+template <typename T>
+void* fieldset_sys_t(ofdft_batch_eval* b, void* const* rho, void* const* v) {
+    std::vector<PbSys<T>> h(b->S);
+    memcpy(h.data(), b->h_sys.data(), b->S * sizeof(PbSys<T>));
+    for (int s = 0; s < b->S; ++s) {
+        h[s].rho = (const T*)rho[s];
+        h[s].V = (T*)v[s];
+    }
+    void* d = nullptr;
+    OFDFT_CK(cudaMalloc(&d, b->S * sizeof(PbSys<T>)));
+    upload_now(d, h.data(), b->S * sizeof(PbSys<T>));
+    return d;
+}
+
+}  // namespace
+
+// A batched evaluation for the optimiser, or nullptr when some system is not
+// eligible.  rho/v: fields of every system the autotuner may use (v is
+// overwritten).
+ofdft_batch_eval* batch_eval_open(int n, ofdft_eval** evs, void* const* rho, void* const* v, cudaStream_t st) {
+    for (int i = 0; i < n; ++i)
+        if (!eligible(evs[i], nullptr) || e_grid(evs[i])->prec != e_grid(evs[0])->prec) return nullptr;
+    ofdft_batch_eval* b = nullptr;
+    const int rc = ofdft_batch_eval_create(n, evs, 1, rho, v, (ofdft_stream)st, &b);
+    if (rc != OFDFT_OK) OFDFT_REQUIRE(false, "batched evaluation: %s", ofdft_last_error());
+    OFDFT_CK(cudaStreamCreateWithFlags(&b->gst, cudaStreamNonBlocking));
+    OFDFT_CK(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+    OFDFT_CK(cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming));
+    return b;
+}
+
+void batch_eval_close(ofdft_batch_eval* b) { delete b; }
+
+// Enqueue the evaluation of the systems with act[s] on st: rho[s] -> v[s].
+// Energies are readable with batch_eval_energies once st has been synchronised.
+void batch_eval_enqueue(ofdft_batch_eval* b, void* const* rho, void* const* v, const unsigned char* act,
+                        cudaStream_t st) {
+    std::vector<void*> key(rho, rho + b->S);
+    key.insert(key.end(), v, v + b->S);
+    ofdft_batch_eval::FieldSet* f = nullptr;
+    for (auto& x : b->sets)
+        if (x.key == key) f = &x;
+    if (!f) {
+        b->sets.emplace_back();
+        f = &b->sets.back();
+        f->key = key;
+        f->d_sys = b->prec == OFDFT_F64 ? fieldset_sys_t<double>(b, rho, v) : fieldset_sys_t<float>(b, rho, v);
+    }
+    // the mask is read by the copy at its turn in the stream: fill it after the
+    // previous evaluation's copies are done (the caller synchronised st since)
+    for (int s = 0; s < b->S; ++s) b->h_act[s] = act[s] ? 1 : 0;
+    OFDFT_CK(cudaEventRecord(b->fork_ev, st));
+    OFDFT_CK(cudaStreamWaitEvent(b->gst, b->fork_ev, 0));
+    if (!f->exec && !f->graph_failed) {
+        cudaGraph_t graph = nullptr;
+        bool ok = cudaStreamBeginCapture(b->gst, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            cudaMemcpyAsync(b->d_act, b->h_act, b->S, cudaMemcpyHostToDevice, b->gst);
+            try {
+                launch(b, b->gst, f->d_sys);
+            } catch (const Error&) {
+                ok = false;
+            }
+            cudaMemcpyAsync(b->h_E, b->d_E, (size_t)b->S * OFDFT_NE * sizeof(double), cudaMemcpyDeviceToHost,
+                            b->gst);
+            ok = cudaStreamEndCapture(b->gst, &graph) == cudaSuccess && ok && graph;
+            if (ok) ok = cudaGraphInstantiate(&f->exec, graph, 0) == cudaSuccess;
+            if (graph) cudaGraphDestroy(graph);
+        }
+        if (!ok) {
+            // cooperative launches that cannot be captured here run uncaptured
+            f->exec = nullptr;
+            f->graph_failed = true;
+            cudaGetLastError();
+        }
+    }
+    if (f->exec) {
+        OFDFT_CK(cudaGraphLaunch(f->exec, b->gst));
+    } else {
+        OFDFT_CK(cudaMemcpyAsync(b->d_act, b->h_act, b->S, cudaMemcpyHostToDevice, b->gst));
+        launch(b, b->gst, f->d_sys);
+        OFDFT_CK(cudaMemcpyAsync(b->h_E, b->d_E, (size_t)b->S * OFDFT_NE * sizeof(double), cudaMemcpyDeviceToHost,
+                                 b->gst));
+    }
+    OFDFT_CK(cudaEventRecord(b->join_ev, b->gst));
+    OFDFT_CK(cudaStreamWaitEvent(st, b->join_ev, 0));
+}
+
+// the total energy of system s of the last evaluation (after st was synchronised)
+double batch_eval_energy(const ofdft_batch_eval* b, int s) { return b->h_E[(size_t)s * OFDFT_NE + OFDFT_E_TOTAL]; }
+bool batch_eval_graphed(const ofdft_batch_eval* b) {
+    for (const auto& f : b->sets)
+        if (f.exec) return true;
+    return false;
+}
 
 // ---------------------------------------------------------------- C ABI
 extern "C" {

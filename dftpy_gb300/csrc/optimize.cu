@@ -353,6 +353,11 @@ ofdft_grid* e_grid(ofdft_eval* e);
 // an evaluation enqueued without waiting, and its energies after a synchronisation (total.cu)
 void eval_enqueue(ofdft_eval* e, const void* rho, void* v_out, unsigned calc, cudaStream_t st);
 void eval_collect(ofdft_eval* e, double* energies);
+ofdft_batch_eval* batch_eval_open(int n, ofdft_eval** evs, void* const* rho, void* const* v, cudaStream_t st);
+void batch_eval_close(ofdft_batch_eval* b);
+void batch_eval_enqueue(ofdft_batch_eval* b, void* const* rho, void* const* v, const unsigned char* act,
+                        cudaStream_t st);
+double batch_eval_energy(const ofdft_batch_eval* b, int s);
 bool eval_capturable(const ofdft_eval* e);
 
 namespace {
@@ -1233,8 +1238,36 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
     std::vector<char> accepted_any(S, 0);  // mu then lives in the device scalars
     auto active = [&](const std::vector<char>& m) { b.set_active(m); };
     auto any = [](const std::vector<char>& m) { return std::any_of(m.begin(), m.end(), [](char c) { return c != 0; }); };
+    // persistent mode: one cooperative launch per round for every active system
+    struct PbOwner {
+        ofdft_batch_eval* p = nullptr;
+        ~PbOwner() {
+            if (p) batch_eval_close(p);
+        }
+    } pb;
+    if (o.batch_persistent) {
+        std::vector<void*> r(S), v(S);
+        for (int s = 0; s < S; ++s) {
+            r[s] = b.h_tab[s].f[BF_RHOIO];
+            v[s] = b.h_tab[s].f[BF_V];
+        }
+        pb.p = batch_eval_open(S, evs, r.data(), v.data(), st);
+    }
     auto evaluate = [&](const std::vector<char>& m, int xrho, int xV) {
         const auto t0 = std::chrono::steady_clock::now();
+        if (pb.p) {
+            std::vector<void*> r(S), v(S);
+            std::vector<unsigned char> act(S);
+            for (int s = 0; s < S; ++s) {
+                r[s] = b.h_tab[s].f[xrho];
+                v[s] = b.h_tab[s].f[xV];
+                act[s] = m[s] ? 1 : 0;
+                if (m[s]) ++b.evals;
+            }
+            batch_eval_enqueue(pb.p, r.data(), v.data(), act.data(), st);
+            b.enqueue_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            return;
+        }
         b.fork();
         for (int s = 0; s < S; ++s)
             if (m[s]) {
@@ -1248,6 +1281,11 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
     };
     const auto t_start = std::chrono::steady_clock::now();
     auto collect = [&](const std::vector<char>& m, std::vector<double>& out) {
+        if (pb.p) {
+            for (int s = 0; s < S; ++s)
+                if (m[s]) out[s] = batch_eval_energy(pb.p, s);
+            return;
+        }
         double En[OFDFT_NE];
         for (int s = 0; s < S; ++s)
             if (m[s]) {
@@ -1519,6 +1557,7 @@ void ofdft_opt_default(ofdft_opt_options* o) {
     o->xtol = 1e-12;
     o->h0 = 1.0;
     o->verbose = 0;
+    o->batch_persistent = 0;
 }
 
 int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, void* v_out,

@@ -184,7 +184,7 @@ class Optimization:
 _BATCH_MAX = 128
 
 
-def optimize_rho_batch(optimizations, guess_rhos, dtype=None, refine=None):
+def optimize_rho_batch(optimizations, guess_rhos, dtype=None, refine=None, persistent=False):
     """Ground states of many independent systems together.
 
     ``optimizations`` are ``Optimization`` objects (L-BFGS, one per system, each
@@ -198,6 +198,11 @@ def optimize_rho_batch(optimizations, guess_rhos, dtype=None, refine=None):
     ``refine="evaluate"``: after a float32 optimisation, evaluate every density
     once in FP64 (electron count restored in float64), as
     ``optimize_rho_mixed(refine="evaluate")`` does for one system.
+    ``persistent=True``: every round of evaluations runs as one persistent
+    cooperative launch for all active systems (``dftpy_gb300.batch``, launch
+    shape from the autotuner), replayed as a CUDA graph, when every system's
+    functional is eligible (TF, vW, LDA, Hartree, local PP); the results then
+    equal the single solves to rounding, not bit for bit.
     Returns the densities; each ``Optimization`` gets ``rho``, ``mu``,
     ``converged``, ``result`` and ``functional``."""
     opts = list(optimizations)
@@ -215,6 +220,7 @@ def optimize_rho_batch(optimizations, guess_rhos, dtype=None, refine=None):
         for f, _ in _lib.OptOptions._fields_:
             if f != "econv" and getattr(s, f) != getattr(base, f):
                 raise ValueError("batched optimisations must share every option but econv (%s differs)" % f)
+    base.batch_persistent = 1 if persistent else 0
     lib = _lib.load()
     out = []
     for c0 in range(0, len(opts), _BATCH_MAX):

@@ -352,6 +352,12 @@ typedef struct {
     int method, maxiter, maxfun, maxls, ncheck, maxcor;
     double econv, c1, c2, xtol, h0;
     int verbose;
+    /* ofdft_optimize_batch only: 1 = every round of evaluations of the batch in one
+     * persistent cooperative launch (ofdft_batch_eval), replayed as a CUDA graph,
+     * when every system is eligible (else as with 0); the results then equal the
+     * single solves to rounding instead of bit for bit.  0 (default): per-system
+     * evaluations on worker streams, bit for bit the single solves. */
+    int batch_persistent;
 } ofdft_opt_options;
 typedef struct {
     int converged;            /* 0 converged, 1 line search failed, 2 max steps (optimization.py:444-516) */

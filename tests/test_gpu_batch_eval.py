@@ -5,9 +5,12 @@ Systems: seven cells of the batching workload (fcc/bcc/sc Al, grids from
 {48, 64, 72, 80, 96}^3) plus a non-orthogonal cell on a 40 x 36 x 30 grid
 (radices 8, 5; 4, 3, 3; 2, 3, 5, and a non-orthogonal G^2), TF + vW + LDA +
 Hartree + PME local PP, seeded smooth densities.  Bars: FP64 energy within
-1e-10 relative (per-atom scale), potential within 1e-9 a.u. max-abs; FP32
-energy within 2e-6 relative and potential within 1e-5 of max|V| against the
-FP32 single-system path.  Repeated runs give the same bits; inactive systems
+1e-10 relative (per-atom scale), potential within 1e-9 a.u. max-abs.  FP32
+against the FP64 single-system result: energy within 2e-6 relative, and the
+potential error no larger than twice that of the FP32 single-system path
+(cuFFT) or 1e-5 of max|V|, whichever is larger (the vW term multiplies the
+float32 transform round-off by G^2, so both FP32 paths sit near 1e-4 of
+max|V| pointwise).  Repeated runs give the same bits; inactive systems
 are left untouched; every autotuned or stored shape gives the same energies to
 rounding."""
 import numpy as np
@@ -51,15 +54,20 @@ def test_batch_matches_single_system_evaluations(dtype):
     shape = be.shape
     assert shape["block"] in (128, 256) and shape["tuned_ms"] > 0
     for (nat, grid, tot, rho), o in zip(sy, outs):
-        ref = tot(rho)
-        v = o.potential.as_subclass(torch.Tensor)
-        vr = ref.potential.as_subclass(torch.Tensor)
+        v = o.potential.as_subclass(torch.Tensor).double()
         if dtype == torch.float64:
+            ref = tot(rho)
+            vr = ref.potential.as_subclass(torch.Tensor)
             assert abs(o.energy - ref.energy) <= 1e-10 * max(nat, abs(ref.energy)), (o.energy, ref.energy)
             assert float((v - vr).abs().max()) <= 1e-9
         else:
+            ref = tot(D.DirectField(grid, data=rho.as_subclass(torch.Tensor).double()))
+            vr = ref.potential.as_subclass(torch.Tensor)
+            single = tot(rho).potential.as_subclass(torch.Tensor).double()
+            e_single = float((single - vr).abs().max())
             assert abs(o.energy - ref.energy) <= 2e-6 * abs(ref.energy), (o.energy, ref.energy)
-            assert float((v - vr).abs().max()) <= 1e-5 * float(vr.abs().max())
+            assert float((v - vr).abs().max()) <= max(2.0 * e_single, 1e-5 * float(vr.abs().max())), \
+                (float((v - vr).abs().max()), e_single)
     # the same bits on a second run
     again = be([r for _, _, _, r in sy])
     for a, b in zip(outs, again):

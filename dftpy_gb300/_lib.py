@@ -125,6 +125,9 @@ _SIGS = {
     "ofdft_optimize_v": (_I, [_P, _P, C.POINTER(OptOptions), C.POINTER(OptResult), _P, _P]),
     "ofdft_optimize_batch": (_I, [_I, C.POINTER(_P), C.POINTER(_P), C.POINTER(OptOptions), C.POINTER(C.c_double),
                                   C.POINTER(OptResult), C.POINTER(_P), _P]),
+    "ofdft_wgc_create": (_I, [_P, _D, _D, _D, _D, _D, C.POINTER(_P)]),
+    "ofdft_wgc_compute": (_I, [_P, _P, _P, C.c_uint, _PD, _P]),
+    "ofdft_wgc_destroy": (None, [_P]),
     "ofdft_batch_eval_eligible": (_I, [_P]),
     "ofdft_batch_eval_create": (_I, [_I, C.POINTER(_P), _I, C.POINTER(_P), C.POINTER(_P), _P, C.POINTER(_P)]),
     "ofdft_batch_eval_run": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_ubyte), _PD, _P]),

@@ -163,29 +163,6 @@ struct GArgs {
     double invN;
 };
 
-__device__ inline double lindhard_dev(double eta, double lbda, double mu) {
-    const double tol = 1e-10, tol2 = tol / 10;
-    double out = eta;
-    if (eta > tol2 && fabs(eta - 1.0) > tol2)
-        out = 1.0 / (0.5 + 0.25 * (1.0 - eta * eta) * log((1.0 + eta) / fabs(1.0 - eta)) / eta) - 3.0 * mu * eta * eta -
-              lbda;
-    if (eta < tol) out = 1.0 - lbda + eta * eta * (1.0 / 3.0 - 3.0 * mu);
-    if (fabs(eta - 1.0) < tol) out = 2.0 - lbda - 3.0 * mu + 20.0 * (eta - 1.0);
-    if (eta > 3.65) {
-        const double c[15] = {-0.13714285714285712, -6.39999999999999875e-2, -3.77825602968460128e-2,
-                              -2.51824061652633074e-2, -1.80879839616166146e-2, -1.36715733124818332e-2,
-                              -1.07236045520990083e-2, -8.65192783339199453e-3, -7.1372762502456763e-3,
-                              -5.9945117538835746e-3, -5.10997527675418131e-3, -4.41060829979912465e-3,
-                              -3.84763737842981233e-3, -3.38745061493813488e-3, -3.00624946457977689e-3};
-        double inv2 = 1.0 / (eta * eta);
-        double acc = c[14] * inv2;
-#pragma unroll
-        for (int k = 13; k >= 0; --k) acc = inv2 * (c[k] + acc);
-        out = 3.0 * (1.0 - mu) * eta * eta - lbda - 0.6 + acc;
-    }
-    return out;
-}
-
 template <typename T>
 __global__ void k_gspace(GArgs<T> a) {
     using M = T;  // working precision of the multipliers

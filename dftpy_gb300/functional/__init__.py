@@ -29,4 +29,10 @@ def Functional(type=None, optional_kwargs=None, **kwargs):
         cls = FunctionalTypeDict[type]
     except KeyError:
         raise AttributeError("Unknown functional type: {}.".format(type))
+    name = str(kwargs.get("name") or kwargs.get("kedf") or "")
+    if type == "KEDF" and name.upper() in ("WGC", "WGC-NL"):
+        # the two-body WGC kernel, beside the fused evaluator (no reference counterpart)
+        from .wgc import WGCKEDF
+        kw = {k: v for k, v in kwargs.items() if k not in ("name", "kedf")}
+        return WGCKEDF(name=name, **kw)
     return cls(**kwargs)

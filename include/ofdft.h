@@ -388,6 +388,20 @@ int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft
 int ofdft_optimize_batch(int n, ofdft_eval** evs, void** rho, const ofdft_opt_options* o, const double* econv,
                          ofdft_opt_result* r, void** v_out, ofdft_stream s);
 
+/* ---- Wang-Govind-Carter nonlocal kinetic kernel with the two-body Fermi wave
+ * vector xi = ((k_F(r)^gamma + k_F(r')^gamma)/2)^(1/gamma) (Phys. Rev. B 60,
+ * 16350 (1999)), through its second-order Taylor expansion about the Fermi
+ * wave vector of rho0, on the Wang-Teter kernel (kernel.py:325-334, lbda = x).
+ * No counterpart in the reference.  rho0 <= 0: the mean density of each call
+ * (kernel tables rebuilt when it moves by more than 1e-6).  compute writes the
+ * nonlocal energy (Hartree) and, with OFDFT_CALC_V, its potential to v_out
+ * (device, grid precision). */
+typedef struct ofdft_wgc ofdft_wgc;
+int ofdft_wgc_create(ofdft_grid* g, double alpha, double beta, double gamma, double x, double rho0,
+                     ofdft_wgc** out);
+int ofdft_wgc_compute(ofdft_wgc* w, const void* rho, void* v_out, unsigned calc, double* energy, ofdft_stream s);
+void ofdft_wgc_destroy(ofdft_wgc* w);
+
 /* ---- Persistent batched evaluation.  No counterpart in the reference, which
  * evaluates one system per call; it serves many small independent systems.
  * One cooperative launch evaluates E and V of every system of a batch (uneven

@@ -322,6 +322,121 @@ class WT:
 
 
 # --------------------------------------------------------------------------
+# Wang-Govind-Carter two-body kernel (no reference implementation: restated
+# from Y. A. Wang, N. Govind, E. A. Carter, Phys. Rev. B 60, 16350 (1999);
+# parity unpinned)
+# --------------------------------------------------------------------------
+def lindhard_d2(eta, lbda, mu, tol=1e-10):
+    """F, eta F' and eta^2 F'' of the inverse Lindhard function, with the
+    branch order of ``lindhard`` (kernel.py:26-35): the closed form, eta < tol,
+    |eta - 1| < tol (eta F' = 48 as LindhardDerivative caps it, eta^2 F'' = 0)
+    and the large-eta series above 3.65, differentiated term by term."""
+    eta = np.asarray(eta, dtype=np.float64)
+    tol2 = tol / 10
+    F = eta.copy()
+    d1 = np.zeros_like(eta)
+    d2 = np.zeros_like(eta)
+    c0 = (eta > tol2) & (np.abs(eta - 1.0) > tol2)
+    e = eta[c0]
+    A = np.log((1.0 + e) / np.abs(1.0 - e))
+    e2 = e * e
+    L = 0.5 + 0.25 * (1.0 - e2) * A / e
+    L1 = -(1.0 + e2) * A / (4.0 * e2) + 0.5 / e
+    L2 = A / (2.0 * e2 * e) - 1.0 / (e2 * (1.0 - e2))
+    F[c0] = 1.0 / L - 3.0 * mu * e2 - lbda
+    d1[c0] = e * (-L1 / L ** 2 - 6.0 * mu * e)
+    d2[c0] = e2 * (-L2 / L ** 2 + 2.0 * L1 ** 2 / L ** 3 - 6.0 * mu)
+    c1 = eta < tol
+    e = eta[c1]
+    sl = 1.0 / 3.0 - 3.0 * mu
+    F[c1] = 1.0 - lbda + e ** 2 * sl
+    d1[c1] = 2.0 * e ** 2 * sl
+    d2[c1] = 2.0 * e ** 2 * sl
+    c2 = np.abs(eta - 1.0) < tol
+    e = eta[c2]
+    F[c2] = 2.0 - lbda - 3.0 * mu + 20.0 * (e - 1.0)
+    d1[c2] = 48.0 * e
+    d2[c2] = 0.0
+    c3 = eta > 3.65
+    e = eta[c3]
+    inv2 = 1.0 / e ** 2
+    f = np.zeros_like(e)
+    g1 = np.zeros_like(e)
+    g2 = np.zeros_like(e)
+    pw = inv2.copy()
+    for k, coef in enumerate(_LARGE):
+        m = 2.0 * (k + 1)
+        f += coef * pw
+        g1 += -m * coef * pw
+        g2 += m * (m + 1.0) * coef * pw
+        pw = pw * inv2
+    F[c3] = 3.0 * (1.0 - mu) * e ** 2 - lbda - 0.6 + f
+    d1[c3] = 6.0 * (1.0 - mu) * e ** 2 + g1
+    d2[c3] = 6.0 * (1.0 - mu) * e ** 2 + g2
+    return F, d1, d2
+
+
+def wgc_taylor(gamma):
+    """Coefficients of xi/k* - 1 = (t + t')/6 + c1 (t^2 + t'^2) + c2 (t + t')^2 + O(t^3)
+    for xi = ((k^gamma + k'^gamma)/2)^(1/gamma), k = k*(1 + t)^(1/3)."""
+    return (gamma / 3.0 - 1.0) / 12.0, (1.0 - gamma) / 72.0
+
+
+def wgc_kernels(grid, rho0, x=1.0, alpha=(5 + 5 ** 0.5) / 6, beta=(5 - 5 ** 0.5) / 6, gamma=2.7):
+    """K0, Ka, Kb, Kc on the half grid: the Wang-Teter kernel K(q; k) =
+    c (k/k*)^p F(q/2k; x, 1) (kernel.py:325-334) with its first and second
+    logarithmic derivatives in k at k* = (3 pi^2 rho0)^(1/3), combined with the
+    Taylor coefficients of xi_gamma; zero at G = 0."""
+    tkf = 2.0 * (3.0 * rho0 * np.pi ** 2) ** (1.0 / 3.0)
+    cTF = 0.3 * (3.0 * np.pi ** 2) ** (2.0 / 3.0)
+    c = 5.0 / (9.0 * alpha * beta * rho0 ** (alpha + beta - 5.0 / 3.0)) * cTF
+    p = 5.0 - 3.0 * (alpha + beta)
+    F, d1, d2 = lindhard_d2(grid.q / tkf, x, 1.0)
+    K0 = c * F
+    K1 = c * (p * F - d1)
+    K2 = c * (p * (p - 1.0) * F + (2.0 - 2.0 * p) * d1 + d2)
+    c1, c2 = wgc_taylor(gamma)
+    Ka = K1 / 6.0
+    Kb = (c1 + c2) * K1 + K2 / 72.0
+    Kc = 2.0 * c2 * K1 + 2.0 / 72.0 * K2
+    out = [K0, Ka, Kb, Kc]
+    for k in out:
+        k.flat[0] = 0.0
+    return out
+
+
+class WGC:
+    """Nonlocal part of the WGC functional, second order in theta = (rho - rho0)/rho0:
+    E = int a0 P0 + a1 P1 + a2 P2 with a_n = rho^alpha theta^n, b_n = rho^beta theta^n,
+    P0 = K0*b0 + Ka*b1 + Kb*b2, P1 = Ka*b0 + Kc*b1, P2 = Kb*b0; V = sum a_n' P_n +
+    b_n' Q_n (Q: the same convolutions of the a_n), rho0 held fixed (as in wt.py)."""
+
+    def __init__(self, x=1.0, alpha=(5 + 5 ** 0.5) / 6, beta=(5 - 5 ** 0.5) / 6, gamma=2.7, rho0=None):
+        self.x, self.alpha, self.beta, self.gamma, self.rho0 = x, alpha, beta, gamma, rho0
+
+    def __call__(self, rho, grid, calc=("E", "V")):
+        rho0 = self.rho0 if self.rho0 is not None else rho.mean()
+        K0, Ka, Kb, Kc = wgc_kernels(grid, rho0, self.x, self.alpha, self.beta, self.gamma)
+        a, b = self.alpha, self.beta
+        rc = np.where(rho < ZERO, ZERO, rho)
+        th = (rho - rho0) / rho0
+        ra, rb = rc ** a, rc ** b
+        A = [fft(ra * th ** n, grid) for n in range(3)]
+        B = [fft(rb * th ** n, grid) for n in range(3)]
+        P = [ifft(K0 * B[0] + Ka * B[1] + Kb * B[2], grid), ifft(Ka * B[0] + Kc * B[1], grid), ifft(Kb * B[0], grid)]
+        out = {}
+        if "E" in calc:
+            out["E"] = (ra * (P[0] + th * (P[1] + th * P[2]))).sum() * grid.dV
+        if "V" in calc:
+            Q = [ifft(K0 * A[0] + Ka * A[1] + Kb * A[2], grid), ifft(Ka * A[0] + Kc * A[1], grid),
+                 ifft(Kb * A[0], grid)]
+            va = a * ra / rc * (P[0] + th * (P[1] + th * P[2])) + ra / rho0 * (P[1] + 2.0 * th * P[2])
+            vb = b * rb / rc * (Q[0] + th * (Q[1] + th * Q[2])) + rb / rho0 * (Q[1] + 2.0 * th * Q[2])
+            out["V"] = va + vb
+        return out
+
+
+# --------------------------------------------------------------------------
 # density-dependent kernel (LWT family; the "WGC table" workload)
 # --------------------------------------------------------------------------
 def wt_kernel_table(eta, x=1.0):

@@ -11,11 +11,15 @@ value     FP32-mixed E+V evaluations/s with rho resident in HBM
 fp64      the same for the plain FP64 path
 e2e       E+V evaluations/s through the public API from pinned host memory:
           host->device copy of rho, the evaluation, device->host copy of V
-roofline  the dominant kernel of this library, bytes it must move / its
-          CUDA-event time, against the measured HBM copy bandwidth
-time_to_ground_state  L-BFGS from the uniform density to econv 1e-7 Ha/atom:
-          plain FP64, and FP32-mixed with one final FP64 E+V evaluation (and,
-          for comparison, with an FP64 L-BFGS continuation); --no-gs skips it
+roofline  the whole E+V evaluation: its algorithmic bytes B = (2 n_FFT + 3) s N
+          over the time per evaluation, against the measured HBM copy
+          bandwidth, with the DRAM traffic of its kernels;
+          roofline_dominant_kernel: the same for the costliest kernel class
+time_to_ground_state  from the uniform density with fixed k_F bounds: the FP64
+          route (L-BFGS to econv 1e-9 Ha/atom, truncated-Newton polish) that
+          defines the reference ground state, against FP32-mixed routes (FP32
+          L-BFGS, then one FP64 E+V, an FP64 L-BFGS continuation or two FP64
+          truncated-Newton iterations); --no-gs skips it
 batch     64 independent systems of uneven grids optimised together: systems/s
           of the lockstep batch (per-system evaluations, and one persistent
           cooperative launch per round of evaluations) against 64 sequential
@@ -71,6 +75,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-gs", action="store_true", help="skip the ground-state timing")
     p.add_argument("--no-batch", action="store_true", help="skip the 64-system batching workload")
+    p.add_argument("--no-wgc", action="store_true", help="skip the two-body WGC kernel timing")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused", "fused-split"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
     p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2", "relax", "oescf"],
@@ -410,10 +415,10 @@ def gpu_arm(args):
     per_launch_ms = d["ms"] / d["launches"]
     ach = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
     ratio = TRAFFIC_RATIO.get(dom)
-    out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
-                       "frac": ach / peak, "traffic": per_launch_bytes * ratio if ratio else None,
-                       "traffic_source": TRAFFIC_SOURCE if ratio else None, "peak_source": src,
-                       "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
+    out["roofline_dominant_kernel"] = {
+        "bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+        "traffic": per_launch_bytes * ratio if ratio else None, "traffic_source": TRAFFIC_SOURCE if ratio else None,
+        "peak_source": src, "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
     tot_ms = sum(v["ms"] for v in r32p["prof"].values())
     out["kernels"] = {k: {"share": v["ms"] / tot_ms if tot_ms else 0.0, "ms_per_step": v["ms"] / ksteps,
                           "GBps": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None,
@@ -426,9 +431,19 @@ def gpu_arm(args):
     n3 = args.n ** 3
     algo_bytes = (2 * 198 + 3) * s32 * n3 if args.nsp == 64 else None
     if algo_bytes:
-        out["eval_roofline"] = {"algorithmic_bytes": algo_bytes, "achieved": algo_bytes / (ms32 * 1e-3) / 1e9,
-                                "frac": algo_bytes / (ms32 * 1e-3) / 1e9 / peak, "unit": "GB/s",
-                                "note": "(2*n_FFT+3)*s*N with n_FFT=198, s=4"}
+        # the whole evaluation as the unit: B = (2 n_FFT + 3) s N, the bytes of n_FFT out-of-place
+        # transforms plus the pointwise passes, over the headline time per evaluation
+        per_eval = {k: v["bytes"] / ksteps for k, v in r32p["prof"].items()}
+        traffic = sum(b * TRAFFIC_RATIO.get(k, 1.0) for k, b in per_eval.items())
+        out["roofline"] = {"bound": "hbm", "kernel": "one E+V evaluation (all %d launches)" % r32["launches"],
+                           "achieved": algo_bytes / (ms32 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                           "frac": algo_bytes / (ms32 * 1e-3) / 1e9 / peak, "traffic": traffic,
+                           "traffic_per_algorithmic_byte": traffic / algo_bytes,
+                           "algorithmic_bytes": algo_bytes, "peak_source": src,
+                           "note": "B = (2*n_FFT+3)*s*N with n_FFT=198, s=4; traffic = each kernel class's bytes "
+                                   "times its ncu DRAM/algorithmic ratio (1 where none was measured)"}
+    else:
+        out["roofline"] = out["roofline_dominant_kernel"]
     # ---- FP64 path
     if not args.no_fp64:
         k64 = min(5, max(2, args.steps // 3))
@@ -484,7 +499,11 @@ def gpu_arm(args):
     del ke_f
     # ---- optional ground state
     if not args.no_gs:
-        out["time_to_ground_state"] = ground_state(D, tot, grid, rho_np, nat)
+        out["time_to_ground_state"] = ground_state(D, pp, grid, rho_np, nat, args.nsp)
+    # ---- the two-body WGC kernel (gamma = 2.7), reported beside the headline: no
+    # reference implementation, so its parity is unpinned
+    if rank == 0 and not args.no_wgc:
+        out["wgc_gamma"] = wgc_gamma(D, pp, grid, rho_np, nat)
     # ---- the batching workload (64 uneven systems) on rank 0
     if rank == 0 and not args.no_batch:
         bw = batch_workload(args, emit=False)
@@ -502,7 +521,9 @@ def gpu_arm(args):
         gs = out.get("time_to_ground_state")
         if gs:
             # the same L-BFGS run on the CPU path: its evaluation count times the sampled time per evaluation
-            out["cpu_baseline"]["time_to_ground_state_s_extrapolated"] = gs["f64"]["nfev"] * per
+            ref = gs["f64_reference"]
+            out["cpu_baseline"]["time_to_ground_state_s_extrapolated"] = (ref["lbfgs"]["nfev"] +
+                                                                          ref["tn_polish"]["nfev"]) * per
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
@@ -523,153 +544,144 @@ def warm_optimizer(D, tot, rho0, method="LBFGS"):
     torch.cuda.synchronize()
 
 
-def ground_state(D, tot, grid, rho_np, nat, method="LBFGS", econv_per_atom=1e-7, f32_factor=1.0):
-    """Wall time of optimize_rho from the uniform density: plain FP64, and
-    FP32-mixed (to the same econv rule) followed by either one FP64 E+V
-    evaluation of its density ("evaluate") or an FP64 L-BFGS continuation
-    ("optimize").  Reports the energy and PP+Ewald force differences of each
-    mixed result against the FP64 ground state."""
+def ground_state(D, pp, grid, rho_np, nat, nsp, method="LBFGS", econv_per_atom=1e-9, econv_f32_per_atom=1e-9):
+    """Time to the ground state from the uniform density, FP64 against
+    FP32-mixed, on the headline functional with fixed k_F bounds (the
+    reference's kfmin/kfmax options: 0.5x and 1.5x the k_F range of the
+    workload's trial density; with the adaptive rule the 64 nodes follow every
+    density's k_F range and the optimisers stall far earlier).
+
+    The FP64 reference ground state: FP64 L-BFGS to econv 1e-9 Ha/atom, then
+    FP64 truncated Newton until its line search stalls (residual dP ~ 3e-7).
+    Its wall time is the plain FP64 route to that state.  Timed against it:
+    the FP64 L-BFGS stage alone (econv 1e-9 Ha/atom) and three FP32-mixed
+    routes, each starting with FP32 L-BFGS to econv 1e-9 Ha/atom: one FP64 E+V
+    of the FP32 density; an FP64 L-BFGS continuation to econv 1e-9 Ha/atom; two
+    FP64 truncated-Newton iterations.  Energies and PP + Ewald forces of each
+    are compared with the reference."""
     import torch
-    econv = econv_per_atom * nat
-    opts = {"econv": econv, "maxiter": 300, "maxfun": 50}
-    res = {"method": method, "econv_Ha": econv, "econv_f32_Ha": f32_factor * econv}
+    kf0 = 2.0 * np.cbrt(3.0 * np.pi ** 2 * rho_np)
+    kfb = dict(kfmin=0.5 * float(kf0.min()), kfmax=1.5 * float(kf0.max()))
+    ke = D.Functional(type="KEDF", name="LWT", nsp=nsp, kdd=3, interp="linear", **kfb, **WGC)
+    tot = D.TotalFunctional(KineticEnergyFunctional=ke, XCFunctional=D.Functional(type="XC", name="LDA"),
+                            HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+    econv, econv32 = econv_per_atom * nat, econv_f32_per_atom * nat
+    res = {"method": method, "kf_bounds": kfb, "econv_Ha_per_atom": econv_per_atom,
+           "econv_f32_Ha_per_atom": econv_f32_per_atom}
     rho0 = D.DirectField(grid) + float(rho_np.mean())
     warm_optimizer(D, tot, rho0, method)
-    for refine in ("evaluate", "optimize"):  # the mixed paths' own first-use costs (host and torch kernels)
-        w = D.Optimization(EnergyEvaluator=tot, optimization_method=method,
-                           optimization_options={"econv": 1e-30, "maxiter": 1, "maxfun": 50})
-        w.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-30, refine=refine, refine_maxiter=1)
+    for m in ("TN", method):  # the kernels of both methods in both precisions are loaded before timing
+        for dt in (torch.float64, torch.float32):
+            w = D.Optimization(EnergyEvaluator=tot, optimization_method=m,
+                               optimization_options={"econv": 1e-30, "maxiter": 1, "maxfun": 3})
+            w.optimize_rho(guess_rho=rho0, dtype=dt)
     torch.cuda.synchronize()
-    opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method, optimization_options=dict(opts))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rho64 = opt.optimize_rho(guess_rho=rho0)
-    torch.cuda.synchronize()
-    e64 = float(opt.functional.energy)
-    res["f64"] = {"seconds": time.perf_counter() - t0, "energy": e64, "converged": int(opt.converged),
-                  "niter": opt.result.niter, "nfev": opt.result.nfev, "dP": opt.result.dP}
-    f64 = tot.get_forces(rho64)
-    for refine in ("evaluate", "optimize"):
-        opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method, optimization_options=dict(opts))
+
+    def solve(fn):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rhom = opt.optimize_rho_mixed(guess_rho=rho0, econv_f32=f32_factor * econv, refine=refine)
+        rho = fn()
         torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
-        em = float(opt.functional.energy)
-        fm = tot.get_forces(rhom)
+        return rho, time.perf_counter() - t0
+
+    def opt(m, ec, maxiter=600):
+        return D.Optimization(EnergyEvaluator=tot, optimization_method=m,
+                              optimization_options={"econv": ec, "maxiter": maxiter, "maxfun": 50})
+
+    def info(o):
+        return {"niter": o.result.niter, "nfev": o.result.nfev, "dP": o.result.dP, "converged": int(o.converged)}
+
+    # FP64: L-BFGS, then the truncated-Newton polish that defines the reference
+    o1 = opt(method, econv)
+    r1, t1 = solve(lambda: o1.optimize_rho(guess_rho=rho0))
+    e1, f1 = float(o1.functional.energy), tot.get_forces(r1)
+    o2 = opt("TN", 1e-13 * nat, maxiter=12)
+    r2, t2 = solve(lambda: o2.optimize_rho(guess_rho=r1))
+    e_ref, f_ref = float(o2.functional.energy), tot.get_forces(r2)
+    res["f64_reference"] = {"seconds": t1 + t2, "energy": e_ref, "lbfgs": dict(info(o1), seconds=t1),
+                            "tn_polish": dict(info(o2), seconds=t2),
+                            "what": "FP64 L-BFGS to econv then FP64 truncated Newton until its line search stalls"}
+    res["f64_lbfgs"] = dict(info(o1), seconds=t1, energy=e1, dE_per_atom_vs_reference=(e1 - e_ref) / nat,
+                            force_max_abs_vs_reference=float(np.abs(f1 - f_ref).max()))
+
+    def mixed(key, refine_fn, what):
+        o32 = opt(method, econv32)
+        r32, ta = solve(lambda: o32.optimize_rho(guess_rho=rho0, dtype=torch.float32))
+        n_target = float(rho0.integral())
+        r64 = DirectField64(D, grid, r32, n_target)
+        (rm, em, extra), tb = solve(lambda: refine_fn(r64))
+        fm = tot.get_forces(rm)
         # precision error of the FP32-mixed forces: the same density evaluated both ways
-        fm32 = tot.get_forces(D.DirectField(grid, data=rhom.as_subclass(torch.Tensor).float(), dtype=torch.float32))
-        key = "f32_mixed" if refine == "evaluate" else "f32_mixed_then_f64_lbfgs"
-        res[key] = {
-            "refine": refine, "seconds": secs, "energy": em, "converged": int(opt.converged), "stages": opt.stages,
-            "dP": opt.result.dP, "dE_per_atom_vs_f64": (em - e64) / nat,
-            "force_max_abs_f32_vs_f64_same_density": float(np.abs(fm32 - fm).max()),
-            "force_max_abs_vs_f64_ground_state": float(np.abs(fm - f64).max()),
-            "speedup_vs_f64": res["f64"]["seconds"] / secs}
-    # FP32-mixed alone (float32 fields, float64 sums), no FP64 stage: the energy is the FP32 functional's
-    opt = D.Optimization(EnergyEvaluator=tot, optimization_method=method, optimization_options=dict(opts))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    opt.optimize_rho(guess_rho=rho0, dtype=torch.float32)
-    torch.cuda.synchronize()
-    secs = time.perf_counter() - t0
-    res["f32_only"] = {"seconds": secs, "energy": float(opt.result.energy), "converged": int(opt.converged),
-                       "niter": opt.result.niter, "nfev": opt.result.nfev,
-                       "dE_per_atom_vs_f64": (float(opt.result.energy) - e64) / nat,
-                       "speedup_vs_f64": res["f64"]["seconds"] / secs}
-    res["speedup"] = res["f64"]["seconds"] / res["f32_mixed"]["seconds"]
-    res["note"] = ("ground states to the reference's econv rule; forces of two independently converged ground states "
-                   "differ at the optimiser's convergence level (the FP64 run at econv 1e-7 Ha/atom and the same run "
-                   "driven until its line search stalls differ by 9e-4 Ha/Bohr), so the FP32 force error is "
-                   "reported on the same density")
+        fm32 = tot.get_forces(D.DirectField(grid, data=rm.as_subclass(torch.Tensor).float(), dtype=torch.float32))
+        res[key] = {"what": what, "seconds": ta + tb, "f32_lbfgs": dict(info(o32), seconds=ta),
+                    "f64_stage_seconds": tb, "energy": em, "dE_per_atom_vs_reference": (em - e_ref) / nat,
+                    "force_max_abs_vs_reference": float(np.abs(fm - f_ref).max()),
+                    "force_max_abs_f32_vs_f64_same_density": float(np.abs(fm32 - fm).max()),
+                    "speedup_vs_f64_reference_route": (t1 + t2) / (ta + tb),
+                    "speedup_vs_f64_lbfgs": t1 / (ta + tb)}
+        res[key].update(extra)
+
+    def one_eval(r):
+        return r, float(tot(r, calcType={"E"}).energy), {}
+
+    def cont(m, ec, maxiter):
+        def run(r):
+            o = opt(m, ec, maxiter)
+            rr = o.optimize_rho(guess_rho=r)
+            return rr, float(o.functional.energy), {"f64_stage": info(o)}
+        return run
+
+    mixed("f32_mixed_one_f64_eval", one_eval, "FP32 L-BFGS, then one FP64 E+V of its density")
+    mixed("f32_mixed", cont(method, econv, 600), "FP32 L-BFGS, then FP64 L-BFGS to the same econv")
+    mixed("f32_mixed_f64_tn", cont("TN", 1e-13 * nat, 3), "FP32 L-BFGS, then two FP64 truncated-Newton iterations")
+    res["speedup"] = res["f32_mixed"]["speedup_vs_f64_lbfgs"]
+    res["note"] = ("forces are PP + Ewald.  The linear k_F interpolation makes the energy piecewise smooth (kinks "
+                   "where a point's k_F crosses a node), so FP64 optimisers stop on it at different points: FP64 "
+                   "L-BFGS at econv 1e-9 Ha/atom is 3e-5 Ha/Bohr from the truncated-Newton reference.  The "
+                   "precision error of the FP32 forces alone is the same-density figure.")
     return res
 
 
-def diff_workload(args):
-    """Differentiation workload: 500-atom two-species random alloy (Z = 3,
-    rc = 1.0 and Z = 2, rc = 1.2; 256-point radial tables), minimum separation
-    4.0 Bohr at 0.18 e/Angstrom^3, 160^3 grid, WT KEDF + LDA + Hartree + PME PP
-    + Ewald, FP32-mixed.  Times the forward E and the adjoint (dE/drho,
-    forces dE/dR, dE/d table), checks them against central differences and the
-    FP64 adjoint, and reports the device memory the evaluation holds."""
+def wgc_gamma(D, pp, grid, rho_np, nat, steps=5):
+    """E+V of TF + vW + the two-body WGC kernel (gamma = 2.7, WGC alpha/beta,
+    second-order Taylor expansion about the mean density) + LDA + Hartree + PME
+    local PP on the headline workload, FP64 and FP32: evaluations/s (CUDA
+    events, the density resident) and the FP32 error against FP64."""
     import torch
-    import dftpy_gb300 as D
-    from dftpy_gb300 import synthetic as syn
-    from dftpy_gb300.autograd import energy_and_gradients, total_energy
-    from dftpy_gb300.constants import BOHR
-    torch.cuda.set_device(0)
-    n = args.n if args.n != 256 else 160
-    lat, pos, spec = syn.random_alloy(500, 0.18 * BOHR ** 3, [3.0, 2.0], 4.0, seed=500)
-    sym = ["Al" if s == 0 else "Mg" for s in spec]
-    ga, va = syn.analytic_vloc(3.0, 1.0, npts=256)
-    gb, vb = syn.analytic_vloc(2.0, 1.2, npts=256)
-    grid = D.DirectGrid(lat, (n, n, n))
-    ions = D.Ions(symbols=sym, positions=pos, cell=lat)
-    pp = D.LocalPseudo(grid=grid, ions=ions, PME=True, PP_list={"Al": D.functional.RECPOT(r=ga, v=va, zval=3),
-                                                                "Mg": D.functional.RECPOT(r=gb, v=vb, zval=2)})
-    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
-                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
-                            PSEUDO=pp)
-    rho_np = syn.atomic_density(lat, (n, n, n), pos, [3.0 if s == 0 else 2.0 for s in spec], width=1.3, floor=0.003)
-    free0 = torch.cuda.mem_get_info()[0]
-    rho32 = D.DirectField(grid, data=rho_np, dtype=torch.float32)
-    keys = pp.species_keys
-    T = torch.tensor(np.concatenate([pp.readpp.vp[k] for k in keys]), requires_grad=True)
-    R = torch.tensor(pos, dtype=torch.float64, requires_grad=True)
-    # warm-up (plans, tables, Ewald forces cached per geometry)
-    E = total_energy(tot, rho32.as_subclass(torch.Tensor).clone().requires_grad_(True), R, T)
-    E.backward()
-    fw, bw = [], []
-    for _ in range(max(3, args.steps)):
-        r = rho32.as_subclass(torch.Tensor).clone().requires_grad_(True)
-        R.grad = None
-        T.grad = None
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WGC", gamma=2.7),
+                            XCFunctional=D.Functional(type="XC", name="LDA"),
+                            HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+    res = {"what": "TF + vW + WGC two-body kernel (gamma 2.7, second-order expansion) + LDA + Hartree + PME PP; "
+                   "the kernel terms run beside the fused evaluator", "parity": "unpinned (no reference "
+                                                                               "implementation)"}
+    outs = {}
+    for dt, key in ((torch.float64, "f64"), (torch.float32, "f32")):
+        rho = D.DirectField(grid, data=rho_np, dtype=dt)
+        for _ in range(2):
+            o = tot(rho)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        E = total_energy(tot, r, R, T)
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            o = tot(rho)
+        e1.record(st)
         torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        E.backward()
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        fw.append(t1 - t0)
-        bw.append(t2 - t1)
-    used = free0 - torch.cuda.mem_get_info()[0]
-    # checks: central differences (h = 1e-4) in FP64, FP32 adjoint against FP64 adjoint
-    rho64 = D.DirectField(grid, data=rho_np)
-    E64, V64, dR64, dT64 = energy_and_gradients(tot, rho64)
-    E32, V32, dR32, dT32 = energy_and_gradients(tot, rho32)
-    h = 1e-4
-    fd_err = []
-    for a, c in ((0, 0), (137, 1), (411, 2)):
-        Rp = R.detach().clone()
-        Rm = R.detach().clone()
-        Rp[a, c] += h
-        Rm[a, c] -= h
-        ep = float(total_energy(tot, rho64.as_subclass(torch.Tensor), Rp, T.detach()))
-        em = float(total_energy(tot, rho64.as_subclass(torch.Tensor), Rm, T.detach()))
-        fd_err.append(abs((ep - em) / (2 * h) - dR64[a, c]))
-    pp.set_positions(pos)
-    tfd = []
-    for idx in (0, 3, 60, 256 + 7, 256 + 100):
-        Tp = T.detach().clone()
-        Tm = T.detach().clone()
-        Tp[idx] += h
-        Tm[idx] -= h
-        ep = float(total_energy(tot, rho64.as_subclass(torch.Tensor), R.detach(), Tp))
-        em = float(total_energy(tot, rho64.as_subclass(torch.Tensor), R.detach(), Tm))
-        tfd.append(abs((ep - em) / (2 * h) - dT64[idx]))
-    out = {"workload": "differentiation: 500-atom Al/Mg-like random alloy, %d^3, WT+LDA+H+PME PP, FP32-mixed" % n,
-           "box_bohr": float(lat[0, 0]), "forward_ms": 1e3 * float(np.median(fw)),
-           "backward_ms": 1e3 * float(np.median(bw)), "backward_over_forward": float(np.median(bw) / np.median(fw)),
-           "device_bytes_held": int(used), "fd_force_max_abs_err": float(max(fd_err)),
-           "fd_table_max_abs_err": float(max(tfd)),
-           "fp32_vs_fp64": {"dE_per_atom": (E32 - E64) / 500, "force_max_abs": float(np.abs(dR32 - dR64).max()),
-                            "dEdtable_max_rel": float(np.abs(dT32 - dT64).max() / np.abs(dT64).max()),
-                            "V_max_abs": float((V32.as_subclass(torch.Tensor).double()
-                                                - V64.as_subclass(torch.Tensor)).abs().max())}}
-    print(json.dumps(out), flush=True)
+        ms = e0.elapsed_time(e1) / steps
+        outs[key] = o
+        res[key] = {"evals_per_s": 1e3 / ms, "ms_per_eval": ms, "energy": float(o.energy)}
+    v64 = outs["f64"].potential.as_subclass(torch.Tensor)
+    v32 = outs["f32"].potential.as_subclass(torch.Tensor).double()
+    res["f32_vs_f64"] = {"dE_per_atom": (res["f32"]["energy"] - res["f64"]["energy"]) / nat,
+                         "V_max_abs_rel": float((v32 - v64).abs().max() / v64.abs().max())}
+    return res
+
+
+def DirectField64(D, grid, r32, n_target):
+    """FP64 copy of an FP32 density with the electron count restored in float64."""
+    import torch
+    r = D.DirectField(grid, data=r32.as_subclass(torch.Tensor).double())
+    return D.DirectField(grid, data=r * (n_target / float(r.integral())))
 
 
 def batch_workload(args, emit=True):

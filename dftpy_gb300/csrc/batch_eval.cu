@@ -512,6 +512,7 @@ bool factorise(int n, PbFft& f) {
 
 struct PbShape {
     int block = 256, rows = 4, lines = 16;
+    double ms = 0.0;  // tuned time of one run (0: not timed)
 };
 
 // tuned shapes by batch signature (precision and grid sizes), for the process
@@ -898,6 +899,7 @@ int ofdft_batch_eval_create(int n, ofdft_eval** evs, int tune, void* const* rho,
             auto it = tuned_shapes().find(sig);
             if (it != tuned_shapes().end()) {
                 b->shape = it->second;
+                b->tuned_ms = it->second.ms;
                 build(b);
             } else if (tune && rho && v_work) {
                 // autotuner: every candidate shape that fits, timed on this batch
@@ -931,6 +933,7 @@ int ofdft_batch_eval_create(int n, ofdft_eval** evs, int tune, void* const* rho,
                             if (ms / 3.0 < best) {
                                 best = ms / 3.0;
                                 bs = b->shape;
+                                bs.ms = best;
                             }
                         }
                 cudaEventDestroy(e0);

@@ -228,6 +228,101 @@ __device__ C* tile_fft(C* b0, C* b1, int nl, int ls, int ps, const PbFft& f, con
     return src;
 }
 
+// The same transform with the length known at compile time: the radices, the
+// butterfly counts and the index divisions become constants.  The batching
+// workload's lengths (and the usual small ones) take this path.
+struct RadixList {
+    int np;
+    int r[kPbMaxPass];
+};
+__host__ __device__ constexpr RadixList radix_list(int n) {
+    RadixList L{0, {0, 0, 0, 0, 0, 0, 0, 0}};
+    int m = n;
+    while (m % 8 == 0) {
+        L.r[L.np++] = 8;
+        m /= 8;
+    }
+    if (m % 4 == 0) {
+        L.r[L.np++] = 4;
+        m /= 4;
+    } else if (m % 2 == 0) {
+        L.r[L.np++] = 2;
+        m /= 2;
+    }
+    while (m % 3 == 0) {
+        L.r[L.np++] = 3;
+        m /= 3;
+    }
+    while (m % 5 == 0) {
+        L.r[L.np++] = 5;
+        m /= 5;
+    }
+    return L;
+}
+__host__ __device__ constexpr int ns_before(int n, int p) {
+    int ns = 1;
+    for (int i = 0; i < p; ++i) ns *= radix_list(n).r[i];
+    return ns;
+}
+
+template <int N, int P, class C>
+__device__ __forceinline__ C* ct_passes(C* src, C* dst, int nl, int ls, int ps, const C* __restrict__ tw, int S) {
+    constexpr RadixList L = radix_list(N);
+    if constexpr (P == L.np) {
+        return src;
+    } else {
+        constexpr int R = L.r[P], NS = ns_before(N, P), M = N / R, STEP = N / (NS * R);
+        for (int b = threadIdx.x; b < nl * M; b += blockDim.x) {
+            const int l = b / M, j = b - l * M;
+            const int k = j % NS;
+            C u[R];
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                C x = src[l * ls + (j + q * M) * ps];
+                if (NS > 1 && q > 0) {
+                    const C w = __ldg(tw + k * q * STEP);
+                    x = S < 0 ? cmul(x, w) : cmulc(x, w);
+                }
+                u[q] = x;
+            }
+            small_dft<R>(u, S);
+            const int base = (j / NS) * NS * R + k;
+#pragma unroll
+            for (int q = 0; q < R; ++q) dst[l * ls + (base + q * NS) * ps] = u[q];
+        }
+        __syncthreads();
+        return ct_passes<N, P + 1>(dst, src, nl, ls, ps, tw, S);
+    }
+}
+
+template <int N, class C>
+__device__ __noinline__ C* tile_fft_ct(C* b0, C* b1, int nl, int ls, int ps, const C* __restrict__ tw, int S) {
+    return ct_passes<N, 0>(b0, b1, nl, ls, ps, tw, S);
+}
+
+// compile-time lengths where available, else the runtime radix list
+template <class C>
+__device__ C* tile_fft_any(C* b0, C* b1, int nl, int ls, int ps, const PbFft& f, const C* __restrict__ tw, int S) {
+    switch (f.n) {
+        case 16: return tile_fft_ct<16>(b0, b1, nl, ls, ps, tw, S);
+        case 20: return tile_fft_ct<20>(b0, b1, nl, ls, ps, tw, S);
+        case 24: return tile_fft_ct<24>(b0, b1, nl, ls, ps, tw, S);
+        case 30: return tile_fft_ct<30>(b0, b1, nl, ls, ps, tw, S);
+        case 32: return tile_fft_ct<32>(b0, b1, nl, ls, ps, tw, S);
+        case 36: return tile_fft_ct<36>(b0, b1, nl, ls, ps, tw, S);
+        case 40: return tile_fft_ct<40>(b0, b1, nl, ls, ps, tw, S);
+        case 48: return tile_fft_ct<48>(b0, b1, nl, ls, ps, tw, S);
+        case 60: return tile_fft_ct<60>(b0, b1, nl, ls, ps, tw, S);
+        case 64: return tile_fft_ct<64>(b0, b1, nl, ls, ps, tw, S);
+        case 72: return tile_fft_ct<72>(b0, b1, nl, ls, ps, tw, S);
+        case 80: return tile_fft_ct<80>(b0, b1, nl, ls, ps, tw, S);
+        case 96: return tile_fft_ct<96>(b0, b1, nl, ls, ps, tw, S);
+        case 120: return tile_fft_ct<120>(b0, b1, nl, ls, ps, tw, S);
+        case 128: return tile_fft_ct<128>(b0, b1, nl, ls, ps, tw, S);
+        default: return tile_fft(b0, b1, nl, ls, ps, f, tw, S);
+    }
+}
+
 // ------------------------------------------------------------------ stages
 // A: pre-pass and the forward row transforms of rows [row0, row0 + rows)
 template <typename T>
@@ -277,7 +372,7 @@ __device__ void pb_rows_fwd(const PbArgs<T>& a, int item, typename Cplx<T>::type
     }
     if (fft) {
         __syncthreads();
-        const C* z = tile_fft(b0, b1, nl, ls, 1, a.fft[y.f2], a.tw + a.fft[y.f2].tw, -1);
+        const C* z = tile_fft_any(b0, b1, nl, ls, 1, a.fft[y.f2], a.tw + a.fft[y.f2].tw, -1);
         const M half = (M)0.5;
         for (int e = threadIdx.x; e < nl * y.n2h; e += blockDim.x) {
             const int l = e / y.n2h, k = e - l * y.n2h;
@@ -314,7 +409,7 @@ __device__ void pb_axis1(const PbArgs<T>& a, int item, int S, typename Cplx<T>::
             b0[p * ps + l] = A[((long long)i0 * y.n1 + p) * y.n2h + k2a + l];
         }
         __syncthreads();
-        const C* z = tile_fft(b0, b1, nl, 1, ps, f, a.tw + f.tw, S);
+        const C* z = tile_fft_any(b0, b1, nl, 1, ps, f, a.tw + f.tw, S);
         for (int e = threadIdx.x; e < y.n1 * nl; e += blockDim.x) {
             const int p = e / nl, l = e - p * nl;
             A[((long long)i0 * y.n1 + p) * y.n2h + k2a + l] = z[p * ps + l];
@@ -345,7 +440,7 @@ __device__ void pb_axis0(const PbArgs<T>& a, int item, typename Cplx<T>::type* b
             b0[p * ps + l] = A[((long long)p * y.n1 + k1) * y.n2h + k2a + l];
         }
         __syncthreads();
-        C* z = tile_fft(b0, b1, nl, 1, ps, f, a.tw + f.tw, -1);
+        C* z = tile_fft_any(b0, b1, nl, 1, ps, f, a.tw + f.tw, -1);
         // G-space factors as the single-system G-space pass applies them
         for (int e = threadIdx.x; e < y.n0 * nl; e += blockDim.x) {
             const int p = e / nl, l = e - p * nl;
@@ -361,7 +456,7 @@ __device__ void pb_axis0(const PbArgs<T>& a, int item, typename Cplx<T>::type* b
         }
         __syncthreads();
         C* other = z == b0 ? b1 : b0;
-        const C* u = tile_fft(z, other, nl, 1, ps, f, a.tw + f.tw, +1);
+        const C* u = tile_fft_any(z, other, nl, 1, ps, f, a.tw + f.tw, +1);
         for (int e = threadIdx.x; e < y.n0 * nl; e += blockDim.x) {
             const int p = e / nl, l = e - p * nl;
             A[((long long)p * y.n1 + k1) * y.n2h + k2a + l] = u[p * ps + l];
@@ -399,7 +494,7 @@ __device__ void pb_rows_inv(const PbArgs<T>& a, int item, typename Cplx<T>::type
             b0[l * ls + p] = upper ? C{H.x + W.y, W.x - H.y} : C{H.x - W.y, H.y + W.x};
         }
         __syncthreads();
-        const C* z = tile_fft(b0, b1, nl, ls, 1, a.fft[y.f2], a.tw + a.fft[y.f2].tw, +1);
+        const C* z = tile_fft_any(b0, b1, nl, ls, 1, a.fft[y.f2], a.tw + a.fft[y.f2].tw, +1);
         const M tiny = (M)1e-30, vw_y = (M)y.vw_y;
         for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
             const int l = e / n2, p = e - l * n2;

@@ -24,6 +24,9 @@ batch     64 independent systems of uneven grids optimised together: systems/s
           of the lockstep batch (per-system evaluations, and one persistent
           cooperative launch per round of evaluations) against 64 sequential
           FP64 solves; --no-batch skips it
+c2, diff, relax, oescf  the other configurations (256 atoms at 128^3 FP64; the
+          500-atom differentiation workload; calculator relaxation steps; OE-SCF),
+          each against the CPU restatement on this host; --no-extra skips them
 cpu_baseline  the numpy restatement of the reference on the host (sampled)
 
 ``--impl reference`` times that CPU restatement alone (sampled per step).
@@ -76,6 +79,8 @@ def parse():
     p.add_argument("--no-gs", action="store_true", help="skip the ground-state timing")
     p.add_argument("--no-batch", action="store_true", help="skip the 64-system batching workload")
     p.add_argument("--no-wgc", action="store_true", help="skip the two-body WGC kernel timing")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the other configurations (c2, differentiation, relaxation, OE-SCF) in the default line")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused", "fused-split"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
     p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2", "relax", "oescf"],
@@ -509,6 +514,11 @@ def gpu_arm(args):
         bw = batch_workload(args, emit=False)
         bw.pop("systems_detail", None)
         out["batch"] = bw
+    # ---- the other configurations, each against the CPU restatement on this host
+    if rank == 0 and not args.no_extra:
+        for key, fn in (("c2", c2_workload), ("diff", diff_workload), ("relax", relax_workload),
+                        ("oescf", oescf_workload)):
+            out[key] = fn(args, emit=False)
     # ---- CPU baseline on rank 0
     if rank == 0 and not args.no_cpu:
         per, det = oracle_sample(lat, pos, gp, vp, rho_np, args.nsp)
@@ -684,6 +694,94 @@ def DirectField64(D, grid, r32, n_target):
     return D.DirectField(grid, data=r * (n_target / float(r.integral())))
 
 
+def diff_workload(args, emit=True):
+    """Differentiation workload: 500-atom two-species random alloy (Z = 3,
+    rc = 1.0 and Z = 2, rc = 1.2; 256-point radial tables), minimum separation
+    4.0 Bohr at 0.18 e/Angstrom^3, 160^3 grid, WT KEDF + LDA + Hartree + PME PP
+    + Ewald, FP32-mixed.  Times the forward E and the adjoint (dE/drho,
+    forces dE/dR, dE/d table), checks them against central differences and the
+    FP64 adjoint, and reports the device memory the evaluation holds."""
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import synthetic as syn
+    from dftpy_gb300.autograd import energy_and_gradients, total_energy
+    from dftpy_gb300.constants import BOHR
+    torch.cuda.set_device(0)
+    n = args.n if args.n != 256 else 160
+    lat, pos, spec = syn.random_alloy(500, 0.18 * BOHR ** 3, [3.0, 2.0], 4.0, seed=500)
+    sym = ["Al" if s == 0 else "Mg" for s in spec]
+    ga, va = syn.analytic_vloc(3.0, 1.0, npts=256)
+    gb, vb = syn.analytic_vloc(2.0, 1.2, npts=256)
+    grid = D.DirectGrid(lat, (n, n, n))
+    ions = D.Ions(symbols=sym, positions=pos, cell=lat)
+    pp = D.LocalPseudo(grid=grid, ions=ions, PME=True, PP_list={"Al": D.functional.RECPOT(r=ga, v=va, zval=3),
+                                                                "Mg": D.functional.RECPOT(r=gb, v=vb, zval=2)})
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"),
+                            PSEUDO=pp)
+    rho_np = syn.atomic_density(lat, (n, n, n), pos, [3.0 if s == 0 else 2.0 for s in spec], width=1.3, floor=0.003)
+    free0 = torch.cuda.mem_get_info()[0]
+    rho32 = D.DirectField(grid, data=rho_np, dtype=torch.float32)
+    keys = pp.species_keys
+    T = torch.tensor(np.concatenate([pp.readpp.vp[k] for k in keys]), requires_grad=True)
+    R = torch.tensor(pos, dtype=torch.float64, requires_grad=True)
+    # warm-up (plans, tables, Ewald forces cached per geometry)
+    E = total_energy(tot, rho32.as_subclass(torch.Tensor).clone().requires_grad_(True), R, T)
+    E.backward()
+    fw, bw = [], []
+    for _ in range(max(3, args.steps)):
+        r = rho32.as_subclass(torch.Tensor).clone().requires_grad_(True)
+        R.grad = None
+        T.grad = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E = total_energy(tot, r, R, T)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        E.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        fw.append(t1 - t0)
+        bw.append(t2 - t1)
+    used = free0 - torch.cuda.mem_get_info()[0]
+    # checks: central differences (h = 1e-4) in FP64, FP32 adjoint against FP64 adjoint
+    rho64 = D.DirectField(grid, data=rho_np)
+    E64, V64, dR64, dT64 = energy_and_gradients(tot, rho64)
+    E32, V32, dR32, dT32 = energy_and_gradients(tot, rho32)
+    h = 1e-4
+    fd_err = []
+    for a, c in ((0, 0), (137, 1), (411, 2)):
+        Rp = R.detach().clone()
+        Rm = R.detach().clone()
+        Rp[a, c] += h
+        Rm[a, c] -= h
+        ep = float(total_energy(tot, rho64.as_subclass(torch.Tensor), Rp, T.detach()))
+        em = float(total_energy(tot, rho64.as_subclass(torch.Tensor), Rm, T.detach()))
+        fd_err.append(abs((ep - em) / (2 * h) - dR64[a, c]))
+    pp.set_positions(pos)
+    tfd = []
+    for idx in (0, 3, 60, 256 + 7, 256 + 100):
+        Tp = T.detach().clone()
+        Tm = T.detach().clone()
+        Tp[idx] += h
+        Tm[idx] -= h
+        ep = float(total_energy(tot, rho64.as_subclass(torch.Tensor), R.detach(), Tp))
+        em = float(total_energy(tot, rho64.as_subclass(torch.Tensor), R.detach(), Tm))
+        tfd.append(abs((ep - em) / (2 * h) - dT64[idx]))
+    out = {"workload": "differentiation: 500-atom Al/Mg-like random alloy, %d^3, WT+LDA+H+PME PP, FP32-mixed" % n,
+           "box_bohr": float(lat[0, 0]), "forward_ms": 1e3 * float(np.median(fw)),
+           "backward_ms": 1e3 * float(np.median(bw)), "backward_over_forward": float(np.median(bw) / np.median(fw)),
+           "device_bytes_held": int(used), "fd_force_max_abs_err": float(max(fd_err)),
+           "fd_table_max_abs_err": float(max(tfd)),
+           "fp32_vs_fp64": {"dE_per_atom": (E32 - E64) / 500, "force_max_abs": float(np.abs(dR32 - dR64).max()),
+                            "dEdtable_max_rel": float(np.abs(dT32 - dT64).max() / np.abs(dT64).max()),
+                            "V_max_abs": float((V32.as_subclass(torch.Tensor).double()
+                                                - V64.as_subclass(torch.Tensor)).abs().max())}}
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
+
+
 def batch_workload(args, emit=True):
     """Batching workload: 64 independent systems of uneven size (fcc/bcc/sc Al
     cells of 4-108 atoms, a uniform in [7.3, 7.9] Bohr, displacements sigma =
@@ -772,7 +870,7 @@ def batch_workload(args, emit=True):
     return out
 
 
-def c2_workload(args):
+def c2_workload(args, emit=True):
     """Scaled-up plain method: fcc Al 4x4x4 (256 atoms, a = 7.60 Bohr, seeded
     displacements sigma = 0.10 Bohr), 128^3 grid, KEDF WT (TF + vW + WT,
     alpha = beta = 5/6) + LDA + Hartree + PME local PP, FP64.  GPU: E+V evals/s
@@ -874,10 +972,12 @@ def c2_workload(args):
            "parity": {"E_total_gpu_minus_cpu_Ha_excl_ewald": (e_gpu - float(E[_lib.E_II])) - e_cpu,
                       "ewald_forces_max_abs": float(np.abs(F_gpu - F_cpu).max()),
                       "stress_max_abs_Ha_per_Bohr3": st_err}}
-    print(json.dumps(out), flush=True)
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
-def relax_workload(args):
+def relax_workload(args, emit=True):
     """Caller integration: the ASE-style calculator (dftpy_gb300.api.DFTpyCalculator)
     relaxing fcc Al 4x4x4 (256 atoms, sigma = 0.10 Bohr, seed 256) at 128^3 with
     WT + LDA + Hartree + PME PP in FP64 by ten steepest-descent steps.  Each step
@@ -975,10 +1075,12 @@ def relax_workload(args):
            "cpu": {"kind": "port", "cores": os.cpu_count(), "ev_s": t_ev, "vloc_s": t_vloc,
                    "forces_stress_s": t_fs, "step_s_estimated": cpu_step},
            "speedup_step": cpu_step / t_step, "steps": steps}
-    print(json.dumps(out), flush=True)
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
-def oescf_workload(args):
+def oescf_workload(args, emit=True):
     """OE-SCF (optimization/scf.py) on fcc Al 4x4x4 (256 atoms, sigma = 0.10 Bohr,
     seed 256) at 128^3 in FP64: vW + LDA + Hartree + PME PP optimised by CG-HS
     with the WT nonlocal part (TF + WT kernel, y = 0) frozen as the embedding,
@@ -1075,7 +1177,9 @@ def oescf_workload(args):
            "cpu": {"kind": "port", "cores": os.cpu_count(), "inner_ev_s": t_ev, "emb_ev_s": t_emb, "mix_s": t_mix,
                    "oescf_s_estimated": cpu},
            "speedup": cpu / t_scf}
-    print(json.dumps(out), flush=True)
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def main():

@@ -83,7 +83,7 @@ def parse():
                    help="skip the other configurations (c2, differentiation, relaxation, OE-SCF) in the default line")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused", "fused-split"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
-    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "c2", "relax", "oescf"],
+    p.add_argument("--workload", default="ev", choices=["ev", "diff", "batch", "batch-eval", "c2", "relax", "oescf"],
                    help="ev: the E+V metric (default); diff: differentiation; batch: 64 uneven systems; "
                         "c2: 256 atoms at 128^3, FP64 against the CPU restatement; relax: calculator steps")
     return p.parse_args()
@@ -513,6 +513,7 @@ def gpu_arm(args):
     if rank == 0 and not args.no_batch:
         bw = batch_workload(args, emit=False)
         bw.pop("systems_detail", None)
+        bw["one_evaluation"] = batch_eval_workload(args, emit=False)
         out["batch"] = bw
     # ---- the other configurations, each against the CPU restatement on this host
     if rank == 0 and not args.no_extra:
@@ -870,6 +871,63 @@ def batch_workload(args, emit=True):
     return out
 
 
+def batch_eval_workload(args, emit=True):
+    """One E+V of all 64 systems of the batching workload (TF + vW + LDA + Hartree +
+    PME PP, each at its uniform density): the persistent cooperative launch
+    (BatchEvaluator, autotuned shape) against the 64 single-system evaluations
+    one after another, FP32 and FP64, CUDA events over 20 repetitions each."""
+    import torch
+    import dftpy_gb300 as D
+    from dftpy_gb300 import synthetic as syn
+    from dftpy_gb300.batch import BatchEvaluator
+    torch.cuda.set_device(0)
+    gp, vp = syn.analytic_vloc(3.0, 1.0)
+    tots, grids, nats = [], [], []
+    for sd in syn.batch_systems(64, seed=64):
+        lat, pos, nr = sd["lattice"], sd["positions"], sd["nr"]
+        grid = D.DirectGrid(lat, nr)
+        ions = D.Ions(symbols=["Al"] * len(pos), positions=pos, cell=lat)
+        pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
+        tots.append(D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="TFVW"),
+                                      XCFunctional=D.Functional(type="XC", name="LDA"),
+                                      HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp))
+        grids.append(grid)
+        nats.append(len(pos))
+    points = sum(int(np.prod(g.nr)) for g in grids)
+    out = {"workload": "one E+V of the 64 batching systems (%d grid points in all)" % points}
+    st = torch.cuda.current_stream()
+    for dt, key in ((torch.float32, "f32"), (torch.float64, "f64")):
+        rhos = [D.DirectField(g, dtype=dt) + 3.0 * n / g.volume for g, n in zip(grids, nats)]
+        be = BatchEvaluator(tots, grids, dtype=dt, tune=True)
+        outs = be(rhos)
+        for _ in range(3):
+            be(rhos)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(20):
+            be(rhos)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_b = e0.elapsed_time(e1) / 20
+        singles = [t(r) for t, r in zip(tots, rhos)]
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(5):
+            for t, r in zip(tots, rhos):
+                t(r)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_s = e0.elapsed_time(e1) / 5
+        dE = max(abs(a.energy - b.energy) / n for a, b, n in zip(outs, singles, nats))
+        out[key] = {"persistent_ms": ms_b, "sequential_ms": ms_s, "speedup": ms_s / ms_b,
+                    "GB_per_s_at_88_bytes_per_point": 88.0 * points * (dt == torch.float64 and 2 or 1) / (ms_b * 1e-3) / 1e9,
+                    "max_abs_dE_per_atom_vs_single": dE, "launch_shape": be.shape}
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
+
+
 def c2_workload(args, emit=True):
     """Scaled-up plain method: fcc Al 4x4x4 (256 atoms, a = 7.60 Bohr, seeded
     displacements sigma = 0.10 Bohr), 128^3 grid, KEDF WT (TF + vW + WT,
@@ -1189,6 +1247,9 @@ def main():
         return
     if args.workload == "batch":
         batch_workload(args)
+        return
+    if args.workload == "batch-eval":
+        batch_eval_workload(args)
         return
     if args.workload == "c2":
         c2_workload(args)

@@ -921,7 +921,8 @@ def batch_eval_workload(args, emit=True):
         ms_s = e0.elapsed_time(e1) / 5
         dE = max(abs(a.energy - b.energy) / n for a, b, n in zip(outs, singles, nats))
         out[key] = {"persistent_ms": ms_b, "sequential_ms": ms_s, "speedup": ms_s / ms_b,
-                    "GB_per_s_at_88_bytes_per_point": 88.0 * points * (dt == torch.float64 and 2 or 1) / (ms_b * 1e-3) / 1e9,
+                    "GB_per_s_at_88_bytes_per_point": 88.0 * points * (2 if dt == torch.float64 else 1)
+                                                      / (ms_b * 1e-3) / 1e9,
                     "max_abs_dE_per_atom_vs_single": dE, "launch_shape": be.shape}
     if emit:
         print(json.dumps(out), flush=True)

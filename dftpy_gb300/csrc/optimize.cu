@@ -174,6 +174,58 @@ struct Dcsrch {
     }
 };
 
+// Line search on the directional derivative alone (no energy comparisons), for
+// stages whose energies carry float32 round-off larger than the decreases near
+// convergence: from stp0, double the step while phi' < 0 (up to amax), then
+// regula falsi between the bracketing steps (a bisection when the secant lands
+// within 1% of an end) until |phi'| <= c2 |phi'(0)| or maxiter evaluations.  The
+// accepted step is the last one evaluated.  False only when phi'(0) >= 0.  Not in
+// the reference (whose line search is scipy's MINPACK-2 on the energy).
+template <class Phi>
+bool grad_search(Phi&& phi, double g0, double stp0, double c2, double amax, int maxiter, double& stp, double& f,
+                 double& g, int& nfev) {
+    nfev = 0;
+    if (!(g0 < 0.0)) return false;
+    const double tol = c2 * std::fabs(g0);
+    double lo = 0.0, glo = g0, hi = std::min(stp0, amax), ghi = 0.0;
+    phi(hi, f, ghi);
+    ++nfev;
+    stp = hi;
+    g = ghi;
+    if (std::fabs(ghi) <= tol) return true;
+    while (ghi < 0.0) {
+        if (hi >= amax || nfev >= maxiter) return true;
+        lo = hi;
+        glo = ghi;
+        hi = std::min(2.0 * hi, amax);
+        phi(hi, f, ghi);
+        ++nfev;
+        stp = hi;
+        g = ghi;
+        if (std::fabs(ghi) <= tol) return true;
+    }
+    while (nfev < maxiter) {
+        const double w = hi - lo;
+        double t = lo - glo * w / (ghi - glo);
+        if (!(t > lo + 0.01 * w && t < hi - 0.01 * w)) t = 0.5 * (lo + hi);
+        double ft, gt;
+        phi(t, ft, gt);
+        ++nfev;
+        stp = t;
+        f = ft;
+        g = gt;
+        if (std::fabs(gt) <= tol) return true;
+        if (gt < 0.0) {
+            lo = t;
+            glo = gt;
+        } else {
+            hi = t;
+            ghi = gt;
+        }
+    }
+    return true;
+}
+
 // scalar_search_wolfe1 semantics: start at stp0, at most maxiter dcsrch calls;
 // returns false when no acceptable step is found.  phi(stp, f, g) evaluates.
 template <class Phi>
@@ -660,7 +712,8 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
         const double g0 = 2.0 * op.dtheta(V, phi, p, phi, 1.0, 0.0) * dV;
         double stp, fnew, gnew;
         int nls = 0;
-        bool ok = wolfe1(phi_fn, E, g0, 1.0, o.c1, o.c2, M_PI, 0.0, o.xtol, 100, stp, fnew, gnew, nls);
+        bool ok = o.ls_grad ? grad_search(phi_fn, g0, 1.0, o.c2, M_PI, 20, stp, fnew, gnew, nls)
+                            : wolfe1(phi_fn, E, g0, 1.0, o.c1, o.c2, M_PI, 0.0, o.xtol, 100, stp, fnew, gnew, nls);
         nfev += nls;
         if (!ok || nls == 0 || stp != last_theta) {
             converged = 1;  // "Line-Search Failed" (optimization.py:444-448)
@@ -701,6 +754,10 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
         if (o.verbose)
             fprintf(stderr, "%-8d%-24.12E%-16.6E%-16.6E%-8d\n", it, E, Ehist[Ehist.size() - 1] - Ehist[Ehist.size() - 2],
                     resN, nls);
+        if (o.pconv > 0.0 && resN <= o.pconv) {  // the residual criterion (off by default)
+            converged = 0;
+            break;
+        }
         // check_converge (optimization.py:527-540)
         bool conv = false;
         if ((int)Ehist.size() - 1 >= o.ncheck) {
@@ -1225,6 +1282,8 @@ template <typename T>
 void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_options& o, const double* econv,
                       ofdft_opt_result* res, void** v_out, cudaStream_t st) {
     OFDFT_REQUIRE(o.method == OFDFT_OPT_LBFGS, "ofdft_optimize_batch: only L-BFGS is batched");
+    OFDFT_REQUIRE(o.pconv == 0.0 && o.ls_grad == 0,
+                  "ofdft_optimize_batch: the residual criterion and the derivative line search are not batched");
     OFDFT_REQUIRE(o.maxcor >= 0 && 2 * (o.maxcor + 1) <= kBF - BF_LB0, "ofdft_optimize_batch: maxcor too large");
     Batch<T> b;
     const int npairs = 2 * (o.maxcor + 1);
@@ -1558,6 +1617,8 @@ void ofdft_opt_default(ofdft_opt_options* o) {
     o->h0 = 1.0;
     o->verbose = 0;
     o->batch_persistent = 0;
+    o->pconv = 0.0;
+    o->ls_grad = 0;
 }
 
 int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, void* v_out,

@@ -32,7 +32,7 @@ class Optimization:
         self.optimization_options = dict(optimization_options or {})
         defaults = {"maxcor": 6, "ftol": 1.0e-7, "xtol": 1.0e-12, "maxfun": 50, "maxiter": 200, "maxls": 30,
                     "econv": 1.0e-5, "c1": 1e-4, "c2": 0.2, "algorithm": "EMM", "vector": "Orthogonalization",
-                    "ncheck": 2, "h0": 1.0}
+                    "ncheck": 2, "h0": 1.0, "pconv": None, "linesearch": "wolfe"}
         for k, v in defaults.items():
             self.optimization_options.setdefault(k, v)
         if EnergyEvaluator is None:
@@ -75,6 +75,12 @@ class Optimization:
         s.c1, s.c2, s.xtol = float(o["c1"]), float(o["c2"]), float(o["xtol"])
         s.h0 = float(o["h0"]) if o["h0"] else 0.0
         s.verbose = 1 if self.verbose else 0
+        # not in the reference: a residual stop and a derivative-only line search
+        # (for float32 stages whose energies are noisier than the last decreases)
+        s.pconv = float(o["pconv"]) if o["pconv"] else 0.0
+        if o["linesearch"] not in ("wolfe", "grad"):
+            raise ValueError("linesearch must be 'wolfe' (the reference's) or 'grad'")
+        s.ls_grad = 1 if o["linesearch"] == "grad" else 0
         return s
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False, lsfun="line_search", dtype=None):
@@ -113,7 +119,7 @@ class Optimization:
         return rho
 
     def optimize_rho_mixed(self, guess_rho=None, econv_f32=None, f32_method=None, refine_method=None,
-                           refine_maxiter=None, refine="optimize"):
+                           refine_maxiter=None, refine="optimize", f32_options=None):
         """FP32-mixed ground state with a final FP64 refinement.
 
         Stage 1 optimises in FP32-mixed (float32 fields and FFTs, float64
@@ -124,6 +130,9 @@ class Optimization:
         FP64 functional.  ``refine="evaluate"``: one FP64 E+V evaluation of the
         stage-1 density (electron count restored in float64), whose energy and
         potential become the result.
+        ``f32_options``: options of the FP32 stage over these (e.g. a residual stop
+        ``pconv`` with ``linesearch="grad"``, which converges on the float32
+        gradient where float32 energies no longer resolve the decrease).
         Returns the FP64 density; ``self.stages`` records both stages."""
         if refine not in ("optimize", "evaluate"):
             raise ValueError("refine must be 'optimize' or 'evaluate'")
@@ -134,11 +143,13 @@ class Optimization:
         stages = []
         m32 = f32_method or ("LBFGS" if self.optimization_method == "TN" else self.optimization_method)
         o32 = dict(o, econv=econv_f32 if econv_f32 is not None else 10.0 * econv64)
+        o32.update(f32_options or {})
         opt32 = Optimization(m32, o32, self.EnergyEvaluator)
         opt32.verbose = self.verbose
         rho32 = opt32.optimize_rho(guess_rho=self.rho, dtype=torch.float32)
         stages.append({"precision": "f32", "method": m32, "niter": opt32.result.niter,
-                       "nfev": opt32.result.nfev, "converged": opt32.converged, "energy": opt32.result.energy})
+                       "nfev": opt32.result.nfev, "converged": opt32.converged, "energy": opt32.result.energy,
+                       "dP": opt32.result.dP})
         o64 = dict(o)
         if refine_maxiter is not None:
             o64["maxiter"] = refine_maxiter

@@ -358,6 +358,14 @@ typedef struct {
      * single solves to rounding instead of bit for bit.  0 (default): per-system
      * evaluations on worker streams, bit for bit the single solves. */
     int batch_persistent;
+    /* Not in the reference (which stops on the energy test alone and searches on
+     * the energy): pconv > 0 also stops once the residual norm dP = int r^2 dV
+     * falls to pconv; ls_grad = 1 searches theta on the directional derivative
+     * alone (doubling, then regula falsi to |phi'| <= c2 |phi'(0)|), for float32
+     * stages whose energies carry round-off larger than the last decreases.
+     * Defaults 0 and 0. */
+    double pconv;
+    int ls_grad;
 } ofdft_opt_options;
 typedef struct {
     int converged;            /* 0 converged, 1 line search failed, 2 max steps (optimization.py:444-516) */

@@ -362,8 +362,10 @@ typedef struct {
      * the energy): pconv > 0 also stops once the residual norm dP = int r^2 dV
      * falls to pconv; ls_grad = 1 searches theta on the directional derivative
      * alone (doubling, then regula falsi to |phi'| <= c2 |phi'(0)|), for float32
-     * stages whose energies carry round-off larger than the last decreases.
-     * Defaults 0 and 0. */
+     * stages whose energies carry round-off larger than the last decreases; it
+     * has no sufficient-decrease test, so it is meant for a stage that starts
+     * near the ground state (after an energy line search has stalled), not from
+     * a uniform density.  Defaults 0 and 0. */
     double pconv;
     int ls_grad;
 } ofdft_opt_options;

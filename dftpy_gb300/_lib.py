@@ -139,6 +139,7 @@ _SIGS = {
     "ofdft_mix_gram": (_I, [_P, C.POINTER(_P), _I, _PD, _P]),
     "ofdft_mix_density": (_I, [_P, _P, _P, C.POINTER(MixArgs), _P, _P]),
     "ofdft_linesearch": (_I, [PHI_FN, _P, _D, _D, _D, _D, _D, _D, _D, _D, _I, _PD, _PD, _PD, _PI]),
+    "ofdft_linesearch_grad": (_I, [PHI_FN, _P, _D, _D, _D, _D, _I, _PD, _PD, _PD, _PI]),
 }
 
 

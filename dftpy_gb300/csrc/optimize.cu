@@ -176,54 +176,55 @@ struct Dcsrch {
 
 // Line search on the directional derivative alone (no energy comparisons), for
 // stages whose energies carry float32 round-off larger than the decreases near
-// convergence: from stp0, double the step while phi' < 0 (up to amax), then
-// regula falsi between the bracketing steps (a bisection when the secant lands
-// within 1% of an end) until |phi'| <= c2 |phi'(0)| or maxiter evaluations.  The
-// accepted step is the last one evaluated.  False only when phi'(0) >= 0.  Not in
-// the reference (whose line search is scipy's MINPACK-2 on the energy).
+// convergence.  The rotation phi cos(theta) + p sin(theta) repeats the density
+// with period pi, so the search stays in (0, amax] with amax well below pi/2:
+// from stp0, steps grow by secant extrapolation of phi' (at most 4x per step)
+// while phi' < 0, then regula falsi between the bracketing steps (a bisection
+// when the secant lands within 1% of an end) until |phi'| <= c2 |phi'(0)|.  The
+// accepted step is the last one evaluated.  Returns false when phi'(0) >= 0, when
+// phi' is still negative at amax or when no bracket is found in maxiter
+// evaluations.  Not in the reference (whose line search is scipy's MINPACK-2 on
+// the energy); meant for a stage that starts near the ground state.
 template <class Phi>
 bool grad_search(Phi&& phi, double g0, double stp0, double c2, double amax, int maxiter, double& stp, double& f,
                  double& g, int& nfev) {
     nfev = 0;
     if (!(g0 < 0.0)) return false;
     const double tol = c2 * std::fabs(g0);
-    double lo = 0.0, glo = g0, hi = std::min(stp0, amax), ghi = 0.0;
-    phi(hi, f, ghi);
-    ++nfev;
-    stp = hi;
-    g = ghi;
-    if (std::fabs(ghi) <= tol) return true;
-    while (ghi < 0.0) {
-        if (hi >= amax || nfev >= maxiter) return true;
-        lo = hi;
-        glo = ghi;
-        hi = std::min(2.0 * hi, amax);
-        phi(hi, f, ghi);
-        ++nfev;
-        stp = hi;
-        g = ghi;
-        if (std::fabs(ghi) <= tol) return true;
-    }
+    double lo = 0.0, glo = g0, hi = 0.0, ghi = 0.0;
+    bool bracket = false;
+    double t = std::min(stp0, amax);
     while (nfev < maxiter) {
-        const double w = hi - lo;
-        double t = lo - glo * w / (ghi - glo);
-        if (!(t > lo + 0.01 * w && t < hi - 0.01 * w)) t = 0.5 * (lo + hi);
         double ft, gt;
         phi(t, ft, gt);
         ++nfev;
         stp = t;
         f = ft;
         g = gt;
+        if (!std::isfinite(gt)) return false;
         if (std::fabs(gt) <= tol) return true;
         if (gt < 0.0) {
+            const double tp = lo, gp = glo;
             lo = t;
             glo = gt;
+            if (!bracket) {
+                if (t >= amax) return false;
+                // root of the secant of phi' through the last two points, at most 4x further
+                double tn = (gt < gp) ? 4.0 * t : t - gt * (t - tp) / (gt - gp);
+                tn = std::min(std::max(tn, 1.5 * t), 4.0 * t);
+                t = std::min(tn, amax);
+                continue;
+            }
         } else {
             hi = t;
             ghi = gt;
+            bracket = true;
         }
+        const double w = hi - lo;
+        t = lo - glo * w / (ghi - glo);
+        if (!(t > lo + 0.01 * w && t < hi - 0.01 * w)) t = 0.5 * (lo + hi);
     }
-    return true;
+    return bracket;
 }
 
 // scalar_search_wolfe1 semantics: start at stp0, at most maxiter dcsrch calls;
@@ -534,6 +535,7 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
     // float64; float32 fields cannot resolve it, so the mixed path uses 1e-4
     const double eps = sizeof(T) == 8 ? 1.0e-9 : 1.0e-4;
     int converged = 2, it = 0, nfev = 1;
+    double last_stp = 0.0;  // the derivative search's last accepted step
     for (it = 1; it < o.maxiter; ++it) {
         if (o.method == OFDFT_OPT_DIIS) {
             // The reference's DIIS (optimization.py:327-333, :429-441, :471-485):
@@ -712,8 +714,11 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
         const double g0 = 2.0 * op.dtheta(V, phi, p, phi, 1.0, 0.0) * dV;
         double stp, fnew, gnew;
         int nls = 0;
-        bool ok = o.ls_grad ? grad_search(phi_fn, g0, 1.0, o.c2, M_PI, 20, stp, fnew, gnew, nls)
+        // the derivative search starts from twice the last accepted step (0.1 at first), within pi/4
+        bool ok = o.ls_grad ? grad_search(phi_fn, g0, last_stp > 0.0 ? 2.0 * last_stp : 0.1, o.c2, M_PI / 4, 20, stp,
+                                          fnew, gnew, nls)
                             : wolfe1(phi_fn, E, g0, 1.0, o.c1, o.c2, M_PI, 0.0, o.xtol, 100, stp, fnew, gnew, nls);
+        if (ok) last_stp = stp;
         nfev += nls;
         if (!ok || nls == 0 || stp != last_theta) {
             converged = 1;  // "Line-Search Failed" (optimization.py:444-448)
@@ -1654,6 +1659,25 @@ int ofdft_optimize_batch(int n, ofdft_eval** evs, void** rho, const ofdft_opt_op
         }
         if (prec == OFDFT_F64) optimize_batch_t<double>(n, evs, rho, *o, econv, r, v_out, (cudaStream_t)s);
         else optimize_batch_t<float>(n, evs, rho, *o, econv, r, v_out, (cudaStream_t)s);
+    });
+}
+
+int ofdft_linesearch_grad(ofdft_phi_fn fn, void* ctx, double g0, double stp0, double c2, double amax, int maxiter,
+                          double* stp_out, double* f_out, double* g_out, int* nfev) {
+    return guard([&] {
+        OFDFT_REQUIRE(fn && stp_out && f_out && g_out && nfev, "ofdft_linesearch_grad: null argument");
+        bool cb_err = false;
+        auto phi = [&](double a, double& f, double& g) {
+            if (fn(a, &f, &g, ctx) != 0) cb_err = true;
+        };
+        double stp = NAN, f = NAN, g = NAN;
+        int n = 0;
+        bool ok = grad_search(phi, g0, stp0, c2, amax, maxiter, stp, f, g, n);
+        OFDFT_REQUIRE(!cb_err, "ofdft_linesearch_grad: callback failed");
+        *stp_out = ok ? stp : NAN;
+        *f_out = f;
+        *g_out = g;
+        *nfev = n;
     });
 }
 

@@ -456,6 +456,11 @@ int ofdft_linesearch(ofdft_phi_fn fn, void* ctx, double f0, double g0, double st
                      double amax, double amin, double xtol, int maxiter, double* stp_out, double* f_out,
                      double* g_out, int* nfev);
 
+/* The derivative-only line search of ls_grad on a host callback (no counterpart
+ * in the reference; exposed for testing): *stp_out is NaN when it fails. */
+int ofdft_linesearch_grad(ofdft_phi_fn fn, void* ctx, double g0, double stp0, double c2, double amax, int maxiter,
+                          double* stp_out, double* f_out, double* g_out, int* nfev);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,3 +104,38 @@ def test_linesearch_matches_scipy(k):
     # identical trial sequence
     assert len(calls) == len(seen)
     np.testing.assert_allclose(calls, seen, rtol=1e-14, atol=0)
+
+
+def _native_grad_ls(fp, stp0, amax=np.pi / 4, c2=0.2, maxiter=20):
+    lib = _lib.load()
+    calls = []
+
+    @_lib.PHI_FN
+    def cb(a, f, g, ctx):
+        calls.append(a)
+        f[0] = 0.0
+        g[0] = fp(a)
+        return 0
+
+    stp, fo, go, n = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+    _lib.check(lib.ofdft_linesearch_grad(cb, None, fp(0.0), stp0, c2, amax, maxiter, C.byref(stp), C.byref(fo),
+                                         C.byref(go), C.byref(n)))
+    return (None if np.isnan(stp.value) else stp.value), go.value, calls
+
+
+@pytest.mark.parametrize("theta_min,stp0", [(0.03, 0.1), (0.5, 0.1), (0.2, 0.2), (1e-4, 0.1)])
+def test_derivative_line_search_finds_the_minimum(theta_min, stp0):
+    """The derivative-only search (ls_grad) on the energy along a rotation,
+    E(theta) = -cos(2 (theta - theta_min)): it returns a step with
+    |E'| <= 0.2 |E'(0)|, and the last trial is the accepted step."""
+    fp = lambda a: 2.0 * np.sin(2.0 * (a - theta_min))
+    stp, g, calls = _native_grad_ls(fp, stp0)
+    assert stp is not None and calls[-1] == stp
+    assert abs(g) <= 0.2 * abs(fp(0.0)) + 1e-15
+    assert abs(stp - theta_min) <= 0.2 * theta_min + 1e-12
+
+
+def test_derivative_line_search_refuses_bad_cases():
+    # not a descent direction; still descending at the step limit (pi/4)
+    assert _native_grad_ls(lambda a: 1.0 + a, 0.1)[0] is None
+    assert _native_grad_ls(lambda a: 2.0 * np.sin(2.0 * (a - 1.2)), 0.1)[0] is None

@@ -119,7 +119,7 @@ class Optimization:
         return rho
 
     def optimize_rho_mixed(self, guess_rho=None, econv_f32=None, f32_method=None, refine_method=None,
-                           refine_maxiter=None, refine="optimize", f32_options=None):
+                           refine_maxiter=None, refine="optimize", f32_options=None, f32_polish=None):
         """FP32-mixed ground state with a final FP64 refinement.
 
         Stage 1 optimises in FP32-mixed (float32 fields and FFTs, float64
@@ -130,9 +130,13 @@ class Optimization:
         FP64 functional.  ``refine="evaluate"``: one FP64 E+V evaluation of the
         stage-1 density (electron count restored in float64), whose energy and
         potential become the result.
-        ``f32_options``: options of the FP32 stage over these (e.g. a residual stop
-        ``pconv`` with ``linesearch="grad"``, which converges on the float32
-        gradient where float32 energies no longer resolve the decrease).
+        ``f32_options``: options of the FP32 stage over these.
+        ``f32_polish``: a dict of options (e.g. ``{"pconv": 2e-6, "maxiter": 150}``)
+        for a second FP32 L-BFGS stage from the first one's density on the
+        derivative-only line search (``linesearch="grad"``, no energy test): it
+        converges on the float32 gradient, which stays accurate where float32
+        energies no longer resolve the decreases, so the FP64 refinement starts
+        at the FP32 functional's own stationary point.
         Returns the FP64 density; ``self.stages`` records both stages."""
         if refine not in ("optimize", "evaluate"):
             raise ValueError("refine must be 'optimize' or 'evaluate'")
@@ -150,6 +154,16 @@ class Optimization:
         stages.append({"precision": "f32", "method": m32, "niter": opt32.result.niter,
                        "nfev": opt32.result.nfev, "converged": opt32.converged, "energy": opt32.result.energy,
                        "dP": opt32.result.dP})
+        if f32_polish is not None:
+            op = dict(o32, econv=0.0, linesearch="grad", maxiter=150)
+            op.update(f32_polish)
+            optp = Optimization("LBFGS", op, self.EnergyEvaluator)
+            optp.verbose = self.verbose
+            rho32 = optp.optimize_rho(guess_rho=rho32, dtype=torch.float32)
+            stages.append({"precision": "f32", "method": "LBFGS, derivative line search",
+                           "niter": optp.result.niter, "nfev": optp.result.nfev, "converged": optp.converged,
+                           "energy": optp.result.energy, "dP": optp.result.dP})
+            opt32 = optp
         o64 = dict(o)
         if refine_maxiter is not None:
             o64["maxiter"] = refine_maxiter

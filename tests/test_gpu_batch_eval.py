@@ -109,3 +109,20 @@ def test_batch_tuning_table_round_trip(tmp_path):
     be2([r for _, _, _, r in sy])
     assert {k: be2.shape[k] for k in ("block", "rows", "lines")} == {k: table[be.signature][k]
                                                                     for k in ("block", "rows", "lines")}
+
+
+def test_batch_refuses_ineligible_systems():
+    """An axis with a factor other than 2, 3 and 5, or a functional beyond TF, vW,
+    LDA, Hartree and the local PP, is refused at construction with a clear error."""
+    torch.cuda.set_device(0)
+    lat = np.diag([7.6, 7.6, 7.6])
+    g28 = D.DirectGrid(lat, (28, 32, 32))
+    tot = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="TFVW"),
+                            XCFunctional=D.Functional(type="XC", name="LDA"), HARTREE=D.Functional(type="HARTREE"))
+    with pytest.raises(NotImplementedError):
+        BatchEvaluator([tot], [g28])
+    g32 = D.DirectGrid(lat, (32, 32, 32))
+    wt = D.TotalFunctional(KineticEnergyFunctional=D.Functional(type="KEDF", name="WT"),
+                           HARTREE=D.Functional(type="HARTREE"))
+    with pytest.raises(NotImplementedError):
+        BatchEvaluator([wt], [g32])

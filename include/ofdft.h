@@ -436,7 +436,9 @@ int ofdft_batch_eval_create(int n, ofdft_eval** evs, int tune, void* const* rho,
 /* E and V of the systems with active[i] != 0 (active NULL: all): rho[i] in,
  * v_out[i] out (device, grid precision).  energies (host, n x OFDFT_NE, may be
  * NULL): filled for the active systems after the stream has been waited for;
- * with NULL the call returns once the work is enqueued. */
+ * with NULL the call returns once the work is enqueued.  Runs on one handle must
+ * not overlap: the active mask and the energies live in the handle's pinned
+ * buffers (wait for a run before starting the next). */
 int ofdft_batch_eval_run(ofdft_batch_eval* b, void* const* rho, void* const* v_out, const unsigned char* active,
                          double* energies, ofdft_stream s);
 /* the launch shape in use: threads per block, rows per row tile, lines per

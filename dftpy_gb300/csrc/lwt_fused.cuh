@@ -27,8 +27,6 @@
 #pragma once
 #include "fz_fft.cuh"
 
-#include <cooperative_groups.h>
-
 namespace {
 
 struct FzDims {
@@ -42,7 +40,7 @@ struct FzTw {
     const float2* t1;  // exp(-2 pi i k/n1), k < n1
     const float2* th;  // exp(-2 pi i k/H),  k < H
     const float2* tr;  // exp(-2 pi i k/n2), k < H
-    const float2* tq;  // exp(-2 pi i k/Q),  k < Q (split path)
+    const float2* tq;  // exp(-2 pi i k/32), k < 32 (split path)
 };
 
 constexpr int kFzLines = 16;  // lines per column tile
@@ -383,10 +381,10 @@ __device__ __forceinline__ float fz_hat(float jf, float fi, float tr) {
 // values) pre-processed for the half-length complex C2R:
 // Z[k] = (X[k] + conj X[H-k]) + i w^k (X[k] - conj X[H-k]), w = exp(+2 pi i/n2),
 // the imaginary parts of X[0] and X[H] dropped.
-template <int H>
+template <int H, int ROWS = kFzRowThreads / (H / kFzRowE)>
 __device__ __forceinline__ void fz_c2r_pre(const float2* st, int l, int t, const float2* __restrict__ twr,
                                            float2 (&v)[kFzRowE]) {
-    constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T;
+    constexpr int E = kFzRowE, T = H / E;
     const float2* r = st + l * H;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -677,373 +675,3 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
 }
 
 }  // namespace
-
-// ---------------------------------------------------------------------------
-// Axis 1 split between the C2R passes (256 x 256 x 256 class of grids: n1 =
-// 256, n2 = 256).  The 256-point inverse transform along axis 1 is a radix-4
-// decimation in frequency: with Q = n1/4 and k1 = kk + Q s,
-//   z_r[kk] = (sum_s x[kk + Q s] e^{+2 pi i s r/4}) e^{+2 pi i kk r/n1}
-//   y[4m + r] = sum_kk z_r[kk] e^{+2 pi i kk m/Q}             (Q-point inverse)
-// k_fz_nodes4 applies the node kernel, transforms axis 0 and forms z_r (the
-// radix-4 stage, through shared memory); it stores z_r[kk] in plane row
-// (i0, kk + Q r).  k_fz_c2r_cl, a cluster of four blocks per (i0, r), does
-// the Q-point transforms (one quarter of the k2 columns each), exchanges the
-// results through distributed shared memory, and finishes with the axis-2 C2R
-// and the interpolation of its 16 rows i1 = 4m + r.  The axis-1 plane pass and
-// its HBM round trip are gone from the C2R chain.
-constexpr int kFzN1 = 256;       // n1 of the split path
-constexpr int kFzQ = kFzN1 / 4;  // Q
-constexpr int kFzCl = 4;         // blocks per cluster of the consumer
-constexpr int kFzX = 20;         // row pitch (float2) of the radix-4 exchange: 16 lines + pad
-
-// Column tile of the split generator: lines l = 4 s + c take k1 = kb + Q s and
-// k2 = 4 q + c (main tiles, kb fastest so that the four tiles writing one
-// 128-byte row segment run side by side), or k2 = H and k1 = (4 q' + c) + Q s
-// (Nyquist tiles).  kk is the radix-4 index of the line's k1.
-__device__ __forceinline__ void fz4_tile(const FzDims& d, int tile, int l, int& k1, int& k2, int& kk, int& q,
-                                         bool& nyq) {
-    const int s = l >> 2, c = l & 3;
-    const int tiles_main = kFzQ * (d.H / 4);
-    if (tile < tiles_main) {
-        const int kb = tile % kFzQ;
-        q = tile / kFzQ;
-        kk = kb;
-        k1 = kb + kFzQ * s;
-        k2 = 4 * q + c;
-        nyq = false;
-    } else {
-        q = tile - tiles_main;
-        kk = 4 * q + c;
-        k1 = kk + kFzQ * s;
-        k2 = d.H;
-        nyq = true;
-    }
-}
-
-inline size_t fz4_gen_smem(int n0, int nb) {
-    const size_t pts = (size_t)n0 * kFzLines;
-    const size_t xch = std::max((size_t)fz::col_slots(n0), (size_t)n0 * kFzX);
-    return xch * sizeof(float2) + pts * (2 * sizeof(float) + sizeof(float2)) + (2 * (size_t)nb + 1) * sizeof(float) +
-           12 * sizeof(float2);
-}
-
-// The node kernel on load, the axis-0 inverse transform, then the radix-4 stage
-// of axis 1 (see above) into plane plane0 + jj.  Block b handles tile b % tiles
-// and node share b / tiles of nsplit.
-template <int N0, bool DERIV>
-__global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
-    k_fz_nodes4(const float2* __restrict__ rbG, float2* __restrict__ XY, FzTab tb, const double* __restrict__ knode,
-                const double* __restrict__ invk, int j0, int nb, int plane0, int tiles, int nsplit, Geo geo,
-                FzDims d, const float2* __restrict__ tw0, const float2* __restrict__ tw1, float invN) {
-    constexpr int E = kFzColE, T = N0 / E, L = kFzLines;
-    constexpr int XCH = fz::col_slots(N0) > N0 * kFzX ? fz::col_slots(N0) : N0 * kFzX;
-    extern __shared__ float2 fz_sm[];
-    float2* sm = fz_sm;
-    float2* sz = fz_sm + XCH;
-    float* sq = reinterpret_cast<float*>(sz + N0 * L);
-    float* siq = sq + N0 * L;
-    float* sik = siq + N0 * L;
-    float* sk2 = sik + nb;
-    const int tile = blockIdx.x % tiles, part = blockIdx.x / tiles;
-    const int per = (nb + nsplit - 1) / nsplit;
-    const int s0 = part * per, s1 = min(nb, s0 + per);
-    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
-        const double k = knode[j0 + q];
-        sik[q] = (float)invk[j0 + q];
-        sk2[q] = (float)(k * k);
-    }
-    const int l = threadIdx.x % L, t = threadIdx.x / L;
-    int k1, k2, kk, q;
-    bool nyq;
-    fz4_tile(d, tile, l, k1, k2, kk, q, nyq);
-    const long long gbase = (long long)k1 * (d.H + 1) + k2, gstride = (long long)d.n1 * (d.H + 1);
-#pragma unroll 4
-    for (int e = 0; e < E; ++e) {
-        const int k0 = t + T * e;
-        const int sidx = k0 * L + l;
-        float2 a = __ldg(rbG + gbase + k0 * gstride);
-        a = make_float2(a.x * invN, a.y * invN);
-        const float q2 = gsq_f(geo, k0, k1, k2);
-        if (k0 == 0 && k1 == 0 && k2 == 0) a = make_float2(0.0f, 0.0f);
-        sz[sidx] = a;
-        sq[sidx] = sqrtf(q2);
-        siq[sidx] = q2 > 0.0f ? 1.0f / q2 : 0.0f;
-    }
-    float2 twr[fz::tw_count<N0, E>()];
-    fz::tw_load<N0, E>(twr, t, tw0);
-    // radix-4 stage: thread tau combines the pairs p = tau + N0 h (h = 0, 1) of
-    // (i0, cp) = (p >> 1, p & 1), i.e. lines c = 2 cp, 2 cp + 1 of every s
-    const int kkq = nyq ? 4 * q : kk;  // kk of line c = 0 (c adds to it on Nyquist tiles)
-    // e^{-2 pi i kk r/n1} of line c (r = 1..3) at stw[3 c + r - 1]
-    float2* stw = reinterpret_cast<float2*>(sk2 + nb);  // 8-byte aligned: 2 N0 L + 2 nb floats from sq
-    if (threadIdx.x < 12) {
-        const int c = threadIdx.x / 3, r = threadIdx.x % 3 + 1;
-        stw[threadIdx.x] = __ldg(tw1 + (nyq ? kkq + c : kkq) * r);
-    }
-    __syncthreads();
-    float qmin = INFINITY;
-#pragma unroll
-    for (int e = 0; e < E; ++e) qmin = fminf(qmin, sq[(t + T * e) * L + l]);
-    qmin = fz_warp_min(qmin);
-    for (int jj = s0; jj < s1; ++jj) {
-        const float ik = sik[jj], kj2 = sk2[jj];
-        float2 v[E];
-        auto scale = [&](auto near) {
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int sidx = (t + T * e) * L + l;
-                const float kv = fz_node_kernel<DERIV, decltype(near)::value>(tb, sq[sidx], ik, siq[sidx], kj2);
-                const float f = DERIV ? kv * ik : kv;
-                const float2 z = sz[sidx];
-                v[e] = make_float2(f * z.x, f * z.y);
-            }
-        };
-        if (qmin * ik < tb.eta_series) scale(std::true_type());
-        else scale(std::false_type());
-        __syncthreads();  // the exchange buffer is free
-        fz::line_fft_r<N0, E, +1>(v, sm + l, fz::ColIdx(), t, twr);
-        __syncthreads();  // every thread has read the transform's last exchange
-#pragma unroll
-        for (int e = 0; e < E; ++e) sm[(t + T * e) * kFzX + l] = v[e];
-        __syncthreads();
-        float2* outp = XY + (long long)(plane0 + jj) * d.plane;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int p = threadIdx.x + N0 * h;
-            const int i0 = p >> 1, cp = p & 1;
-            float2 x[2][4];
-#pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                const float4 pr = *reinterpret_cast<const float4*>(sm + i0 * kFzX + 4 * s + 2 * cp);
-                x[0][s] = make_float2(pr.x, pr.y);
-                x[1][s] = make_float2(pr.z, pr.w);
-            }
-#pragma unroll
-            for (int cc = 0; cc < 2; ++cc) {
-                fz::dft4<+1>(x[cc]);
-#pragma unroll
-                for (int r = 1; r < 4; ++r) x[cc][r] = fz::cmulc(x[cc][r], stw[3 * (2 * cp + cc) + r - 1]);
-            }
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                long long o;
-                if (!nyq) o = ((long long)i0 * d.n1 + kk + kFzQ * r) * d.H + 4 * q + 2 * cp;
-                else o = d.nyq + (long long)i0 * d.n1 + kkq + 2 * cp + kFzQ * r;
-                __stcs(reinterpret_cast<float4*>(outp + o), make_float4(x[0][r].x, x[0][r].y, x[1][r].x, x[1][r].y));
-            }
-        }
-    }
-}
-
-// 64-point inverse transform of the Nyquist column by lanes 0..7 of one warp
-// (radix 8 x 8, in place in 64 shared slots, __syncwarp only): the input is
-// sm[0..63]; lane t returns elements t + 8 e of the output in v[e].
-__device__ __forceinline__ void fz_warp_col64(float2 (&v)[8], float2* sm, int t, const float2* __restrict__ tq) {
-#pragma unroll
-    for (int e = 0; e < 8; ++e) v[e] = sm[t + 8 * e];
-    __syncwarp(0xffu);
-    fz::dft8<+1>(v);
-#pragma unroll
-    for (int r = 0; r < 8; ++r) sm[8 * t + r] = v[r];
-    __syncwarp(0xffu);
-#pragma unroll
-    for (int e = 0; e < 8; ++e) v[e] = sm[t + 8 * e];
-    __syncwarp(0xffu);
-#pragma unroll
-    for (int r = 1; r < 8; ++r) v[r] = fz::cmulc(v[r], __ldg(tq + r * t));
-    fz::dft8<+1>(v);
-}
-
-// shared memory of k_fz_c2r_cl (m nodes staged)
-inline size_t fz_cl_smem(int m) {
-    constexpr int NC = 128 / kFzCl, STAGE = kFzQ * NC + kFzQ, XB = kFzQ * (NC + 1);
-    constexpr int ROWS = kFzRowThreads / (128 / kFzRowE);
-    using Lay = fz::RowLayout<128>;
-    return 16 + (size_t)(2 * STAGE + 2 * XB + ROWS * Lay::slots + ROWS * Lay::slots1 + kFzQ) * sizeof(float2) +
-           (size_t)5 * m * sizeof(float);
-}
-
-// C2R consumer of the split path (n1 = 256, n2 = 256): a cluster of kFzCl
-// blocks per (i0, r).  Block c of the cluster
-//   1. receives z_r[kk][k2] for kk < Q and its 32 columns k2 in [32 c, 32 c + 32)
-//      (the last block also the Nyquist column) by bulk copy, two planes ahead;
-//   2. transforms them along kk (Q-point inverse), giving y[4m + r] per column;
-//   3. after a cluster barrier, gathers rows m in [16 c, 16 c + 16) of all 129
-//      columns from the four blocks' shared memory;
-//   4. runs the axis-2 C2R of those 16 rows (i1 = 4m + r) and interpolates them
-//      into pot (pot1 from the P planes, pot3 from the M planes, SMALL as in
-//      k_fz_c2r_rows).
-// The block-local results of step 2 sit in one of two buffers used in turn, so
-// one cluster barrier per plane suffices: a block overwrites a buffer only after
-// the next plane's barrier, which every block passes after its gather from it.
-template <bool SMALL>
-__global__ void __cluster_dims__(kFzCl, 1, 1) __launch_bounds__(kFzRowThreads, 2)
-    k_fz_c2r_cl(FzRowArgs a, int plane0, float* __restrict__ pot, const float2* __restrict__ tq) {
-    constexpr int H = 128, E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
-    constexpr int NC = H / kFzCl;          // columns per block
-    constexpr int XP = NC + 1;             // row pitch of the exchange buffer (+ the Nyquist column)
-    constexpr int CE = 8, CT = kFzQ / CE;  // column transform: 8 points per thread, CT threads per column
-    constexpr int STAGE = kFzQ * NC + kFzQ, XB = kFzQ * XP;
-    static_assert(NC * CT == kFzRowThreads, "one thread per (column, eighth of a column)");
-    static_assert(ROWS * kFzCl == kFzQ, "the cluster's rows are the Q rows of one (i0, r)");
-    using Lay = fz::RowLayout<H>;
-    namespace cg = cooperative_groups;
-    cg::cluster_group cluster = cg::this_cluster();
-    const int crank = (int)cluster.block_rank();
-    const bool last = crank == kFzCl - 1;
-    const int cl = blockIdx.x / kFzCl;
-    const int i0 = cl >> 2, r = cl & 3;
-    extern __shared__ float4 fz_rsm4[];
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(fz_rsm4);
-    float2* stage = reinterpret_cast<float2*>(fz_rsm4 + 1);
-    float2* X = stage + 2 * STAGE;
-    float2* buf0 = X + 2 * XB;
-    float2* buf1 = buf0 + ROWS * Lay::slots;
-    float2* nyqsm = buf1 + ROWS * Lay::slots1;
-    float* fs = reinterpret_cast<float*>(nyqsm + kFzQ);
-    const int tid = threadIdx.x, lane = tid & 31;
-    const long long prow0 = (long long)i0 * kFzN1 + kFzQ * r;  // plane row of kk = 0
-    __shared__ volatile int fail_flag;
-    volatile int* fail = &fail_flag;
-    int last_issued = -1;  // lane 0 of warp 0: the last plane whose copies it issued
-    auto issue = [&](int jj) {  // warp 0
-        const int s = jj & 1;
-        const float2* src = a.XY + (long long)(plane0 + jj) * a.d.plane;
-        if (lane == 0) fz::mbar_expect_tx(&bar[s], (kFzQ * NC + (last ? kFzQ : 0)) * (unsigned)sizeof(float2));
-        __syncwarp();
-        for (int kk = lane; kk < kFzQ; kk += 32)
-            fz::bulk_load(stage + s * STAGE + kk * NC, src + (prow0 + kk) * H + crank * NC,
-                          NC * (unsigned)sizeof(float2), &bar[s]);
-        if (last && lane == 0)
-            fz::bulk_load(stage + s * STAGE + kFzQ * NC, src + a.d.nyq + prow0, kFzQ * (unsigned)sizeof(float2),
-                          &bar[s]);
-    };
-    if (tid == 0) {
-        fail_flag = 0;
-        fz::mbar_init(&bar[0], 1);
-        fz::mbar_init(&bar[1], 1);
-        fz::mbar_fence_init();
-    }
-    __syncwarp();
-    if (tid < 32) {
-        issue(0);
-        if (a.nb > 1) issue(1);
-        last_issued = a.nb > 1 ? 1 : 0;
-    }
-    const FzNodeSm nodes = fz_stage_nodes(a, fs);
-    __syncthreads();
-    // row phase: thread (l, t), row l of the block's 16
-    const int t = tid % T, l = tid / T;
-    const long long row = (long long)i0 * kFzN1 + 4 * (crank * ROWS + l) + r;
-    const int n2 = 2 * H;
-    float2* b0 = buf0 + l * Lay::slots;
-    float2* b1 = buf1 + l * Lay::slots1;
-    const typename Lay::Idx ix;
-    const typename Lay::Idx1 ix1;
-    const float clipdn = __double2float_rd(a.kfclip);
-    const float2* kfrow = reinterpret_cast<const float2*>(a.kf + row * n2) + t;
-    float fi[P], tr[P], acc[P];
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const float2 kk2 = __ldg(kfrow + T * e);
-        fz_interval_state(kk2.x, a, nodes, clipdn, fi[2 * e], tr[2 * e]);
-        fz_interval_state(kk2.y, a, nodes, clipdn, fi[2 * e + 1], tr[2 * e + 1]);
-        acc[2 * e] = acc[2 * e + 1] = 0.0f;
-    }
-    float2 twr[fz::tw_count<H, E>()];
-    fz::tw_load<H, E>(twr, t, a.tw.th);
-    // column phase: thread (col, ct), elements ct + CT e of column col
-    const int col = tid % NC, ct = tid / NC;
-    struct XIdx {
-        __device__ __forceinline__ int operator()(int n) const { return n * XP; }
-    };
-    float2* S = buf0;  // the gathered rows: [ROWS][H], then their Nyquist values [ROWS]
-    for (int jj = 0; jj < a.nb; ++jj) {
-        const int j = a.j0 + jj;
-        const int s = jj & 1;
-        if (!*fail && !fz::mbar_wait(&bar[s], (jj >> 1) & 1)) {
-            *fail = 1;
-            atomicOr(a.err, 1u);
-        }
-        const float2* st = stage + s * STAGE;
-        float2 u[CE];
-#pragma unroll
-        for (int e = 0; e < CE; ++e) u[e] = st[(ct + CT * e) * NC + col];
-        const bool nyqw = last && tid < CT;
-        if (nyqw) {  // the Nyquist column leaves the stage before the stage is refilled
-#pragma unroll
-            for (int e = 0; e < CE; ++e) nyqsm[tid + CT * e] = st[kFzQ * NC + tid + CT * e];
-        }
-        __syncthreads();  // stage s is read
-        if (tid < 32) {  // warp 0 decides as one (lane 0's view of the flag), then issues together
-            const bool go = __shfl_sync(0xffffffffu, jj + 2 < a.nb && !*fail, 0);
-            if (go) {
-                fz::fence_proxy_async();
-                issue(jj + 2);
-                last_issued = jj + 2;
-            }
-        }
-        float2* Xb = X + s * XB;
-        fz::line_fft<kFzQ, CE, +1>(u, Xb + col, XIdx(), ct, tq);
-        __syncthreads();  // the transform's last exchange is read
-#pragma unroll
-        for (int e = 0; e < CE; ++e) Xb[(ct + CT * e) * XP + col] = u[e];
-        if (nyqw) {
-            float2 un[CE];
-            fz_warp_col64(un, nyqsm, tid, tq);
-#pragma unroll
-            for (int e = 0; e < CE; ++e) Xb[(tid + CT * e) * XP + NC] = un[e];
-        }
-        cluster.sync();  // every block's Xb is complete
-        for (int idx = tid; idx < ROWS * (H + 1); idx += kFzRowThreads) {
-            int lr, k, owner, cc;
-            if (idx < ROWS * H) {
-                lr = idx / H;
-                k = idx % H;
-                owner = k / NC;
-                cc = k % NC;
-            } else {
-                lr = idx - ROWS * H;
-                k = H;
-                owner = kFzCl - 1;
-                cc = NC;
-            }
-            const float2* peer = cluster.map_shared_rank(Xb, owner);
-            S[k < H ? lr * H + k : ROWS * H + lr] = peer[(crank * ROWS + lr) * XP + cc];
-        }
-        __syncthreads();
-        float2 v[E];
-        fz_c2r_pre<H>(S, l, t, a.tw.tr, v);
-        __syncthreads();  // S (the first exchange buffer of the row transform) is read
-        fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, ix1, t, twr);
-        const float jf = (float)j;
-#pragma unroll
-        for (int qq = 0; qq < P; ++qq) {
-            const float pv = (qq & 1) ? v[qq >> 1].y : v[qq >> 1].x;
-            acc[qq] = fmaf(fz_hat(jf, fi[qq], tr[qq]), pv, acc[qq]);
-        }
-        if (SMALL && j == 0) {
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const float2 kk2 = __ldg(kfrow + T * e);
-                acc[2 * e] = fmaf(fz_small_weight(kk2.x, a, nodes, clipdn, true), v[e].x, acc[2 * e]);
-                acc[2 * e + 1] = fmaf(fz_small_weight(kk2.y, a, nodes, clipdn, true), v[e].y, acc[2 * e + 1]);
-            }
-        }
-    }
-    cluster.sync();  // no block leaves while a peer may still read its exchange buffers
-    if (tid == 0 && *fail) {
-        for (int qq = (last_issued > 0 ? last_issued - 1 : 0); qq <= last_issued; ++qq)
-            fz::mbar_wait(&bar[qq & 1], (qq >> 1) & 1);
-    }
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-        float2* p = reinterpret_cast<float2*>(pot + row * n2) + t + T * e;
-        float2 o = make_float2(acc[2 * e], acc[2 * e + 1]);
-        if (!a.first) {
-            const float2 old = *p;
-            o = make_float2(old.x + o.x, old.y + o.y);
-        }
-        *p = o;
-    }
-}

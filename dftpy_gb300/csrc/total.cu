@@ -766,7 +766,7 @@ __global__ void k_zero(T* p, long long n) {
 
 }  // namespace
 
-#include "lwt_fused.cuh"
+#include "lwt_split.cuh"
 
 // ------------------------------------------------------------------ handle
 struct ofdft_eval {
@@ -1027,7 +1027,7 @@ void fz_tables(ofdft_eval* e) {
     if (e->fz_tw) return;
     const ofdft_grid* g = e->g;
     const int n0 = g->nr[0], n1 = g->nr[1], n2 = g->nr[2], H = n2 / 2;
-    std::vector<float2> h((size_t)n0 + n1 + 2 * (size_t)H + kFzQ);
+    std::vector<float2> h((size_t)n0 + n1 + 2 * (size_t)H + 32);
     auto fill = [&](size_t off, int count, int n) {
         for (int k = 0; k < count; ++k) {
             const double a = -2.0 * M_PI * (double)k / (double)n;
@@ -1038,7 +1038,7 @@ void fz_tables(ofdft_eval* e) {
     fill((size_t)n0, n1, n1);
     fill((size_t)n0 + n1, H, H);
     fill((size_t)n0 + n1 + H, H, n2);
-    fill((size_t)n0 + n1 + 2 * (size_t)H, kFzQ, kFzQ);  // the Q-point column transforms of the split path
+    fill((size_t)n0 + n1 + 2 * (size_t)H, 32, 32);  // the 32-point stage of the split path
     OFDFT_CK(cudaMalloc(&e->fz_tw, h.size() * sizeof(float2)));
     upload_now(e->fz_tw, h.data(), h.size() * sizeof(float2));
     OFDFT_CK(cudaMalloc(&e->d_fz_err, sizeof(unsigned)));
@@ -1147,32 +1147,31 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
         ra.tw = tw;
         ra.err = e->d_fz_err;
         if (split) {
-            // axis 0 + the radix-4 stage of axis 1, then the cluster consumer
+            // axis 0 + the radix-8 stage of axis 1, then the 32-point stage with the rows
             with_col(n0, [&](auto c0) {
                 constexpr int N0 = decltype(c0)::value;
-                const size_t smem = fz4_gen_smem(N0, nb);
+                const size_t smem = fz8_nodes_smem(N0, nb);
                 auto launch = [&](auto kern, int plane0) {
                     fz_smem_optin(kern, smem);
-                    timed(e, P_LWT_NODES, Ncd * 8.0 * (nsplit + nb), st, [&] {
-                        kern<<<tiles0 * nsplit, kFzLines * (N0 / kFzColE), smem, st>>>(
-                            r.rbG, XY, tb, knode, invk, j0, nb, plane0, tiles0, nsplit, g->geo, d, tw.t0, tw.t1,
-                            invN);
+                    timed(e, P_LWT_NODES, Ncd * 8.0 * (1 + nb), st, [&] {
+                        kern<<<fz8_tiles(H), kS8L * (N0 / kFzColE), smem, st>>>(
+                            r.rbG, XY, tb, knode, invk, j0, nb, plane0, g->geo, d, tw.t0, tw.t1, invN);
                     });
                     OFDFT_LAUNCH_CHECK();
                 };
-                launch(k_fz_nodes4<N0, false>, 0);
-                if (mc) launch(k_fz_nodes4<N0, true>, nb);
+                launch(k_fz_n8<N0, false>, 0);
+                if (mc) launch(k_fz_n8<N0, true>, nb);
             });
-            const size_t smem = fz_cl_smem(r.m);
-            const int grid = n0 * 4 * kFzCl;
+            const size_t smem = fz8_row_smem(r.m, 2);
+            const int grid = n0 * 8;
             auto launch = [&](auto kern, int plane0, float* pot) {
                 fz_smem_optin(kern, smem);
                 timed(e, P_LWT_INTERP, Ncd * 8.0 * nb + Nd * 4.0 * (1 + (first ? 1 : 2)), st,
-                      [&] { kern<<<grid, kFzRowThreads, smem, st>>>(ra, plane0, pot, tw.tq); });
+                      [&] { kern<<<grid, kS8RowThreads, smem, st>>>(ra, plane0, pot); });
                 OFDFT_LAUNCH_CHECK();
             };
-            launch(k_fz_c2r_cl<true>, 0, r.pot1);
-            if (mc) launch(k_fz_c2r_cl<false>, nb, r.pot3);
+            launch(k_fz_c2r_s8<true>, 0, r.pot1);
+            if (mc) launch(k_fz_c2r_s8<false>, nb, r.pot3);
             launches += mc ? 4 : 2;
         }
         if (!split) with_col(n0, [&](auto c0) {
@@ -1218,7 +1217,27 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
             // then axis 0 into pot2(G)
             FzRowArgs ra2 = ra;
             ra2.XY = XY2;
-            with_row(H, [&](auto ch) {
+            if (split) {
+                // hat weights, axis 2 and the 32-point stage of axis 1; then the
+                // radix-8 stage, axis 0 and the sum into pot2(G)
+                const size_t smem = fz8_row_smem(r.m, 1);
+                fz_smem_optin(k_fz_r2c_s8, smem);
+                timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st2,
+                      [&] { k_fz_r2c_s8<<<n0 * 8, kS8RowThreads, smem, st2>>>(ra2); });
+                OFDFT_LAUNCH_CHECK();
+                with_col(n0, [&](auto c0) {
+                    constexpr int N0 = decltype(c0)::value;
+                    const size_t smem0 = fz8_pot2_smem(N0, nb);
+                    fz_smem_optin(k_fz_pot2_s8<N0>, smem0);
+                    timed(e, P_LWT_POT2, Ncd * 8.0 * (nb + (first ? 1 : 2)), st2, [&] {
+                        k_fz_pot2_s8<N0><<<fz8_tiles(H), kS8L * (N0 / kFzColE), smem0, st2>>>(
+                            XY2, r.pot2G, tb, knode, invk, j0, nb, first ? 1 : 0, g->geo, d, tw.t0, invN);
+                    });
+                });
+                OFDFT_LAUNCH_CHECK();
+                launches += 2;
+            }
+            if (!split) with_row(H, [&](auto ch) {
                 constexpr int HH = decltype(ch)::value;
                 constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
                 const size_t smem = fz_row_smem(HH, r.m, false);
@@ -1228,14 +1247,14 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
                       [&] { k_fz_r2c_rows<HH><<<grid, kFzRowThreads, smem, st2>>>(ra2); });
             });
             OFDFT_LAUNCH_CHECK();
-            with_col(n1, [&](auto c1) {
+            if (!split) with_col(n1, [&](auto c1) {
                 constexpr int N1 = decltype(c1)::value;
                 const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
                 timed(e, P_FZ_AXIS1, Ncd * 16.0 * nb, st2,
                       [&] { k_fz_axis1<N1, -1><<<tiles1 * nb, N1, smem, st2>>>(XY2, d, tw.t1); });
             });
             OFDFT_LAUNCH_CHECK();
-            with_col(n0, [&](auto c0) {
+            if (!split) with_col(n0, [&](auto c0) {
                 constexpr int N0 = decltype(c0)::value;
                 const size_t smem = fz_col_smem(N0, nb, false);
                 fz_smem_optin(k_fz_pot2<N0>, smem);
@@ -1245,7 +1264,7 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
                 });
             });
             OFDFT_LAUNCH_CHECK();
-            launches += 3;
+            if (!split) launches += 3;
         }
     }
     if (two) {
@@ -1504,8 +1523,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         bool fused = false;
         if (c.lwt_pipeline != OFDFT_LWT_PIPE_CUFFT) {
             fused = c.lwt_family == OFDFT_LWT_FAMILY_LWT && fz_applies(g, hermite, m);
-            OFDFT_REQUIRE(c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT ||
-                              (g->nr[1] == kFzN1 && g->nr[2] == 256),
+            OFDFT_REQUIRE(c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT || (g->nr[1] == 256 && g->nr[2] == 256),
                           "FUSED_SPLIT k_F-node pipeline: needs n1 = n2 = 256");
             OFDFT_REQUIRE(fused || (c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED && c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT),
                           "fused k_F-node pipeline: needs a float32 grid, linear interpolation, at most %d nodes and "

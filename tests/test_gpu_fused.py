@@ -9,9 +9,9 @@ The cases cover every tile-FFT length the fused path instantiates (columns
 32..256, rows 16..256), kdd 1, 2 and 3, node batches that accumulate into
 pot1/pot3/pot2 over several passes, and user k_F bounds that put points in the
 small-k_F branch of the first node and clip the largest k_F; on n1 = n2 = 256
-grids the split variant (the axis-1 transform of the C2R chain split between
-the axis-0 pass and a cluster row pass), which must also agree with the
-three-pass pipeline.
+grids the split variant (the axis-1 transform of both chains factored as
+radix 8 x 32 between their column and row passes, so no axis-1 plane pass),
+which must also agree with the three-pass pipeline.
 """
 import numpy as np
 import pytest
@@ -37,7 +37,7 @@ CASES = [
     ((128, 128, 128), 64, 3, {}),
     ((64, 64, 64), 32, 3, {"max_batch": 7}),
     ((64, 64, 64), 24, 3, {"kfmin": "lift", "kfmax": "cut"}),
-    # n1 = n2 = 256: the C2R chain with axis 1 split between its two passes
+    # n1 = n2 = 256: both chains with axis 1 split between their two passes
     ((32, 256, 256), 16, 3, {}),
     ((64, 256, 256), 24, 3, {"max_batch": 7}),
     ((32, 256, 256), 12, 2, {"kfmin": "lift", "kfmax": "cut"}),
@@ -92,10 +92,10 @@ def test_fused_repeatable_bitwise():
 
 @pytest.mark.parametrize("nr,nsp,kdd", [((32, 256, 256), 16, 3), ((64, 256, 256), 64, 3)])
 def test_split_axis1_matches_three_passes(nr, nsp, kdd):
-    """The split C2R chain (radix-4 stage in the axis-0 pass, Q-point transforms
-    in a 4-block cluster) and the three-pass chain compute the same float32
-    transforms in a different order: same energy and potential to float32
-    round-off, and the split path is bitwise repeatable."""
+    """The split chains (a radix-8 stage of axis 1 in the column passes, its
+    32-point stage in the row passes) and the three-pass chains compute the
+    same float32 transforms in a different order: same energy and potential to
+    float32 round-off, and the split path is bitwise repeatable."""
     lat, rho = _density(nr, seed=7)
     grid = D.DirectGrid(lat, nr)
     e3, v3 = _run(grid, rho, torch.float32, "fused", nsp, kdd, {})

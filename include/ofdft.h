@@ -114,9 +114,11 @@ enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
  * not apply.  FUSED folds the node kernel, the interpolation and the pot2 sum
  * into the library's own tile FFTs; CUFFT runs them as separate passes around
  * batched cuFFT transforms.  Both compute the same quantities.  FUSED_SPLIT
- * (grids with n1 = n2 = 256 only) is FUSED with the axis-1 transform of the C2R
- * chain split between its axis-0 pass and a four-block cluster row pass, so that
- * chain has no axis-1 plane pass. */
+ * (grids with n1 = n2 = 256 only) is FUSED with the axis-1 transform of both
+ * chains factored as radix 8 x 32 between their column and row passes, so
+ * neither chain has an axis-1 plane pass and each node plane crosses HBM twice;
+ * it moves half the DRAM bytes of FUSED but runs slower on GB300 (its column
+ * tiles take a whole SM each), so AUTO does not take it. */
 enum { OFDFT_LWT_PIPE_AUTO = 0, OFDFT_LWT_PIPE_CUFFT = 1, OFDFT_LWT_PIPE_FUSED = 2, OFDFT_LWT_PIPE_FUSED_SPLIT = 3 };
 /* kernel table of the k_F-node kernel (lwt.py:535-548): the WT table
  * (kernel.py:344-352, LWT) or the MGP table (kernel.py:267-322; LMGP, and with

@@ -598,11 +598,15 @@ def ground_state(D, pp, grid, rho_np, nat, nsp):
     ``--workload gs-linear``) and fixed k_F bounds.
 
     FP64 reference: FP64 L-BFGS to econv 1e-12 Ha/atom.  The plain FP64 path at
-    the bars: FP64 L-BFGS to econv 1e-10 Ha/atom.  FP32-mixed: FP32 L-BFGS to
-    econv 1e-9 Ha/atom, then FP32 L-BFGS on the derivative-only line search
-    until the float32 residual stops falling (150 iterations), then one FP64 E+V
-    of that density; and, for comparison, FP32 L-BFGS then FP64 L-BFGS to econv
-    1e-10 Ha/atom."""
+    the bars: FP64 L-BFGS to econv 1e-10 Ha/atom, once with the reference's line
+    searches (first trial step theta = 1) and once with every line search
+    started at the direction's own length (the quasi-Newton step); the faster
+    of the two that meets the force bar is the FP64 time (``f64_baseline``).
+    FP32-mixed (``f32_mixed``): FP32 L-BFGS to econv 1e-9 Ha/atom, then FP32
+    L-BFGS on the derivative-only line search until the float32 residual stops
+    falling (150 iterations), both with the direction start, then one FP64 E+V
+    of that density; for comparison the same with the reference's first steps,
+    and FP32 L-BFGS then FP64 L-BFGS to econv 1e-10 Ha/atom."""
     import torch
     tot, kfb = _gs_functional(D, pp, rho_np, nsp, "hermite")
     res = {"functional": "the headline 64-node k_F kernel (WGC alpha/beta, kdd 3) with Hermite interpolation, fixed "
@@ -622,9 +626,10 @@ def ground_state(D, pp, grid, rho_np, nat, nsp):
         torch.cuda.synchronize()
         return r, time.perf_counter() - t0
 
-    def opt(ec):
+    def opt(ec, start="reference"):
         return D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
-                              optimization_options={"econv": ec * nat, "maxiter": 600, "maxfun": 50})
+                              optimization_options={"econv": ec * nat, "maxiter": 600, "maxfun": 50,
+                                                    "linesearch_start": start})
 
     def info(o):
         return {"niter": o.result.niter, "nfev": o.result.nfev, "dP": o.result.dP, "converged": int(o.converged)}
@@ -634,12 +639,22 @@ def ground_state(D, pp, grid, rho_np, nat, nsp):
     e_ref, f_ref = float(o.functional.energy), tot.get_forces(r_ref)
     res["f64_reference"] = dict(info(o), seconds=t_ref, energy=e_ref,
                                 what="FP64 L-BFGS to econv 1e-12 Ha/atom")
-    o = opt(1e-10)
-    r64, t64 = solve(lambda: o.optimize_rho(guess_rho=rho0))
-    res["f64"] = dict(info(o), seconds=t64, what="FP64 L-BFGS to econv 1e-10 Ha/atom (the plain FP64 path at the "
-                                                  "bars)", dE_per_atom_vs_reference=(float(o.functional.energy)
-                                                                                     - e_ref) / nat,
-                      force_max_abs_vs_reference=float(np.abs(tot.get_forces(r64) - f_ref).max()))
+    f64_routes = {}
+    for key, start, what in (("f64", "reference", "FP64 L-BFGS to econv 1e-10 Ha/atom, line searches from theta = 1 "
+                                                 "(the reference's algorithm in FP64)"),
+                             ("f64_direction_start", "direction", "FP64 L-BFGS to econv 1e-10 Ha/atom, each line "
+                                                                  "search from the direction's own length")):
+        o = opt(1e-10, start)
+        r64, t64 = solve(lambda: o.optimize_rho(guess_rho=rho0))
+        res[key] = dict(info(o), seconds=t64, what=what,
+                        dE_per_atom_vs_reference=(float(o.functional.energy) - e_ref) / nat,
+                        force_max_abs_vs_reference=float(np.abs(tot.get_forces(r64) - f_ref).max()))
+        f64_routes[key] = t64
+    # the FP32-mixed routes are timed against the faster FP64 route at the bars
+    best64 = min((k for k in f64_routes if res[k]["force_max_abs_vs_reference"] <= 1e-5), key=f64_routes.get,
+                 default="f64")
+    t64 = f64_routes[best64]
+    res["f64_baseline"] = best64
 
     def mixed(key, fn, what):
         o = opt(1e-10)
@@ -653,16 +668,21 @@ def ground_state(D, pp, grid, rho_np, nat, nsp):
                     "speedup_vs_f64": t64 / tm, "speedup_vs_f64_reference_route": t_ref / tm}
 
     mixed("f32_mixed", lambda o: o.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-9 * nat, refine="evaluate",
-                                                      f32_polish={"maxiter": 150}),
-          "FP32 L-BFGS (econv 1e-9 Ha/atom), FP32 L-BFGS on the derivative line search (150 iterations), one FP64 "
-          "E+V")
+                                                      f32_options={"linesearch_start": "direction"},
+                                                      f32_polish={"maxiter": 150, "linesearch_start": "direction"}),
+          "FP32 L-BFGS (econv 1e-9 Ha/atom), FP32 L-BFGS on the derivative line search (150 iterations), both "
+          "starting each line search at the direction's own length, one FP64 E+V")
+    mixed("f32_mixed_reference_start", lambda o: o.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-9 * nat,
+                                                                      refine="evaluate",
+                                                                      f32_polish={"maxiter": 150}),
+          "as f32_mixed with the reference's first trial steps")
     mixed("f32_mixed_f64_lbfgs", lambda o: o.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-9 * nat,
                                                                 refine="optimize"),
           "FP32 L-BFGS (econv 1e-9 Ha/atom), then FP64 L-BFGS to econv 1e-10 Ha/atom")
     m = res["f32_mixed"]
     res["speedup"] = m["speedup_vs_f64"]
     res["bars_met"] = bool(abs(m["dE_per_atom_vs_reference"]) <= 1e-6 and m["force_max_abs_vs_reference"] <= 1e-5
-                           and res["f64"]["force_max_abs_vs_reference"] <= 1e-5 and res["speedup"] >= 3.0)
+                           and res[best64]["force_max_abs_vs_reference"] <= 1e-5 and res["speedup"] >= 3.0)
     return res
 
 

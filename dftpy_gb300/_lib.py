@@ -58,7 +58,7 @@ class OptOptions(C.Structure):
         ("method", C.c_int), ("maxiter", C.c_int), ("maxfun", C.c_int), ("maxls", C.c_int), ("ncheck", C.c_int),
         ("maxcor", C.c_int), ("econv", C.c_double), ("c1", C.c_double), ("c2", C.c_double), ("xtol", C.c_double),
         ("h0", C.c_double), ("verbose", C.c_int), ("batch_persistent", C.c_int),
-        ("pconv", C.c_double), ("ls_grad", C.c_int),
+        ("pconv", C.c_double), ("ls_grad", C.c_int), ("ls_start", C.c_int),
     ]
 
 

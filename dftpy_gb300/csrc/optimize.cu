@@ -535,7 +535,8 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
     // float64; float32 fields cannot resolve it, so the mixed path uses 1e-4
     const double eps = sizeof(T) == 8 ? 1.0e-9 : 1.0e-4;
     int converged = 2, it = 0, nfev = 1;
-    double last_stp = 0.0;  // the derivative search's last accepted step
+    double last_stp = 0.0;    // the derivative search's last accepted step
+    double last_scale = 0.0;  // ls_start: the last accepted step over its direction's length (0: none yet)
     for (it = 1; it < o.maxiter; ++it) {
         if (o.method == OFDFT_OPT_DIIS) {
             // The reference's DIIS (optimization.py:327-333, :429-441, :471-485):
@@ -693,12 +694,15 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
                 op.lincomb(p, -1.0, rsd);
             }
         }
+        // the direction's length before normalisation: the quasi-Newton (L-BFGS) or
+        // Newton (TN) step along it, the first trial step when ls_start = 1
         double theta0 = op.orth_norm(p, phi);
-        (void)theta0;
+        bool natural = o.ls_start == 1 && (o.method == OFDFT_OPT_LBFGS || o.method == OFDFT_OPT_TN);
         if (op.dtheta(V, phi, p, phi, 1.0, 0.0) * 2.0 > 0) {
             // uphill: steepest descent (optimization.py:373-380)
             op.lincomb(p, -1.0, rsd);
             op.orth_norm(p, phi);
+            natural = false;
         }
         // ---- line search on theta (ValueAndDerivative, optimization.py:228-280)
         double lastE = NAN, last_theta = NAN;
@@ -714,11 +718,18 @@ void optimize_t(ofdft_eval* e, T* rho_io, const ofdft_opt_options& o, ofdft_opt_
         const double g0 = 2.0 * op.dtheta(V, phi, p, phi, 1.0, 0.0) * dV;
         double stp, fnew, gnew;
         int nls = 0;
-        // the derivative search starts from twice the last accepted step (0.1 at first), within pi/4
-        bool ok = o.ls_grad ? grad_search(phi_fn, g0, last_stp > 0.0 ? 2.0 * last_stp : 0.1, o.c2, M_PI / 4, 20, stp,
-                                          fnew, gnew, nls)
-                            : wolfe1(phi_fn, E, g0, 1.0, o.c1, o.c2, M_PI, 0.0, o.xtol, 100, stp, fnew, gnew, nls);
+        // first trial step: the reference's 1.0 for the energy search; twice the last accepted
+        // step (0.1 at first) for the derivative search; with ls_start = 1, once a step has been
+        // accepted, the direction's length theta0 times the last accepted step's ratio to its
+        // direction's length (the quasi-Newton step with its scale corrected), within each
+        // search's bound (pi or pi/4)
+        const bool nat = natural && theta0 > 0.0 && std::isfinite(theta0) && last_scale > 0.0;
+        const double s0w = nat ? std::min(theta0 * last_scale, M_PI) : 1.0;
+        const double s0g = nat ? std::min(theta0 * last_scale, M_PI / 4) : (last_stp > 0.0 ? 2.0 * last_stp : 0.1);
+        bool ok = o.ls_grad ? grad_search(phi_fn, g0, s0g, o.c2, M_PI / 4, 20, stp, fnew, gnew, nls)
+                            : wolfe1(phi_fn, E, g0, s0w, o.c1, o.c2, M_PI, 0.0, o.xtol, 100, stp, fnew, gnew, nls);
         if (ok) last_stp = stp;
+        if (ok && natural && theta0 > 0.0 && std::isfinite(theta0)) last_scale = stp / theta0;
         nfev += nls;
         if (!ok || nls == 0 || stp != last_theta) {
             converged = 1;  // "Line-Search Failed" (optimization.py:444-448)
@@ -1287,7 +1298,7 @@ template <typename T>
 void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_options& o, const double* econv,
                       ofdft_opt_result* res, void** v_out, cudaStream_t st) {
     OFDFT_REQUIRE(o.method == OFDFT_OPT_LBFGS, "ofdft_optimize_batch: only L-BFGS is batched");
-    OFDFT_REQUIRE(o.pconv == 0.0 && o.ls_grad == 0,
+    OFDFT_REQUIRE(o.pconv == 0.0 && o.ls_grad == 0 && o.ls_start == 0,
                   "ofdft_optimize_batch: the residual criterion and the derivative line search are not batched");
     OFDFT_REQUIRE(o.maxcor >= 0 && 2 * (o.maxcor + 1) <= kBF - BF_LB0, "ofdft_optimize_batch: maxcor too large");
     Batch<T> b;
@@ -1624,6 +1635,7 @@ void ofdft_opt_default(ofdft_opt_options* o) {
     o->batch_persistent = 0;
     o->pconv = 0.0;
     o->ls_grad = 0;
+    o->ls_start = 0;
 }
 
 int ofdft_optimize_v(ofdft_eval* e, void* rho, const ofdft_opt_options* o, ofdft_opt_result* r, void* v_out,

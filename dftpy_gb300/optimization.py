@@ -32,7 +32,7 @@ class Optimization:
         self.optimization_options = dict(optimization_options or {})
         defaults = {"maxcor": 6, "ftol": 1.0e-7, "xtol": 1.0e-12, "maxfun": 50, "maxiter": 200, "maxls": 30,
                     "econv": 1.0e-5, "c1": 1e-4, "c2": 0.2, "algorithm": "EMM", "vector": "Orthogonalization",
-                    "ncheck": 2, "h0": 1.0, "pconv": None, "linesearch": "wolfe"}
+                    "ncheck": 2, "h0": 1.0, "pconv": None, "linesearch": "wolfe", "linesearch_start": "reference"}
         for k, v in defaults.items():
             self.optimization_options.setdefault(k, v)
         if EnergyEvaluator is None:
@@ -81,6 +81,11 @@ class Optimization:
         if o["linesearch"] not in ("wolfe", "grad"):
             raise ValueError("linesearch must be 'wolfe' (the reference's) or 'grad'")
         s.ls_grad = 1 if o["linesearch"] == "grad" else 0
+        # not in the reference either: L-BFGS and TN may start each line search at the
+        # direction's own length (the quasi-Newton step) instead of theta = 1
+        if o["linesearch_start"] not in ("reference", "direction"):
+            raise ValueError("linesearch_start must be 'reference' or 'direction'")
+        s.ls_start = 1 if o["linesearch_start"] == "direction" else 0
         return s
 
     def optimize_rho(self, guess_rho=None, guess_phi=None, lphi=False, lsfun="line_search", dtype=None):

@@ -370,6 +370,15 @@ typedef struct {
      * a uniform density.  Defaults 0 and 0. */
     double pconv;
     int ls_grad;
+    /* Not in the reference (whose searches start at theta = 1): ls_start = 1
+     * starts the line searches of L-BFGS and TN, from the second iteration on,
+     * at the length of the search direction before its normalisation (the
+     * quasi-Newton or Newton step along it) times the previous accepted step's
+     * ratio to its direction's length, capped at the search's bound; 0
+     * (default) keeps the reference's start (and twice the last accepted step
+     * for ls_grad).  The same sizeof as without it: it fills the padding after
+     * ls_grad. */
+    int ls_start;
 } ofdft_opt_options;
 typedef struct {
     int converged;            /* 0 converged, 1 line search failed, 2 max steps (optimization.py:444-516) */

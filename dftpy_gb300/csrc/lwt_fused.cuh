@@ -6,6 +6,9 @@
 //   pot1 (+)= linear interpolation of P over each point's k_F interval
 //   pot3 (+)= the same interpolation of M                          (kdd = 3)
 //   pot2(G) (+)= sum_j K_j(G) FFT(rho^alpha W_j)(G)/N              (kdd > 1)
+// or, with the cubic Hermite interpolation, pot1 and pot3 from both P and M
+// and pot2(G) (+)= sum_j K_j FFT(rho^alpha W_j)/N + K'_j/k_j FFT(rho^alpha WD_j)/N
+// with the Hermite basis weights W_j, WD_j (fz_hermite_w)
 // with the node kernel, the interpolation and the hat weights folded into
 // hand-written tile FFTs, so the node planes cross HBM three times each
 // instead of five and no real-space plane is stored:
@@ -284,13 +287,13 @@ struct FzRowArgs {
     unsigned* err;  // set to 1 when a copy into shared memory did not complete in time
 };
 
-// Node bounds of the interval search in float32, staged per block (5 m floats):
+// Node bounds of the interval search in float32, staged per block (6 m floats):
 //   kdn  = kn rounded down:  kn < kf  <=> kdn < kf,  kf <= kn <=> kf <= kdn
 //   kupu = kup rounded up:   kf < kup <=> kf < kupu
-//   khi + klo = kn (two floats), iw = 1/(kn[i+1] - kn[i])
-// for float32 kf.  iw[m-1] holds 1/kn[0] (the small-k_F coordinate).
+//   khi + klo = kn (two floats), iw = 1/(kn[i+1] - kn[i]), dk = kn[i+1] - kn[i]
+// for float32 kf.  iw[m-1] holds 1/kn[0] (the small-k_F coordinate), dk[m-1] 0.
 struct FzNodeSm {
-    const float *kdn, *kupu, *khi, *klo, *iw;
+    const float *kdn, *kupu, *khi, *klo, *iw, *dk;
 };
 
 __device__ __forceinline__ FzNodeSm fz_stage_nodes(const FzRowArgs& a, float* s) {
@@ -303,6 +306,7 @@ __device__ __forceinline__ FzNodeSm fz_stage_nodes(const FzRowArgs& a, float* s)
         s[2 * m + q] = hi;
         s[3 * m + q] = __double2float_rn(k - (double)hi);
         s[4 * m + q] = __double2float_rn(q + 1 < m ? 1.0 / (a.kn[q + 1] - k) : 1.0 / a.kn[0]);
+        s[5 * m + q] = q + 1 < m ? __double2float_rn(a.kn[q + 1] - k) : 0.0f;
     }
     FzNodeSm n;
     n.kdn = s;
@@ -310,7 +314,29 @@ __device__ __forceinline__ FzNodeSm fz_stage_nodes(const FzRowArgs& a, float* s)
     n.khi = s + 2 * m;
     n.klo = s + 3 * m;
     n.iw = s + 4 * m;
+    n.dk = s + 5 * m;
     return n;
+}
+
+// Cubic Hermite weights of node j at a point of interval coordinate t whose
+// interval starts at j (lo) or ends at j (hi), as the reference forms them
+// (lwt.py:275-306, h00 = 2t^3 - 3t^2 + 1, h01 = 1 - h00, h10 = t^3 - 2t^2 + t,
+// h11 = t^3 - t^2 and their t-derivatives): for the P planes w1 = h00 | h01 and
+// w3 = h00' / D0 | h01' / D1; for the M planes w1 = D0 h10 | D1 h11 and
+// w3 = h10' | h11'; D0 = k_{j+1} - k_j, D1 = k_j - k_{j-1}; zero elsewhere.
+template <bool MPLANE>
+__device__ __forceinline__ void fz_hermite_w(float t, bool lo, bool hi, float D0, float D1, float iD0, float iD1,
+                                             float& w1, float& w3) {
+    if constexpr (!MPLANE) {
+        const float h00 = fmaf(t * t, fmaf(2.0f, t, -3.0f), 1.0f);
+        const float hd = 6.0f * t * (t - 1.0f);  // h00'; h01' = -h00'
+        w1 = lo ? h00 : (hi ? 1.0f - h00 : 0.0f);
+        w3 = lo ? hd * iD0 : (hi ? -hd * iD1 : 0.0f);
+    } else {
+        const float u = t * (t - 1.0f);
+        w1 = lo ? D0 * (u * (t - 1.0f)) : (hi ? D1 * (u * t) : 0.0f);
+        w3 = lo ? (3.0f * t - 1.0f) * (t - 1.0f) : (hi ? t * (3.0f * t - 2.0f) : 0.0f);
+    }
 }
 
 // Interval membership of the reference (lwt.py:252-306) in float32 with the
@@ -407,7 +433,7 @@ __device__ __forceinline__ void fz_c2r_pre(const float2* st, int l, int t, const
 inline size_t fz_row_smem(int H, int m, bool with_stages) {
     const int T = H / kFzRowE, ROWS = kFzRowThreads / T;
     const size_t slots = (H + (H >> 4) + 1) + (H + 8 * (H >> 6) + 1);
-    size_t b = 16 + (size_t)ROWS * slots * sizeof(float2) + (size_t)5 * m * sizeof(float);
+    size_t b = 16 + (size_t)ROWS * slots * sizeof(float2) + (size_t)6 * m * sizeof(float);
     if (with_stages) b += 2 * (size_t)(ROWS * H + ROWS) * sizeof(float2);
     return b;
 }
@@ -417,7 +443,10 @@ inline size_t fz_row_smem(int H, int m, bool with_stages) {
 // P planes, pot3 from the M planes (SMALL: the small-k_F branch of node 0
 // counts, which it does for pot1 only).  The block's rows of each plane (16 KB
 // at n2 = 256) arrive by bulk copy two planes ahead of their use.
-template <int H, bool SMALL>
+// HERM = 1 (P planes) or 2 (M planes): the cubic Hermite interpolation, whose
+// P and M planes both feed pot1 and (kdd = 3) pot3 (fz_hermite_w); `pot` is
+// then unused, and the M pass adds to what the P pass of the batch wrote.
+template <int H, bool SMALL, int HERM = 0>
 __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, int plane0, float* __restrict__ pot) {
     constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
     constexpr int STAGE = ROWS * H + ROWS;  // float2: the block's rows, then their Nyquist values
@@ -463,15 +492,19 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
     const float clipdn = __double2float_rd(a.kfclip);
     const float2* kfrow = reinterpret_cast<const float2*>(a.kf + row * n2) + t;
     float fi[P], tr[P], acc[P];
+    float acc3[HERM ? P : 1];
+    const bool has3 = HERM && a.pot3 != nullptr;  // pot3 exists for kdd = 3 only
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const float2 kk = __ldg(kfrow + T * e);
         fz_interval_state(kk.x, a, nodes, clipdn, fi[2 * e], tr[2 * e]);
         fz_interval_state(kk.y, a, nodes, clipdn, fi[2 * e + 1], tr[2 * e + 1]);
         acc[2 * e] = acc[2 * e + 1] = 0.0f;
+        if constexpr (HERM != 0) acc3[2 * e] = acc3[2 * e + 1] = 0.0f;
     }
-    float2 twr[fz::tw_count<H, E>()];
-    fz::tw_load<H, E>(twr, t, a.tw.th);
+    // register twiddles, except for the Hermite passes (their second accumulator takes the registers)
+    float2 twr[HERM ? 1 : fz::tw_count<H, E>()];
+    if constexpr (HERM == 0) fz::tw_load<H, E>(twr, t, a.tw.th);
     for (int jj = 0; jj < a.nb; ++jj) {
         const int j = a.j0 + jj;
         const int s = jj & 1;
@@ -485,7 +518,8 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
         }
         float2 v[E];
         fz_c2r_pre<H>(stage + s * STAGE, l, t, a.tw.tr, v);
-        fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, ix1, t, twr);
+        if constexpr (HERM == 0) fz::line_fft_ppr<H, E, +1>(v, b0, b1, ix, ix1, t, twr);
+        else fz::line_fft_pp<H, E, +1>(v, b0, b1, ix, t, a.tw.th);
         // every thread has passed the transform's first barrier, so stage s is read
         if (threadIdx.x == 0 && jj + 2 < a.nb && !*fail) {
             fz::fence_proxy_async();
@@ -493,10 +527,24 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
             last_issued = jj + 2;
         }
         const float jf = (float)j;
+        if constexpr (HERM == 0) {
 #pragma unroll
-        for (int q = 0; q < P; ++q) {
-            const float pv = (q & 1) ? v[q >> 1].y : v[q >> 1].x;
-            acc[q] = fmaf(fz_hat(jf, fi[q], tr[q]), pv, acc[q]);
+            for (int q = 0; q < P; ++q) {
+                const float pv = (q & 1) ? v[q >> 1].y : v[q >> 1].x;
+                acc[q] = fmaf(fz_hat(jf, fi[q], tr[q]), pv, acc[q]);
+            }
+        } else {
+            const float D0 = nodes.dk[j], D1 = j > 0 ? nodes.dk[j - 1] : 0.0f;
+            const float iD0 = D0 > 0.0f ? 1.0f / D0 : 0.0f, iD1 = D1 > 0.0f ? 1.0f / D1 : 0.0f;
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const float pv = (q & 1) ? v[q >> 1].y : v[q >> 1].x;
+                const float dd = jf - fi[q];
+                float w1, w3;
+                fz_hermite_w<HERM == 2>(tr[q], dd == 0.0f, dd == 1.0f, D0, D1, iD0, iD1, w1, w3);
+                acc[q] = fmaf(w1, pv, acc[q]);
+                if (has3) acc3[q] = fmaf(w3, pv, acc3[q]);
+            }
         }
         if (SMALL && j == 0) {
 #pragma unroll
@@ -512,15 +560,29 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
         for (int q = (last_issued > 0 ? last_issued - 1 : 0); q <= last_issued; ++q)
             fz::mbar_wait(&bar[q & 1], (q >> 1) & 1);
     }
+    // the P pass of a first batch writes; every other pass adds
+    const bool add = !a.first || HERM == 2;
+    float* const pot1 = HERM ? a.pot1 : pot;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-        float2* p = reinterpret_cast<float2*>(pot + row * n2) + t + T * e;
+        float2* p = reinterpret_cast<float2*>(pot1 + row * n2) + t + T * e;
         float2 o = make_float2(acc[2 * e], acc[2 * e + 1]);
-        if (!a.first) {
+        if (add) {
             const float2 old = *p;
             o = make_float2(old.x + o.x, old.y + o.y);
         }
         *p = o;
+        if constexpr (HERM != 0) {
+            if (has3) {
+                float2* p3 = reinterpret_cast<float2*>(a.pot3 + row * n2) + t + T * e;
+                float2 o3 = make_float2(acc3[2 * e], acc3[2 * e + 1]);
+                if (add) {
+                    const float2 old = *p3;
+                    o3 = make_float2(old.x + o3.x, old.y + o3.y);
+                }
+                *p3 = o3;
+            }
+        }
     }
 }
 
@@ -528,7 +590,10 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_c2r_rows(FzRowArgs a, i
 // The post-processing pairs (k, H-k) are exchanged between the row's threads
 // with shuffles: element H-k of thread t's slot e sits in thread (T - t) % T,
 // slot E-1-e (t > 0) or in thread 0, slot (E-e) % E (t = 0).
-template <int H>
+// HERM: the cubic Hermite interpolation's two hat planes per node, rho^alpha
+// times h00 | h01 into plane jj and rho^alpha times D0 h10 | D1 h11 into plane
+// nb + jj (lwt.py:285-296; fz_hermite_w's w1 of the P and M planes).
+template <int H, bool HERM = false>
 __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
     constexpr int E = kFzRowE, T = H / E, ROWS = kFzRowThreads / T, P = 2 * E;
     static_assert(T <= 32, "a row must fit in one warp");
@@ -551,36 +616,35 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
     const int partner = (lane & ~(T - 1)) | ((T - t) & (T - 1));
     const float2* kfrow = reinterpret_cast<const float2*>(a.kf + row * n2) + t;
     const float2* rarow = reinterpret_cast<const float2*>(a.rA + row * n2) + t;
-    float fi[P], tr[P], ra[P];
+    // rho^alpha of the thread's points in registers (with the Hermite planes: read again per node)
+    float fi[P], tr[P], ra_r[HERM ? 1 : P];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const float2 kk = __ldg(kfrow + T * e);
-        const float2 rr = __ldg(rarow + T * e);
         fz_interval_state(kk.x, a, nodes, clipdn, fi[2 * e], tr[2 * e]);
         fz_interval_state(kk.y, a, nodes, clipdn, fi[2 * e + 1], tr[2 * e + 1]);
-        ra[2 * e] = rr.x;
-        ra[2 * e + 1] = rr.y;
-    }
-    float2 twr[fz::tw_count<H, E>()];
-    fz::tw_load<H, E>(twr, t, a.tw.th);
-    for (int jj = 0; jj < a.nb; ++jj) {
-        const int j = a.j0 + jj;
-        const float jf = (float)j;
-        float2 v[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e)
-            v[e] = make_float2(ra[2 * e] * fz_hat(jf, fi[2 * e], tr[2 * e]),
-                               ra[2 * e + 1] * fz_hat(jf, fi[2 * e + 1], tr[2 * e + 1]));
-        if (j == 0) {
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const float2 kk = __ldg(kfrow + T * e);
-                v[e].x = fmaf(ra[2 * e], fz_small_weight(kk.x, a, nodes, clipdn, false), v[e].x);
-                v[e].y = fmaf(ra[2 * e + 1], fz_small_weight(kk.y, a, nodes, clipdn, false), v[e].y);
-            }
+        if constexpr (!HERM) {
+            const float2 rr = __ldg(rarow + T * e);
+            ra_r[2 * e] = rr.x;
+            ra_r[2 * e + 1] = rr.y;
         }
-        fz::line_fft_ppr<H, E, -1>(v, b0, b1, ix, ix1, t, twr);
-        float2* dst = a.XY + (long long)jj * a.d.plane;
+    }
+    auto ra = [&](int q) {
+        if constexpr (HERM) {
+            const float2 rr = __ldg(rarow + T * (q >> 1));
+            return (q & 1) ? rr.y : rr.x;
+        } else {
+            return ra_r[q];
+        }
+    };
+    // register twiddles, except with the Hermite planes (the two transforms per node take the registers)
+    float2 twr[HERM ? 1 : fz::tw_count<H, E>()];
+    if constexpr (!HERM) fz::tw_load<H, E>(twr, t, a.tw.th);
+    // the row transform of v, post-processed and stored into plane pl
+    auto emit = [&](float2 (&v)[E], int pl) {
+        if constexpr (!HERM) fz::line_fft_ppr<H, E, -1>(v, b0, b1, ix, ix1, t, twr);
+        else fz::line_fft_pp<H, E, -1>(v, b0, b1, ix, t, a.tw.th);
+        float2* dst = a.XY + (long long)pl * a.d.plane;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int k = t + T * e;
@@ -596,13 +660,58 @@ __global__ void __launch_bounds__(kFzRowThreads, 2) k_fz_r2c_rows(FzRowArgs a) {
             __stcs(dst + row * H + k, make_float2(A.x + wB.y, A.y - wB.x));
         }
         if (t == 0) __stcs(dst + a.d.nyq + row, make_float2(v[0].x - v[0].y, 0.0f));
+    };
+    for (int jj = 0; jj < a.nb; ++jj) {
+        const int j = a.j0 + jj;
+        const float jf = (float)j;
+        float2 v[E];
+        float D0 = 0.0f, D1 = 0.0f;
+        if constexpr (HERM) {
+            D0 = nodes.dk[j];
+            D1 = j > 0 ? nodes.dk[j - 1] : 0.0f;
+        }
+        // hat weight of node j at point q: linear, or the P planes' w1 of the Hermite interpolation
+        auto wP = [&](int q) {
+            if constexpr (HERM) {
+                const float dd = jf - fi[q];
+                float w1, w3;
+                fz_hermite_w<false>(tr[q], dd == 0.0f, dd == 1.0f, D0, D1, 0.0f, 0.0f, w1, w3);
+                return w1;
+            } else {
+                return fz_hat(jf, fi[q], tr[q]);
+            }
+        };
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = make_float2(ra(2 * e) * wP(2 * e), ra(2 * e + 1) * wP(2 * e + 1));
+        if (j == 0) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const float2 kk = __ldg(kfrow + T * e);
+                v[e].x = fmaf(ra(2 * e), fz_small_weight(kk.x, a, nodes, clipdn, false), v[e].x);
+                v[e].y = fmaf(ra(2 * e + 1), fz_small_weight(kk.y, a, nodes, clipdn, false), v[e].y);
+            }
+        }
+        emit(v, jj);
+        if constexpr (HERM) {
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const float dd = jf - fi[q];
+                float w1, w3;
+                fz_hermite_w<true>(tr[q], dd == 0.0f, dd == 1.0f, D0, D1, 0.0f, 0.0f, w1, w3);
+                if (q & 1) v[q >> 1].y = ra(q) * w1;
+                else v[q >> 1].x = ra(q) * w1;
+            }
+            emit(v, a.nb + jj);
+        }
     }
 }
 
 // Axis-0 forward transform of the batch's planes, K_j(G)/N applied and summed
 // into pot2(G) (lwt.py:266-296; the sum starts from the previous batches').
-// K_j(0) = 0: the G = 0 element keeps its starting value.
-template <int N0>
+// K_j(0) = 0: the G = 0 element keeps its starting value.  HERM: plane nb + jj
+// (the Hermite interpolation's second hat plane) adds K'_j(G)/k_j/N times its
+// transform, the M planes' kernel.
+template <int N0, bool HERM = false>
 __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
     k_fz_pot2(const float2* __restrict__ XY, float2* __restrict__ pot2G, FzTab tb, const double* __restrict__ knode,
               const double* __restrict__ invk, int j0, int nb, int first, Geo geo, FzDims d,
@@ -624,7 +733,7 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
     long long pbase, pstride, gbase, gstride;
     fz_axis0_tile(d, blockIdx.x, l, k1, k2, pbase, pstride, gbase, gstride);
     float2 acc[E];
-#pragma unroll 4
+#pragma unroll
     for (int e = 0; e < E; ++e) {
         const int k0 = t + T * e;
         const int s = k0 * L + l;
@@ -635,8 +744,9 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
     }
     const bool g0 = (t == 0 && k1 == 0 && k2 == 0);
     const float2 acc00 = acc[0];
-    float2 twr[fz::tw_count<N0, E>()];
-    fz::tw_load<N0, E>(twr, t, tw);
+    // register twiddles, except with the Hermite planes (two transforms per node)
+    float2 twr[HERM ? 1 : fz::tw_count<N0, E>()];
+    if constexpr (!HERM) fz::tw_load<N0, E>(twr, t, tw);
     float qmin = INFINITY;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -644,29 +754,59 @@ __global__ void __launch_bounds__(kFzLines * (N0 / kFzColE), 2)
         qmin = fminf(qmin, sqrtf(gsq_f(geo, k0, k1, k2)));
     }
     qmin = fz_warp_min(qmin);
-    for (int jj = 0; jj < nb; ++jj) {
-        const float2* inp = XY + (long long)jj * d.plane + pbase;
+    // plane pl transformed along axis 0, times the node kernel of node jj (DERIV: K'_j/k_j), into acc
+    auto accumulate = [&](int pl, int jj, auto deriv) {
+        constexpr bool DERIV = decltype(deriv)::value;
+        const float2* inp = XY + (long long)pl * d.plane + pbase;
         float2 v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = __ldcs(inp + (t + T * e) * pstride);
         __syncthreads();  // the exchange buffer is free; the node and |G| tables are staged
-        fz::line_fft_r<N0, E, -1>(v, sm + l, fz::ColIdx(), t, twr);
+        if constexpr (!HERM) fz::line_fft_r<N0, E, -1>(v, sm + l, fz::ColIdx(), t, twr);
+        else fz::line_fft<N0, E, -1>(v, sm + l, fz::ColIdx(), t, tw);
         const float ik = sik[jj], kj2 = sk2[jj];
-        float f[E];
-        auto factors = [&](auto near) {
+        if constexpr (!HERM) {
+            float f[E];
+            auto factors = [&](auto near) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const int s = (t + T * e) * L + l;
+                    const float kv = fz_node_kernel<DERIV, decltype(near)::value>(tb, sq[s], ik, siq[s], kj2);
+                    f[e] = (DERIV ? kv * ik : kv) * invN;
+                }
+            };
+            // warp-uniform: does any point of this warp need the spline for node j?
+            if (qmin * ik < tb.eta_series) factors(std::true_type());
+            else factors(std::false_type());
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const int s = (t + T * e) * L + l;
-                f[e] = fz_node_kernel<false, decltype(near)::value>(tb, sq[s], ik, siq[s], kj2) * invN;
+                acc[e].x = fmaf(f[e], v[e].x, acc[e].x);
+                acc[e].y = fmaf(f[e], v[e].y, acc[e].y);
             }
-        };
-        // warp-uniform: does any point of this warp need the spline for node j?
-        if (qmin * ik < tb.eta_series) factors(std::true_type());
-        else factors(std::false_type());
+        } else {
+            // each factor goes into the sum at once (fewer live registers beside two transforms per node)
+            auto factors = [&](auto near) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            acc[e].x = fmaf(f[e], v[e].x, acc[e].x);
-            acc[e].y = fmaf(f[e], v[e].y, acc[e].y);
+                for (int e = 0; e < E; ++e) {
+                    const int s = (t + T * e) * L + l;
+                    const float kv = fz_node_kernel<DERIV, decltype(near)::value>(tb, sq[s], ik, siq[s], kj2);
+                    const float f = (DERIV ? kv * ik : kv) * invN;
+                    acc[e].x = fmaf(f, v[e].x, acc[e].x);
+                    acc[e].y = fmaf(f, v[e].y, acc[e].y);
+                }
+            };
+            if (qmin * ik < tb.eta_series) factors(std::true_type());
+            else factors(std::false_type());
+        }
+    };
+    if constexpr (!HERM) {
+        for (int jj = 0; jj < nb; ++jj) accumulate(jj, jj, std::false_type());
+    } else {
+        // one loop body over the 2 nb planes (node jj's planes jj and nb + jj in turn)
+        for (int pp = 0; pp < 2 * nb; ++pp) {
+            const int jj = pp >> 1;
+            if (pp & 1) accumulate(nb + jj, jj, std::true_type());
+            else accumulate(jj, jj, std::false_type());
         }
     }
     if (g0) acc[0] = acc00;

@@ -70,7 +70,7 @@ inline size_t fz8_pot2_smem(int n0, int nb) { return fz8_nodes_smem(n0, nb); }
 inline size_t fz8_row_smem(int m, int stages) {
     using Lay = fz::RowLayout<128>;
     return 16 + (size_t)stages * (kS8Rows * 128 + kS8Rows) * sizeof(float2) +
-           (size_t)kS8Rows * (Lay::slots + Lay::slots1) * sizeof(float2) + (size_t)5 * m * sizeof(float);
+           (size_t)kS8Rows * (Lay::slots + Lay::slots1) * sizeof(float2) + (size_t)6 * m * sizeof(float);
 }
 
 // The 32-point transform (sign S) along the row index of a staged row block

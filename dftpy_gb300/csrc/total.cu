@@ -987,13 +987,13 @@ struct LwtPlan {
 };
 
 // ------------------------------------------------ fused k_F-node pipeline (host)
-constexpr int kFzMaxNodes = 1024;  // node bounds (5 floats each) staged in shared memory
+constexpr int kFzMaxNodes = 1024;  // node bounds (6 floats each) staged in shared memory
 constexpr int kFzMaxBatch = 256;   // node reciprocals staged in shared memory
 
-bool fz_applies(const ofdft_grid* g, bool hermite, int m) {
+bool fz_applies(const ofdft_grid* g, int m) {
     auto p2 = [](int n, int lo, int hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; };
-    return g->prec == OFDFT_F32 && !hermite && m <= kFzMaxNodes && p2(g->nr[0], 32, 256) &&
-           p2(g->nr[1], 32, 256) && p2(g->nr[2], 32, 512);
+    return g->prec == OFDFT_F32 && m <= kFzMaxNodes && p2(g->nr[0], 32, 256) && p2(g->nr[1], 32, 256) &&
+           p2(g->nr[2], 32, 512);
 }
 
 // column lengths (axes 0 and 1)
@@ -1060,6 +1060,7 @@ struct FzRun {
     Table<float> tab;
     Nodes nd;
     int m, kdd;
+    bool hermite;  // cubic Hermite interpolation (else linear)
     double kfclip;
 };
 
@@ -1092,10 +1093,14 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     // the C2R chain with axis 1 split between its two passes (no axis-1 plane pass)
     const bool split = e->cfg.lwt_pipeline == OFDFT_LWT_PIPE_FUSED_SPLIT;
     const size_t cb = g->cplx_bytes();
-    const bool mc = r.kdd == 3;  // M planes feed pot3 only
-    // planes per node: P (and M) for the C2R chain, one more for the R2C chain,
+    // M planes: pot3 (kdd = 3), and pot1 with the Hermite interpolation
+    const bool mc = r.kdd == 3 || r.hermite;
+    OFDFT_REQUIRE(!(split && r.hermite), "FUSED_SPLIT k_F-node pipeline: linear interpolation only");
+    // hat planes per node of the R2C chain: one, two with the Hermite interpolation
+    const int hp = r.kdd > 1 ? (r.hermite ? 2 : 1) : 0;
+    // planes per node: P (and M) for the C2R chain, hp more for the R2C chain,
     // which runs on a second stream at the same time and needs its own planes
-    const int per_node = (mc ? 2 : 1) + (r.kdd > 1 ? 1 : 0);
+    const int per_node = (mc ? 2 : 1) + hp;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     int B = c.lwt_max_batch > 0 ? c.lwt_max_batch : 64;
@@ -1104,7 +1109,7 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
     if (fit < B) B = (int)std::max(1LL, fit);
     B = std::min(B, r.m);
     float2* XY = (float2*)e->sc.get("lwtXY", (size_t)(mc ? 2 : 1) * B * cb);
-    float2* XY2 = r.kdd > 1 ? (float2*)e->sc.get("lwtXY2", (size_t)B * cb) : nullptr;
+    float2* XY2 = r.kdd > 1 ? (float2*)e->sc.get("lwtXY2", (size_t)hp * B * cb) : nullptr;
     // the R2C chain (hat planes -> pot2) does not depend on the C2R chain (node
     // planes -> pot1/pot3): fork it onto the second stream, join before return.
     // With per-kernel profiling on, both chains stay on st so that each
@@ -1208,8 +1213,14 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
                       [&] { kern<<<grid, kFzRowThreads, smem, st>>>(ra, plane0, pot); });
                 OFDFT_LAUNCH_CHECK();
             };
-            launch(k_fz_c2r_rows<HH, true>, 0, r.pot1);
-            if (mc) launch(k_fz_c2r_rows<HH, false>, nb, r.pot3);
+            if (r.hermite) {
+                // P and M planes both feed pot1 and pot3
+                launch(k_fz_c2r_rows<HH, true, 1>, 0, r.pot1);
+                launch(k_fz_c2r_rows<HH, false, 2>, nb, r.pot1);
+            } else {
+                launch(k_fz_c2r_rows<HH, true>, 0, r.pot1);
+                if (mc) launch(k_fz_c2r_rows<HH, false>, nb, r.pot3);
+            }
         });
         if (!split) launches += mc ? 5 : 3;
         if (r.kdd > 1) {
@@ -1242,26 +1253,34 @@ int fz_run(ofdft_eval* e, const FzRun& r, cudaStream_t st) {
                 constexpr int ROWS = kFzRowThreads / (HH / kFzRowE);
                 const size_t smem = fz_row_smem(HH, r.m, false);
                 const int grid = (int)((long long)n0 * n1 / ROWS);
-                fz_smem_optin(k_fz_r2c_rows<HH>, smem);
-                timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * nb, st2,
-                      [&] { k_fz_r2c_rows<HH><<<grid, kFzRowThreads, smem, st2>>>(ra2); });
+                auto hat = [&](auto kern) {
+                    fz_smem_optin(kern, smem);
+                    timed(e, P_FZ_HAT, Nd * 8.0 + Ncd * 8.0 * hp * nb, st2,
+                          [&] { kern<<<grid, kFzRowThreads, smem, st2>>>(ra2); });
+                };
+                if (r.hermite) hat(k_fz_r2c_rows<HH, true>);
+                else hat(k_fz_r2c_rows<HH>);
             });
             OFDFT_LAUNCH_CHECK();
             if (!split) with_col(n1, [&](auto c1) {
                 constexpr int N1 = decltype(c1)::value;
                 const size_t smem = std::max(fz::col_slots(N1), kFzLines * fz::row_slots(N1)) * sizeof(float2);
-                timed(e, P_FZ_AXIS1, Ncd * 16.0 * nb, st2,
-                      [&] { k_fz_axis1<N1, -1><<<tiles1 * nb, N1, smem, st2>>>(XY2, d, tw.t1); });
+                timed(e, P_FZ_AXIS1, Ncd * 16.0 * hp * nb, st2,
+                      [&] { k_fz_axis1<N1, -1><<<tiles1 * hp * nb, N1, smem, st2>>>(XY2, d, tw.t1); });
             });
             OFDFT_LAUNCH_CHECK();
             if (!split) with_col(n0, [&](auto c0) {
                 constexpr int N0 = decltype(c0)::value;
                 const size_t smem = fz_col_smem(N0, nb, false);
-                fz_smem_optin(k_fz_pot2<N0>, smem);
-                timed(e, P_LWT_POT2, Ncd * 8.0 * (nb + (first ? 1 : 2)), st2, [&] {
-                    k_fz_pot2<N0><<<tiles0, kFzLines * (N0 / kFzColE), smem, st2>>>(
-                        XY2, r.pot2G, tb, knode, invk, j0, nb, first ? 1 : 0, g->geo, d, tw.t0, invN);
-                });
+                auto pot2 = [&](auto kern) {
+                    fz_smem_optin(kern, smem);
+                    timed(e, P_LWT_POT2, Ncd * 8.0 * (hp * nb + (first ? 1 : 2)), st2, [&] {
+                        kern<<<tiles0, kFzLines * (N0 / kFzColE), smem, st2>>>(
+                            XY2, r.pot2G, tb, knode, invk, j0, nb, first ? 1 : 0, g->geo, d, tw.t0, invN);
+                    });
+                };
+                if (r.hermite) pot2(k_fz_pot2<N0, true>);
+                else pot2(k_fz_pot2<N0>);
             });
             OFDFT_LAUNCH_CHECK();
             if (!split) launches += 3;
@@ -1522,11 +1541,11 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
         nd.invk = e->d_nodes + kMaxNodes;
         bool fused = false;
         if (c.lwt_pipeline != OFDFT_LWT_PIPE_CUFFT) {
-            fused = c.lwt_family == OFDFT_LWT_FAMILY_LWT && fz_applies(g, hermite, m);
+            fused = c.lwt_family == OFDFT_LWT_FAMILY_LWT && fz_applies(g, m);
             OFDFT_REQUIRE(c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT || (g->nr[1] == 256 && g->nr[2] == 256),
                           "FUSED_SPLIT k_F-node pipeline: needs n1 = n2 = 256");
             OFDFT_REQUIRE(fused || (c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED && c.lwt_pipeline != OFDFT_LWT_PIPE_FUSED_SPLIT),
-                          "fused k_F-node pipeline: needs a float32 grid, linear interpolation, at most %d nodes and "
+                          "fused k_F-node pipeline: needs a float32 grid, at most %d nodes and "
                           "power-of-two axes (32..256, the last 32..512)",
                           kFzMaxNodes);
         }
@@ -1543,6 +1562,7 @@ void compute_t(ofdft_eval* e, const T* rho, T* V, unsigned calc, double* energie
                 fr.nd = nd;
                 fr.m = m;
                 fr.kdd = kdd;
+                fr.hermite = hermite;
                 fr.kfclip = lp.kfclip;
                 launches += fz_run(e, fr, st);
                 e->fz_ran = true;

@@ -109,12 +109,13 @@ enum { OFDFT_GGA_LKT = 0, OFDFT_GGA_LKTVW, OFDFT_GGA_DK, OFDFT_GGA_LLP, OFDFT_GG
        OFDFT_GGA_GE2, OFDFT_GGA_GE4, OFDFT_GGA_PGSL, OFDFT_GGA_PGSLR, OFDFT_GGA_NFORMULAS };
 enum { OFDFT_INTERP_LINEAR = 0, OFDFT_INTERP_HERMITE = 1 };
 /* k_F-node kernel pipeline: AUTO takes FUSED where it applies (float32 grid,
- * linear interpolation, every axis a power of two in 32..256, the last axis
- * up to 512) and CUFFT otherwise; FUSED fails with OFDFT_EINVAL where it does
- * not apply.  FUSED folds the node kernel, the interpolation and the pot2 sum
- * into the library's own tile FFTs; CUFFT runs them as separate passes around
- * batched cuFFT transforms.  Both compute the same quantities.  FUSED_SPLIT
- * (grids with n1 = n2 = 256 only) is FUSED with the axis-1 transform of both
+ * the LWT family, every axis a power of two in 32..256, the last axis up to
+ * 512; linear or cubic Hermite interpolation) and CUFFT otherwise; FUSED fails
+ * with OFDFT_EINVAL where it does not apply.  FUSED folds the node kernel, the
+ * interpolation and the pot2 sum into the library's own tile FFTs; CUFFT runs
+ * them as separate passes around batched cuFFT transforms.  Both compute the
+ * same quantities.  FUSED_SPLIT (grids with n1 = n2 = 256 and the linear
+ * interpolation only) is FUSED with the axis-1 transform of both
  * chains factored as radix 8 x 32 between their column and row passes, so
  * neither chain has an axis-1 plane pass and each node plane crosses HBM twice;
  * it moves half the DRAM bytes of FUSED but runs slower on GB300 (its column

@@ -82,6 +82,8 @@ def parse():
     p.add_argument("--no-wgc", action="store_true", help="skip the two-body WGC kernel timing")
     p.add_argument("--no-extra", action="store_true",
                    help="skip the other configurations (c2, differentiation, relaxation, OE-SCF) in the default line")
+    p.add_argument("--interp", default="linear", choices=["linear", "hermite"],
+                   help="k_F interpolation of the E+V workload (the metric's configuration is linear)")
     p.add_argument("--lwt-pipeline", default="auto", choices=["auto", "cufft", "fused", "fused-split"],
                    help="k_F-node kernel pipeline: fused tile FFTs (auto where they apply) or cuFFT passes")
     p.add_argument("--workload", default="ev",
@@ -295,8 +297,8 @@ def reference_arm(args):
 
 def config(args, nat):
     return {"workload": "fcc Al %dx%dx%d (%d atoms), %d^3 grid, TF+vW+kF-node NL kernel (nsp=%d, kdd=3, "
-                        "linear, WGC alpha/beta) + LDA + Hartree + PME local PP + Ewald"
-                        % (args.reps, args.reps, args.reps, nat, args.n, args.nsp),
+                        "%s, WGC alpha/beta) + LDA + Hartree + PME local PP + Ewald"
+                        % (args.reps, args.reps, args.reps, nat, args.n, args.nsp, getattr(args, "interp", "linear")),
             "grid": [args.n] * 3, "atoms": nat, "nsp": args.nsp,
             "l2": "per-step working set (tens of GB) far exceeds the 126 MB L2; a 512 MB buffer is "
                   "written between timed steps",
@@ -342,7 +344,7 @@ def gpu_arm(args):
     grid = D.DirectGrid(lat, (args.n,) * 3)
     ions = D.Ions(symbols=["Al"] * nat, positions=pos, cell=lat)
     pp = D.LocalPseudo(grid=grid, ions=ions, PP_list={"Al": D.functional.RECPOT(r=gp, v=vp, zval=3)}, PME=True)
-    ke = D.Functional(type="KEDF", name="LWT", nsp=args.nsp, kdd=3, interp="linear", pipeline=args.lwt_pipeline,
+    ke = D.Functional(type="KEDF", name="LWT", nsp=args.nsp, kdd=3, interp=args.interp, pipeline=args.lwt_pipeline,
                       **WGC)
     tot = D.TotalFunctional(KineticEnergyFunctional=ke, XCFunctional=D.Functional(type="XC", name="LDA"),
                             HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
@@ -436,7 +438,9 @@ def gpu_arm(args):
                            (ksteps, r32p["ms_total"] / ksteps))
     s32 = 4
     n3 = args.n ** 3
-    algo_bytes = (2 * 198 + 3) * s32 * n3 if args.nsp == 64 else None
+    # n_FFT = 198 for the linear interpolation; the Hermite one adds 64 hat-plane R2C (262)
+    n_fft = 198 if args.interp == "linear" else 262
+    algo_bytes = (2 * n_fft + 3) * s32 * n3 if args.nsp == 64 else None
     if algo_bytes:
         # the whole evaluation as the unit: B = (2 n_FFT + 3) s N, the bytes of n_FFT out-of-place
         # transforms plus the pointwise passes, over the headline time per evaluation
@@ -447,8 +451,8 @@ def gpu_arm(args):
                            "frac": algo_bytes / (ms32 * 1e-3) / 1e9 / peak, "traffic": traffic,
                            "traffic_per_algorithmic_byte": traffic / algo_bytes,
                            "algorithmic_bytes": algo_bytes, "peak_source": src,
-                           "note": "B = (2*n_FFT+3)*s*N with n_FFT=198, s=4; traffic = each kernel class's bytes "
-                                   "times its ncu DRAM/algorithmic ratio (1 where none was measured)"}
+                           "note": "B = (2*n_FFT+3)*s*N with n_FFT=%d, s=4; traffic = each kernel class's bytes "
+                                   "times its ncu DRAM/algorithmic ratio (1 where none was measured)" % n_fft}
     else:
         out["roofline"] = out["roofline_dominant_kernel"]
     # ---- FP64 path
@@ -964,9 +968,10 @@ def batch_workload(args, emit=True):
         tot(D.DirectField(grid, data=rho0.numpy(), dtype=torch.float32))
         built.append((sd, nat, tot, rho0))
 
-    def opt(tot, nat):
+    def opt(tot, nat, start="reference"):
         return D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
-                              optimization_options={"econv": 1e-7 * nat, "maxiter": 500, "maxfun": 50})
+                              optimization_options={"econv": 1e-7 * nat, "maxiter": 500, "maxfun": 50,
+                                                    "linesearch_start": start})
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -980,20 +985,28 @@ def batch_workload(args, emit=True):
     # and precision allocates the optimizer's work fields, captures the
     # evaluation graphs and (persistent) tunes the launch shape, which a
     # repeated solve does not pay again
-    modes = [("batch_f64", torch.float64, None, False), ("batch_f32_mixed", torch.float32, "evaluate", False),
-             ("persistent_f64", torch.float64, None, True),
-             ("persistent_f32_mixed", torch.float32, "evaluate", True)]
-    for _, dt, refine, pers in modes:
-        optimize_rho_batch([opt(t, n) for _, n, t, _ in built], guesses, dtype=dt, refine=refine, persistent=pers)
+    modes = [("batch_f64", torch.float64, None, False, "reference"),
+             ("batch_f32_mixed", torch.float32, "evaluate", False, "reference"),
+             ("persistent_f64", torch.float64, None, True, "reference"),
+             ("persistent_f32_mixed", torch.float32, "evaluate", True, "reference"),
+             ("batch_f32_mixed_direction_start", torch.float32, "evaluate", False, "direction")]
+    for _, dt, refine, pers, start in modes:
+        optimize_rho_batch([opt(t, n, start) for _, n, t, _ in built], guesses, dtype=dt, refine=refine,
+                           persistent=pers)
     seq = [opt(t, n) for _, n, t, _ in built]
     t_seq, _ = timed(lambda: [o.optimize_rho(guess_rho=r) for o, r in zip(seq, guesses)])
+    seqd = [opt(t, n, "direction") for _, n, t, _ in built]
+    t_seqd, _ = timed(lambda: [o.optimize_rho(guess_rho=r) for o, r in zip(seqd, guesses)])
     n = len(built)
     out = {"workload": "batching: 64 systems (fcc/bcc/sc Al, 4-108 atoms, grids {48..96}^3), TF+vW+LDA+Hartree+PME "
                        "PP, L-BFGS from the uniform density to econv 1e-7 Ha/atom",
-           "systems": n, "sequential_f64": {"seconds": t_seq, "systems_per_s": n / t_seq}}
+           "systems": n, "sequential_f64": {"seconds": t_seq, "systems_per_s": n / t_seq},
+           "sequential_f64_direction_start": {"seconds": t_seqd, "systems_per_s": n / t_seqd,
+                                              "what": "the same solves with each line search started at the "
+                                                      "scaled length of the L-BFGS direction"}}
     runs = {}
-    for key, dt, refine, pers in modes:
-        os_ = [opt(t, nn) for _, nn, t, _ in built]
+    for key, dt, refine, pers, start in modes:
+        os_ = [opt(t, nn, start) for _, nn, t, _ in built]
         t, _ = timed(lambda: optimize_rho_batch(os_, guesses, dtype=dt, refine=refine, persistent=pers))
         runs[key] = os_
         dE = [(o.functional.energy - s1.functional.energy) / nn for o, s1, (_, nn, _, _) in zip(os_, seq, built)]
@@ -1009,6 +1022,8 @@ def batch_workload(args, emit=True):
                                                          "batch), FP32")
     out["speedup_batch_mixed_vs_sequential_f64"] = t_seq / out["batch_f32_mixed"]["seconds"]
     out["speedup_persistent_mixed_vs_sequential_f64"] = t_seq / out["persistent_f32_mixed"]["seconds"]
+    out["speedup_batch_mixed_direction_start_vs_sequential_f64_direction_start"] = (
+        t_seqd / out["batch_f32_mixed_direction_start"]["seconds"])
     out["systems_detail"] = [{"kind": sd["kind"], "atoms": nn, "grid": sd["nr"][0], "niter_f64": s1.result.niter}
                              for (sd, nn, _, _), s1 in zip(built, seq)]
     if emit:

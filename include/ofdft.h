@@ -377,8 +377,9 @@ typedef struct {
      * quasi-Newton or Newton step along it) times the previous accepted step's
      * ratio to its direction's length, capped at the search's bound; 0
      * (default) keeps the reference's start (and twice the last accepted step
-     * for ls_grad).  The same sizeof as without it: it fills the padding after
-     * ls_grad. */
+     * for ls_grad).  ofdft_optimize_batch applies it per system with the same
+     * results as the single solves.  The same sizeof as without it: it fills
+     * the padding after ls_grad. */
     int ls_start;
 } ofdft_opt_options;
 typedef struct {

@@ -855,7 +855,7 @@ struct BArgs {
 // L-BFGS coefficients and the per-system coefficients of the next field update,
 // so that the two-loop recursion and the normalisations run without the host.
 constexpr int kHist = kBF;  // alpha_i of the two-loop, by pair position
-enum ScRow { SC_D0 = 0, SC_D1, SC_NE, SC_MU, SC_NEL, SC_C0, SC_C1, SC_C2, SC_AL0, SC_LBRHO0 = SC_AL0 + kHist,
+enum ScRow { SC_D0 = 0, SC_D1, SC_NE, SC_MU, SC_NEL, SC_C0, SC_C1, SC_C2, SC_TH0, SC_AL0, SC_LBRHO0 = SC_AL0 + kHist,
              kSc = SC_LBRHO0 + kBF };
 
 __device__ __forceinline__ double* scrow(double* sc, int r) { return sc + (size_t)r * kBatchMax; }
@@ -889,9 +889,12 @@ __global__ void k_bscalar(const BTab<T>* __restrict__ tab, BArgs a, double* sc, 
             c1 = -(__dmul_rn(d1, dV) / ne);
             break;
         }
-        case OP_ORTH_N:  // p *= sqrt(Ne / ((p.p) dV))
-            c0 = sqrt(scrow(sc, SC_NE)[s] / __dmul_rn(d0, dV));
+        case OP_ORTH_N: {  // p *= sqrt(Ne / ((p.p) dV)); the direction's length sqrt((p.p) dV / Ne)
+            const double pn = __dmul_rn(d0, dV), ne = scrow(sc, SC_NE)[s];
+            scrow(sc, SC_TH0)[s] = sqrt(pn / ne);
+            c0 = sqrt(ne / pn);
             break;
+        }
         case OP_MU: {  // Nel = sum(rho) dV; mu = (V.rho) dV / Nel
             const double nel = __dmul_rn(d0, dV);
             const double mu = __dmul_rn(d1, dV) / nel;
@@ -1243,6 +1246,13 @@ struct Batch {
         OFDFT_LAUNCH_CHECK();
         return finish_row();
     }
+    // queues device scalar row `row` for the host, like a reduction's row
+    int queue_sc(int row) {
+        OFDFT_REQUIRE(rows < kMaxRound, "batched optimiser: too many scalars queued in one round");
+        OFDFT_CK(cudaMemcpyAsync(d_out + (size_t)rows * S, d_sc + (size_t)row * kBatchMax, (size_t)S * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
+        return rows++;
+    }
     // device-only reductions: the result stays in device scalar row `row`
     double* d_sc = nullptr;  // kSc x kBatchMax
     void fin_dev(int row) {
@@ -1298,7 +1308,7 @@ template <typename T>
 void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_options& o, const double* econv,
                       ofdft_opt_result* res, void** v_out, cudaStream_t st) {
     OFDFT_REQUIRE(o.method == OFDFT_OPT_LBFGS, "ofdft_optimize_batch: only L-BFGS is batched");
-    OFDFT_REQUIRE(o.pconv == 0.0 && o.ls_grad == 0 && o.ls_start == 0,
+    OFDFT_REQUIRE(o.pconv == 0.0 && o.ls_grad == 0,
                   "ofdft_optimize_batch: the residual criterion and the derivative line search are not batched");
     OFDFT_REQUIRE(o.maxcor >= 0 && 2 * (o.maxcor + 1) <= kBF - BF_LB0, "ofdft_optimize_batch: maxcor too large");
     Batch<T> b;
@@ -1399,6 +1409,7 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
     };
     std::deque<Pair> lb;
     int pool_i = 0;
+    std::vector<double> last_scale(S, 0.0);  // ls_start: optimize_t's last_scale per system
     for (int it = 1; it < o.maxiter && any(run); ++it) {
         for (int s = 0; s < S; ++s)
             if (run[s]) niter[s] = it;
@@ -1422,8 +1433,11 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
             b.lincomb_dc(BF_P, BF_P, lb[i].s);
         }
         b.orth_norm_dev();
+        // ls_start: the direction's length before normalisation (optimize_t's theta0)
+        const int rth = o.ls_start == 1 ? b.queue_sc(SC_TH0) : -1;
         // uphill: steepest descent (optimization.py:373-380); otherwise this dtheta is g0
-        std::vector<double> g0(S, 0.0);
+        std::vector<double> g0(S, 0.0), theta0(S, 0.0);
+        std::vector<char> natural(S, 0);
         {
             for (int s = 0; s < S; ++s) b.coef(s, 1.0, 0.0);
             const int r = b.dtheta(BF_V, BF_PHI);
@@ -1432,6 +1446,8 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
             for (int s = 0; s < S; ++s) {
                 up[s] = run[s] && b.at(r, s) * 2.0 > 0;
                 g0[s] = 2.0 * b.at(r, s) * dV[s];
+                if (rth >= 0) theta0[s] = b.at(rth, s);
+                natural[s] = rth >= 0 && run[s] && !up[s];
             }
             if (any(up)) {
                 active(up);
@@ -1454,6 +1470,9 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         std::vector<Task> task(S, FG);
         for (int s = 0; s < S; ++s) {
             if (!run[s]) continue;
+            // first trial step as optimize_t's (ls_start: the scaled direction length once known)
+            if (natural[s] && theta0[s] > 0.0 && std::isfinite(theta0[s]) && last_scale[s] > 0.0)
+                stp[s] = std::min(theta0[s] * last_scale[s], M_PI);
             Dcsrch& d = ls[s];
             d.ftol = o.c1;
             d.gtol = o.c2;
@@ -1511,6 +1530,7 @@ void optimize_batch_t(int S, ofdft_eval** evs, void** rho_io, const ofdft_opt_op
         std::vector<char> acc(S, 0);
         for (int s = 0; s < S; ++s) {
             if (!run[s]) continue;
+            if (ok[s] && natural[s] && theta0[s] > 0.0 && std::isfinite(theta0[s])) last_scale[s] = stp[s] / theta0[s];
             nfev[s] += nls[s];
             if (!ok[s] || nls[s] == 0 || stp[s] != last_theta[s]) {
                 conv[s] = 1;  // "Line-Search Failed" (optimization.py:444-448)

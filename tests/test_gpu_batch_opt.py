@@ -37,21 +37,26 @@ def _systems(dtype):
     return out
 
 
-def _opt(tot, nat, econv_pa):
+def _opt(tot, nat, econv_pa, start="reference"):
     return D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
-                          optimization_options={"econv": econv_pa * nat, "maxiter": 200, "maxfun": 50})
+                          optimization_options={"econv": econv_pa * nat, "maxiter": 200, "maxfun": 50,
+                                                "linesearch_start": start})
 
 
+@pytest.mark.parametrize("start", ["reference", "direction"])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_batch_equals_single_solves(dtype):
+def test_batch_equals_single_solves(dtype, start):
+    """Also with every line search started at the scaled length of the L-BFGS
+    direction (linesearch_start="direction"), whose lengths the batch computes
+    on the device."""
     systems = _systems(dtype)
     econvs = [1e-7, 1e-8, 1e-7, 1e-6, 1e-7]
     singles = []
     for (tot, rho0, nat), ec in zip(systems, econvs):
-        o = _opt(tot, nat, ec)
+        o = _opt(tot, nat, ec, start)
         r = o.optimize_rho(guess_rho=rho0, dtype=dtype)
         singles.append((o, r))
-    batch = [_opt(tot, nat, ec) for (tot, rho0, nat), ec in zip(systems, econvs)]
+    batch = [_opt(tot, nat, ec, start) for (tot, rho0, nat), ec in zip(systems, econvs)]
     rhos = optimize_rho_batch(batch, [rho0 for _, rho0, _ in systems], dtype=dtype)
     for (o1, r1), o2, r2 in zip(singles, batch, rhos):
         assert o2.converged == o1.converged

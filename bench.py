@@ -606,9 +606,10 @@ def ground_state(D, pp, grid, rho_np, nat, nsp):
     searches (first trial step theta = 1) and once with every line search
     started at the direction's own length (the quasi-Newton step); the faster
     of the two that meets the force bar is the FP64 time (``f64_baseline``).
-    FP32-mixed (``f32_mixed``): FP32 L-BFGS to econv 1e-9 Ha/atom, then FP32
-    L-BFGS on the derivative-only line search until the float32 residual stops
-    falling (150 iterations), both with the direction start, then one FP64 E+V
+    FP32-mixed (``f32_mixed``): FP32 L-BFGS to econv 1e-9 Ha/atom, then 80
+    iterations of FP32 L-BFGS on the derivative-only line search (the float32
+    gradient keeps improving the density where float32 energies no longer
+    resolve the decreases), both with the direction start, then one FP64 E+V
     of that density; for comparison the same with the reference's first steps,
     and FP32 L-BFGS then FP64 L-BFGS to econv 1e-10 Ha/atom."""
     import torch
@@ -673,12 +674,12 @@ def ground_state(D, pp, grid, rho_np, nat, nsp):
 
     mixed("f32_mixed", lambda o: o.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-9 * nat, refine="evaluate",
                                                       f32_options={"linesearch_start": "direction"},
-                                                      f32_polish={"maxiter": 150, "linesearch_start": "direction"}),
-          "FP32 L-BFGS (econv 1e-9 Ha/atom), FP32 L-BFGS on the derivative line search (150 iterations), both "
-          "starting each line search at the direction's own length, one FP64 E+V")
+                                                      f32_polish={"maxiter": 80, "linesearch_start": "direction"}),
+          "FP32 L-BFGS (econv 1e-9 Ha/atom), FP32 L-BFGS on the derivative line search (80 iterations), both "
+          "starting each line search at the scaled length of the L-BFGS direction, one FP64 E+V")
     mixed("f32_mixed_reference_start", lambda o: o.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-9 * nat,
                                                                       refine="evaluate",
-                                                                      f32_polish={"maxiter": 150}),
+                                                                      f32_polish={"maxiter": 80}),
           "as f32_mixed with the reference's first trial steps")
     mixed("f32_mixed_f64_lbfgs", lambda o: o.optimize_rho_mixed(guess_rho=rho0, econv_f32=1e-9 * nat,
                                                                 refine="optimize"),

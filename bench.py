@@ -15,6 +15,8 @@ roofline  the whole E+V evaluation: its algorithmic bytes B = (2 n_FFT + 3) s N
           over the time per evaluation, against the measured HBM copy
           bandwidth, with the DRAM traffic of its kernels;
           roofline_dominant_kernel: the same for the costliest kernel class
+split_pipeline  the same E+V on the opt-in split k_F-node pipeline (no axis-1
+          plane pass: half the DRAM traffic, but slower on GB300)
 time_to_ground_state  from the uniform density at the accuracy bars (|dE| <= 1e-6
           Ha/atom, forces within 1e-5 Ha/Bohr of the FP64 ground state) on the
           headline functional with Hermite k_F interpolation and fixed bounds:
@@ -52,6 +54,14 @@ METRIC = "E+V evals/s & time-to-ground-state at 256^3 WGC: FP32-mixed vs FP64 on
 WGC = dict(alpha=(5 + 5 ** 0.5) / 6, beta=(5 - 5 ** 0.5) / 6)
 HBM_FALLBACK = 6800.0
 
+# DRAM traffic per algorithmic byte of the split pipeline's kernel classes (k_fz_n8,
+# k_fz_c2r_s8, k_fz_r2c_s8, k_fz_pot2_s8), from one ncu capture at 256^3 with 16 nodes.
+TRAFFIC_RATIO_SPLIT = {
+    "lwt_nodes": (0.0723 + 1.0267) / ((16 + 1) * 67633152 / 1e9),
+    "lwt_interp": (1.1494 + 0.0658) / ((16 * 67633152 + 2 * 4 * 16777216) / 1e9),
+    "lwt_pot2": (1.0845 + 0.0635) / ((16 + 1) * 67633152 / 1e9),
+    "fz_hat": (0.1345 + 1.0206) / ((16 * 67633152 + 2 * 4 * 16777216) / 1e9),
+}
 # DRAM traffic per algorithmic byte of each kernel class, from one ncu capture of
 # the same kernels on the 256^3 grid with 16 nodes (dram__bytes_read.sum +
 # dram__bytes_write.sum over the bytes the launch must move); a launch at 64
@@ -355,10 +365,11 @@ def gpu_arm(args):
         if dist is not None:
             dist.barrier()
 
-    def run(dtype, steps, warmup, profile=False, sampler=None):
+    def run(dtype, steps, warmup, profile=False, sampler=None, total=None):
+        total = total or tot
         rho = D.DirectField(grid, data=rho_np, dtype=dtype)
-        ev = tot.evaluator(grid, dtype)
-        tot.prepare(ev, grid, dtype)
+        ev = total.evaluator(grid, dtype)
+        total.prepare(ev, grid, dtype)
         V = torch.empty_like(rho.as_subclass(torch.Tensor))
         calc = _lib.CALC_E | _lib.CALC_V
         if sampler:
@@ -455,6 +466,26 @@ def gpu_arm(args):
                                    "times its ncu DRAM/algorithmic ratio (1 where none was measured)" % n_fft}
     else:
         out["roofline"] = out["roofline_dominant_kernel"]
+    # ---- the opt-in split pipeline (axis 1 factored between the column and row passes, no
+    # axis-1 plane pass): its time, roofline fraction and traffic on the same workload
+    if algo_bytes and args.interp == "linear" and args.n == 256 and args.lwt_pipeline == "auto":
+        ke_s = D.Functional(type="KEDF", name="LWT", nsp=args.nsp, kdd=3, interp="linear", pipeline="fused-split",
+                            **WGC)
+        tot_s = D.TotalFunctional(KineticEnergyFunctional=ke_s, XCFunctional=D.Functional(type="XC", name="LDA"),
+                                  HARTREE=D.Functional(type="HARTREE"), PSEUDO=pp)
+        ks = max(3, min(args.steps, 10))
+        rs = run(torch.float32, ks, 3, total=tot_s)
+        rsp = run(torch.float32, 3, 1, profile=True, total=tot_s)
+        ms_s = maxrank(rs["ms_total"]) / ks
+        traffic_s = sum(v["bytes"] / 3 * TRAFFIC_RATIO_SPLIT.get(k, 1.0) for k, v in rsp["prof"].items())
+        out["split_pipeline"] = {
+            "what": "the same E+V with OFDFT_LWT_PIPE_FUSED_SPLIT (opt-in): each node plane written once and read "
+                    "once; slower on GB300 (one 512-thread block per SM in its column and row passes)",
+            "value": world * 1e3 / ms_s, "unit": "evals/s", "ms_per_step": ms_s, "steps": ks,
+            "roofline_frac": algo_bytes / (ms_s * 1e-3) / 1e9 / peak, "traffic": traffic_s,
+            "traffic_per_algorithmic_byte": traffic_s / algo_bytes,
+            "dE_vs_default_pipeline_per_atom": (rs["E"] - r32["E"]) / nat,
+            "kernels_ms_per_step": {k: v["ms"] / 3 for k, v in rsp["prof"].items() if v["launches"]}}
     # ---- FP64 path
     if not args.no_fp64:
         k64 = min(5, max(2, args.steps // 3))

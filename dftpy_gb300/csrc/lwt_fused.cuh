@@ -78,8 +78,9 @@ FzTab fz_tab(const Table<float>& t) {
 
 // Coefficients c_k of the large-eta series of the inverse Lindhard function
 // with mu = 1 (kernel.py:79-133): F = -lbda - 0.6 + sum_k c_k eta^{-2(k+1)}.
-// For eta >= 4 the terms after k = 7 are below 1e-12 of F, so eight terms
-// reproduce the table to float32 precision.
+// For eta >= 2.5 the terms after k = 7 are below 5e-10 of F, and those of
+// -eta F' after k = 9 below 1e-8 of it, so eight terms (ten for the
+// derivative) reproduce the table to float32 precision.
 __device__ __forceinline__ constexpr float fz_series_c(int k) {
     return k == 0   ? -0.13714285714285712f
            : k == 1 ? -6.39999999999999875e-2f
@@ -88,7 +89,9 @@ __device__ __forceinline__ constexpr float fz_series_c(int k) {
            : k == 4 ? -1.80879839616166146e-2f
            : k == 5 ? -1.36715733124818332e-2f
            : k == 6 ? -1.07236045520990083e-2f
-                    : -8.65192783339199453e-3f;
+           : k == 7 ? -8.65192783339199453e-3f
+           : k == 8 ? -7.1372762502456763e-3f
+                    : -5.9945117538835746e-3f;
 }
 
 __device__ __forceinline__ float fz_spline(const float* c, int nint, float step, float inv_step, float eta) {
@@ -110,9 +113,9 @@ __device__ __forceinline__ float fz_node_kernel(const FzTab& tb, float q, float 
     const float u = iq2 * kj2;
     float r;
     if constexpr (DERIV) {
-        float d = 16.0f * fz_series_c(7);
+        float d = 20.0f * fz_series_c(9);
 #pragma unroll
-        for (int k = 6; k >= 0; --k) d = fmaf(d, u, (float)(2 * (k + 1)) * fz_series_c(k));
+        for (int k = 8; k >= 0; --k) d = fmaf(d, u, (float)(2 * (k + 1)) * fz_series_c(k));
         r = tb.factor * (d * u);
         r = eta >= tb.etamax ? tb.limitd : r;
     } else {

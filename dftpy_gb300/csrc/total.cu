@@ -332,8 +332,10 @@ __device__ inline void scale_node(const Table<T>& tab, T c, T& K, T& kd, T KD) {
 
 // Large-eta branch of the inverse Lindhard function (kernel.py:79-133) with
 // mu = 1: F = -lbda - 0.6 + sum_k c_k eta^{-2k}, and -eta dF/deta = sum_k 2k c_k
-// eta^{-2k}.  The 50000-point spline of the table reproduces this smooth
-// series to ~1e-12 for eta >= 4, so the FP32 path evaluates it in registers.
+// eta^{-2k}.  The series converges for eta > 1; the reference's table holds it
+// above eta = 3.65 (kernel.py:27) and the same function in closed form below, so
+// at and above eta = 2.5 the truncated series reproduces the table to ~5e-10 of F
+// (below float32 resolution) and the FP32 paths evaluate it in registers there.
 __constant__ float cLargeF[15] = {-0.13714285714285712f, -6.39999999999999875e-2f, -3.77825602968460128e-2f,
                                   -2.51824061652633074e-2f, -1.80879839616166146e-2f, -1.36715733124818332e-2f,
                                   -1.07236045520990083e-2f, -8.65192783339199453e-3f, -7.1372762502456763e-3f,
@@ -975,7 +977,7 @@ Table<T> table_of(const ofdft_eval* e) {
     t.factor = 4.0 / 5.0 * 0.3 * std::pow(3.0 * M_PI * M_PI, 2.0 / 3.0);
     t.lbda = e->cfg.lwt_x;
     // the large-eta series is the inverse Lindhard function's: WT tables only
-    t.eta_series = e->cfg.lwt_kernel == OFDFT_LWT_KERNEL_WT ? 4.0 : INFINITY;
+    t.eta_series = e->cfg.lwt_kernel == OFDFT_LWT_KERNEL_WT ? 2.5 : INFINITY;
     t.hc = e->cfg.lwt_family == OFDFT_LWT_FAMILY_HC ? 1 : 0;
     return t;
 }

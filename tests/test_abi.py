@@ -54,6 +54,25 @@ def test_config_defaults_match_reference():
     _lib.load().ofdft_opt_default(C.byref(o))
     assert (o.maxiter, o.maxfun, o.ncheck, o.maxcor) == (200, 50, 2, 6)
     assert (o.c1, o.c2, o.xtol, o.econv) == (1e-4, 0.2, 1e-12, 1e-5)
+    # the options the reference lacks are off by default
+    assert (o.pconv, o.ls_grad, o.ls_start) == (0.0, 0, 0)
+
+
+def test_optimizer_line_search_options():
+    """linesearch / linesearch_start map to ls_grad / ls_start; unknown values fail
+    where the options are read (no GPU needed: the struct is filled on the host)."""
+    import dftpy_gb300 as D
+    tot = D.TotalFunctional()
+    o = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
+                       optimization_options={"linesearch": "grad", "linesearch_start": "direction"})
+    s = o.options_struct()
+    assert (s.ls_grad, s.ls_start) == (1, 1)
+    s = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS").options_struct()
+    assert (s.ls_grad, s.ls_start) == (0, 0)
+    bad = D.Optimization(EnergyEvaluator=tot, optimization_method="LBFGS",
+                         optimization_options={"linesearch_start": "newton"})
+    with pytest.raises(ValueError):
+        bad.options_struct()
 
 
 def _native_ls(f, fp, c1=1e-4, c2=0.2, amax=np.pi, amin=0.0, xtol=1e-12):
